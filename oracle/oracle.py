@@ -1,0 +1,613 @@
+"""CPU oracle for the strata-fdtd time-step path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline and
+reference legs may import this module.  The product package never does.
+
+It restates the reference's solver API (same class names, arguments and step
+order; paths relative to src/strata_fdtd/ of rjwalters/strata-fdtd) on top of
+``liboracle.so`` (oracle/sf_oracle.c), the C restatement of the reference
+native kernels.  ``precision="f32"`` reproduces FDTDSolver(backend="native")
+bit for bit (pinned against the reference's own outputs in tests/golden/);
+``precision="f64"`` runs the same arithmetic in double to state the error of
+an FP32 result.  ADE materials are stepped in the order of
+_step_python_uniform (core/solver.py:2135-2193) with the native ADE kernels'
+arithmetic (the reference's native step skips ADE altogether).
+
+Voxelisation restates geometry/sdf.py with the same NumPy calls, so on one
+machine it reproduces SDFPrimitive.voxelize exactly.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def lib():
+    """Load (building on first use) oracle/_build/liboracle.so."""
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "_build", "liboracle.so")
+        src = os.path.join(HERE, "sf_oracle.c")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+        _LIB = ctypes.CDLL(path)
+        _declare(_LIB)
+    return _LIB
+
+
+def _declare(L):
+    P, I, L64, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+    for suf, R in (("f32", ctypes.c_float), ("f64", ctypes.c_double)):
+        sig = {
+            "update_velocity": [P, P, P, P, I, I, I, R],
+            "update_pressure": [P, P, P, P, P, I, I, I, R],
+            "apply_rigid": [P, P, P, P, I, I, I],
+            "boundary_faces": [P, I, I, I, I, P],
+            "pml_decay": [P, I, R, P],
+            "pml_velocity": [P, P, P, P, P, P, I, I, I],
+            "pml_pressure": [P, P, P, P, I, I, I],
+            "inject": [P, P, I, I, I, I, I, I, I, D],
+            "ade_debye": [P, P, P, I, R, R, L64],
+            "ade_lorentz": [P, P, P, P, I, R, R, R, L64],
+            "ade_velocity_correction": [P, P, P, P, P, I, R, I, I, I],
+            "ade_pressure_correction": [P, P, P, I, R, L64],
+            "divergence": [P, P, P, P, I, I, I, R],
+            "run_plain": [P, P, P, P, P, L64, P, P],
+            "omp_threads": [],
+            "set_threads": [I],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, f"orc_{name}_{suf}")
+            fn.argtypes = args
+            fn.restype = L64 if name == "boundary_faces" else (I if name == "omp_threads" else None)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class _PlanF(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("cv", ctypes.c_float), ("cp", ctypes.c_float),
+                ("geom", ctypes.c_void_p), ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p),
+                ("dz", ctypes.c_void_p), ("n_src", ctypes.c_int), ("src", ctypes.c_void_p),
+                ("n_probe", ctypes.c_int), ("probe_cell", ctypes.c_void_p)]
+
+
+class _PlanD(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("cv", ctypes.c_double), ("cp", ctypes.c_double),
+                ("geom", ctypes.c_void_p), ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p),
+                ("dz", ctypes.c_void_p), ("n_src", ctypes.c_int), ("src", ctypes.c_void_p),
+                ("n_probe", ctypes.c_int), ("probe_cell", ctypes.c_void_p)]
+
+
+def set_threads(n):
+    lib().orc_set_threads_f32(int(n))
+
+
+def threads():
+    return int(lib().orc_omp_threads_f32())
+
+
+# ---------------------------------------------------------------------------
+# Grid (core/grid.py:51-146)
+class UniformGrid:
+    def __init__(self, shape, resolution):
+        self.shape = tuple(int(n) for n in shape)
+        self.resolution = float(resolution)
+        r = self.resolution
+        self.x_coords = np.arange(self.shape[0]) * r + r / 2
+        self.y_coords = np.arange(self.shape[1]) * r + r / 2
+        self.z_coords = np.arange(self.shape[2]) * r + r / 2
+        self.min_spacing = r
+        self.is_uniform = True
+
+
+# ---------------------------------------------------------------------------
+# Source (core/solver.py:152-207)
+@dataclass
+class GaussianPulse:
+    position: object
+    frequency: float
+    bandwidth: float | None = None
+    amplitude: float = 1.0
+    source_type: str = "point"
+
+    def __post_init__(self):
+        if self.bandwidth is None:
+            self.bandwidth = 2.0 * self.frequency
+
+    def waveform(self, t, dt):
+        sigma = 1.0 / (np.pi * self.bandwidth)
+        t0 = 4.0 * sigma
+        envelope = np.exp(-((t - t0) ** 2) / (2 * sigma**2))
+        carrier = np.sin(2 * np.pi * self.frequency * (t - t0))
+        return self.amplitude * envelope * carrier
+
+
+# ---------------------------------------------------------------------------
+# Materials (materials/base.py:55-213, 509-545)
+class PoleType(enum.Enum):
+    DEBYE = "debye"
+    LORENTZ = "lorentz"
+
+
+@dataclass
+class Pole:
+    pole_type: PoleType
+    delta_chi: float
+    target: str
+    tau: float | None = None
+    omega_0: float | None = None
+    gamma: float | None = None
+
+    @property
+    def is_debye(self):
+        return self.pole_type == PoleType.DEBYE
+
+    def fdtd_coefficients(self, dt):
+        if self.is_debye:
+            tau_dt = self.tau / dt
+            denom = 1 + tau_dt
+            return (tau_dt / denom, self.delta_chi / denom)
+        w0, g = self.omega_0, self.gamma
+        dt2 = dt * dt
+        c = 1 + g * dt / 2
+        a = (2 - w0**2 * dt2) / c
+        b = -(1 - g * dt / 2) / c
+        d = self.delta_chi * w0**2 * dt2 / c
+        return (a, b, d)
+
+
+@dataclass
+class SimpleMaterial:
+    name: str
+    _rho: float = 1.2
+    _c: float = 343.0
+    _poles: list = field(default_factory=list)
+
+    @property
+    def rho_inf(self):
+        return self._rho
+
+    @property
+    def K_inf(self):
+        return self._rho * self._c**2
+
+    @property
+    def poles(self):
+        return self._poles
+
+
+# ---------------------------------------------------------------------------
+# PML (boundaries/_boundaries.py:104-377): sigma profile + multiplicative decay
+class PML:
+    def __init__(self, depth=10, axis="all", max_sigma=None, order=3):
+        self.depth = depth
+        self.order = order
+        self.axes = ("x", "y", "z") if axis == "all" else ((axis,) if isinstance(axis, str) else axis)
+        self._max_sigma = max_sigma
+
+    def initialize(self, solver):
+        nx, ny, nz = solver.shape
+        if self._max_sigma is None:
+            R_target = 1e-6
+            d = self.depth * solver.grid.min_spacing
+            self._max_sigma = -(self.order + 1) * solver.c * np.log(R_target) / (2 * d)
+        dtype = np.float64 if solver.precision == "f64" else np.float32
+        sig = [self._profile(n, dtype) if a in self.axes else None
+               for n, a in zip((nx, ny, nz), ("x", "y", "z"))]
+        self._sigma_x, self._sigma_y, self._sigma_z = sig
+        self.decay = []
+        for s in sig:
+            if s is None:
+                self.decay.append(None)
+            elif solver.precision == "f64":
+                self.decay.append(np.exp(-s * solver.dt))
+            else:  # pml.cpp:13-45, expf in float with dt rounded to float
+                out = np.zeros(len(s), dtype=np.float32)
+                lib().orc_pml_decay_f32(s.ctypes.data, len(s), float(np.float32(solver.dt)),
+                                        out.ctypes.data)
+                self.decay.append(out)
+
+    def _profile(self, n, dtype):
+        sigma = np.zeros(n, dtype=dtype)
+        d = self.depth
+        for i in range(d):
+            sigma[i] = self._max_sigma * (((d - i) / d) ** self.order)
+        for i in range(n - d, n):
+            sigma[i] = self._max_sigma * (((i - (n - d - 1)) / d) ** self.order)
+        return sigma
+
+
+# ---------------------------------------------------------------------------
+# SDF (geometry/sdf.py), same NumPy calls as the reference
+class SDFPrimitive:
+    def voxelize(self, grid):
+        X, Y, Z = np.meshgrid(grid.x_coords, grid.y_coords, grid.z_coords, indexing="ij")
+        pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+        return self.sdf(pts).reshape(grid.shape) <= 0
+
+    def translate(self, offset):
+        return Translate(self, offset)
+
+    def scale(self, factor):
+        return Scale(self, factor)
+
+
+class Box(SDFPrimitive):  # sdf.py:232-299
+    def __init__(self, center=None, size=None, min_corner=None, max_corner=None):
+        if center is not None and size is not None:
+            self.center = np.array(center, dtype=np.float64)
+            self.size = np.array(size, dtype=np.float64)
+        else:
+            lo = np.array(min_corner, dtype=np.float64)
+            hi = np.array(max_corner, dtype=np.float64)
+            self.center = (lo + hi) / 2
+            self.size = hi - lo
+
+    def sdf(self, points):
+        q = np.abs(np.asarray(points, dtype=np.float64) - self.center) - self.size / 2
+        return np.linalg.norm(np.maximum(q, 0), axis=1) + np.minimum(np.max(q, axis=1), 0)
+
+
+class Sphere(SDFPrimitive):  # sdf.py:302-338
+    def __init__(self, center, radius):
+        self.center = np.array(center, dtype=np.float64)
+        self.radius = float(radius)
+
+    def sdf(self, points):
+        return np.linalg.norm(np.asarray(points, dtype=np.float64) - self.center, axis=1) - self.radius
+
+
+class Cylinder(SDFPrimitive):  # sdf.py:341-433
+    def __init__(self, p1, p2, radius):
+        self.p1 = np.array(p1, dtype=np.float64)
+        self.p2 = np.array(p2, dtype=np.float64)
+        self.radius = float(radius)
+        self.axis = self.p2 - self.p1
+        self.length = np.linalg.norm(self.axis)
+        self.axis_normalized = self.axis / self.length
+
+    def sdf(self, points):
+        points = np.asarray(points, dtype=np.float64)
+        v = points - self.p1
+        t = np.dot(v, self.axis_normalized)
+        tc = np.clip(t, 0, self.length)
+        closest = self.p1 + tc[:, np.newaxis] * self.axis_normalized
+        radial = np.linalg.norm(points - closest, axis=1)
+        axial = np.maximum(0, np.abs(t - self.length / 2) - self.length / 2)
+        inside = (t >= 0) & (t <= self.length)
+        return np.where(inside, radial - self.radius,
+                        np.sqrt((radial - self.radius) ** 2 + axial**2))
+
+
+class Union(SDFPrimitive):  # sdf.py:549-609
+    def __init__(self, *children):
+        self.children = children
+
+    def sdf(self, points):
+        if not self.children:
+            return np.full(len(points), np.inf)
+        return np.minimum.reduce([c.sdf(points) for c in self.children])
+
+
+class Intersection(SDFPrimitive):  # sdf.py:612-682
+    def __init__(self, *children):
+        self.children = children
+
+    def sdf(self, points):
+        if not self.children:
+            return np.full(len(points), -np.inf)
+        return np.maximum.reduce([c.sdf(points) for c in self.children])
+
+
+class Difference(SDFPrimitive):  # sdf.py:685-733
+    def __init__(self, base, *subtracted):
+        self.base = base
+        self.subtracted = subtracted
+
+    def sdf(self, points):
+        r = self.base.sdf(points)
+        for s in self.subtracted:
+            r = np.maximum(r, -s.sdf(points))
+        return r
+
+
+class Translate(SDFPrimitive):  # sdf.py:1199-1236
+    def __init__(self, child, offset):
+        self.child = child
+        self.offset = np.asarray(offset, dtype=np.float64)
+
+    def sdf(self, points):
+        return self.child.sdf(points - self.offset)
+
+
+class Scale(SDFPrimitive):  # sdf.py:1239-1300
+    def __init__(self, child, scale):
+        self.child = child
+        if np.isscalar(scale):
+            self.scale = np.array([scale, scale, scale], dtype=np.float64)
+            self.uniform = True
+        else:
+            self.scale = np.asarray(scale, dtype=np.float64)
+            self.uniform = np.allclose(self.scale, self.scale[0])
+
+    def sdf(self, points):
+        d = self.child.sdf(points / self.scale)
+        return d * self.scale[0] if self.uniform else d * np.min(self.scale)
+
+
+class HelmholtzResonator(SDFPrimitive):  # geometry/resonator.py:59-297
+    def __init__(self, position, cavity_shape="box", cavity_size=(0.03, 0.03, 0.03),
+                 neck_length=0.01, neck_radius=0.005, neck_direction=(0.0, 0.0, 1.0)):
+        self.position = np.asarray(position, dtype=np.float64)
+        nd = np.asarray(neck_direction, dtype=np.float64)
+        self.neck_direction = nd / np.linalg.norm(nd)
+        self.cavity_shape, self.cavity_size = cavity_shape, cavity_size
+        if cavity_shape == "box":
+            cav = Box(center=tuple(self.position), size=cavity_size)
+            half = np.array(cavity_size, dtype=np.float64) / 2
+            start = self.position + self.neck_direction * np.min(
+                half / (np.abs(self.neck_direction) + 1e-10))
+        elif cavity_shape == "sphere":
+            cav = Sphere(center=tuple(self.position), radius=cavity_size[0])
+            start = self.position + self.neck_direction * cavity_size[0]
+        else:
+            r, length = cavity_size
+            ax = self.neck_direction * length
+            cav = Cylinder(p1=tuple(self.position - ax / 2), p2=tuple(self.position + ax / 2),
+                           radius=r)
+            start = self.position + self.neck_direction * (length / 2)
+        end = start + self.neck_direction * neck_length
+        self._combined = Union(cav, Cylinder(p1=tuple(start), p2=tuple(end), radius=neck_radius))
+
+    def sdf(self, points):
+        return self._combined.sdf(points)
+
+
+# ---------------------------------------------------------------------------
+# Solver (core/solver.py:1441-2606, native step semantics)
+class Probe:
+    def __init__(self, name, position):
+        self.name, self.position, self.data = name, position, []
+
+
+class FDTDSolver:
+    def __init__(self, shape=None, resolution=None, grid=None, c=343.0, rho=1.2, courant=0.95,
+                 backend="native", precision="f32"):
+        self.grid = grid if grid is not None else UniformGrid(shape, resolution)
+        self.shape = self.grid.shape
+        self.dx = self.grid.min_spacing
+        self.c, self.rho, self.precision = c, rho, precision
+        dt_max = self.grid.min_spacing / (self.c * np.sqrt(3))
+        self.dt = courant * dt_max
+        self._coeff_p = -self.rho * self.c**2 * self.dt / self.dx
+        self._coeff_v = -self.dt / (self.rho * self.dx)
+        self.real = np.float64 if precision == "f64" else np.float32
+        self.p = np.zeros(self.shape, dtype=self.real)
+        self.vx = np.zeros(self.shape, dtype=self.real)
+        self.vy = np.zeros(self.shape, dtype=self.real)
+        self.vz = np.zeros(self.shape, dtype=self.real)
+        self.geometry = np.ones(self.shape, dtype=bool)
+        self._geometry_set = False
+        self._sources, self._probes, self._boundaries = [], {}, []
+        self._materials = {}
+        self._material_id = np.zeros(self.shape, dtype=np.uint8)
+        self._ade = None
+        self._step_count, self._time = 0, 0.0
+
+    # -- setup (solver.py:1682-1990)
+    def set_geometry(self, mask):
+        if isinstance(mask, SDFPrimitive):
+            mask = mask.voxelize(self.grid)
+        self.geometry = np.ascontiguousarray(mask, dtype=bool)
+        self._geometry_set = True
+
+    def _to_index(self, pos):
+        if isinstance(pos, tuple) and len(pos) == 3 and any(
+                isinstance(p, float) and p < max(self.shape) for p in pos):
+            return tuple(int(round(p / self.dx)) for p in pos)
+        return pos
+
+    def add_source(self, source):
+        if source.source_type == "point":
+            source.position = self._to_index(source.position)
+        self._sources.append(source)
+
+    def add_probe(self, name, position):
+        self._probes[name] = Probe(name, self._to_index(position))
+
+    def add_boundary(self, b):
+        b.initialize(self)
+        self._boundaries.append(b)
+
+    def register_material(self, material, material_id=None):
+        if material_id is None:
+            material_id = next(i for i in range(1, 256) if i not in self._materials)
+        self._materials[material_id] = material
+        self._ade = None
+        return material_id
+
+    def set_material_region(self, mask, material_id):
+        self._material_id[mask] = material_id
+        self._ade = None
+
+    def set_material_box(self, material_id, x_range, y_range, z_range):
+        m = np.zeros(self.shape, dtype=bool)
+        m[x_range[0]:x_range[1], y_range[0]:y_range[1], z_range[0]:z_range[1]] = True
+        self.set_material_region(m, material_id)
+
+    # -- ADE tables (solver.py:2944-3083): one field per pole, Debye and
+    # Lorentz numbered separately in registration order
+    def _init_ade(self):
+        R = self.real
+        n = int(np.prod(self.shape))
+        dt_r = R(self.dt)
+        inv_dx = R(1.0 / self.dx)
+        debye, lorentz = [], []
+        for mid, mat in self._materials.items():
+            rho_inf, k_inf = R(mat.rho_inf), R(mat.K_inf)
+            for pole in mat.poles:
+                tgt = 0 if pole.target == "density" else 1
+                co = tuple(R(v) for v in pole.fdtd_coefficients(self.dt))
+                # ade.cpp:263 / :420: coefficients formed in the kernel's precision
+                cvel = R(R(-dt_r) / rho_inf) * inv_dx
+                cpre = R(-k_inf) * dt_r
+                e = dict(mid=mid, target=tgt, co=co, cvel=R(cvel), cpre=R(cpre))
+                (debye if pole.is_debye else lorentz).append(e)
+        for e in debye:
+            e["J"] = np.zeros(n, dtype=R)
+        for e in lorentz:
+            e["J"] = np.zeros(n, dtype=R)
+            e["Jp"] = np.zeros(n, dtype=R)
+        self._ade = dict(debye=debye, lorentz=lorentz, inv_dx=inv_dx,
+                         div=np.zeros(n, dtype=R))
+
+    # -- stepping
+    def _fns(self):
+        L = lib()
+        s = "f64" if self.precision == "f64" else "f32"
+        return lambda name: getattr(L, f"orc_{name}_{s}")
+
+    def _pml(self):
+        dx = dy = dz = None
+        for b in self._boundaries:
+            dx, dy, dz = b.decay
+        return dx, dy, dz
+
+    def step(self):
+        F = self._fns()
+        nx, ny, nz = self.shape
+        R = self.real
+        cv, cp = R(self._coeff_v), R(self._coeff_p)
+        p, vx, vy, vz = self.p, self.vx, self.vy, self.vz
+        mat = self._material_id
+        if self._materials and self._ade is None:
+            self._init_ade()
+        ade = self._ade if self._materials else None
+        ncell = int(p.size)
+        if ade:  # density poles, before the velocity update (solver.py:2138)
+            for e in ade["debye"]:
+                if e["target"] == 0:
+                    F("ade_debye")(_ptr(e["J"]), _ptr(p), _ptr(mat), e["mid"], *e["co"], ncell)
+            for e in ade["lorentz"]:
+                if e["target"] == 0:
+                    F("ade_lorentz")(_ptr(e["J"]), _ptr(e["Jp"]), _ptr(p), _ptr(mat), e["mid"],
+                                     *e["co"], ncell)
+        F("update_velocity")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz, cv)
+        if ade:
+            for e in ade["debye"] + ade["lorentz"]:
+                if e["target"] == 0:
+                    F("ade_velocity_correction")(_ptr(vx), _ptr(vy), _ptr(vz), _ptr(e["J"]),
+                                                 _ptr(mat), e["mid"], e["cvel"], nx, ny, nz)
+        if self._geometry_set:
+            F("apply_rigid")(_ptr(vx), _ptr(vy), _ptr(vz), _ptr(self.geometry.view(np.uint8)),
+                             nx, ny, nz)
+        if ade and any(e["target"] == 1 for e in ade["debye"] + ade["lorentz"]):
+            F("divergence")(_ptr(ade["div"]), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz,
+                            ade["inv_dx"])
+            for e in ade["debye"]:
+                if e["target"] == 1:
+                    F("ade_debye")(_ptr(e["J"]), _ptr(ade["div"]), _ptr(mat), e["mid"], *e["co"],
+                                   ncell)
+            for e in ade["lorentz"]:
+                if e["target"] == 1:
+                    F("ade_lorentz")(_ptr(e["J"]), _ptr(e["Jp"]), _ptr(ade["div"]), _ptr(mat),
+                                     e["mid"], *e["co"], ncell)
+        F("update_pressure")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz),
+                             _ptr(self.geometry.view(np.uint8)), nx, ny, nz, cp)
+        if ade:
+            for e in ade["debye"] + ade["lorentz"]:
+                if e["target"] == 1:
+                    F("ade_pressure_correction")(_ptr(p), _ptr(e["J"]), _ptr(mat), e["mid"],
+                                                 e["cpre"], ncell)
+            p[~self.geometry] = 0.0
+        for b in self._boundaries:
+            F("pml_velocity")(_ptr(vx), _ptr(vy), _ptr(vz), *(_ptr(d) for d in b.decay),
+                              nx, ny, nz)
+        for b in self._boundaries:
+            F("pml_pressure")(_ptr(p), *(_ptr(d) for d in b.decay), nx, ny, nz)
+        g = _ptr(self.geometry.view(np.uint8))
+        for s in self._sources:
+            val = float(s.waveform(np.array([self._time]), self.dt)[0])
+            kind, a, b_, c = self._src_desc(s)
+            F("inject")(_ptr(p), g, nx, ny, nz, kind, a, b_, c, val)
+        for pr in self._probes.values():
+            pr.data.append(p[pr.position])
+        self._step_count += 1
+        self._time += self.dt
+
+    @staticmethod
+    def _src_desc(s):
+        if s.source_type == "point":
+            return (0, *s.position)
+        return (1, s.position["axis"], s.position["index"], 0)
+
+    def run_steps(self, n):
+        """n steps of the plain path through one C call (no ADE, one PML)."""
+        assert not self._materials and len(self._boundaries) <= 1
+        nx, ny, nz = self.shape
+        R = self.real
+        vals = np.zeros((n, max(1, len(self._sources))), dtype=np.float64)
+        t = self._time
+        for q in range(n):
+            for si, s in enumerate(self._sources):
+                vals[q, si] = s.waveform(np.array([t]), self.dt)[0]
+            t += self.dt
+        src = np.array([self._src_desc(s) for s in self._sources] or [[0, 0, 0, 0]],
+                       dtype=np.int32)
+        probes = list(self._probes.values())
+        cells = np.array([np.ravel_multi_index(pr.position, self.shape) for pr in probes] or [0],
+                         dtype=np.int64)
+        trace = np.zeros((n, max(1, len(probes))), dtype=R)
+        dx, dy, dz = self._pml()
+        Plan = _PlanD if self.precision == "f64" else _PlanF
+        plan = Plan(nx, ny, nz, R(self._coeff_v), R(self._coeff_p),
+                    _ptr(self.geometry.view(np.uint8)) if self._geometry_set else None,
+                    _ptr(dx), _ptr(dy), _ptr(dz), len(self._sources), _ptr(src),
+                    len(probes), _ptr(cells))
+        self._fns()("run_plain")(ctypes.addressof(plan), _ptr(self.p), _ptr(self.vx),
+                                 _ptr(self.vy), _ptr(self.vz), n, _ptr(vals), _ptr(trace))
+        for qi, pr in enumerate(probes):
+            pr.data.extend(trace[:, qi].tolist())
+        self._step_count += n
+        for _ in range(n):
+            self._time += self.dt
+
+    def get_probe_data(self, name=None):
+        names = [name] if name is not None else list(self._probes)
+        return {k: np.array(self._probes[k].data, dtype=np.float32) for k in names}
+
+
+def boundary_faces(geometry, axis):
+    """precompute_boundary_cells lists (boundaries.cpp:13-64) for one axis."""
+    g = np.ascontiguousarray(geometry, dtype=np.uint8)
+    nx, ny, nz = g.shape
+    f = lib().orc_boundary_faces_f32
+    n = f(g.ctypes.data, nx, ny, nz, axis, None)
+    out = np.zeros(n, dtype=np.int32)
+    f(g.ctypes.data, nx, ny, nz, axis, out.ctypes.data)
+    return out
+
+
+api = None
+
+
+def make_api():
+    """Namespace with the reference API names, for tests/golden/cases.py."""
+    import types
+    return types.SimpleNamespace(
+        FDTDSolver=FDTDSolver, UniformGrid=UniformGrid, PML=PML, GaussianPulse=GaussianPulse,
+        Box=Box, Sphere=Sphere, Cylinder=Cylinder, Union=Union, Intersection=Intersection,
+        Difference=Difference, HelmholtzResonator=HelmholtzResonator, Pole=Pole,
+        PoleType=PoleType, SimpleMaterial=SimpleMaterial)

@@ -1,0 +1,281 @@
+"""Golden-vector cases, written once against the reference API.
+
+Each case is plain data plus a builder that drives any module exposing the
+reference's solver API (``FDTDSolver``, ``UniformGrid``, ``PML``,
+``GaussianPulse``, the SDF classes and the material classes).  The same
+builder runs the reference itself (``make_golden.py``, in a container where
+the reference tree exists) and ``strata_fdtd_gb300`` (the GPU tests), so a
+golden fixture and its replay cannot drift apart.
+
+Reference API used (paths relative to src/strata_fdtd/ of
+rjwalters/strata-fdtd): FDTDSolver.__init__ core/solver.py:1507-1518,
+add_boundary :1983, set_geometry :1682, add_source :1782, add_probe :1843,
+register_material :2836, set_material_box :2900, PML boundaries/_boundaries.py:125,
+GaussianPulse core/solver.py:152, SDF geometry/sdf.py, HelmholtzResonator
+geometry/resonator.py:59, Pole/SimpleMaterial materials/base.py:55,509.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+AIR = dict(c=343.0, rho=1.204)
+
+
+def _mask_blocks(shape, seed, n_boxes=2, n_spheres=1):
+    """Seeded solid blocks and balls, True = air (the reference convention)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    g = np.ones(shape, dtype=bool)
+    for _ in range(n_boxes):
+        lo = [int(rng.integers(1, n - 4)) for n in shape]
+        hi = [min(n, l + int(rng.integers(2, max(3, n // 3)))) for l, n in zip(lo, shape)]
+        g[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] = False
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    for _ in range(n_spheres):
+        c = [int(rng.integers(2, n - 2)) for n in shape]
+        r = int(rng.integers(2, max(3, min(shape) // 4)))
+        g[(ii - c[0]) ** 2 + (jj - c[1]) ** 2 + (kk - c[2]) ** 2 <= r * r] = False
+    return g
+
+
+# --------------------------------------------------------------------------
+# Plain path: reference FDTDSolver(backend="native") step for step.
+# source tuple: (kind, position, frequency, amplitude); a plane position is a
+# dict {"axis": a, "index": n}.
+PLAIN_CASES = {
+    "c1_tiny": dict(
+        shape=(32, 32, 32), res=1e-3, courant=0.5, pml=dict(depth=6),
+        sources=[("point", (16, 16, 16), 20000.0, 1.0)],
+        probes=[("out", (24, 16, 16)), ("src", (16, 16, 16))],
+        steps=200, store_fields=True,
+    ),
+    "blocks_odd": dict(
+        shape=(17, 23, 29), res=1e-3, courant=0.5, pml=dict(depth=3),
+        geometry=dict(kind="blocks", seed=3),
+        sources=[("point", (3, 4, 5), 30000.0, 2.0), ("point", (3, 4, 5), 15000.0, -0.5)],
+        probes=[("a", (8, 11, 14)), ("b", (1, 20, 27)), ("c", (16, 22, 28))],
+        steps=150, store_fields=True,
+    ),
+    "plane_x_pml_x": dict(
+        shape=(24, 20, 16), res=1e-3, courant=0.5, pml=dict(depth=4, axis="x"),
+        sources=[("plane", {"axis": 0, "index": 5}, 25000.0, 1.0)],
+        probes=[("p0", (18, 10, 8)), ("p1", (5, 0, 0))],
+        steps=120, store_fields=True,
+    ),
+    "plane_yz_geom": dict(
+        shape=(20, 18, 22), res=2e-3, courant=0.9, pml=dict(depth=2, axis=("y", "z")),
+        geometry=dict(kind="blocks", seed=11, n_boxes=3, n_spheres=2),
+        sources=[("plane", {"axis": 1, "index": 7}, 12000.0, 1.0),
+                 ("plane", {"axis": 2, "index": 20}, 8000.0, 0.5),
+                 ("point", (10, 9, 11), 9000.0, 1.0)],
+        probes=[("q", (12, 3, 4))],
+        steps=100, store_fields=True,
+    ),
+    "impulse_default_coeffs": dict(
+        # reference defaults: rho 1.2, courant 0.95, no PML; impulse written
+        # straight into solver.p as tests/test_native_extension.py:247-249 does
+        shape=(20, 20, 20), res=2e-3, courant=None, rho=None, pml=None,
+        impulse=((10, 10, 10), 1.0), sources=[], probes=[("c", (10, 10, 10))],
+        steps=60, store_fields=True,
+    ),
+    "meters_positions": dict(
+        shape=(30, 26, 22), res=1e-3, courant=0.5, pml=dict(depth=5),
+        sources=[("point", (0.012, 0.0133, 0.009), 18000.0, 1.0)],
+        probes=[("m", (0.02, 0.011, 0.0151))],
+        steps=90, store_fields=True,
+    ),
+    "sdf_geometry": dict(
+        shape=(36, 30, 40), res=1e-3, courant=0.5, pml=dict(depth=4),
+        geometry=dict(kind="sdf", which="small_enclosure"),
+        sources=[("point", (18, 15, 20), 20000.0, 1.0)],
+        probes=[("in", (18, 15, 14)), ("out", (5, 5, 5))],
+        steps=160, store_fields=True,
+    ),
+    "c1_full": dict(
+        # the reference quick start, 100^3 x 1000 steps (hashes + traces only)
+        shape=(100, 100, 100), res=1e-3, courant=0.5, pml=dict(depth=10),
+        sources=[("point", (50, 50, 50), 1000.0, 1.0)],
+        probes=[("output", (75, 50, 50))],
+        steps=1000, store_fields=False,
+    ),
+    "c2_enclosure_20": dict(
+        # the 400^3 enclosure workload, first 20 steps (hashes + traces only)
+        shape=(400, 400, 400), res=1e-3, courant=0.5, pml=dict(depth=16),
+        geometry=dict(kind="sdf", which="c2_enclosure"),
+        sources=[("point", (200, 200, 200), 2000.0, 1.0)],
+        probes="c2", steps=20, store_fields=False, big=True,
+    ),
+}
+
+# --------------------------------------------------------------------------
+# ADE path.  The reference's native step never runs the ADE kernels, so the
+# golden is the reference's own ADE kernels called in the order of
+# _step_python_uniform (core/solver.py:2135-2193).
+# pole tuple: ("debye", target, delta_chi, tau) | ("lorentz", target, delta_chi, omega_0, gamma)
+ADE_CASES = {
+    "debye_2pole": dict(
+        shape=(24, 24, 24), res=1e-3, courant=0.5, pml=dict(depth=4),
+        materials=[dict(id=1, rho=1.204, c=343.0,
+                        poles=[("debye", "density", 0.3, 2e-4), ("debye", "modulus", 0.5, 5e-4)],
+                        box=((6, 18), (5, 17), (8, 20)))],
+        sources=[("point", (12, 12, 3), 20000.0, 1.0)],
+        probes=[("in", (12, 12, 12)), ("after", (12, 12, 21))],
+        steps=150, store_fields=True,
+    ),
+    "lorentz_mixed_geom": dict(
+        shape=(22, 20, 26), res=1e-3, courant=0.5, pml=dict(depth=3),
+        geometry=dict(kind="blocks", seed=5, n_boxes=1, n_spheres=1),
+        materials=[
+            dict(id=1, rho=1.5, c=300.0,
+                 poles=[("lorentz", "density", 0.2, 2 * np.pi * 8000.0, 3000.0),
+                        ("debye", "modulus", 0.4, 1e-4)],
+                 box=((3, 12), (2, 10), (4, 15))),
+            dict(id=3, rho=1.1, c=360.0,
+                 poles=[("lorentz", "modulus", 0.3, 2 * np.pi * 12000.0, 5000.0),
+                        ("debye", "density", 0.25, 3e-4)],
+                 box=((12, 20), (8, 18), (12, 24))),
+        ],
+        sources=[("point", (11, 10, 2), 25000.0, 1.0)],
+        probes=[("x", (8, 6, 10)), ("y", (16, 13, 18))],
+        steps=120, store_fields=True,
+    ),
+}
+
+# --------------------------------------------------------------------------
+# Voxelisation: SDFPrimitive.voxelize (geometry/sdf.py:99-125), masks stored
+# bit-packed.  (name, grid shape, resolution, tree builder name)
+VOXEL_CASES = {
+    "box": ((32, 40, 24), 1e-3, "box"),
+    "sphere": ((30, 30, 30), 1e-3, "sphere"),
+    "cyl_axes": ((40, 36, 32), 1e-3, "cyl_axes"),
+    "cyl_oblique": ((32, 32, 32), 1e-3, "cyl_oblique"),
+    "csg_mix": ((48, 40, 44), 1e-3, "csg_mix"),
+    "translate_scale": ((40, 40, 40), 1e-3, "translate_scale"),
+    "helmholtz": ((60, 48, 56), 1e-3, "helmholtz"),
+    "small_enclosure": ((36, 30, 40), 1e-3, "small_enclosure"),
+    "c2_enclosure_4mm": ((100, 100, 100), 4e-3, "c2_enclosure"),
+}
+
+
+def sdf_tree(api, which):
+    """Build a named SDF tree from the API's SDF classes."""
+    Box, Sphere, Cylinder = api.Box, api.Sphere, api.Cylinder
+    Union, Intersection, Difference = api.Union, api.Intersection, api.Difference
+    if which == "box":
+        return Box(center=(0.016, 0.0205, 0.0117), size=(0.0101, 0.0203, 0.0071))
+    if which == "sphere":
+        return Sphere(center=(0.0151, 0.0149, 0.0153), radius=0.0097)
+    if which == "cyl_axes":
+        return Union(
+            Cylinder(p1=(0.005, 0.018, 0.016), p2=(0.035, 0.018, 0.016), radius=0.0041),
+            Cylinder(p1=(0.02, 0.003, 0.0105), p2=(0.02, 0.033, 0.0105), radius=0.0035),
+            Cylinder(p1=(0.0295, 0.0095, 0.002), p2=(0.0295, 0.0095, 0.03), radius=0.0050),
+        )
+    if which == "cyl_oblique":
+        return Cylinder(p1=(0.004, 0.006, 0.005), p2=(0.027, 0.025, 0.028), radius=0.0045)
+    if which == "csg_mix":
+        a = Box(center=(0.024, 0.02, 0.022), size=(0.03, 0.024, 0.028))
+        b = Sphere(center=(0.024, 0.02, 0.022), radius=0.016)
+        c = Cylinder(p1=(0.024, 0.02, 0.0), p2=(0.024, 0.02, 0.044), radius=0.005)
+        d = Box(min_corner=(0.002, 0.002, 0.002), max_corner=(0.01, 0.012, 0.042))
+        return Union(Difference(Intersection(a, b), c), d)
+    if which == "translate_scale":
+        s = Sphere(center=(0.0, 0.0, 0.0), radius=0.006).translate((0.02, 0.021, 0.019))
+        b = Box(center=(0.0, 0.0, 0.0), size=(0.01, 0.006, 0.008)).scale(1.5).translate(
+            (0.012, 0.028, 0.03))
+        return Union(s, b)
+    if which == "helmholtz":
+        H = api.HelmholtzResonator
+        return Union(
+            H(position=(0.015, 0.012, 0.015), cavity_shape="box", cavity_size=(0.016, 0.014, 0.012),
+              neck_length=0.008, neck_radius=0.003, neck_direction=(0, 0, 1)),
+            H(position=(0.042, 0.014, 0.02), cavity_shape="sphere", cavity_size=(0.008,),
+              neck_length=0.007, neck_radius=0.0035, neck_direction=(0, 1, 0)),
+            H(position=(0.03, 0.034, 0.036), cavity_shape="cylinder", cavity_size=(0.007, 0.014),
+              neck_length=0.006, neck_radius=0.004, neck_direction=(1, 0, 0)),
+        )
+    if which == "small_enclosure":
+        outer = Box(center=(0.018, 0.015, 0.02), size=(0.024, 0.018, 0.03))
+        inner = Box(center=(0.018, 0.015, 0.02), size=(0.018, 0.012, 0.024))
+        port = Cylinder(p1=(0.018, 0.015, 0.005), p2=(0.018, 0.015, 0.013), radius=0.0035)
+        return Difference(outer, inner, port)
+    if which == "c2_enclosure":
+        return c2_solid(api)
+    raise KeyError(which)
+
+
+def c2_solid(api):
+    """The enclosure of the 400^3 workload: a 200 x 120 x 300 mm box with
+    12 mm walls centred at (0.2, 0.2, 0.2) m, and a radius-25 mm port through
+    the z-min wall at its face centre, 80 mm long from the outer face inward."""
+    centre = (0.2, 0.2, 0.2)
+    outer = api.Box(center=centre, size=(0.2, 0.12, 0.3))
+    inner = api.Box(center=centre, size=(0.176, 0.096, 0.276))
+    z0 = 0.2 - 0.15
+    port = api.Cylinder(p1=(0.2, 0.2, z0), p2=(0.2, 0.2, z0 + 0.08), radius=0.025)
+    return api.Difference(outer, inner, port)
+
+
+def c2_probes(geometry, pml_depth=16, n=8, seed=0):
+    """8 seeded uniform-random air cells outside the enclosure walls and
+    outside the PML (cells outside the outer box's bounding cells)."""
+    rng = np.random.default_rng(seed)
+    n_cells = geometry.shape[0]
+    lo_box = np.array([100, 140, 50]) - 1   # outer box spans 0.1..0.3, 0.14..0.26, 0.05..0.35 m
+    hi_box = np.array([300, 260, 350]) + 1
+    out = []
+    while len(out) < n:
+        c = rng.integers(pml_depth, n_cells - pml_depth, size=3)
+        inside_bb = np.all(c >= lo_box) and np.all(c < hi_box)
+        if inside_bb or not geometry[tuple(c)]:
+            continue
+        out.append(tuple(int(v) for v in c))
+    return [(f"probe{q}", pos) for q, pos in enumerate(out)]
+
+
+def build_case(api, case, ade=False):
+    """Construct a solver for ``case`` through the reference-shaped ``api``."""
+    kw = dict(grid=api.UniformGrid(shape=case["shape"], resolution=case["res"]),
+              c=AIR["c"], backend="native")
+    rho = case.get("rho", AIR["rho"])
+    if rho is not None:          # None: the reference default (1.2)
+        kw["rho"] = rho
+    if case.get("courant") is not None:
+        kw["courant"] = case["courant"]
+    solver = api.FDTDSolver(**kw)
+    if case.get("pml"):
+        solver.add_boundary(api.PML(**case["pml"]))
+    geo = case.get("geometry")
+    if geo:
+        if geo["kind"] == "blocks":
+            solver.set_geometry(_mask_blocks(case["shape"], geo["seed"],
+                                             geo.get("n_boxes", 2), geo.get("n_spheres", 1)))
+        else:
+            solver.set_geometry(~sdf_tree(api, geo["which"]).voxelize(solver.grid))
+    for m in case.get("materials", []):
+        poles = []
+        for pd in m["poles"]:
+            if pd[0] == "debye":
+                poles.append(api.Pole(pole_type=api.PoleType.DEBYE, delta_chi=pd[2],
+                                      target=pd[1], tau=pd[3]))
+            else:
+                poles.append(api.Pole(pole_type=api.PoleType.LORENTZ, delta_chi=pd[2],
+                                      target=pd[1], omega_0=pd[3], gamma=pd[4]))
+        mat = api.SimpleMaterial(name=f"m{m['id']}", _rho=m["rho"], _c=m["c"], _poles=poles)
+        mid = solver.register_material(mat, material_id=m["id"])
+        solver.set_material_box(mid, *m["box"])
+    for kind, pos, f, a in case.get("sources", []):
+        if kind == "point":
+            solver.add_source(api.GaussianPulse(position=pos, frequency=f, amplitude=a))
+        else:
+            solver.add_source(api.GaussianPulse(position=dict(pos), frequency=f, amplitude=a,
+                                                source_type="plane"))
+    probes = case.get("probes", [])
+    if probes == "c2":
+        probes = c2_probes(solver.geometry)
+    for name, pos in probes:
+        solver.add_probe(name, pos)
+    if case.get("impulse"):
+        pos, val = case["impulse"]
+        solver.p[pos] = val
+    return solver
