@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark: the 400^3 enclosure solve (strata-fdtd time-step path) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (one GPU per rank, replicas only -- the path does not shard): 400^3
+uniform grid, 1 mm cells, air, PML 16, rigid walls voxelised from the box
+enclosure with its port, 2 kHz pulse, 8 probes (strata_fdtd_gb300.workloads).
+One bench step = ``--inner`` (default 100) FDTD time steps; the default
+K = 40 covers the workload's 4000 steps.
+
+Metric: Gcell-updates/s (cells x time steps / s), whole job (sum over ranks
+/ max-over-ranks time).  ``value`` is device-timed with inputs resident in
+HBM (the 1.1 GB state is larger than L2, so no flush is needed); ``e2e`` is
+the same metric through the public API with host-resident (pinned) fields
+uploaded and the pressure field and probe traces read back every bench step.
+``roofline`` relates the fused step kernel to HBM bandwidth (33 algorithmic
+bytes per cell-update: 16 read + 16 written for p, vx, vy, vz, plus the 1-byte
+cell-flag read); ``cpu_baseline`` is the CPU oracle (the bit-exact C
+restatement of the reference native kernels, OpenMP) on a bounded sample.
+
+--impl reference times that CPU implementation alone (all host threads) on
+the same workload and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CELLS = 400 ** 3
+BYTES_PER_CELL = 33
+METRIC = "Gcell-updates/s"
+WORKLOAD = "enclosure_400: 400^3 uniform 1 mm, PML 16, box enclosure 200x120x300 mm (12 mm walls, r25x80 mm port), 2 kHz pulse, 8 probes, 4000 steps"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--inner", type=int, default=100, help="FDTD time steps per bench step")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_step_enclosure_400.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch_400:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_id), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def smi_id(torch, local):
+    """The nvidia-smi id (UUID) of the CUDA device ``local`` of this process."""
+    try:
+        u = str(torch.cuda.get_device_properties(local).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+        return cvd.split(",")[local] if cvd else str(local)
+
+
+def oracle_enclosure(geometry):
+    """The workload on the CPU oracle (float, reference native semantics)."""
+    from oracle import oracle as O
+    from strata_fdtd_gb300.workloads import enclosure_probes
+
+    o = O.FDTDSolver(shape=(400, 400, 400), resolution=1e-3, c=343.0, rho=1.204, courant=0.5)
+    o.add_boundary(O.PML(depth=16))
+    o.set_geometry(geometry)
+    o.add_source(O.GaussianPulse(position=(200, 200, 200), frequency=2000.0))
+    for q, pos in enumerate(enclosure_probes(geometry)):
+        o.add_probe(f"probe{q}", pos)
+    return o
+
+
+def oracle_geometry():
+    """Enclosure mask from the oracle's NumPy SDF restatement, in i-slabs."""
+    from oracle import oracle as O
+
+    c = (0.2, 0.2, 0.2)
+    solid = O.Difference(O.Box(center=c, size=(0.2, 0.12, 0.3)),
+                         O.Box(center=c, size=(0.176, 0.096, 0.276)),
+                         O.Cylinder(p1=(0.2, 0.2, 0.05), p2=(0.2, 0.2, 0.13), radius=0.025))
+    g = O.UniformGrid((400, 400, 400), 1e-3)
+    out = np.empty((400, 400, 400), dtype=bool)
+    Y, Z = np.meshgrid(g.y_coords, g.z_coords, indexing="ij")
+    for i0 in range(0, 400, 25):
+        xs = g.x_coords[i0:i0 + 25]
+        X = np.repeat(xs, Y.size)
+        pts = np.stack([X, np.tile(Y.ravel(), len(xs)), np.tile(Z.ravel(), len(xs))], axis=1)
+        out[i0:i0 + 25] = (solid.sdf(pts) <= 0).reshape(len(xs), 400, 400)
+    return ~out
+
+
+def time_oracle(o, seconds):
+    """Run the oracle for about ``seconds``; returns (Gcell/s, steps, threads)."""
+    from oracle import oracle as O
+
+    t0 = time.perf_counter()
+    o.run_steps(2)
+    per = (time.perf_counter() - t0) / 2
+    n = max(2, int(seconds / max(per, 1e-6)))
+    t0 = time.perf_counter()
+    o.run_steps(n)
+    dt = time.perf_counter() - t0
+    return CELLS * n / dt / 1e9, n, O.threads()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    geometry = oracle_geometry()
+    o = oracle_enclosure(geometry)
+    inner = 2
+    for _ in range(args.warmup):
+        o.run_steps(inner)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.run_steps(inner)
+    el = time.perf_counter() - t0
+    v = CELLS * inner * args.steps / el / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "bench_step": f"{inner} FDTD steps on the CPU"},
+        "cpu_baseline": {"value": v, "unit": METRIC, "cores": O.threads(), "kind": "port",
+                         "sample": f"{inner * args.steps} FDTD steps of the 400^3 enclosure "
+                                   "workload (oracle/sf_oracle.c, bit-exact restatement of the "
+                                   "reference native kernels; OpenMP)"},
+        "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    import strata_fdtd_gb300 as S
+    from strata_fdtd_gb300 import _native
+    from strata_fdtd_gb300.workloads import enclosure_400
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    lib = _native.load()
+    s = enclosure_400()
+    inner, K, W = args.inner, args.steps, args.warmup
+    n_src = len(s._sources)
+    n_probe = len(s._probes)
+    # device-resident inputs for every timed step: waveform table and trace buffer
+    s._sync_tables()
+    s._upload_exposed()
+    total = (W + K) * inner
+    vals = torch.from_numpy(s._source_values(total)).to("cuda")
+    trace = torch.empty((total, n_probe), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def bench_step(q):
+        rc = lib.sf_plan_step(s._plan, inner, vals.data_ptr() + q * inner * n_src * 8,
+                              trace.data_ptr() + q * inner * n_probe * 4, stream.cuda_stream)
+        _native.check(rc, "sf_plan_step")
+
+    for q in range(W):
+        bench_step(q)
+    barrier()
+    clocks = ClockSampler(smi_id(torch, local))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for q in range(W, W + K):
+        bench_step(q)
+    end.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = start.elapsed_time(end)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = K * (inner + 1)
+    value = world * CELLS * inner * K / (ms / 1e3) / 1e9
+    kernel_ms = ms / (K * inner)  # every timed launch attributed to the step kernel
+    hbm, peak_kind = peaks()
+    achieved = BYTES_PER_CELL * CELLS / (kernel_ms / 1e3) / 1e9
+    traffic = profiled_traffic()
+    s._mark_device_newer()
+    s._step_count += (W + K) * inner
+
+    # end to end through the public API: pinned host fields in, p and traces out
+    e2e = None
+    if not args.no_e2e:
+        host = {f: torch.zeros((400, 400, 400), dtype=torch.float32).pin_memory().numpy()
+                for f in ("p", "vx", "vy", "vz")}
+        for f in host:
+            np.copyto(host[f], getattr(s, f))
+        Ke = max(3, min(K, 10))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(Ke):
+            for f in host:
+                setattr(s, f, host[f])
+            s.run_steps(inner)
+            _ = s.p
+            _ = s.get_probe_data()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([el], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": world * CELLS * inner * Ke / el / 1e9, "unit": METRIC,
+               "h2d_bytes_per_step": 4 * CELLS * 4 + inner * n_src * 8,
+               "d2h_bytes_per_step": CELLS * 4 + inner * n_probe * 4,
+               "steps": Ke, "path": "FDTDSolver fields assigned from pinned host arrays, "
+                                    "run_steps(inner), solver.p and get_probe_data() read back"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        o = oracle_enclosure(s.geometry)
+        v, n, th = time_oracle(o, args.cpu_seconds)
+        cpu = {"value": v, "unit": METRIC, "cores": th, "kind": "port",
+               "sample": f"{n} FDTD steps of the same 400^3 enclosure workload on the CPU "
+                         "oracle (bit-exact C restatement of the reference native kernels, "
+                         "OpenMP, all host threads)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "bench_step": f"{inner} FDTD time steps",
+                       "global_batch": world, "parallelism": f"replicas x{world}",
+                       "l2": "state 1.1 GB per replica > 129 MB L2, no flush"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                         "bytes_per_cell": BYTES_PER_CELL,
+                         "kernel": "k_step<GEOM> (fused step, sf_step.cu)"},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "device": torch.cuda.get_device_name(local),
+            "library": lib.sf_version().decode(),
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

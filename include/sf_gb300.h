@@ -1,0 +1,183 @@
+/*
+ * sf_gb300.h -- C ABI of the GB300 (sm_103a) time-step path for the
+ * strata-fdtd acoustic FDTD solver.
+ *
+ * This library replaces the reference's pybind11 module `_kernels`
+ * (src/strata_fdtd/_kernels/kernels.cpp:74-924 of rjwalters/strata-fdtd),
+ * which the solver calls once per kernel per step with host NumPy arrays.
+ * Here the boundary sits one level higher: a *plan* holds one grid's
+ * device-resident state description, and one call advances it by many steps.
+ *
+ * Conventions
+ *  - Every function returns int status: 0 = ok, nonzero = error; the message
+ *    is in sf_last_error() (thread-local).  No C++ exception crosses the ABI.
+ *  - Field buffers are caller-owned device memory (the Python layer uses
+ *    PyTorch tensors), float32, C order: idx = (i*ny + j)*nz + k.
+ *  - Work is enqueued on the caller's stream (cudaStream_t passed as void*,
+ *    NULL = legacy default stream) and is asynchronous unless stated.
+ *  - A plan is used by one host thread at a time.
+ *  - Arithmetic reproduces the reference native path bit for bit (FP32, no
+ *    fused multiply-add, reference operation order).
+ */
+#ifndef SF_GB300_H
+#define SF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SF_ABI_VERSION 1
+#define SF_MAX_SOURCES 16
+#define SF_MAX_POLES 16
+
+typedef struct sf_plan sf_plan;
+
+/* Grid description.  coeff_v / coeff_p are the FP32-rounded scalars that the
+ * reference passes as `float` through pybind11 (core/solver.py:1584-1586 ->
+ * kernels.cpp:113,146). */
+typedef struct {
+    int32_t nx, ny, nz;
+    float coeff_v; /* -dt / (rho*dx) */
+    float coeff_p; /* -rho*c^2*dt / dx */
+    uint32_t flags; /* reserved, 0 */
+} sf_grid_desc;
+
+/* Source descriptor (core/solver.py:2413-2433): kind 0 = point at (a,b,c);
+ * kind 1 = plane with axis a (0,1,2) at index b.  Sources inject into air
+ * cells only, in the order given. */
+typedef struct {
+    int32_t kind, a, b, c;
+} sf_source;
+
+/* ADE pole (materials/base.py:157-188, ade.hpp:44-109).  kind 0 = Debye
+ * (c0 = alpha, c1 = beta), kind 1 = Lorentz (c0 = a, c1 = b, c2 = d).
+ * target 0 = density, 1 = modulus.  corr is the FP32 correction coefficient
+ * as ade.cpp forms it: density (-dt / rho_inf) * inv_dx (ade.cpp:263);
+ * modulus -K_inf * dt (ade.cpp:420).  J / J_prev are caller-owned device
+ * arrays of nx*ny*nz floats (J_prev only for Lorentz). */
+typedef struct {
+    int32_t material_id, kind, target, reserved;
+    float c0, c1, c2, corr;
+    float* J;
+    float* J_prev;
+} sf_pole;
+
+/* SDF program node for sf_voxelize (geometry/sdf.py).  Nodes run in order
+ * on a distance stack and a point stack:
+ *   op 1 BOX      a = centre, b = size
+ *   op 2 SPHERE   a = centre, s0 = radius
+ *   op 3 CYLINDER a = p1, b = unit axis, s0 = length, s1 = radius
+ *   op 10 UNION n          pop n, push min (child order)
+ *   op 11 INTERSECTION n   pop n, push max
+ *   op 12 DIFFERENCE n     pop n (base first), push max(base, -s1, -s2 ...)
+ *   op 20 PUSH_TRANSLATE a push point - a
+ *   op 21 PUSH_SCALE a     push point / a
+ *   op 22 POP_POINT
+ *   op 23 SCALE_DIST s0    top distance *= s0
+ *   op 24 NEGATE           top distance = -top                         */
+typedef struct {
+    int32_t op, n;
+    double a[3], b[3];
+    double s0, s1;
+} sf_sdf_node;
+
+typedef struct {
+    int32_t device, sm_count, cc_major, cc_minor;
+    int64_t total_mem;
+    int32_t l2_bytes, max_smem_per_block;
+    char name[96];
+} sf_device_info_t;
+
+/* --- library ------------------------------------------------------------ */
+/* Replaces _kernels.__version__ / has_openmp (kernels.cpp:76-84). */
+const char* sf_version(void);
+const char* sf_last_error(void);
+int sf_device_info(int device, sf_device_info_t* out);
+
+/* --- plans --------------------------------------------------------------- */
+/* Replaces the per-call shape checks of kernels.cpp:21-65 and the
+ * coefficient hand-off of core/solver.py:1584-1586. */
+int sf_plan_create(const sf_grid_desc* desc, sf_plan** out);
+int sf_plan_destroy(sf_plan* plan);
+
+/* Bind the two ping-pong copies of p, vx, vy, vz (8 device buffers of
+ * nx*ny*nz floats).  Set 0 holds the current state.  The plan never frees
+ * them.  Replaces the NumPy arrays passed to update_velocity /
+ * update_pressure (kernels.cpp:108-176). */
+int sf_plan_bind_fields(sf_plan* plan, float* p0, float* vx0, float* vy0, float* vz0,
+                        float* p1, float* vx1, float* vy1, float* vz1);
+/* Which set (0 or 1) holds the current state after the steps so far. */
+int sf_plan_current(const sf_plan* plan);
+/* Choose which set holds the current state (after a host upload). */
+int sf_plan_set_current(sf_plan* plan, int which);
+
+/* Geometry mask (device, nx*ny*nz bytes, nonzero = air) or NULL for all
+ * air.  Builds the plan's per-cell face flags on the stream.  Replaces
+ * precompute_boundary_cells + apply_rigid_boundaries (kernels.cpp:226-273,
+ * boundaries.cpp:13-89) and the geometry argument of update_pressure. */
+int sf_plan_set_geometry(sf_plan* plan, const uint8_t* geometry_dev, void* stream);
+
+/* PML sigma profiles (host float arrays of nx, ny, nz, or NULL = axis off)
+ * and dt as the float the reference passes; decays exp(-sigma*dt) are formed
+ * on the host in float exactly as initialize_pml (pml.cpp:13-45,
+ * kernels.cpp:286-329) and applied as apply_pml_velocity / apply_pml_pressure
+ * (pml.cpp:47-149). */
+int sf_plan_set_pml(sf_plan* plan, const float* sigma_x, const float* sigma_y,
+                    const float* sigma_z, float dt);
+/* Same, with decay factors supplied directly (host float arrays or NULL). */
+int sf_plan_set_pml_decay(sf_plan* plan, const float* decay_x, const float* decay_y,
+                          const float* decay_z);
+
+/* Sources (at most SF_MAX_SOURCES) -- replaces _inject_sources
+ * (core/solver.py:2386-2433). */
+int sf_plan_set_sources(sf_plan* plan, int n, const sf_source* sources);
+/* Probe cells (flat indices, host array) -- replaces _record_probes
+ * (core/solver.py:2435-2439). */
+int sf_plan_set_probes(sf_plan* plan, int n, const int64_t* cells);
+
+/* ADE materials: material_id (device, nx*ny*nz bytes) and the pole table
+ * (at most SF_MAX_POLES; Debye poles first, then Lorentz, each in field
+ * order, as ADEMaterialData holds them).  inv_dx = float(1/dx).  Replaces
+ * update_ade_* / apply_ade_*_correction / compute_divergence
+ * (kernels.cpp:670-886, ade.cpp:25-580) in the order of
+ * core/solver.py:2135-2193. n = 0 turns ADE off. */
+int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const sf_pole* poles,
+                    float inv_dx);
+
+/* Advance n_steps.  src_values_dev: device doubles [n_steps][n_sources]
+ * (the waveform at each step's time; may be NULL when there are no
+ * sources).  trace_dev: device floats [n_steps][n_probes] receiving p at
+ * each probe after each step (may be NULL when there are no probes).
+ * Replaces FDTDSolver.step's native dispatch (core/solver.py:2003-2102). */
+int sf_plan_step(sf_plan* plan, int64_t n_steps, const double* src_values_dev,
+                 float* trace_dev, void* stream);
+
+/* Acoustic energy of the current state, (1/2) sum(p^2/(rho c^2) + rho v^2)
+ * dV over air cells, as compute_energy (core/solver.py:2689-2705); result
+ * written to a host double after a stream sync.  scratch_dev: device
+ * doubles, at least sf_energy_scratch_doubles() of them. */
+int64_t sf_energy_scratch_doubles(const sf_plan* plan);
+int sf_plan_energy(sf_plan* plan, double rho, double c, double dx, double* scratch_dev,
+                   double* out_host, void* stream);
+
+/* --- voxelisation -------------------------------------------------------- */
+/* mask[i,j,k] = sdf(cell centre) <= 0, cell centre = (i + 0.5)*res, as
+ * SDFPrimitive.voxelize (geometry/sdf.py:99-125) with grid coordinates
+ * np.arange(n)*res + res/2 (core/grid.py:86-88).  invert != 0 stores the
+ * complement (air = outside a solid).  out_dev: nx*ny*nz bytes. */
+int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, double res,
+                int invert, uint8_t* out_dev, void* stream);
+
+/* Signed distance of the same program at n points (device doubles, n x 3,
+ * row major) into out_dev[n]; replaces SDFPrimitive.sdf
+ * (geometry/sdf.py:67-80).  Synchronous. */
+int sf_sdf_eval(const sf_sdf_node* nodes, int n_nodes, const double* points_dev, int64_t n,
+                double* out_dev, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SF_GB300_H */

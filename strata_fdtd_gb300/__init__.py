@@ -1,0 +1,25 @@
+"""strata_fdtd_gb300 -- the strata-fdtd time-step path on GB300 (sm_103a).
+
+A drop-in for ``FDTDSolver(backend="native")`` of rjwalters/strata-fdtd:
+same classes and arguments, with the per-step stencil, rigid walls, PML, ADE
+materials, sources, probes and SDF voxelisation running as hand-written CUDA
+kernels behind a C ABI (include/sf_gb300.h) loaded with ctypes.
+"""
+from ._native import NativeError, build
+from .boundaries import PML, RigidBoundary
+from .grid import UniformGrid
+from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
+from .resonator import HelmholtzResonator, helmholtz_array
+from .sdf import (Box, CSGNode, Cylinder, Difference, Intersection, Scale, SDFPrimitive, Sphere,
+                  Translate, Union)
+from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_native_kernels
+
+__version__ = "0.1.0"
+
+__all__ = [
+    "FDTDSolver", "GaussianPulse", "Probe", "UniformGrid", "PML", "RigidBoundary", "Pole",
+    "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
+    "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale",
+    "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",
+    "NativeError",
+]

@@ -1,0 +1,394 @@
+// sf_api.cu -- the extern "C" boundary declared in include/sf_gb300.h.
+//
+// Host-side plan management.  A plan describes one grid: its coefficients,
+// the caller's two ping-pong field sets, and the small device tables it owns
+// (face flags, PML decays, probe cells).  sf_plan_step enqueues one fused
+// kernel per time step on the caller's stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sf_common.cuh"
+
+#ifndef SF_VERSION_STRING
+#define SF_VERSION_STRING "0.1.0"
+#endif
+
+// launchers (sf_step.cu, sf_voxel.cu)
+int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, int nz,
+                          cudaStream_t st);
+int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& poles, bool geom,
+                   cudaStream_t st);
+int sf_launch_probe_gather(const float* p, const long long* cells, int n, float* out,
+                           cudaStream_t st);
+long long sf_energy_blocks(long long n);
+int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,
+                     const uint8_t* flags, long long n, double* scratch, double* out2,
+                     cudaStream_t st);
+int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny, int nz,
+                       double res, int invert, uint8_t* out, int* err_dev, cudaStream_t st);
+
+int sf_launch_sdf_points(const sf_sdf_node* prog_dev, int n_nodes, const double* pts, long long n,
+                         double* out, int* err_dev, cudaStream_t st);
+
+namespace {
+thread_local std::string g_err;
+}
+
+int sf_fail(const char* msg) {
+    g_err = msg;
+    return 1;
+}
+
+int sf_fail_cuda(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file,
+                  line);
+    g_err = buf;
+    return 2;
+}
+
+struct sf_plan {
+    sf_grid_desc d{};
+    long long n = 0;
+    int device = 0;
+    float* f[2][4] = {{nullptr}};
+    int cur = 0;
+    bool bound = false;
+    uint8_t* flags = nullptr;  // owned; null = no geometry (all air)
+    float* decay[3] = {nullptr, nullptr, nullptr};  // owned, 1.0f where axis off
+    SfSources src{};
+    long long* probe_cells = nullptr;  // owned
+    int n_probe = 0;
+    SfPoles poles{};
+    const uint8_t* mat = nullptr;  // caller-owned
+};
+
+namespace {
+
+int set_decays(sf_plan* P, const float* host[3]) {
+    const int n[3] = {P->d.nx, P->d.ny, P->d.nz};
+    for (int a = 0; a < 3; ++a) {
+        std::vector<float> h(n[a], 1.0f);
+        if (host[a]) std::memcpy(h.data(), host[a], sizeof(float) * n[a]);
+        SF_CUDA_OK(cudaMemcpy(P->decay[a], h.data(), sizeof(float) * n[a], cudaMemcpyHostToDevice));
+    }
+    return 0;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* sf_version(void) {
+    return "strata_fdtd_gb300 " SF_VERSION_STRING " (sm_103a, abi " "1" ")";
+}
+
+const char* sf_last_error(void) { return g_err.c_str(); }
+
+int sf_device_info(int device, sf_device_info_t* out) {
+    if (!out) return sf_fail("sf_device_info: out is NULL");
+    cudaDeviceProp pr;
+    SF_CUDA_OK(cudaGetDeviceProperties(&pr, device));
+    std::memset(out, 0, sizeof(*out));
+    out->device = device;
+    out->sm_count = pr.multiProcessorCount;
+    out->cc_major = pr.major;
+    out->cc_minor = pr.minor;
+    out->total_mem = (int64_t)pr.totalGlobalMem;
+    out->l2_bytes = pr.l2CacheSize;
+    out->max_smem_per_block = (int32_t)pr.sharedMemPerBlockOptin;
+    std::strncpy(out->name, pr.name, sizeof(out->name) - 1);
+    return 0;
+}
+
+int sf_plan_create(const sf_grid_desc* desc, sf_plan** out) {
+    if (!desc || !out) return sf_fail("sf_plan_create: NULL argument");
+    if (desc->nx < 1 || desc->ny < 1 || desc->nz < 1)
+        return sf_fail("sf_plan_create: grid dimensions must be >= 1");
+    if (desc->nx > 65535) return sf_fail("sf_plan_create: nx > 65535 is not supported");
+    auto* P = new sf_plan();
+    P->d = *desc;
+    P->n = (long long)desc->nx * desc->ny * desc->nz;
+    cudaGetDevice(&P->device);
+    const int n[3] = {desc->nx, desc->ny, desc->nz};
+    for (int a = 0; a < 3; ++a) {
+        if (cudaMalloc(&P->decay[a], sizeof(float) * n[a]) != cudaSuccess) {
+            sf_plan_destroy(P);
+            return sf_fail("sf_plan_create: cudaMalloc of PML tables failed");
+        }
+    }
+    const float* none[3] = {nullptr, nullptr, nullptr};
+    if (int rc = set_decays(P, none)) {
+        sf_plan_destroy(P);
+        return rc;
+    }
+    *out = P;
+    return 0;
+}
+
+int sf_plan_destroy(sf_plan* P) {
+    if (!P) return 0;
+    DeviceGuard g(P->device);
+    for (auto& d : P->decay) cudaFree(d);
+    cudaFree(P->flags);
+    cudaFree(P->probe_cells);
+    delete P;
+    return 0;
+}
+
+int sf_plan_bind_fields(sf_plan* P, float* p0, float* vx0, float* vy0, float* vz0, float* p1,
+                        float* vx1, float* vy1, float* vz1) {
+    if (!P) return sf_fail("sf_plan_bind_fields: NULL plan");
+    float* all[8] = {p0, vx0, vy0, vz0, p1, vx1, vy1, vz1};
+    for (int q = 0; q < 8; ++q) {
+        if (!all[q]) return sf_fail("sf_plan_bind_fields: NULL field buffer");
+        if (reinterpret_cast<uintptr_t>(all[q]) % 16 != 0)
+            return sf_fail("sf_plan_bind_fields: field buffers must be 16-byte aligned");
+        P->f[q / 4][q % 4] = all[q];
+    }
+    P->bound = true;
+    P->cur = 0;
+    return 0;
+}
+
+int sf_plan_current(const sf_plan* P) { return P ? P->cur : -1; }
+
+int sf_plan_set_current(sf_plan* P, int which) {
+    if (!P || (which != 0 && which != 1)) return sf_fail("sf_plan_set_current: bad argument");
+    P->cur = which;
+    return 0;
+}
+
+int sf_plan_set_geometry(sf_plan* P, const uint8_t* geom, void* stream) {
+    if (!P) return sf_fail("sf_plan_set_geometry: NULL plan");
+    DeviceGuard g(P->device);
+    if (!geom) {
+        cudaFree(P->flags);
+        P->flags = nullptr;
+        return 0;
+    }
+    if (!P->flags) SF_CUDA_OK(cudaMalloc(&P->flags, (size_t)P->n));
+    return sf_launch_build_flags(geom, P->flags, P->d.nx, P->d.ny, P->d.nz,
+                                 static_cast<cudaStream_t>(stream));
+}
+
+int sf_plan_set_pml(sf_plan* P, const float* sx, const float* sy, const float* sz, float dt) {
+    if (!P) return sf_fail("sf_plan_set_pml: NULL plan");
+    DeviceGuard g(P->device);
+    const int n[3] = {P->d.nx, P->d.ny, P->d.nz};
+    const float* sig[3] = {sx, sy, sz};
+    std::vector<float> dec[3];
+    const float* host[3] = {nullptr, nullptr, nullptr};
+    for (int a = 0; a < 3; ++a) {
+        if (!sig[a]) continue;
+        dec[a].resize(n[a]);
+        // pml.cpp:13-45: std::exp on float arguments, dt already a float
+        for (int q = 0; q < n[a]; ++q) dec[a][q] = std::exp(-sig[a][q] * dt);
+        host[a] = dec[a].data();
+    }
+    return set_decays(P, host);
+}
+
+int sf_plan_set_pml_decay(sf_plan* P, const float* dx, const float* dy, const float* dz) {
+    if (!P) return sf_fail("sf_plan_set_pml_decay: NULL plan");
+    DeviceGuard g(P->device);
+    const float* host[3] = {dx, dy, dz};
+    return set_decays(P, host);
+}
+
+int sf_plan_set_sources(sf_plan* P, int n, const sf_source* s) {
+    if (!P) return sf_fail("sf_plan_set_sources: NULL plan");
+    if (n < 0 || n > SF_MAX_SOURCES) return sf_fail("sf_plan_set_sources: at most 16 sources");
+    if (n > 0 && !s) return sf_fail("sf_plan_set_sources: NULL source table");
+    const int dims[3] = {P->d.nx, P->d.ny, P->d.nz};
+    for (int q = 0; q < n; ++q) {
+        if (s[q].kind == 0) {
+            if (s[q].a < 0 || s[q].a >= dims[0] || s[q].b < 0 || s[q].b >= dims[1] ||
+                s[q].c < 0 || s[q].c >= dims[2])
+                return sf_fail("sf_plan_set_sources: point source outside the grid");
+        } else if (s[q].kind == 1) {
+            if (s[q].a < 0 || s[q].a > 2 || s[q].b < 0 || s[q].b >= dims[s[q].a])
+                return sf_fail("sf_plan_set_sources: plane source outside the grid");
+        } else {
+            return sf_fail("sf_plan_set_sources: kind must be 0 (point) or 1 (plane)");
+        }
+    }
+    P->src.n = n;
+    for (int q = 0; q < n; ++q) P->src.s[q] = s[q];
+    return 0;
+}
+
+int sf_plan_set_probes(sf_plan* P, int n, const int64_t* cells) {
+    if (!P) return sf_fail("sf_plan_set_probes: NULL plan");
+    if (n < 0 || (n > 0 && !cells)) return sf_fail("sf_plan_set_probes: bad probe table");
+    for (int q = 0; q < n; ++q)
+        if (cells[q] < 0 || cells[q] >= P->n) return sf_fail("sf_plan_set_probes: cell outside the grid");
+    DeviceGuard g(P->device);
+    cudaFree(P->probe_cells);
+    P->probe_cells = nullptr;
+    P->n_probe = n;
+    if (n == 0) return 0;
+    SF_CUDA_OK(cudaMalloc(&P->probe_cells, sizeof(long long) * n));
+    SF_CUDA_OK(cudaMemcpy(P->probe_cells, cells, sizeof(long long) * n, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int sf_plan_set_ade(sf_plan* P, const uint8_t* mat, int n, const sf_pole* poles, float inv_dx) {
+    if (!P) return sf_fail("sf_plan_set_ade: NULL plan");
+    if (n < 0 || n > SF_MAX_POLES) return sf_fail("sf_plan_set_ade: at most 16 poles");
+    if (n > 0 && (!mat || !poles)) return sf_fail("sf_plan_set_ade: NULL material ids or poles");
+    SfPoles T{};
+    T.inv_dx = inv_dx;
+    for (int q = 0; q < n; ++q) {
+        const sf_pole& pl = poles[q];
+        if (pl.kind != 0 && pl.kind != 1) return sf_fail("sf_plan_set_ade: bad pole kind");
+        if (pl.target != 0 && pl.target != 1) return sf_fail("sf_plan_set_ade: bad pole target");
+        if (pl.material_id < 1 || pl.material_id > 255)
+            return sf_fail("sf_plan_set_ade: material id must be 1..255");
+        if (!pl.J || (pl.kind == 1 && !pl.J_prev))
+            return sf_fail("sf_plan_set_ade: missing auxiliary field buffer");
+        if (q > 0 && poles[q - 1].kind == 1 && pl.kind == 0)
+            return sf_fail("sf_plan_set_ade: Debye poles must precede Lorentz poles");
+        T.p[q] = pl;
+        if (pl.target == 0) ++T.n_density; else ++T.n_modulus;
+    }
+    T.n = n;
+    P->poles = T;
+    P->mat = n > 0 ? mat : nullptr;
+    return 0;
+}
+
+int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* trace,
+                 void* stream) {
+    if (!P) return sf_fail("sf_plan_step: NULL plan");
+    if (!P->bound) return sf_fail("sf_plan_step: fields not bound");
+    if (n_steps < 0) return sf_fail("sf_plan_step: negative step count");
+    if (P->src.n > 0 && !src_values) return sf_fail("sf_plan_step: sources need src_values");
+    if (n_steps == 0) return 0;
+    DeviceGuard g(P->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    static const double kNoSources[SF_MAX_SOURCES] = {0};
+    (void)kNoSources;
+    SfStepArgs a{};
+    a.nx = P->d.nx;
+    a.ny = P->d.ny;
+    a.nz = P->d.nz;
+    a.plane = (long long)P->d.ny * P->d.nz;
+    a.cv = P->d.coeff_v;
+    a.cp = P->d.coeff_p;
+    a.flags = P->flags;
+    a.dx = P->decay[0];
+    a.dy = P->decay[1];
+    a.dz = P->decay[2];
+    a.n_probe = trace ? P->n_probe : 0;
+    a.probe_cells = P->probe_cells;
+    a.mat = P->mat;
+    for (int64_t s = 0; s < n_steps; ++s) {
+        const int in = P->cur, out = 1 - P->cur;
+        a.p = P->f[in][0];
+        a.vx = P->f[in][1];
+        a.vy = P->f[in][2];
+        a.vz = P->f[in][3];
+        a.po = P->f[out][0];
+        a.vxo = P->f[out][1];
+        a.vyo = P->f[out][2];
+        a.vzo = P->f[out][3];
+        a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
+        a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
+        if (int rc = sf_launch_step(a, P->src, P->poles, P->flags != nullptr, st)) return rc;
+        P->cur = out;
+    }
+    if (trace && P->n_probe > 0)
+        return sf_launch_probe_gather(P->f[P->cur][0], P->probe_cells, P->n_probe,
+                                      trace + (n_steps - 1) * P->n_probe, st);
+    return 0;
+}
+
+int64_t sf_energy_scratch_doubles(const sf_plan* P) {
+    return P ? 2 * sf_energy_blocks(P->n) + 2 : 0;
+}
+
+int sf_plan_energy(sf_plan* P, double rho, double c, double dx, double* scratch,
+                   double* out_host, void* stream) {
+    if (!P || !scratch || !out_host) return sf_fail("sf_plan_energy: NULL argument");
+    if (!P->bound) return sf_fail("sf_plan_energy: fields not bound");
+    DeviceGuard g(P->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const long long nb = sf_energy_blocks(P->n);
+    float* const* f = P->f[P->cur];
+    if (int rc = sf_launch_energy(f[0], f[1], f[2], f[3], P->flags, P->n, scratch,
+                                  scratch + 2 * nb, st))
+        return rc;
+    double sums[2];
+    SF_CUDA_OK(cudaMemcpyAsync(sums, scratch + 2 * nb, sizeof(sums), cudaMemcpyDeviceToHost, st));
+    SF_CUDA_OK(cudaStreamSynchronize(st));
+    const double dV = dx * dx * dx;
+    *out_host = 0.5 * sums[0] / (rho * c * c) * dV + 0.5 * rho * sums[1] * dV;
+    return 0;
+}
+
+int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, double res,
+                int invert, uint8_t* out_dev, void* stream) {
+    if (!nodes || n_nodes < 1 || !out_dev) return sf_fail("sf_voxelize: bad program or output");
+    if (nx < 1 || ny < 1 || nz < 1 || nx > 65535) return sf_fail("sf_voxelize: bad grid");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    sf_sdf_node* prog = nullptr;
+    int* err = nullptr;
+    SF_CUDA_OK(cudaMalloc(&prog, sizeof(sf_sdf_node) * n_nodes + 16));
+    err = reinterpret_cast<int*>(reinterpret_cast<char*>(prog) + sizeof(sf_sdf_node) * n_nodes);
+    int rc = 0;
+    int herr = 0;
+    if (cudaMemcpyAsync(prog, nodes, sizeof(sf_sdf_node) * n_nodes, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) {
+        rc = sf_fail("sf_voxelize: upload failed");
+    }
+    if (!rc) rc = sf_launch_voxelize(prog, n_nodes, nx, ny, nz, res, invert, out_dev, err, st);
+    if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess))
+        rc = sf_fail("sf_voxelize: kernel failed");
+    cudaFree(prog);
+    if (!rc && herr) rc = sf_fail("sf_voxelize: malformed SDF program (stack error)");
+    return rc;
+}
+
+int sf_sdf_eval(const sf_sdf_node* nodes, int n_nodes, const double* points_dev, int64_t n,
+                double* out_dev, void* stream) {
+    if (!nodes || n_nodes < 1 || (n > 0 && (!points_dev || !out_dev)))
+        return sf_fail("sf_sdf_eval: bad program, points or output");
+    if (n == 0) return 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    sf_sdf_node* prog = nullptr;
+    SF_CUDA_OK(cudaMalloc(&prog, sizeof(sf_sdf_node) * n_nodes + 16));
+    int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(prog) + sizeof(sf_sdf_node) * n_nodes);
+    int rc = 0, herr = 0;
+    if (cudaMemcpyAsync(prog, nodes, sizeof(sf_sdf_node) * n_nodes, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess)
+        rc = sf_fail("sf_sdf_eval: upload failed");
+    if (!rc) rc = sf_launch_sdf_points(prog, n_nodes, points_dev, n, out_dev, err, st);
+    if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess))
+        rc = sf_fail("sf_sdf_eval: kernel failed");
+    cudaFree(prog);
+    if (!rc && herr) rc = sf_fail("sf_sdf_eval: malformed SDF program (stack error)");
+    return rc;
+}
+
+}  // extern "C"

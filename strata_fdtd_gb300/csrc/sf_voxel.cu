@@ -1,0 +1,186 @@
+// sf_voxel.cu -- SDF/CSG voxelisation on the GPU.
+//
+// Restates SDFPrimitive.voxelize (geometry/sdf.py:99-125 of
+// rjwalters/strata-fdtd): the mask is sdf(cell centre) <= 0 with cell centres
+// np.arange(n)*res + res/2 (core/grid.py:86-88).  Each thread evaluates one
+// cell in FP64 with the reference's operation order and no fused
+// multiply-add, so the mask matches NumPy bit for bit:
+//   Box      sdf.py:274-293  |p-c| - size/2; norm(max(q,0)) + min(max_d q, 0)
+//   Sphere   sdf.py:320-332  norm(p-c) - r
+//   Cylinder sdf.py:382-424  projection, clamp, radial/axial distance
+//   Union / Intersection / Difference  sdf.py:566-584, 629-647, 704-721
+//   Translate / Scale        sdf.py:1225-1236, 1285-1294
+// np.linalg.norm over three components sums ((x0^2 + x1^2) + x2^2).  The
+// cylinder's axis projection uses np.dot (BLAS), whose rounding depends on
+// the BLAS build; here it is ((v0*a0 + v1*a1) + v2*a2), which equals any
+// BLAS result exactly when the axis is a coordinate axis.
+#include <cuda_runtime.h>
+
+#include "sf_common.cuh"
+
+namespace {
+
+constexpr int VX_DSTACK = 32;
+constexpr int VX_PSTACK = 12;
+
+__device__ __forceinline__ double norm3(double a, double b, double c) {
+    return __dsqrt_rn(d_add(d_add(d_mul(a, a), d_mul(b, b)), d_mul(c, c)));
+}
+__device__ __forceinline__ double dmax(double a, double b) {  // np.maximum
+    return (a >= b || a != a) ? a : b;
+}
+__device__ __forceinline__ double dmin(double a, double b) {  // np.minimum
+    return (a <= b || a != a) ? a : b;
+}
+
+__device__ double eval_sdf(const sf_sdf_node* __restrict__ prog, int n, double x, double y,
+                           double z, int* err) {
+    double ds[VX_DSTACK];
+    double px[VX_PSTACK], py[VX_PSTACK], pz[VX_PSTACK];
+    int dtop = 0, ptop = 0;
+    px[0] = x;
+    py[0] = y;
+    pz[0] = z;
+    for (int q = 0; q < n; ++q) {
+        const sf_sdf_node& N = prog[q];
+        const double X = px[ptop], Y = py[ptop], Z = pz[ptop];
+        switch (N.op) {
+            case 1: {  // BOX
+                const double q0 = d_sub(fabs(d_sub(X, N.a[0])), d_mul(N.b[0], 0.5));
+                const double q1 = d_sub(fabs(d_sub(Y, N.a[1])), d_mul(N.b[1], 0.5));
+                const double q2 = d_sub(fabs(d_sub(Z, N.a[2])), d_mul(N.b[2], 0.5));
+                const double out = norm3(dmax(q0, 0.0), dmax(q1, 0.0), dmax(q2, 0.0));
+                const double ins = dmin(fmax(fmax(q0, q1), q2), 0.0);
+                if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
+                ds[dtop++] = d_add(out, ins);
+                break;
+            }
+            case 2: {  // SPHERE
+                if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
+                ds[dtop++] = d_sub(norm3(d_sub(X, N.a[0]), d_sub(Y, N.a[1]), d_sub(Z, N.a[2])), N.s0);
+                break;
+            }
+            case 3: {  // CYLINDER: a = p1, b = unit axis, s0 = length, s1 = radius
+                const double v0 = d_sub(X, N.a[0]), v1 = d_sub(Y, N.a[1]), v2 = d_sub(Z, N.a[2]);
+                const double t = d_add(d_add(d_mul(v0, N.b[0]), d_mul(v1, N.b[1])), d_mul(v2, N.b[2]));
+                const double L = N.s0;
+                const double tc = dmin(dmax(t, 0.0), L);
+                const double c0 = d_add(N.a[0], d_mul(tc, N.b[0]));
+                const double c1 = d_add(N.a[1], d_mul(tc, N.b[1]));
+                const double c2 = d_add(N.a[2], d_mul(tc, N.b[2]));
+                const double radial = norm3(d_sub(X, c0), d_sub(Y, c1), d_sub(Z, c2));
+                const double half = d_mul(L, 0.5);
+                const double axial = dmax(0.0, d_sub(fabs(d_sub(t, half)), half));
+                const bool inside = (t >= 0.0) && (t <= L);
+                const double rr = d_sub(radial, N.s1);
+                if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
+                ds[dtop++] = inside ? rr : __dsqrt_rn(d_add(d_mul(rr, rr), d_mul(axial, axial)));
+                break;
+            }
+            case 10:    // UNION n
+            case 11: {  // INTERSECTION n
+                if (N.n == 0) {
+                    if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
+                    ds[dtop++] = (N.op == 10) ? __longlong_as_double(0x7ff0000000000000LL)
+                                              : __longlong_as_double((long long)0xfff0000000000000ULL);
+                    break;
+                }
+                if (N.n > dtop) { *err = 2; return 1.0; }
+                const int base = dtop - N.n;
+                double r = ds[base];
+                for (int c = 1; c < N.n; ++c) r = (N.op == 10) ? dmin(r, ds[base + c]) : dmax(r, ds[base + c]);
+                dtop = base;
+                ds[dtop++] = r;
+                break;
+            }
+            case 12: {  // DIFFERENCE n: base, then subtracted
+                if (N.n > dtop || N.n < 1) { *err = 2; return 1.0; }
+                const int base = dtop - N.n;
+                double r = ds[base];
+                for (int c = 1; c < N.n; ++c) r = dmax(r, -ds[base + c]);
+                dtop = base;
+                ds[dtop++] = r;
+                break;
+            }
+            case 20:    // PUSH_TRANSLATE
+            case 21: {  // PUSH_SCALE
+                if (ptop + 1 >= VX_PSTACK) { *err = 3; return 1.0; }
+                ++ptop;
+                if (N.op == 20) {
+                    px[ptop] = d_sub(X, N.a[0]);
+                    py[ptop] = d_sub(Y, N.a[1]);
+                    pz[ptop] = d_sub(Z, N.a[2]);
+                } else {
+                    px[ptop] = __ddiv_rn(X, N.a[0]);
+                    py[ptop] = __ddiv_rn(Y, N.a[1]);
+                    pz[ptop] = __ddiv_rn(Z, N.a[2]);
+                }
+                break;
+            }
+            case 22:
+                if (ptop == 0) { *err = 3; return 1.0; }
+                --ptop;
+                break;
+            case 23:
+                if (dtop < 1) { *err = 2; return 1.0; }
+                ds[dtop - 1] = d_mul(ds[dtop - 1], N.s0);
+                break;
+            case 24:
+                if (dtop < 1) { *err = 2; return 1.0; }
+                ds[dtop - 1] = -ds[dtop - 1];
+                break;
+            default:
+                *err = 4;
+                return 1.0;
+        }
+    }
+    if (dtop != 1) { *err = 2; return 1.0; }
+    return ds[0];
+}
+
+__global__ void k_voxelize(const sf_sdf_node* __restrict__ prog, int n_nodes, int nx, int ny,
+                           int nz, double res, int invert, uint8_t* __restrict__ out,
+                           int* __restrict__ err_flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    const double half = d_mul(res, 0.5);
+    const double x = d_add(d_mul((double)i, res), half);
+    const double y = d_add(d_mul((double)j, res), half);
+    const double z = d_add(d_mul((double)k, res), half);
+    int err = 0;
+    const double d = eval_sdf(prog, n_nodes, x, y, z, &err);
+    if (err) atomicExch(err_flag, err);
+    const bool inside = d <= 0.0;
+    out[((long long)i * ny + j) * nz + k] = (uint8_t)(inside != (invert != 0));
+}
+
+__global__ void k_sdf_points(const sf_sdf_node* __restrict__ prog, int n_nodes,
+                             const double* __restrict__ pts, long long n, double* __restrict__ out,
+                             int* __restrict__ err_flag) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        int err = 0;
+        out[q] = eval_sdf(prog, n_nodes, pts[3 * q], pts[3 * q + 1], pts[3 * q + 2], &err);
+        if (err) atomicExch(err_flag, err);
+    }
+}
+
+}  // namespace
+
+int sf_launch_sdf_points(const sf_sdf_node* prog_dev, int n_nodes, const double* pts, long long n,
+                         double* out, int* err_dev, cudaStream_t st) {
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (blocks < 1) blocks = 1;
+    k_sdf_points<<<(int)blocks, 256, 0, st>>>(prog_dev, n_nodes, pts, n, out, err_dev);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_sdf_points launch failed");
+}
+
+int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny, int nz,
+                       double res, int invert, uint8_t* out, int* err_dev, cudaStream_t st) {
+    dim3 blk(32, 8, 1), grd((nz + 31) / 32, (ny + 7) / 8, nx);
+    k_voxelize<<<grd, blk, 0, st>>>(prog_dev, n_nodes, nx, ny, nz, res, invert, out, err_dev);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_voxelize launch failed");
+}

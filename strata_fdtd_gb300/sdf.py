@@ -1,0 +1,281 @@
+"""SDF primitives and CSG, evaluated on the GPU (geometry/sdf.py of
+rjwalters/strata-fdtd).
+
+Each shape compiles to a short stack program (``sf_sdf_node``, see
+include/sf_gb300.h) that the voxelisation kernel runs per cell in FP64 with
+the reference's operation order, so ``voxelize`` returns the same mask as the
+reference's NumPy ``SDFPrimitive.voxelize`` (sdf.py:99-125).  Shape
+construction (centres, sizes, unit axes, lengths) runs on the host in the
+reference's own NumPy arithmetic, so the constants the kernel sees are the
+reference's constants.
+
+Supported: Box, Sphere, Cylinder, Union, Intersection, Difference, Translate,
+Scale, HelmholtzResonator (geometry/resonator.py).  Rotation, smooth CSG,
+cones and horns are outside the time-step path and raise on use.
+"""
+from __future__ import annotations
+
+import ctypes
+from functools import cached_property
+
+import numpy as np
+
+from . import _native
+
+OP_BOX, OP_SPHERE, OP_CYLINDER = 1, 2, 3
+OP_UNION, OP_INTERSECTION, OP_DIFFERENCE = 10, 11, 12
+OP_PUSH_TRANSLATE, OP_PUSH_SCALE, OP_POP_POINT, OP_SCALE_DIST, OP_NEGATE = 20, 21, 22, 23, 24
+
+
+def _node(op, n=0, a=(0.0, 0.0, 0.0), b=(0.0, 0.0, 0.0), s0=0.0, s1=0.0):
+    nd = _native.SfSdfNode()
+    nd.op, nd.n = op, n
+    for q in range(3):
+        nd.a[q] = float(a[q])
+        nd.b[q] = float(b[q])
+    nd.s0, nd.s1 = float(s0), float(s1)
+    return nd
+
+
+class SDFPrimitive:
+    """Base class: negative distance inside, positive outside."""
+
+    def _emit(self, prog: list) -> None:
+        raise NotImplementedError(f"{type(self).__name__} is not supported by the GPU voxeliser")
+
+    def program(self):
+        prog: list = []
+        self._emit(prog)
+        arr = (_native.SfSdfNode * len(prog))(*prog)
+        return arr, len(prog)
+
+    # -- evaluation ---------------------------------------------------------
+    def voxelize_device(self, grid, invert: bool = False, out=None, stream=None):
+        """Voxelise on the GPU into a torch.uint8 CUDA tensor of grid.shape
+        (1 = inside, or 1 = outside when ``invert``)."""
+        import torch
+
+        nx, ny, nz = grid.shape
+        if out is None:
+            out = torch.empty((nx, ny, nz), dtype=torch.uint8, device="cuda")
+        prog, n = self.program()
+        st = (stream or torch.cuda.current_stream()).cuda_stream
+        _native.check(_native.load().sf_voxelize(ctypes.addressof(prog), n, nx, ny, nz,
+                                                 float(grid.min_spacing), int(invert),
+                                                 out.data_ptr(), st), "sf_voxelize")
+        return out
+
+    def voxelize(self, grid) -> np.ndarray:
+        """Boolean mask of grid.shape, True inside (geometry/sdf.py:99-125)."""
+        return self.voxelize_device(grid).cpu().numpy().astype(bool)
+
+    def sdf(self, points) -> np.ndarray:
+        """Signed distance at an (N, 3) array of points, evaluated on the GPU."""
+        import torch
+
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+        if pts.ndim != 2 or pts.shape[1] != 3:
+            raise ValueError(f"points must be Nx3 array, got shape {pts.shape}")
+        dev = torch.from_numpy(pts).cuda()
+        out = torch.empty(len(pts), dtype=torch.float64, device="cuda")
+        prog, n = self.program()
+        lib = _native.load()
+        _native.check(lib.sf_sdf_eval(ctypes.addressof(prog), n, dev.data_ptr(), len(pts),
+                                      out.data_ptr(), torch.cuda.current_stream().cuda_stream),
+                      "sf_sdf_eval")
+        return out.cpu().numpy()
+
+    def contains(self, points) -> np.ndarray:
+        return self.sdf(points) <= 0
+
+    # -- fluent transforms (sdf.py:127-229) ----------------------------------
+    def translate(self, offset):
+        return Translate(self, offset)
+
+    def scale(self, factor):
+        return Scale(self, factor)
+
+
+class Box(SDFPrimitive):
+    """Axis-aligned box from (center, size) or (min_corner, max_corner)."""
+
+    def __init__(self, center=None, size=None, min_corner=None, max_corner=None):
+        if center is not None and size is not None:
+            self.center = np.array(center, dtype=np.float64)
+            self.size = np.array(size, dtype=np.float64)
+        elif min_corner is not None and max_corner is not None:
+            lo = np.array(min_corner, dtype=np.float64)
+            hi = np.array(max_corner, dtype=np.float64)
+            self.center = (lo + hi) / 2
+            self.size = hi - lo
+        else:
+            raise ValueError("Must provide either (center, size) or (min_corner, max_corner)")
+        if np.any(self.size <= 0):
+            raise ValueError(f"Box size must be positive, got {self.size}")
+
+    def _emit(self, prog):
+        prog.append(_node(OP_BOX, a=self.center, b=self.size))
+
+    @property
+    def bounding_box(self):
+        h = self.size / 2
+        return self.center - h, self.center + h
+
+
+class Sphere(SDFPrimitive):
+    def __init__(self, center, radius):
+        self.center = np.array(center, dtype=np.float64)
+        self.radius = float(radius)
+        if self.radius <= 0:
+            raise ValueError(f"Sphere radius must be positive, got {self.radius}")
+
+    def _emit(self, prog):
+        prog.append(_node(OP_SPHERE, a=self.center, s0=self.radius))
+
+    @property
+    def bounding_box(self):
+        r = np.array([self.radius] * 3)
+        return self.center - r, self.center + r
+
+
+class Cylinder(SDFPrimitive):
+    """Capped cylinder between p1 and p2 (sdf.py:341-433)."""
+
+    def __init__(self, p1, p2, radius):
+        self.p1 = np.array(p1, dtype=np.float64)
+        self.p2 = np.array(p2, dtype=np.float64)
+        self.radius = float(radius)
+        if self.radius <= 0:
+            raise ValueError(f"Cylinder radius must be positive, got {self.radius}")
+        self.axis = self.p2 - self.p1
+        self.length = np.linalg.norm(self.axis)
+        if self.length == 0:
+            raise ValueError("Cylinder endpoints must be distinct")
+        self.axis_normalized = self.axis / self.length
+
+    def _emit(self, prog):
+        prog.append(_node(OP_CYLINDER, a=self.p1, b=self.axis_normalized, s0=self.length,
+                          s1=self.radius))
+
+    @property
+    def bounding_box(self):
+        r = np.array([self.radius] * 3)
+        return np.minimum(self.p1, self.p2) - r, np.maximum(self.p1, self.p2) + r
+
+
+class CSGNode(SDFPrimitive):
+    pass
+
+
+class Union(CSGNode):
+    """min over children (sdf.py:549-609)."""
+
+    def __init__(self, *children):
+        self.children = children
+
+    def _emit(self, prog):
+        for c in self.children:
+            c._emit(prog)
+        prog.append(_node(OP_UNION, n=len(self.children)))
+
+    @cached_property
+    def bounding_box(self):
+        if not self.children:
+            return np.array([np.inf] * 3), np.array([-np.inf] * 3)
+        return (np.minimum.reduce([c.bounding_box[0] for c in self.children]),
+                np.maximum.reduce([c.bounding_box[1] for c in self.children]))
+
+
+class Intersection(CSGNode):
+    """max over children (sdf.py:612-682)."""
+
+    def __init__(self, *children):
+        self.children = children
+
+    def _emit(self, prog):
+        for c in self.children:
+            c._emit(prog)
+        prog.append(_node(OP_INTERSECTION, n=len(self.children)))
+
+    @cached_property
+    def bounding_box(self):
+        if not self.children:
+            return np.array([-np.inf] * 3), np.array([np.inf] * 3)
+        lo = np.maximum.reduce([c.bounding_box[0] for c in self.children])
+        hi = np.minimum.reduce([c.bounding_box[1] for c in self.children])
+        if np.any(lo > hi):
+            return np.array([np.inf] * 3), np.array([-np.inf] * 3)
+        return lo, hi
+
+
+class Difference(CSGNode):
+    """max(base, -s1, -s2, ...) (sdf.py:685-733)."""
+
+    def __init__(self, base, *subtracted):
+        self.base = base
+        self.subtracted = subtracted
+
+    def _emit(self, prog):
+        self.base._emit(prog)
+        for s in self.subtracted:
+            s._emit(prog)
+        prog.append(_node(OP_DIFFERENCE, n=1 + len(self.subtracted)))
+
+    @cached_property
+    def bounding_box(self):
+        return self.base.bounding_box
+
+
+class Transform(SDFPrimitive):
+    def __init__(self, child):
+        self.child = child
+
+
+class Translate(Transform):
+    """Evaluate the child at point - offset (sdf.py:1199-1236)."""
+
+    def __init__(self, child, offset):
+        super().__init__(child)
+        self.offset = np.asarray(offset, dtype=np.float64)
+        if self.offset.shape != (3,):
+            raise ValueError(f"offset must be a 3-element vector, got shape {self.offset.shape}")
+
+    def _emit(self, prog):
+        prog.append(_node(OP_PUSH_TRANSLATE, a=self.offset))
+        self.child._emit(prog)
+        prog.append(_node(OP_POP_POINT))
+
+    @property
+    def bounding_box(self):
+        lo, hi = self.child.bounding_box
+        return lo + self.offset, hi + self.offset
+
+
+class Scale(Transform):
+    """Evaluate the child at point / scale, scale the distance by scale[0]
+    (uniform) or min(scale) (sdf.py:1239-1300)."""
+
+    def __init__(self, child, scale):
+        super().__init__(child)
+        if np.isscalar(scale):
+            self.scale = np.array([scale, scale, scale], dtype=np.float64)
+            self.uniform = True
+        else:
+            self.scale = np.asarray(scale, dtype=np.float64)
+            self.uniform = np.allclose(self.scale, self.scale[0])
+        if self.scale.shape != (3,):
+            raise ValueError("scale must be scalar or 3-element vector")
+        if np.any(self.scale <= 0):
+            raise ValueError(f"scale factors must be positive, got {self.scale}")
+
+    def _emit(self, prog):
+        prog.append(_node(OP_PUSH_SCALE, a=self.scale))
+        self.child._emit(prog)
+        prog.append(_node(OP_POP_POINT))
+        f = self.scale[0] if self.uniform else np.min(self.scale)
+        prog.append(_node(OP_SCALE_DIST, s0=float(f)))
+
+    @property
+    def bounding_box(self):
+        lo, hi = self.child.bounding_box
+        return lo * self.scale, hi * self.scale

@@ -1,0 +1,715 @@
+"""FDTDSolver on the GB300: the reference API (core/solver.py of
+rjwalters/strata-fdtd) over the sf_* C ABI.
+
+What stays as in the reference: constructor arguments, dt and the update
+coefficients (core/solver.py:1576-1602, same FP64 expressions), the public
+NumPy fields ``p``, ``vx``, ``vy``, ``vz`` and ``geometry``, source and probe
+handling (index vs metre positions, :1782-1885), the FP64 ``_time``
+accumulation (:2071-2072), ``step``/``run`` semantics (:2003-2077,
+:2520-2606) and ``get_probe_data`` returning float32 arrays.
+
+What changes: the fields live in HBM as two ping-pong sets of CUDA tensors;
+one fused kernel per time step does the velocity, rigid-wall, pressure, PML,
+ADE, source and probe work; ``run`` issues all steps of a call in one C-ABI
+call with the waveform values precomputed (same NumPy call per step as the
+reference) and the probe traces kept on the device until read.
+
+Host/device coherence: reading ``solver.p`` (etc.) copies the current device
+state into one persistent NumPy array per field, and marks it as possibly
+modified, so the next step uploads it again -- in-place edits such as
+``solver.p[i, j, k] = 1.0`` behave as they do on the reference.
+
+There is no CPU fallback: without a CUDA device or the compiled library the
+constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import warnings
+from dataclasses import dataclass, field
+from typing import Literal
+
+import numpy as np
+
+from . import _native
+from .boundaries import PML, RigidBoundary
+from .grid import UniformGrid
+from .sdf import SDFPrimitive
+
+_FIELDS = ("p", "vx", "vy", "vz")
+_MAX_CHUNK = 1 << 16  # steps per C-ABI call inside run()
+
+
+@dataclass
+class GaussianPulse:
+    """Gaussian-modulated sinusoid (core/solver.py:152-207)."""
+
+    position: tuple | dict
+    frequency: float
+    bandwidth: float | None = None
+    amplitude: float = 1.0
+    source_type: Literal["point", "plane"] = "point"
+
+    def __post_init__(self):
+        if self.bandwidth is None:
+            self.bandwidth = 2.0 * self.frequency
+
+    def waveform(self, t, dt):
+        sigma = 1.0 / (np.pi * self.bandwidth)
+        t0 = 4.0 * sigma
+        envelope = np.exp(-((t - t0) ** 2) / (2 * sigma**2))
+        carrier = np.sin(2 * np.pi * self.frequency * (t - t0))
+        return self.amplitude * envelope * carrier
+
+
+@dataclass
+class Probe:
+    """Pressure probe at a grid cell (core/solver.py:758-781).  Samples are
+    held on the device and copied out when ``data`` or ``get_data`` is read."""
+
+    name: str
+    position: tuple
+    _samples: list = field(default_factory=list, repr=False)
+    _solver: object = field(default=None, repr=False)
+
+    @property
+    def data(self) -> list:
+        if self._solver is not None:
+            self._solver._flush_traces()
+        return self._samples
+
+    def record(self, pressure: float) -> None:
+        self._samples.append(float(pressure))
+
+    def get_data(self) -> np.ndarray:
+        return np.array(self.data, dtype=np.float32)
+
+    def clear(self) -> None:
+        if self._solver is not None:
+            self._solver._flush_traces()
+        self._samples.clear()
+
+
+def step_coefficients(grid, c: float, rho: float, courant: float):
+    """dt, coeff_v, coeff_p with the FP64 expressions of core/solver.py:1576-1586."""
+    dx = grid.min_spacing
+    dt_max = grid.min_spacing / (c * np.sqrt(3))
+    dt = courant * dt_max
+    coeff_p = -rho * c**2 * dt / dx
+    coeff_v = -dt / (rho * dx)
+    return dt, coeff_v, coeff_p
+
+
+def has_native_kernels() -> bool:
+    """True when a CUDA device is present and the sm_103a library loads."""
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return False
+        _native.load()
+        return True
+    except Exception:
+        return False
+
+
+def get_native_info() -> dict:
+    import torch
+
+    info = {"available": has_native_kernels(), "version": None, "device": None}
+    if info["available"]:
+        info["version"] = _native.load().sf_version().decode()
+        info["device"] = torch.cuda.get_device_name()
+    return info
+
+
+class FDTDSolver:
+    """3-D acoustic FDTD solver on a staggered grid, stepped on the GPU.
+
+    Arguments as the reference (core/solver.py:1507-1518).  ``backend`` may be
+    "auto" or "native"; both select the GB300 kernels.  ``device`` picks the
+    CUDA device (default: the current one).
+    """
+
+    def __init__(self, shape=None, resolution=None, grid=None, c: float = 343.0,
+                 rho: float = 1.2, courant: float = 0.95,
+                 backend: Literal["auto", "native"] = "auto", warn_energy_drift: bool = False,
+                 energy_drift_threshold: float = 0.01, device=None):
+        import torch
+
+        if grid is not None:
+            self._grid = grid
+            self.shape = tuple(grid.shape)
+        elif shape is not None and resolution is not None:
+            self._grid = UniformGrid(shape=shape, resolution=resolution)
+            self.shape = tuple(self._grid.shape)
+        else:
+            raise ValueError("Must provide either 'grid' or both 'shape' and 'resolution'")
+        if not getattr(self._grid, "is_uniform", True):
+            raise NotImplementedError("nonuniform grids are not supported by the GB300 backend")
+        if backend not in ("auto", "native"):
+            raise ValueError(f"backend must be 'auto' or 'native' (GB300 kernels), got {backend!r}")
+        if not torch.cuda.is_available():
+            raise RuntimeError("strata_fdtd_gb300 needs a CUDA device; none is available")
+        self._lib = _native.load()
+        self._torch = torch
+        self._device = torch.device("cuda", torch.cuda.current_device() if device is None
+                                    else torch.device(device).index or 0)
+
+        self.dx = self._grid.min_spacing
+        self.c = c
+        self.rho = rho
+        self._use_native = True
+        self.dt, self._coeff_v, self._coeff_p = step_coefficients(self._grid, c, rho, courant)
+
+        nx, ny, nz = self.shape
+        self._n = nx * ny * nz
+        with torch.cuda.device(self._device):
+            self._dev = [[torch.zeros(self.shape, dtype=torch.float32, device=self._device)
+                          for _ in _FIELDS] for _ in range(2)]
+        self._host = {f: np.zeros(self.shape, dtype=np.float32) for f in _FIELDS}
+        self._host_fresh = {f: True for f in _FIELDS}
+        self._host_exposed = {f: False for f in _FIELDS}
+        self._geometry = np.ones(self.shape, dtype=bool)
+        self._geometry_dev = None
+        self._geometry_set = False
+
+        desc = _native.SfGridDesc(nx, ny, nz, float(self._coeff_v), float(self._coeff_p), 0)
+        plan = ctypes.c_void_p()
+        _native.check(self._lib.sf_plan_create(ctypes.byref(desc), ctypes.byref(plan)),
+                      "sf_plan_create")
+        self._plan = plan
+        ptrs = [t.data_ptr() for s in self._dev for t in s]
+        _native.check(self._lib.sf_plan_bind_fields(self._plan, *ptrs), "sf_plan_bind_fields")
+
+        self._sources: list = []
+        self._probes: dict[str, Probe] = {}
+        self._boundaries: list = []
+        self._microphones: dict = {}
+        self._src_dirty = True
+        self._probe_dirty = True
+        self._probe_order: list[str] = []
+        self._pending_traces: list = []
+
+        self._step_count = 0
+        self._time = 0.0
+        self._snapshots: list = []
+        self._velocity_snapshots: list = []
+        self._snapshot_interval = None
+        self._snapshot_velocity = False
+
+        self._warn_energy_drift = warn_energy_drift
+        self._energy_drift_threshold = energy_drift_threshold
+        self._energy_history: list = []
+        self._track_energy = False
+        self._energy_sample_interval = 1
+        self._energy_scratch = None
+
+        self._materials: dict = {}
+        self._material_id = np.zeros(self.shape, dtype=np.uint8)
+        self._ade_initialized = False
+        self._ade_debye: list = []
+        self._ade_lorentz: list = []
+        self._mat_dev = None
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None and plan.value:
+            try:
+                self._lib.sf_plan_destroy(plan)
+            except Exception:
+                pass
+            self._plan = None
+
+    # ------------------------------------------------------------------ fields
+    def _stream(self):
+        return self._torch.cuda.current_stream(self._device).cuda_stream
+
+    def _cur(self) -> int:
+        return int(self._lib.sf_plan_current(self._plan))
+
+    def _field(self, name):
+        if not self._host_fresh[name]:
+            src = self._dev[self._cur()][_FIELDS.index(name)]
+            self._torch.from_numpy(self._host[name]).copy_(src)
+            self._host_fresh[name] = True
+        self._host_exposed[name] = True
+        return self._host[name]
+
+    def _set_field(self, name, value):
+        arr = np.asarray(value)
+        if arr.shape != self.shape:
+            raise ValueError(f"{name} shape {arr.shape} doesn't match solver shape {self.shape}")
+        if not (arr.dtype == np.float32 and arr.flags.c_contiguous and arr.flags.writeable):
+            arr = np.ascontiguousarray(arr, dtype=np.float32).copy()
+        self._host[name] = arr
+        self._host_fresh[name] = True
+        self._host_exposed[name] = True
+
+    p = property(lambda s: s._field("p"), lambda s, v: s._set_field("p", v))
+    vx = property(lambda s: s._field("vx"), lambda s, v: s._set_field("vx", v))
+    vy = property(lambda s: s._field("vy"), lambda s, v: s._set_field("vy", v))
+    vz = property(lambda s: s._field("vz"), lambda s, v: s._set_field("vz", v))
+
+    def device_fields(self) -> dict:
+        """The current state as CUDA tensors (no copy); valid until the next step."""
+        self._upload_exposed()
+        cur = self._cur()
+        return {f: self._dev[cur][q] for q, f in enumerate(_FIELDS)}
+
+    def _upload_exposed(self):
+        cur = None
+        for q, f in enumerate(_FIELDS):
+            if self._host_exposed[f]:
+                cur = self._cur() if cur is None else cur
+                self._dev[cur][q].copy_(self._torch.from_numpy(self._host[f]))
+                self._host_exposed[f] = False
+
+    def _mark_device_newer(self):
+        for f in _FIELDS:
+            self._host_fresh[f] = False
+
+    # --------------------------------------------------------------- geometry
+    @property
+    def geometry(self) -> np.ndarray:
+        return self._geometry
+
+    @geometry.setter
+    def geometry(self, mask):
+        self.set_geometry(np.asarray(mask))
+
+    @property
+    def time(self) -> float:
+        return self._time
+
+    @property
+    def step_count(self) -> int:
+        return self._step_count
+
+    @property
+    def using_native(self) -> bool:
+        return True
+
+    @property
+    def using_gpu(self) -> bool:
+        return True
+
+    @property
+    def grid(self):
+        return self._grid
+
+    def set_geometry(self, geometry) -> None:
+        """Boolean mask (True = air) or an SDFPrimitive voxelised on the GPU
+        with inside = air (core/solver.py:1682-1780)."""
+        torch = self._torch
+        if isinstance(geometry, SDFPrimitive):
+            dev = geometry.voxelize_device(self._grid)
+            self._geometry = dev.cpu().numpy().astype(bool)
+            self._material_id.fill(0)
+        else:
+            mask = np.asarray(geometry)
+            if mask.shape != self.shape:
+                raise ValueError(f"Geometry shape {mask.shape} doesn't match solver shape {self.shape}")
+            self._geometry = mask.astype(bool)
+            dev = torch.from_numpy(np.ascontiguousarray(self._geometry).view(np.uint8)).to(
+                self._device)
+        self._geometry_dev = dev
+        self._geometry_set = True
+        _native.check(self._lib.sf_plan_set_geometry(self._plan, dev.data_ptr(), self._stream()),
+                      "sf_plan_set_geometry")
+
+    def set_geometry_sdf(self, solid: SDFPrimitive) -> None:
+        """Geometry from a solid's SDF: air is the complement of the solid
+        (``~solid.voxelize(grid)``), voxelised straight into HBM."""
+        dev = solid.voxelize_device(self._grid, invert=True)
+        self._geometry = dev.cpu().numpy().astype(bool)
+        self._geometry_dev = dev
+        self._geometry_set = True
+        _native.check(self._lib.sf_plan_set_geometry(self._plan, dev.data_ptr(), self._stream()),
+                      "sf_plan_set_geometry")
+
+    # --------------------------------------------------------- sources/probes
+    def _to_index(self, pos, what):
+        if isinstance(pos, tuple) and len(pos) == 3 and any(
+                isinstance(p, float) and p < max(self.shape) for p in pos):
+            idx = tuple(int(round(p / self.dx)) for p in pos)
+            for a, (v, n) in enumerate(zip(idx, self.shape)):
+                if not 0 <= v < n:
+                    raise ValueError(f"{what} {'xyz'[a]} position {pos[a]:.4f}m "
+                                     f"(index {v}) is outside grid (0-{n - 1})")
+            return idx
+        return pos
+
+    def add_source(self, source) -> None:
+        """core/solver.py:1782-1841 (point and plane GaussianPulse sources)."""
+        if source.source_type == "point":
+            source.position = self._to_index(source.position, "Source")
+            if any(not 0 <= int(v) < n for v, n in zip(source.position, self.shape)):
+                raise ValueError(f"Source position {source.position} is outside the grid")
+        elif source.source_type == "plane":
+            ax, idx = source.position["axis"], source.position["index"]
+            if ax not in (0, 1, 2) or not 0 <= idx < self.shape[ax]:
+                raise ValueError(f"Plane source {source.position} is outside the grid")
+        else:
+            raise NotImplementedError(f"source_type {source.source_type!r} is not supported")
+        if len(self._sources) >= 16:
+            raise ValueError("at most 16 sources are supported")
+        self._sources.append(source)
+        self._src_dirty = True
+
+    def add_probe(self, name: str, position) -> None:
+        """core/solver.py:1843-1885."""
+        if name in self._probes:
+            raise ValueError(f"Probe '{name}' already exists")
+        position = self._to_index(position, "Probe")
+        if any(not 0 <= int(v) < n for v, n in zip(position, self.shape)):
+            raise ValueError(f"Probe position {position} is outside the grid")
+        self._flush_traces()
+        self._probes[name] = Probe(name=name, position=tuple(int(v) for v in position),
+                                   _solver=self)
+        self._probe_dirty = True
+
+    def add_microphone(self, *args, **kwargs):
+        raise NotImplementedError("microphones are not implemented by the GB300 backend")
+
+    def add_boundary(self, boundary) -> None:
+        if isinstance(boundary, RigidBoundary):
+            boundary.initialize(self)
+            self._boundaries.append(boundary)
+            return
+        if not isinstance(boundary, PML):
+            raise NotImplementedError(f"{type(boundary).__name__} is not supported by the GB300 backend")
+        if any(isinstance(b, PML) for b in self._boundaries):
+            raise NotImplementedError("one PML per solver is supported by the GB300 backend")
+        boundary.initialize(self)
+        self._boundaries.append(boundary)
+        sx, sy, sz = boundary.sigmas
+        ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        _native.check(self._lib.sf_plan_set_pml(self._plan, ptr(sx), ptr(sy), ptr(sz),
+                                                float(self.dt)), "sf_plan_set_pml")
+        self._pml_keepalive = (sx, sy, sz)
+
+    def enable_snapshots(self, interval: int, capture_velocity: bool = False) -> None:
+        self._snapshot_interval = interval
+        self._snapshot_velocity = capture_velocity
+
+    # --------------------------------------------------------------- materials
+    def register_material(self, material, material_id: int | None = None) -> int:
+        if material_id is None:
+            material_id = next((i for i in range(1, 256) if i not in self._materials), None)
+            if material_id is None:
+                raise ValueError("Maximum of 255 materials reached")
+        if not 1 <= material_id <= 255:
+            raise ValueError("material_id must be in range 1-255 (0 is reserved for air)")
+        if material_id in self._materials:
+            raise ValueError(f"Material ID {material_id} is already registered")
+        self._materials[material_id] = material
+        self._ade_initialized = False
+        return material_id
+
+    def set_material_region(self, mask, material_id: int) -> None:
+        mask = np.asarray(mask)
+        if mask.shape != self.shape:
+            raise ValueError(f"Mask shape {mask.shape} doesn't match solver shape {self.shape}")
+        if material_id != 0 and material_id not in self._materials:
+            raise ValueError(f"Material ID {material_id} not registered. Use register_material() first.")
+        self._material_id[mask] = material_id
+        self._ade_initialized = False
+
+    def set_material_box(self, material_id, x_range, y_range, z_range) -> None:
+        mask = np.zeros(self.shape, dtype=bool)
+        mask[x_range[0]:x_range[1], y_range[0]:y_range[1], z_range[0]:z_range[1]] = True
+        self.set_material_region(mask, material_id)
+
+    def get_material_at(self, position):
+        mid = int(self._material_id[position])
+        return None if mid == 0 else self._materials.get(mid)
+
+    @property
+    def has_materials(self) -> bool:
+        return len(self._materials) > 0
+
+    @property
+    def material_count(self) -> int:
+        return len(self._materials)
+
+    def _initialize_ade_fields(self) -> None:
+        """Pole table and auxiliary fields as _initialize_ade_native
+        (core/solver.py:2996-3083): one J per pole, Debye and Lorentz numbered
+        separately in registration order; FP32 coefficients formed the way
+        ade.cpp forms them (-dt/rho_inf*inv_dx, ade.cpp:263; -K_inf*dt,
+        ade.cpp:420)."""
+        torch = self._torch
+        f32 = np.float32
+        dt32 = f32(self.dt)
+        inv_dx = f32(1.0 / self.dx)
+        debye, lorentz = [], []
+        for mid, mat in self._materials.items():
+            rho_inf, k_inf = f32(mat.rho_inf), f32(mat.K_inf)
+            for pole in mat.poles:
+                tgt = 0 if pole.target == "density" else 1
+                co = [f32(v) for v in pole.fdtd_coefficients(self.dt)]
+                corr = f32(f32(-dt32) / rho_inf) * inv_dx if tgt == 0 else f32(-k_inf) * dt32
+                e = dict(mid=mid, target=tgt, co=co, corr=f32(corr),
+                         J=torch.zeros(self._n, dtype=torch.float32, device=self._device))
+                if pole.is_debye:
+                    debye.append(e)
+                else:
+                    e["Jp"] = torch.zeros(self._n, dtype=torch.float32, device=self._device)
+                    lorentz.append(e)
+        self._ade_debye, self._ade_lorentz = debye, lorentz
+        poles = (_native.SfPole * max(1, len(debye) + len(lorentz)))()
+        for q, e in enumerate(debye + lorentz):
+            pl = poles[q]
+            pl.material_id, pl.kind, pl.target = e["mid"], 0 if "Jp" not in e else 1, e["target"]
+            c = list(e["co"]) + [0.0] * (3 - len(e["co"]))
+            pl.c0, pl.c1, pl.c2, pl.corr = float(c[0]), float(c[1]), float(c[2]), float(e["corr"])
+            pl.J = e["J"].data_ptr()
+            pl.J_prev = e["Jp"].data_ptr() if "Jp" in e else None
+        n = len(debye) + len(lorentz)
+        if n > 16:
+            raise NotImplementedError("at most 16 ADE poles are supported")
+        self._mat_dev = torch.from_numpy(self._material_id.reshape(-1)).to(self._device)
+        _native.check(self._lib.sf_plan_set_ade(self._plan, self._mat_dev.data_ptr(), n,
+                                                ctypes.addressof(poles), float(inv_dx)),
+                      "sf_plan_set_ade")
+        self._ade_initialized = True
+
+    @property
+    def _ade_J_debye(self) -> np.ndarray:
+        parts = [e["J"].cpu().numpy() for e in self._ade_debye]
+        return np.concatenate(parts) if parts else np.zeros(1, dtype=np.float32)
+
+    @property
+    def _ade_J_lorentz(self) -> np.ndarray:
+        parts = [e["J"].cpu().numpy() for e in self._ade_lorentz]
+        return np.concatenate(parts) if parts else np.zeros(1, dtype=np.float32)
+
+    @property
+    def _ade_J_lorentz_prev(self) -> np.ndarray:
+        parts = [e["Jp"].cpu().numpy() for e in self._ade_lorentz]
+        return np.concatenate(parts) if parts else np.zeros(1, dtype=np.float32)
+
+    # ---------------------------------------------------------------- stepping
+    def _sync_tables(self):
+        if self._src_dirty:
+            tab = (_native.SfSource * max(1, len(self._sources)))()
+            for q, s in enumerate(self._sources):
+                if s.source_type == "point":
+                    tab[q].kind, (tab[q].a, tab[q].b, tab[q].c) = 0, tuple(int(v) for v in s.position)
+                else:
+                    tab[q].kind, tab[q].a, tab[q].b, tab[q].c = 1, int(s.position["axis"]), int(
+                        s.position["index"]), 0
+            _native.check(self._lib.sf_plan_set_sources(self._plan, len(self._sources),
+                                                        ctypes.addressof(tab)), "sf_plan_set_sources")
+            self._src_dirty = False
+        if self._probe_dirty:
+            self._probe_order = list(self._probes)
+            cells = np.array([np.ravel_multi_index(self._probes[n].position, self.shape)
+                              for n in self._probe_order] or [0], dtype=np.int64)
+            _native.check(self._lib.sf_plan_set_probes(self._plan, len(self._probe_order),
+                                                       cells.ctypes.data), "sf_plan_set_probes")
+            self._probe_dirty = False
+        if self.has_materials and not self._ade_initialized:
+            self._initialize_ade_fields()
+
+    def _source_values(self, n: int) -> np.ndarray:
+        """Waveform per step at the FP64-accumulated times, one NumPy call
+        per source and step exactly as _inject_sources (core/solver.py:2413)."""
+        vals = np.zeros((n, len(self._sources)), dtype=np.float64)
+        if not self._sources:
+            return vals
+        t = self._time
+        for q in range(n):
+            for s, src in enumerate(self._sources):
+                vals[q, s] = src.waveform(np.array([t]), self.dt)[0]
+            t += self.dt
+        return vals
+
+    def _advance(self, n: int) -> None:
+        """Run n time steps through one sf_plan_step call."""
+        torch = self._torch
+        if n <= 0:
+            return
+        self._sync_tables()
+        self._upload_exposed()
+        vals = self._source_values(n)
+        src_dev = torch.from_numpy(vals).to(self._device) if self._sources else None
+        n_probe = len(self._probe_order)
+        trace = (torch.empty((n, n_probe), dtype=torch.float32, device=self._device)
+                 if n_probe else None)
+        rc = self._lib.sf_plan_step(self._plan, n,
+                                    None if src_dev is None else src_dev.data_ptr(),
+                                    None if trace is None else trace.data_ptr(), self._stream())
+        _native.check(rc, "sf_plan_step")
+        if trace is not None:
+            self._pending_traces.append((trace, list(self._probe_order)))
+        self._mark_device_newer()
+        self._step_count += n
+        for _ in range(n):
+            self._time += self.dt
+
+    def _flush_traces(self):
+        for trace, names in self._pending_traces:
+            host = trace.cpu().numpy()
+            for q, name in enumerate(names):
+                if name in self._probes:
+                    self._probes[name]._samples.extend(host[:, q].tolist())
+        self._pending_traces.clear()
+
+    def step(self) -> None:
+        """Advance one time step (core/solver.py:2003-2077)."""
+        self._advance(1)
+        self._after_steps(self._step_count - 1, self._step_count)
+
+    def _after_steps(self, first: int, last: int):
+        """Snapshots and energy samples for steps first..last-1 (only the
+        last of them can be due, run() splits chunks at these points)."""
+        s = last - 1
+        if self._snapshot_interval and s % self._snapshot_interval == 0:
+            t = self._time - self.dt
+            self._snapshots.append((t, self.p.copy()))
+            if self._snapshot_velocity:
+                self._velocity_snapshots.append((t, *self._centred_velocity()))
+        if self._track_energy and last % self._energy_sample_interval == 0:
+            self._energy_history.append((last, self._time, self.compute_energy()))
+
+    def _centred_velocity(self):
+        """Staggered velocities averaged to cell centres (core/solver.py:2647-2687)."""
+        vx, vy, vz = self.vx, self.vy, self.vz
+        cx = np.zeros(self.shape, dtype=np.float32)
+        cx[1:] = 0.5 * (vx[:-1] + vx[1:])
+        cx[0] = 0.5 * vx[0]
+        cy = np.zeros(self.shape, dtype=np.float32)
+        cy[:, 1:] = 0.5 * (vy[:, :-1] + vy[:, 1:])
+        cy[:, 0] = 0.5 * vy[:, 0]
+        cz = np.zeros(self.shape, dtype=np.float32)
+        cz[:, :, 1:] = 0.5 * (vz[:, :, :-1] + vz[:, :, 1:])
+        cz[:, :, 0] = 0.5 * vz[:, :, 0]
+        return cx, cy, cz
+
+    def run(self, duration: float, progress: bool = False, track_energy: bool = False,
+            energy_sample_interval: int = 1, output_file: str | None = None,
+            script_content: str | None = None, callback=None,
+            snapshot_interval: int | None = None) -> None:
+        """Advance ceil(duration/dt) steps (core/solver.py:2520-2606)."""
+        if output_file:
+            raise NotImplementedError("HDF5 output is not implemented by the GB300 backend")
+        n_steps = int(np.ceil(duration / self.dt))
+        self.run_steps(n_steps, track_energy=track_energy,
+                       energy_sample_interval=energy_sample_interval, callback=callback)
+
+    def run_steps(self, n_steps: int, track_energy: bool = False,
+                  energy_sample_interval: int = 1, callback=None) -> None:
+        """Advance exactly n_steps, in as few C-ABI calls as the snapshot,
+        energy and callback settings allow."""
+        self._track_energy = track_energy
+        self._energy_sample_interval = energy_sample_interval
+        if track_energy and not self._energy_history:
+            self._energy_history.append((self._step_count, self._time, self.compute_energy()))
+        done = 0
+        while done < n_steps:
+            chunk = min(n_steps - done, _MAX_CHUNK)
+            if callback is not None:
+                chunk = 1
+            if self._snapshot_interval:
+                iv = self._snapshot_interval
+                nxt = ((self._step_count + iv - 1) // iv) * iv  # next due pre-increment index
+                chunk = min(chunk, nxt - self._step_count + 1)
+            if track_energy:
+                iv = energy_sample_interval
+                nxt = ((self._step_count // iv) + 1) * iv
+                chunk = min(chunk, nxt - self._step_count)
+            first = self._step_count
+            self._advance(chunk)
+            self._after_steps(first, self._step_count)
+            if callback is not None:
+                callback(self._step_count - 1)
+            done += chunk
+        if self._warn_energy_drift and len(self._energy_history) >= 2:
+            rep = self.energy_report()
+            if abs(rep["energy_change_percent"]) > self._energy_drift_threshold * 100:
+                warnings.warn(f"Energy drift detected: {rep['energy_change_percent']:.2f}% change",
+                              UserWarning, stacklevel=2)
+
+    def synchronize(self) -> None:
+        self._torch.cuda.synchronize(self._device)
+
+    # ----------------------------------------------------------------- outputs
+    def get_probe_data(self, name: str | None = None) -> dict:
+        self._flush_traces()
+        if name is not None:
+            if name not in self._probes:
+                raise KeyError(f"Probe '{name}' not found")
+            return {name: self._probes[name].get_data()}
+        return {n: pr.get_data() for n, pr in self._probes.items()}
+
+    def get_snapshots(self):
+        return self._snapshots
+
+    def get_velocity_snapshots(self):
+        return self._velocity_snapshots
+
+    def compute_energy(self) -> float:
+        """(1/2)(p^2/(rho c^2) + rho |v|^2) dV summed over air cells, reduced
+        in FP64 on the GPU (core/solver.py:2689-2705 sums in FP32)."""
+        torch = self._torch
+        self._upload_exposed()
+        need = int(self._lib.sf_energy_scratch_doubles(self._plan))
+        if self._energy_scratch is None or self._energy_scratch.numel() < need:
+            self._energy_scratch = torch.empty(need, dtype=torch.float64, device=self._device)
+        out = ctypes.c_double()  # without a geometry every cell counts as air
+        _native.check(self._lib.sf_plan_energy(self._plan, float(self.rho), float(self.c),
+                                               float(self.dx), self._energy_scratch.data_ptr(),
+                                               ctypes.byref(out), self._stream()), "sf_plan_energy")
+        return float(out.value)
+
+    def get_energy_history(self):
+        return self._energy_history.copy()
+
+    def energy_report(self) -> dict:
+        if not self._energy_history:
+            raise ValueError("No energy history recorded. Call run() with track_energy=True first.")
+        e = np.array([v for _, _, v in self._energy_history])
+        e0, e1 = e[0], e[-1]
+        change = (0.0 if e1 == 0 else float("inf")) if e0 == 0 else (e1 - e0) / e0 * 100
+        status = "stable" if abs(change) <= 1.0 else ("growing" if change > 0 else "decaying")
+        return {"initial_energy": float(e0), "final_energy": float(e1),
+                "max_energy": float(e.max()), "min_energy": float(e.min()),
+                "energy_change_percent": change, "conservation_status": status,
+                "n_samples": len(e)}
+
+    def reset(self) -> None:
+        """core/solver.py:2781-2800."""
+        for s in self._dev:
+            for t in s:
+                t.zero_()
+        for f in _FIELDS:
+            self._host[f].fill(0)
+            self._host_fresh[f] = True
+            self._host_exposed[f] = False
+        self._step_count = 0
+        self._time = 0.0
+        self._snapshots.clear()
+        self._energy_history.clear()
+        self._track_energy = False
+        self._pending_traces.clear()
+        for pr in self._probes.values():
+            pr._samples.clear()
+        for e in self._ade_debye + self._ade_lorentz:
+            e["J"].zero_()
+            if "Jp" in e:
+                e["Jp"].zero_()
+
+    def get_sample_rate(self) -> float:
+        return 1.0 / self.dt
+
+    def get_frequency_response(self, probe_name: str, n_fft: int | None = None):
+        data = self.get_probe_data(probe_name)[probe_name]
+        if n_fft is None:
+            n_fft = int(2 ** np.ceil(np.log2(len(data))))
+        spectrum = np.fft.rfft(data, n=n_fft)
+        return np.fft.rfftfreq(n_fft, self.dt), np.abs(spectrum)
+
+
+__all__ = ["FDTDSolver", "GaussianPulse", "Probe", "has_native_kernels", "get_native_info"]

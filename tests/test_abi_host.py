@@ -1,0 +1,131 @@
+"""CPU-only checks of the product: the C-ABI library loads and exports every
+symbol that include/sf_gb300.h declares, and the host-side arithmetic that
+feeds the kernels (coefficients, PML profiles and decays, waveform values,
+pole coefficients, SDF programs) equals the reference's values stored in
+tests/golden/.  No compute call is made without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import strata_fdtd_gb300 as S
+from conftest import ROOT, golden
+from strata_fdtd_gb300 import _native
+from strata_fdtd_gb300.solver import step_coefficients
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _native.build()
+    return _native.load()
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "sf_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(sf_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_the_abi():
+    names = declared_symbols()
+    for must in ("sf_plan_create", "sf_plan_step", "sf_voxelize", "sf_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+    assert set(declared_symbols()) <= set(_native.SIGNATURES), "ctypes signatures incomplete"
+
+
+def test_version_and_error_strings_without_gpu(lib):
+    assert lib.sf_version().startswith(b"strata_fdtd_gb300")
+    # argument validation happens before any device call
+    assert lib.sf_plan_create(None, None) != 0
+    assert b"NULL" in lib.sf_last_error()
+    desc = _native.SfGridDesc(0, 4, 4, 0.0, 0.0, 0)
+    plan = ctypes.c_void_p()
+    assert lib.sf_plan_create(ctypes.byref(desc), ctypes.byref(plan)) != 0
+    assert b"dimensions" in lib.sf_last_error()
+
+
+def test_step_coefficients_match_reference(manifest):
+    for key, case in (("plain_c1_full", dict(shape=(100, 100, 100), res=1e-3, c=343.0, rho=1.204,
+                                             courant=0.5)),
+                      ("plain_impulse_default_coeffs", dict(shape=(20, 20, 20), res=2e-3, c=343.0,
+                                                            rho=1.2, courant=0.95))):
+        g = S.UniformGrid(case["shape"], case["res"])
+        dt, cv, cp = step_coefficients(g, case["c"], case["rho"], case["courant"])
+        info = manifest[key]
+        assert (dt, cv, cp) == (info["dt"], info["coeff_v"], info["coeff_p"])
+
+
+def test_pml_profile_and_host_decay_match_reference():
+    h = golden("host_values")
+    from oracle import oracle as O
+    for n, depth, res, courant in ((100, 10, 1e-3, 0.5), (37, 6, 2e-3, 0.9), (400, 16, 1e-3, 0.5)):
+        pml = S.PML(depth=depth, axis="x")
+
+        class _Stub:
+            shape = (n, 4, 4)
+            c = 343.0
+            grid = S.UniformGrid((n, 4, 4), res)
+
+        pml.initialize(_Stub())
+        np.testing.assert_array_equal(pml.sigmas[0], h[f"sigma__{n}"])
+        dt = step_coefficients(_Stub.grid, 343.0, 1.204, courant)[0]
+        assert dt == h[f"dt__{n}"][0]
+        # the oracle's expf restatement and the reference decays agree
+        out = np.zeros(n, dtype=np.float32)
+        O.lib().orc_pml_decay_f32(pml.sigmas[0].ctypes.data, n, float(np.float32(dt)),
+                                  out.ctypes.data)
+        np.testing.assert_array_equal(out, h[f"decay__{n}"])
+
+
+def test_waveform_and_pole_coefficients_match_reference():
+    h = golden("host_values")
+    for f in (1000, 2000, 20000):
+        g = S.GaussianPulse(position=(0, 0, 0), frequency=float(f),
+                            bandwidth=15000.0 if f == 20000 else None, amplitude=1.3)
+        dt = 0.5 * (1e-3 / (343.0 * np.sqrt(3)))
+        vals = [g.waveform(np.array([t]), dt)[0] for t in h[f"wave_t__{f}"]]
+        np.testing.assert_array_equal(np.array(vals), h[f"wave__{f}"])
+    for row in h["pole_rows"]:
+        dt, kind = row[0], int(row[1])
+        if kind == 0:
+            p = S.Pole(S.PoleType.DEBYE, delta_chi=row[3], target="density", tau=row[2])
+            assert p.fdtd_coefficients(dt) == tuple(row[4:6])
+        else:
+            p = S.Pole(S.PoleType.LORENTZ, delta_chi=0.2, target="modulus", omega_0=row[2],
+                       gamma=row[3])
+            assert p.fdtd_coefficients(dt) == tuple(row[4:7])
+
+
+def test_sdf_program_layout():
+    tree = S.Difference(S.Box(center=(0.1, 0.1, 0.1), size=(0.2, 0.1, 0.3)),
+                        S.Sphere(center=(0.1, 0.1, 0.1), radius=0.02),
+                        S.Cylinder(p1=(0.1, 0.1, 0.0), p2=(0.1, 0.1, 0.05), radius=0.01)
+                        .translate((0.0, 0.0, 0.001)))
+    prog, n = tree.program()
+    ops = [prog[q].op for q in range(n)]
+    assert ops == [1, 2, 20, 3, 22, 12]
+    assert prog[n - 1].n == 3
+    assert prog[3].s0 == 0.05 and prog[3].b[2] == 1.0
+    assert ctypes.sizeof(_native.SfSdfNode) == 72
+    assert ctypes.sizeof(_native.SfPole) == 48
+
+
+def test_helmholtz_constants_match_oracle_construction():
+    from oracle import oracle as O
+    for shape, size in (("box", (0.016, 0.014, 0.012)), ("sphere", (0.008,)),
+                        ("cylinder", (0.007, 0.014))):
+        a = S.HelmholtzResonator(position=(0.03, 0.02, 0.04), cavity_shape=shape,
+                                 cavity_size=size, neck_length=0.007, neck_radius=0.003,
+                                 neck_direction=(0, 1, 0))
+        b = O.HelmholtzResonator(position=(0.03, 0.02, 0.04), cavity_shape=shape,
+                                 cavity_size=size, neck_length=0.007, neck_radius=0.003,
+                                 neck_direction=(0, 1, 0))
+        na, nb = a._combined.children[1], b._combined.children[1]
+        assert np.array_equal(na.p1, nb.p1) and np.array_equal(na.p2, nb.p2)
+        assert na.length == nb.length

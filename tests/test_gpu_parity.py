@@ -1,0 +1,259 @@
+"""GPU parity: the sm_103a kernels against the reference's golden vectors and
+the CPU oracle, bit for bit.
+
+Tolerance: none -- FP32 fields, probe traces and masks must be identical
+(the reference native path is deterministic FP32 without FMA, and so are the
+kernels).  Every case goes through the public drop-in API
+(strata_fdtd_gb300.FDTDSolver), i.e. through the C ABI.
+"""
+import types
+
+import numpy as np
+import pytest
+
+import cases as C
+from conftest import golden, sha256
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import strata_fdtd_gb300 as S  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+API = types.SimpleNamespace(
+    FDTDSolver=S.FDTDSolver, UniformGrid=S.UniformGrid, PML=S.PML, GaussianPulse=S.GaussianPulse,
+    Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
+    Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
+    PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial)
+ORACLE = O.make_api()
+SMALL = [k for k, v in C.PLAIN_CASES.items() if not v.get("big") and k != "c1_full"]
+
+
+def _compare(solver, key, manifest, fields=True):
+    info = manifest[key]
+    g = golden(key)
+    for name in g["probe_names"]:
+        np.testing.assert_array_equal(solver.get_probe_data()[str(name)], g[f"trace__{name}"],
+                                      err_msg=f"{key}: probe {name}")
+    if fields:
+        for f in ("p", "vx", "vy", "vz"):
+            arr = getattr(solver, f)
+            if f"field__{f}" in g.files:
+                np.testing.assert_array_equal(arr, g[f"field__{f}"], err_msg=f"{key}: {f}")
+            assert sha256(arr) == info[f"sha_{f}"], f"{key}: {f} differs from the reference"
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_plain_cases_one_call(name, manifest):
+    case = C.PLAIN_CASES[name]
+    s = C.build_case(API, case)
+    s.run_steps(case["steps"])
+    _compare(s, "plain_" + name, manifest)
+    if case.get("geometry"):
+        assert sha256(s.geometry) == manifest["plain_" + name]["sha_geometry"]
+
+
+@pytest.mark.parametrize("name", ["c1_tiny", "blocks_odd", "plane_yz_geom"])
+def test_plain_cases_step_by_step(name, manifest):
+    case = C.PLAIN_CASES[name]
+    s = C.build_case(API, case)
+    for q in range(case["steps"]):
+        s.step()
+        if q == case["steps"] // 2:
+            _ = s.p[0, 0, 0]  # host read in the middle: forces a download + re-upload
+    _compare(s, "plain_" + name, manifest)
+
+
+@pytest.mark.parametrize("name", list(C.ADE_CASES))
+def test_ade_cases(name, manifest):
+    case = C.ADE_CASES[name]
+    s = C.build_case(API, case)
+    s.run_steps(case["steps"])
+    _compare(s, "ade_" + name, manifest)
+    g = golden("ade_" + name)
+    if s._ade_debye:
+        np.testing.assert_array_equal(s._ade_J_debye, g["ade_ade_J_debye"])
+    if s._ade_lorentz:
+        np.testing.assert_array_equal(s._ade_J_lorentz, g["ade_ade_J_lorentz"])
+        np.testing.assert_array_equal(s._ade_J_lorentz_prev, g["ade_ade_J_lorentz_prev"])
+
+
+def test_c1_quick_start_1000_steps(manifest):
+    """The reference quick start, 100^3 x 1000 steps, through run(duration)."""
+    case = C.PLAIN_CASES["c1_full"]
+    s = C.build_case(API, case)
+    s.run(duration=case["steps"] * s.dt * 0.9999)
+    assert s.step_count == 1000
+    _compare(s, "plain_c1_full", manifest)
+
+
+def test_c2_enclosure_full_size_20_steps(manifest):
+    """400^3 with the GPU-voxelised enclosure: mask, traces and fields equal
+    the reference's after 20 steps."""
+    case = C.PLAIN_CASES["c2_enclosure_20"]
+    info = manifest["plain_c2_enclosure_20"]
+    s = S.FDTDSolver(grid=S.UniformGrid(case["shape"], case["res"]), c=343.0, rho=1.204,
+                     courant=0.5, backend="native")
+    s.add_boundary(S.PML(depth=16))
+    s.set_geometry_sdf(C.c2_solid(API))
+    assert sha256(s.geometry) == info["sha_geometry"]
+    s.add_source(S.GaussianPulse(position=(200, 200, 200), frequency=2000.0, amplitude=1.0))
+    for name, pos in info["probes"]:
+        s.add_probe(name, tuple(pos))
+    s.run_steps(case["steps"])
+    _compare(s, "plain_c2_enclosure_20", manifest)
+
+
+@pytest.mark.parametrize("name", list(C.VOXEL_CASES))
+def test_voxelize_matches_reference(name):
+    shape, res, which = C.VOXEL_CASES[name]
+    grid = S.UniformGrid(shape, res)
+    mask = C.sdf_tree(API, which).voxelize(grid)
+    ref = np.unpackbits(golden("voxel")["mask__" + name])[: mask.size].reshape(shape).astype(bool)
+    if which == "cyl_oblique":
+        # np.dot rounds through BLAS; only cells within rounding of the surface may differ
+        diff = mask != ref
+        if diff.any():
+            d = C.sdf_tree(ORACLE, which).sdf(np.stack(np.meshgrid(
+                grid.x_coords, grid.y_coords, grid.z_coords, indexing="ij"), -1).reshape(-1, 3))
+            assert np.all(np.abs(d.reshape(shape)[diff]) < 1e-15)
+    else:
+        np.testing.assert_array_equal(mask, ref)
+
+
+def test_sdf_point_evaluation_matches_oracle():
+    tree = C.sdf_tree(API, "csg_mix")
+    pts = np.random.default_rng(0).uniform(0, 0.05, (5000, 3))
+    np.testing.assert_array_equal(tree.sdf(pts), C.sdf_tree(ORACLE, "csg_mix").sdf(pts))
+
+
+def _random_case(seed):
+    rng = np.random.default_rng(seed)
+    shape = tuple(int(v) for v in rng.integers(5, 41, size=3))
+    pml = int(rng.integers(1, max(2, min(shape) // 3)))
+    axes = [("x", "y", "z"), ("x",), ("y", "z"), ("z",)][int(rng.integers(0, 4))]
+    srcs = []
+    for _ in range(int(rng.integers(1, 4))):
+        if rng.random() < 0.7:
+            srcs.append(("point", tuple(int(rng.integers(0, n)) for n in shape),
+                         float(rng.uniform(5e3, 4e4)), float(rng.uniform(-2, 2))))
+        else:
+            ax = int(rng.integers(0, 3))
+            srcs.append(("plane", {"axis": ax, "index": int(rng.integers(0, shape[ax]))},
+                         float(rng.uniform(5e3, 4e4)), 1.0))
+    probes = [(f"q{q}", tuple(int(rng.integers(0, n)) for n in shape)) for q in range(3)]
+    case = dict(shape=shape, res=float(rng.choice([1e-3, 2e-3, 5e-4])),
+                courant=float(rng.uniform(0.3, 0.99)), pml=dict(depth=pml, axis=axes),
+                sources=srcs, probes=probes, steps=int(rng.integers(20, 90)))
+    if rng.random() < 0.7:
+        case["geometry"] = dict(kind="blocks", seed=int(seed), n_boxes=2, n_spheres=1)
+    return case
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_cases_against_oracle(seed):
+    case = _random_case(seed)
+    try:
+        ref = C.build_case(ORACLE, case)
+    except (IndexError, ValueError):
+        pytest.skip("case outside what the reference accepts")
+    ref.run_steps(case["steps"])
+    s = C.build_case(API, case)
+    s.run_steps(case["steps"])
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f"seed {seed} {f}")
+    for name in ref.get_probe_data():
+        np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (1, 6, 9), (7, 1, 5), (4, 5, 1), (2, 2, 2)])
+def test_degenerate_shapes_against_oracle(shape):
+    case = dict(shape=shape, res=1e-3, courant=0.5, pml=None, impulse=((0, 0, 0), 1.0),
+                sources=[("point", (0, 0, 0), 20000.0, 1.0)], probes=[("a", (0, 0, 0))],
+                steps=25)
+    ref = C.build_case(ORACLE, case)
+    ref.run_steps(25)
+    s = C.build_case(API, case)
+    s.run_steps(25)
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(s, f), getattr(ref, f))
+
+
+def test_full_size_against_oracle_and_scaling_property():
+    """400^3 with the enclosure: 6 steps bit-exact against the C oracle, and
+    doubling the source amplitude doubles every field exactly (FP32 scaling
+    by 2 commutes with every rounding) over 60 steps."""
+    solid = C.c2_solid(API)
+    a = S.FDTDSolver(shape=(400, 400, 400), resolution=1e-3, c=343.0, rho=1.204, courant=0.5)
+    a.add_boundary(S.PML(depth=16))
+    a.set_geometry_sdf(solid)
+    a.add_source(S.GaussianPulse(position=(200, 200, 200), frequency=2000.0, amplitude=1.0))
+    a.add_probe("x", (200, 200, 230))
+    o = O.FDTDSolver(shape=(400, 400, 400), resolution=1e-3, c=343.0, rho=1.204, courant=0.5)
+    o.add_boundary(O.PML(depth=16))
+    o.set_geometry(a.geometry)
+    o.add_source(O.GaussianPulse(position=(200, 200, 200), frequency=2000.0, amplitude=1.0))
+    # a nonzero state so the stencil is exercised everywhere
+    rng = np.random.default_rng(7)
+    init = rng.standard_normal((400, 400, 400), dtype=np.float32) * np.float32(1e-3)
+    init[~a.geometry] = 0.0
+    a.p = init.copy()
+    o.p = init
+    a.run_steps(6)
+    o.run_steps(6)
+    for f in ("p", "vx", "vy", "vz"):
+        assert sha256(getattr(a, f)) == sha256(getattr(o, f)), f
+    b = S.FDTDSolver(shape=(400, 400, 400), resolution=1e-3, c=343.0, rho=1.204, courant=0.5)
+    b.add_boundary(S.PML(depth=16))
+    b.set_geometry_sdf(solid)
+    b.add_source(S.GaussianPulse(position=(200, 200, 200), frequency=2000.0, amplitude=2.0))
+    c1 = S.FDTDSolver(shape=(400, 400, 400), resolution=1e-3, c=343.0, rho=1.204, courant=0.5)
+    c1.add_boundary(S.PML(depth=16))
+    c1.set_geometry_sdf(solid)
+    c1.add_source(S.GaussianPulse(position=(200, 200, 200), frequency=2000.0, amplitude=1.0))
+    b.run_steps(60)
+    c1.run_steps(60)
+    for f in ("p", "vx"):
+        x1, x2 = getattr(c1, f), getattr(b, f)
+        assert np.abs(x1).max() > 0
+        np.testing.assert_array_equal(x2, 2 * x1)
+
+
+def test_host_edits_between_steps_are_seen():
+    """solver.p[...] = v between steps, as the reference tests do
+    (tests/test_native_extension.py:247-249)."""
+    case = dict(shape=(20, 22, 24), res=1e-3, courant=0.5, pml=dict(depth=3), sources=[],
+                probes=[("c", (10, 11, 12))], steps=30)
+    s = C.build_case(API, case)
+    o = C.build_case(ORACLE, case)
+    for solver in (s, o):
+        solver.p[10, 11, 12] = 1.0
+        for q in range(30):
+            solver.step()
+            if q == 10:
+                solver.vx[3, 4, 5] = 0.25
+    np.testing.assert_array_equal(s.p, o.p)
+    np.testing.assert_array_equal(s.get_probe_data()["c"], o.get_probe_data()["c"])
+
+
+def test_energy_matches_host_sum():
+    case = C.PLAIN_CASES["blocks_odd"]
+    s = C.build_case(API, case)
+    s.run_steps(80)
+    e = s.compute_energy()
+    g = s.geometry
+    dV = s.dx**3
+    pe = 0.5 * np.sum(s.p[g].astype(np.float64) ** 2) / (s.rho * s.c**2) * dV
+    v2 = s.vx.astype(np.float64) ** 2 + s.vy.astype(np.float64) ** 2 + s.vz.astype(np.float64) ** 2
+    ke = 0.5 * s.rho * np.sum(v2[g]) * dV
+    assert e == pytest.approx(pe + ke, rel=1e-12)
+
+
+def test_errors_are_loud():
+    with pytest.raises(ValueError):
+        S.FDTDSolver(shape=(8, 8, 8), resolution=1e-3, backend="python")
+    s = S.FDTDSolver(shape=(8, 8, 8), resolution=1e-3)
+    with pytest.raises(ValueError):
+        s.add_source(S.GaussianPulse(position=(9, 0, 0), frequency=1000.0))
+    with pytest.raises(NotImplementedError):
+        s.add_microphone(position=(0.001, 0.001, 0.001))
