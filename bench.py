@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--size", type=int, default=400, help="grid edge (400 = the workload)")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "march"])
+    ap.add_argument("--ichunk", type=int, default=0, help="planes per block (march)")
     return ap.parse_args()
 
 
@@ -216,7 +219,7 @@ def run_gpu(args):
 
     import strata_fdtd_gb300 as S
     from strata_fdtd_gb300 import _native
-    from strata_fdtd_gb300.workloads import enclosure_400
+    from strata_fdtd_gb300.workloads import enclosure
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -233,7 +236,10 @@ def run_gpu(args):
         torch.cuda.synchronize()
 
     lib = _native.load()
-    s = enclosure_400()
+    n_edge = args.size
+    cells = n_edge ** 3
+    s = enclosure(n_edge)
+    s.set_kernel(args.kernel, args.ichunk)
     inner, K, W = args.inner, args.steps, args.warmup
     n_src = len(s._sources)
     n_probe = len(s._probes)
@@ -267,10 +273,10 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     launches = K * (inner + 1)
-    value = world * CELLS * inner * K / (ms / 1e3) / 1e9
+    value = world * cells * inner * K / (ms / 1e3) / 1e9
     kernel_ms = ms / (K * inner)  # every timed launch attributed to the step kernel
     hbm, peak_kind = peaks()
-    achieved = BYTES_PER_CELL * CELLS / (kernel_ms / 1e3) / 1e9
+    achieved = BYTES_PER_CELL * cells / (kernel_ms / 1e3) / 1e9
     traffic = profiled_traffic()
     s._mark_device_newer()
     s._step_count += (W + K) * inner
@@ -278,7 +284,7 @@ def run_gpu(args):
     # end to end through the public API: pinned host fields in, p and traces out
     e2e = None
     if not args.no_e2e:
-        host = {f: torch.zeros((400, 400, 400), dtype=torch.float32).pin_memory().numpy()
+        host = {f: torch.zeros((n_edge,) * 3, dtype=torch.float32).pin_memory().numpy()
                 for f in ("p", "vx", "vy", "vz")}
         for f in host:
             np.copyto(host[f], getattr(s, f))
@@ -297,14 +303,14 @@ def run_gpu(args):
             t = torch.tensor([el], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             el = float(t.item())
-        e2e = {"value": world * CELLS * inner * Ke / el / 1e9, "unit": METRIC,
-               "h2d_bytes_per_step": 4 * CELLS * 4 + inner * n_src * 8,
-               "d2h_bytes_per_step": CELLS * 4 + inner * n_probe * 4,
+        e2e = {"value": world * cells * inner * Ke / el / 1e9, "unit": METRIC,
+               "h2d_bytes_per_step": 4 * cells * 4 + inner * n_src * 8,
+               "d2h_bytes_per_step": cells * 4 + inner * n_probe * 4,
                "steps": Ke, "path": "FDTDSolver fields assigned from pinned host arrays, "
                                     "run_steps(inner), solver.p and get_probe_data() read back"}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and n_edge == 400:
         o = oracle_enclosure(s.geometry)
         v, n, th = time_oracle(o, args.cpu_seconds)
         cpu = {"value": v, "unit": METRIC, "cores": th, "kind": "port",
@@ -317,13 +323,16 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "bench_step": f"{inner} FDTD time steps",
+            "config": {"workload": WORKLOAD if n_edge == 400 else f"enclosure at {n_edge}^3",
+                       "bench_step": f"{inner} FDTD time steps", "kernel": args.kernel,
+                       "i_chunk": args.ichunk,
                        "global_batch": world, "parallelism": f"replicas x{world}",
                        "l2": "state 1.1 GB per replica > 129 MB L2, no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_cell": BYTES_PER_CELL,
-                         "kernel": "k_step<GEOM> (fused step, sf_step.cu)"},
+                         "kernel": "fused step kernel (k_step_march, sf_step_march.cu)"
+                                   if args.kernel != "cell" else "k_step (sf_step.cu)"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "device": torch.cuda.get_device_name(local),
             "library": lib.sf_version().decode(),

@@ -15,6 +15,11 @@ __device__ __forceinline__ double d_add(double a, double b) { return __dadd_rn(a
 __device__ __forceinline__ double d_sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double d_mul(double a, double b) { return __dmul_rn(a, b); }
 
+// One face velocity: v + cv*(p_hi - p_lo) (fdtd_step.cpp:44,61,78).
+__device__ __forceinline__ float face_update(float v, float cv, float p_hi, float p_lo) {
+    return f_add(v, f_mul(cv, f_sub(p_hi, p_lo)));
+}
+
 // Per-cell flag byte built from the geometry mask by sf_plan_set_geometry.
 //   bit 0: cell is air
 //   bit 1/2/3: the +x/+y/+z face of the cell joins two air cells (open)

@@ -33,11 +33,6 @@ namespace {
 constexpr int BX = 32;  // threads along k (contiguous)
 constexpr int BY = 8;   // threads along j
 
-// One face velocity: v + cv*(p_hi - p_lo).
-__device__ __forceinline__ float face_update(float v, float cv, float p_hi, float p_lo) {
-    return f_add(v, f_mul(cv, f_sub(p_hi, p_lo)));
-}
-
 // Density-pole velocity correction on the face between cells lo and hi
 // (ade.cpp:228-401): v += corr*(J[hi]-J[lo]) for each density pole whose
 // material holds both cells, Debye poles first then Lorentz.

@@ -632,6 +632,14 @@ class FDTDSolver:
                 warnings.warn(f"Energy drift detected: {rep['energy_change_percent']:.2f}% change",
                               UserWarning, stacklevel=2)
 
+    def set_kernel(self, variant: str = "auto", i_chunk: int = 0) -> None:
+        """Choose the step kernel: "auto" (slab march, per-cell kernel with
+        ADE), "cell" (one thread per cell) or "march" (2.5-D slab march with
+        ``i_chunk`` planes per block, 0 = automatic).  Results are identical."""
+        v = {"auto": 0, "cell": 1, "march": 2}[variant]
+        _native.check(self._lib.sf_plan_set_kernel(self._plan, v, int(i_chunk)),
+                      "sf_plan_set_kernel")
+
     def synchronize(self) -> None:
         self._torch.cuda.synchronize(self._device)
 

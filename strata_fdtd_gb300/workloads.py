@@ -32,10 +32,13 @@ def enclosure_solid():
 
 
 def enclosure_probes(geometry, pml_depth=16, n=8, seed=0):
+    """Seeded air cells outside the enclosure's bounding cells and the PML
+    (cell indices for the 0.4 m cube at any resolution)."""
     rng = np.random.default_rng(seed)
     size = geometry.shape[0]
-    lo_box = np.array([100, 140, 50]) - 1
-    hi_box = np.array([300, 260, 350]) + 1
+    res = 0.4 / size
+    lo_box = np.floor(np.array([0.1, 0.14, 0.05]) / res).astype(int) - 1
+    hi_box = np.ceil(np.array([0.3, 0.26, 0.35]) / res).astype(int) + 1
     out = []
     while len(out) < n:
         c = rng.integers(pml_depth, size - pml_depth, size=3)
@@ -45,15 +48,24 @@ def enclosure_probes(geometry, pml_depth=16, n=8, seed=0):
     return out
 
 
-def enclosure_400(amplitude=1.0, **kw) -> FDTDSolver:
-    s = FDTDSolver(grid=UniformGrid((400, 400, 400), 1e-3), c=C_AIR, rho=RHO_AIR, courant=0.5,
+def enclosure(n=400, amplitude=1.0, **kw) -> FDTDSolver:
+    """The enclosure workload on an n^3 grid over the same 0.4 m cube
+    (n = 400: 1 mm cells, PML 16; smaller n for profiling runs)."""
+    res = 1e-3 if n == 400 else 0.4 / n
+    pml = 16 if n == 400 else max(4, round(16 * n / 400))
+    s = FDTDSolver(grid=UniformGrid((n, n, n), res), c=C_AIR, rho=RHO_AIR, courant=0.5,
                    backend="native", **kw)
-    s.add_boundary(PML(depth=16))
+    s.add_boundary(PML(depth=pml))
     s.set_geometry_sdf(enclosure_solid())
-    s.add_source(GaussianPulse(position=(200, 200, 200), frequency=2000.0, amplitude=amplitude))
-    for q, pos in enumerate(enclosure_probes(s.geometry)):
+    s.add_source(GaussianPulse(position=(n // 2, n // 2, n // 2), frequency=2000.0,
+                               amplitude=amplitude))
+    for q, pos in enumerate(enclosure_probes(s.geometry, pml_depth=pml)):
         s.add_probe(f"probe{q}", pos)
     return s
+
+
+def enclosure_400(amplitude=1.0, **kw) -> FDTDSolver:
+    return enclosure(400, amplitude, **kw)
 
 
 def quick_start_100(**kw) -> FDTDSolver:

@@ -166,6 +166,34 @@ def test_random_cases_against_oracle(seed):
         np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
 
 
+@pytest.mark.parametrize("variant,i_chunk", [("cell", 0), ("march", 1), ("march", 3),
+                                             ("march", 7), ("march", 0)])
+@pytest.mark.parametrize("seed", [0, 3, 5, 8])
+def test_kernel_variants_against_oracle(seed, variant, i_chunk):
+    case = _random_case(100 + seed)
+    try:
+        ref = C.build_case(ORACLE, case)
+    except (IndexError, ValueError):
+        pytest.skip("case outside what the reference accepts")
+    ref.run_steps(case["steps"])
+    s = C.build_case(API, case)
+    s.set_kernel(variant, i_chunk)
+    s.run_steps(case["steps"])
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f"{variant} {f}")
+    for name in ref.get_probe_data():
+        np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
+
+
+@pytest.mark.parametrize("variant", ["cell", "march"])
+def test_c1_quick_start_both_kernels(variant, manifest):
+    case = C.PLAIN_CASES["c1_full"]
+    s = C.build_case(API, case)
+    s.set_kernel(variant)
+    s.run_steps(case["steps"])
+    _compare(s, "plain_c1_full", manifest)
+
+
 @pytest.mark.parametrize("shape", [(1, 1, 1), (1, 6, 9), (7, 1, 5), (4, 5, 1), (2, 2, 2)])
 def test_degenerate_shapes_against_oracle(shape):
     case = dict(shape=shape, res=1e-3, courant=0.5, pml=None, impulse=((0, 0, 0), 1.0),
@@ -216,7 +244,12 @@ def test_full_size_against_oracle_and_scaling_property():
     for f in ("p", "vx"):
         x1, x2 = getattr(c1, f), getattr(b, f)
         assert np.abs(x1).max() > 0
-        np.testing.assert_array_equal(x2, 2 * x1)
+        # exact where the values are normal; subnormal results round on an
+        # absolute grid, so scaling is not exact there
+        normal = np.abs(x1) > 1e-30
+        assert normal.sum() > 1000
+        np.testing.assert_array_equal(x2[normal], 2 * x1[normal])
+        np.testing.assert_allclose(x2[~normal], 2 * x1[~normal], rtol=0, atol=1e-37)
 
 
 def test_host_edits_between_steps_are_seen():
