@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--size", type=int, default=400, help="grid edge (400 = the workload)")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "march"])
+    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "march", "col", "col1"])
     ap.add_argument("--ichunk", type=int, default=0, help="planes per block (march)")
     return ap.parse_args()
 

@@ -147,10 +147,12 @@ int sf_plan_set_probes(sf_plan* plan, int n, const int64_t* cells);
 int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const sf_pole* poles,
                     float inv_dx);
 
-/* Step kernel choice: variant 0 = automatic (the slab march unless ADE
- * poles are set), 1 = one thread per cell, 2 = slab march along i with
- * i_chunk planes per block (0 = automatic).  All variants give identical
- * results.  No counterpart in the reference (its kernels are CPU loops). */
+/* Step kernel choice: variant 0 = automatic (columns; the per-cell kernel
+ * when ADE poles are set), 1 = one thread per cell, 2 = slab march along i
+ * (shared-memory halos), 3 = thread columns along i (float4 along k when
+ * nz % 4 == 0), 4 = thread columns, scalar.  i_chunk = planes per block for
+ * 2-4 (0 = automatic).  All variants give identical results.  No
+ * counterpart in the reference (its kernels are CPU loops). */
 int sf_plan_set_kernel(sf_plan* plan, int variant, int i_chunk);
 
 /* Advance n_steps.  src_values_dev: device doubles [n_steps][n_sources]

@@ -27,6 +27,8 @@ int sf_launch_probe_gather(const float* p, const long long* cells, int n, float*
                            cudaStream_t st);
 int sf_launch_step_march(const SfStepArgs& a, const SfSources& src, bool geom, int ich,
                          cudaStream_t st);
+int sf_launch_step_col(const SfStepArgs& a, const SfSources& src, bool geom, int vec, int ich,
+                       cudaStream_t st);
 long long sf_energy_blocks(long long n);
 int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,
                      const uint8_t* flags, long long n, double* scratch, double* out2,
@@ -74,11 +76,11 @@ struct sf_plan {
 
 // Planes per block for the slab march: enough (j,k)-tile x i-chunk blocks
 // for about four waves of 8 resident blocks on each of the SMs.
-static int auto_chunk(const sf_plan* P) {
+static int auto_chunk(const sf_plan* P, int kspan) {
     int sms = 152;
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long tiles = (long long)((P->d.nz + 31) / 32) * ((P->d.ny + 7) / 8);
+    const long long tiles = (long long)((P->d.nz + kspan - 1) / kspan) * ((P->d.ny + 7) / 8);
     long long chunks = (4LL * 8 * sms + tiles - 1) / tiles;
     if (chunks < 1) chunks = 1;
     long long ich = (P->d.nx + chunks - 1) / chunks;
@@ -295,7 +297,7 @@ int sf_plan_set_ade(sf_plan* P, const uint8_t* mat, int n, const sf_pole* poles,
 
 int sf_plan_set_kernel(sf_plan* P, int variant, int i_chunk) {
     if (!P) return sf_fail("sf_plan_set_kernel: NULL plan");
-    if (variant < 0 || variant > 2) return sf_fail("sf_plan_set_kernel: variant must be 0, 1 or 2");
+    if (variant < 0 || variant > 4) return sf_fail("sf_plan_set_kernel: variant must be 0..4");
     if (i_chunk < 0) return sf_fail("sf_plan_set_kernel: negative i_chunk");
     P->variant = variant;
     P->i_chunk = i_chunk;
@@ -327,8 +329,12 @@ int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* t
     a.n_probe = trace ? P->n_probe : 0;
     a.probe_cells = P->probe_cells;
     a.mat = P->mat;
-    const bool march = P->poles.n == 0 && P->variant != 1;
-    const int ich = P->i_chunk > 0 ? P->i_chunk : auto_chunk(P);
+    // variant: 1 per-cell, 2 slab march, 3 columns (float4 when nz % 4 == 0),
+    // 4 columns (scalar); ADE poles always take the per-cell kernel
+    int variant = P->variant == 0 ? 3 : P->variant;
+    if (P->poles.n > 0) variant = 1;
+    const int vec = (variant == 3 && P->d.nz % 4 == 0) ? 4 : 1;
+    const int ich = P->i_chunk > 0 ? P->i_chunk : auto_chunk(P, 32 * vec);
     for (int64_t s = 0; s < n_steps; ++s) {
         const int in = P->cur, out = 1 - P->cur;
         a.p = P->f[in][0];
@@ -341,8 +347,11 @@ int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* t
         a.vzo = P->f[out][3];
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
         a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
-        const int rc = march ? sf_launch_step_march(a, P->src, P->flags != nullptr, ich, st)
-                             : sf_launch_step(a, P->src, P->poles, P->flags != nullptr, st);
+        const bool g = P->flags != nullptr;
+        int rc;
+        if (variant == 2) rc = sf_launch_step_march(a, P->src, g, ich, st);
+        else if (variant >= 3) rc = sf_launch_step_col(a, P->src, g, vec, ich, st);
+        else rc = sf_launch_step(a, P->src, P->poles, g, st);
         if (rc) return rc;
         P->cur = out;
     }

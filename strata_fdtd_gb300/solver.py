@@ -633,10 +633,12 @@ class FDTDSolver:
                               UserWarning, stacklevel=2)
 
     def set_kernel(self, variant: str = "auto", i_chunk: int = 0) -> None:
-        """Choose the step kernel: "auto" (slab march, per-cell kernel with
-        ADE), "cell" (one thread per cell) or "march" (2.5-D slab march with
-        ``i_chunk`` planes per block, 0 = automatic).  Results are identical."""
-        v = {"auto": 0, "cell": 1, "march": 2}[variant]
+        """Choose the step kernel: "auto", "cell" (one thread per cell),
+        "march" (2.5-D slab march with shared-memory halos), "col" (thread
+        columns along i, float4 along k when nz % 4 == 0) or "col1" (thread
+        columns, scalar); ``i_chunk`` planes per block (0 = automatic).  ADE
+        materials always use "cell".  Results are identical."""
+        v = {"auto": 0, "cell": 1, "march": 2, "col": 3, "col1": 4}[variant]
         _native.check(self._lib.sf_plan_set_kernel(self._plan, v, int(i_chunk)),
                       "sf_plan_set_kernel")
 

@@ -166,7 +166,8 @@ def test_random_cases_against_oracle(seed):
         np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
 
 
-@pytest.mark.parametrize("variant,i_chunk", [("cell", 0), ("march", 1), ("march", 3),
+@pytest.mark.parametrize("variant,i_chunk", [("cell", 0), ("march", 1), ("march", 3), ("col", 0),
+                                             ("col", 1), ("col", 5), ("col1", 0), ("col1", 2),
                                              ("march", 7), ("march", 0)])
 @pytest.mark.parametrize("seed", [0, 3, 5, 8])
 def test_kernel_variants_against_oracle(seed, variant, i_chunk):
@@ -185,7 +186,30 @@ def test_kernel_variants_against_oracle(seed, variant, i_chunk):
         np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
 
 
-@pytest.mark.parametrize("variant", ["cell", "march"])
+@pytest.mark.parametrize("shape,ich", [((9, 7, 8), 0), ((17, 21, 36), 0), ((12, 30, 132), 5),
+                                       ((40, 9, 8), 1), ((33, 40, 40), 0)])
+def test_col_float4_against_oracle(shape, ich):
+    """The float4 column kernel (nz % 4 == 0) with solids, a plane source
+    along k and sources on the float4 lane boundaries."""
+    case = dict(shape=shape, res=1e-3, courant=0.6, pml=dict(depth=2),
+                geometry=dict(kind="blocks", seed=sum(shape), n_boxes=2, n_spheres=1),
+                sources=[("point", (shape[0] // 2, shape[1] // 2, 3), 25000.0, 1.0),
+                         ("plane", {"axis": 2, "index": shape[2] - 1}, 15000.0, 0.7),
+                         ("point", (1, 1, 0), 30000.0, -1.0)],
+                probes=[("a", (shape[0] // 2, shape[1] // 2, shape[2] // 2)),
+                        ("b", (shape[0] - 1, shape[1] - 1, shape[2] - 1))], steps=70)
+    ref = C.build_case(ORACLE, case)
+    ref.run_steps(case["steps"])
+    s = C.build_case(API, case)
+    s.set_kernel("col", ich)
+    s.run_steps(case["steps"])
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f"{shape} {f}")
+    for name in ref.get_probe_data():
+        np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
+
+
+@pytest.mark.parametrize("variant", ["cell", "march", "col", "col1"])
 def test_c1_quick_start_both_kernels(variant, manifest):
     case = C.PLAIN_CASES["c1_full"]
     s = C.build_case(API, case)
