@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--size", type=int, default=400, help="grid edge (400 = the workload)")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "cell", "march", "col", "col1"])
+    ap.add_argument("--kernel", default="auto", help="auto (autotuned) or a kernel configuration name")
     ap.add_argument("--ichunk", type=int, default=0, help="planes per block (march)")
     return ap.parse_args()
 
@@ -239,7 +239,14 @@ def run_gpu(args):
     n_edge = args.size
     cells = n_edge ** 3
     s = enclosure(n_edge)
-    s.set_kernel(args.kernel, args.ichunk)
+    tune = None
+    if args.kernel == "auto":
+        s.set_kernel("auto", args.ichunk)
+        tune = s.autotune(launches=10)  # times each configuration; state unchanged
+        chosen = tune["best"]
+    else:
+        s.set_kernel(args.kernel, args.ichunk)
+        chosen = args.kernel
     inner, K, W = args.inner, args.steps, args.warmup
     n_src = len(s._sources)
     n_probe = len(s._probes)
@@ -324,15 +331,14 @@ def run_gpu(args):
             "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD if n_edge == 400 else f"enclosure at {n_edge}^3",
-                       "bench_step": f"{inner} FDTD time steps", "kernel": args.kernel,
-                       "i_chunk": args.ichunk,
+                       "bench_step": f"{inner} FDTD time steps", "kernel": chosen,
+                       "i_chunk": args.ichunk, "autotune_ms_per_step": tune,
                        "global_batch": world, "parallelism": f"replicas x{world}",
                        "l2": "state 1.1 GB per replica > 129 MB L2, no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_cell": BYTES_PER_CELL,
-                         "kernel": "fused step kernel (k_step_march, sf_step_march.cu)"
-                                   if args.kernel != "cell" else "k_step (sf_step.cu)"},
+                         "kernel": f"fused step kernel, configuration {chosen}"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "device": torch.cuda.get_device_name(local),
             "library": lib.sf_version().decode(),

@@ -147,13 +147,27 @@ int sf_plan_set_probes(sf_plan* plan, int n, const int64_t* cells);
 int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const sf_pole* poles,
                     float inv_dx);
 
-/* Step kernel choice: variant 0 = automatic (columns; the per-cell kernel
- * when ADE poles are set), 1 = one thread per cell, 2 = slab march along i
- * (shared-memory halos), 3 = thread columns along i (float4 along k when
- * nz % 4 == 0), 4 = thread columns, scalar.  i_chunk = planes per block for
- * 2-4 (0 = automatic).  All variants give identical results.  No
- * counterpart in the reference (its kernels are CPU loops). */
-int sf_plan_set_kernel(sf_plan* plan, int variant, int i_chunk);
+/* Step-kernel configuration.  config 0 = automatic (the autotuned
+ * configuration if sf_plan_autotune ran, else the default), 1 = one thread
+ * per cell, 2 = slab march along i with shared-memory halos, 3.. = thread
+ * columns along i in the variants named by sf_kernel_config_name (vector
+ * width, block rows, register cap, streaming stores; a vector width that
+ * does not divide nz falls back to scalar columns).  i_chunk = planes per
+ * block (0 = automatic).  ADE poles always run the per-cell kernel.  Every
+ * configuration gives identical results.  No counterpart in the reference
+ * (its kernels are CPU loops). */
+int sf_plan_set_kernel(sf_plan* plan, int config, int i_chunk);
+int sf_kernel_config_count(void);
+const char* sf_kernel_config_name(int config);
+
+/* Autotuner: times every configuration that fits the grid for `launches`
+ * step launches each (reading the current state and writing the other set
+ * without swapping, no sources, no probes -- the state is unchanged) and
+ * makes the fastest the plan's automatic choice.  ms_out (host, may be NULL)
+ * receives sf_kernel_config_count() per-launch times (-1 = not run);
+ * best_out (may be NULL) the chosen configuration.  Synchronises the stream.
+ * No counterpart in the reference. */
+int sf_plan_autotune(sf_plan* plan, int launches, void* stream, float* ms_out, int* best_out);
 
 /* Advance n_steps.  src_values_dev: device doubles [n_steps][n_sources]
  * (the waveform at each step's time; may be NULL when there are no
@@ -170,6 +184,7 @@ int sf_plan_step(sf_plan* plan, int64_t n_steps, const double* src_values_dev,
 int64_t sf_energy_scratch_doubles(const sf_plan* plan);
 int sf_plan_energy(sf_plan* plan, double rho, double c, double dx, double* scratch_dev,
                    double* out_host, void* stream);
+
 
 /* --- voxelisation -------------------------------------------------------- */
 /* mask[i,j,k] = sdf(cell centre) <= 0, cell centre = (i + 0.5)*res, as

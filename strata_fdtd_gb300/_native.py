@@ -112,6 +112,9 @@ SIGNATURES = {
     "sf_plan_set_probes": (_I, [_P, _I, _P]),
     "sf_plan_set_ade": (_I, [_P, _P, _I, _P, _F]),
     "sf_plan_set_kernel": (_I, [_P, _I, _I]),
+    "sf_kernel_config_count": (_I, []),
+    "sf_kernel_config_name": (ctypes.c_char_p, [_I]),
+    "sf_plan_autotune": (_I, [_P, _I, _P, _P, _P]),
     "sf_plan_step": (_I, [_P, _I64, _P, _P, _P]),
     "sf_energy_scratch_doubles": (_I64, [_P]),
     "sf_plan_energy": (_I, [_P, _D, _D, _D, _P, _P, _P]),

@@ -18,26 +18,12 @@
 #define SF_VERSION_STRING "0.1.0"
 #endif
 
-// launchers (sf_step.cu, sf_voxel.cu)
-int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, int nz,
-                          cudaStream_t st);
-int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& poles, bool geom,
-                   cudaStream_t st);
-int sf_launch_probe_gather(const float* p, const long long* cells, int n, float* out,
-                           cudaStream_t st);
-int sf_launch_step_march(const SfStepArgs& a, const SfSources& src, bool geom, int ich,
-                         cudaStream_t st);
-int sf_launch_step_col(const SfStepArgs& a, const SfSources& src, bool geom, int vec, int ich,
-                       cudaStream_t st);
-long long sf_energy_blocks(long long n);
-int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,
-                     const uint8_t* flags, long long n, double* scratch, double* out2,
-                     cudaStream_t st);
-int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny, int nz,
-                       double res, int invert, uint8_t* out, int* err_dev, cudaStream_t st);
+#include "sf_kernels.h"
 
-int sf_launch_sdf_points(const sf_sdf_node* prog_dev, int n_nodes, const double* pts, long long n,
-                         double* out, int* err_dev, cudaStream_t st);
+// Step-kernel configuration used when the plan has not been autotuned.
+#ifndef SF_CFG_DEFAULT
+#define SF_CFG_DEFAULT (SF_CFG_COL_FIRST + 0)
+#endif
 
 namespace {
 thread_local std::string g_err;
@@ -70,8 +56,9 @@ struct sf_plan {
     int n_probe = 0;
     SfPoles poles{};
     const uint8_t* mat = nullptr;  // caller-owned
-    int variant = 0;               // 0 auto, 1 per-cell, 2 slab march
-    int i_chunk = 0;               // planes per block in the slab march (0 = auto)
+    int variant = 0;               // kernel configuration (SF_CFG_*), 0 = auto
+    int i_chunk = 0;               // planes per block in march / column kernels (0 = auto)
+    int tuned = 0;                 // configuration chosen by sf_plan_autotune (0 = none)
 };
 
 // Planes per block for the slab march: enough (j,k)-tile x i-chunk blocks
@@ -295,27 +282,33 @@ int sf_plan_set_ade(sf_plan* P, const uint8_t* mat, int n, const sf_pole* poles,
     return 0;
 }
 
-int sf_plan_set_kernel(sf_plan* P, int variant, int i_chunk) {
+int sf_plan_set_kernel(sf_plan* P, int config, int i_chunk) {
     if (!P) return sf_fail("sf_plan_set_kernel: NULL plan");
-    if (variant < 0 || variant > 4) return sf_fail("sf_plan_set_kernel: variant must be 0..4");
+    if (config < 0 || config >= SF_CFG_COL_FIRST + kSfColConfigCount)
+        return sf_fail("sf_plan_set_kernel: unknown kernel configuration");
     if (i_chunk < 0) return sf_fail("sf_plan_set_kernel: negative i_chunk");
-    P->variant = variant;
+    P->variant = config;
     P->i_chunk = i_chunk;
     return 0;
 }
 
-int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* trace,
-                 void* stream) {
-    if (!P) return sf_fail("sf_plan_step: NULL plan");
-    if (!P->bound) return sf_fail("sf_plan_step: fields not bound");
-    if (n_steps < 0) return sf_fail("sf_plan_step: negative step count");
-    if (P->src.n > 0 && !src_values) return sf_fail("sf_plan_step: sources need src_values");
-    if (n_steps == 0) return 0;
-    DeviceGuard g(P->device);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    static const double kNoSources[SF_MAX_SOURCES] = {0};
-    (void)kNoSources;
-    SfStepArgs a{};
+int sf_kernel_config_count(void) { return SF_CFG_COL_FIRST + kSfColConfigCount; }
+
+const char* sf_kernel_config_name(int config) {
+    if (config == SF_CFG_AUTO) return "auto";
+    if (config == SF_CFG_CELL) return "cell";
+    if (config == SF_CFG_MARCH) return "march";
+    if (config >= SF_CFG_COL_FIRST && config < SF_CFG_COL_FIRST + kSfColConfigCount)
+        return kSfColConfigs[config - SF_CFG_COL_FIRST].name;
+    return nullptr;
+}
+
+}  // extern "C"
+
+namespace {
+
+void fill_args(const sf_plan* P, SfStepArgs& a, bool with_trace) {
+    a = SfStepArgs{};
     a.nx = P->d.nx;
     a.ny = P->d.ny;
     a.nz = P->d.nz;
@@ -326,38 +319,134 @@ int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* t
     a.dx = P->decay[0];
     a.dy = P->decay[1];
     a.dz = P->decay[2];
-    a.n_probe = trace ? P->n_probe : 0;
+    a.n_probe = with_trace ? P->n_probe : 0;
     a.probe_cells = P->probe_cells;
     a.mat = P->mat;
-    // variant: 1 per-cell, 2 slab march, 3 columns (float4 when nz % 4 == 0),
-    // 4 columns (scalar); ADE poles always take the per-cell kernel
-    int variant = P->variant == 0 ? 3 : P->variant;
-    if (P->poles.n > 0) variant = 1;
-    const int vec = (variant == 3 && P->d.nz % 4 == 0) ? 4 : 1;
-    const int ich = P->i_chunk > 0 ? P->i_chunk : auto_chunk(P, 32 * vec);
+}
+
+void set_io(const sf_plan* P, SfStepArgs& a, int in) {
+    const int out = 1 - in;
+    a.p = P->f[in][0];
+    a.vx = P->f[in][1];
+    a.vy = P->f[in][2];
+    a.vz = P->f[in][3];
+    a.po = P->f[out][0];
+    a.vxo = P->f[out][1];
+    a.vyo = P->f[out][2];
+    a.vzo = P->f[out][3];
+}
+
+// The configuration a step of this plan runs: ADE poles need the per-cell
+// kernel; otherwise the explicit choice, else the autotuned one, else the
+// default.
+int effective_config(const sf_plan* P) {
+    if (P->poles.n > 0) return SF_CFG_CELL;
+    if (P->variant != SF_CFG_AUTO) return P->variant;
+    return P->tuned > 0 ? P->tuned : SF_CFG_DEFAULT;
+}
+
+int chunk_for(const sf_plan* P, int cfg) {
+    if (P->i_chunk > 0) return P->i_chunk;
+    int kspan = 32;
+    if (cfg >= SF_CFG_COL_FIRST) {
+        const int vec = kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec;
+        if (P->d.nz % vec == 0) kspan = 32 * vec;
+    }
+    return auto_chunk(P, kspan);
+}
+
+int launch_config(const sf_plan* P, int cfg, int ich, const SfStepArgs& a, const SfSources& src,
+                  cudaStream_t st) {
+    const bool g = P->flags != nullptr;
+    if (cfg == SF_CFG_MARCH) return sf_launch_step_march(a, src, g, ich, st);
+    if (cfg >= SF_CFG_COL_FIRST)
+        return sf_launch_step_col_cfg(a, src, g, cfg - SF_CFG_COL_FIRST, ich, st);
+    return sf_launch_step(a, src, P->poles, g, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* trace,
+                 void* stream) {
+    if (!P) return sf_fail("sf_plan_step: NULL plan");
+    if (!P->bound) return sf_fail("sf_plan_step: fields not bound");
+    if (n_steps < 0) return sf_fail("sf_plan_step: negative step count");
+    if (P->src.n > 0 && !src_values) return sf_fail("sf_plan_step: sources need src_values");
+    if (n_steps == 0) return 0;
+    DeviceGuard g(P->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SfStepArgs a;
+    fill_args(P, a, trace != nullptr);
+    const int cfg = effective_config(P);
+    const int ich = chunk_for(P, cfg);
     for (int64_t s = 0; s < n_steps; ++s) {
-        const int in = P->cur, out = 1 - P->cur;
-        a.p = P->f[in][0];
-        a.vx = P->f[in][1];
-        a.vy = P->f[in][2];
-        a.vz = P->f[in][3];
-        a.po = P->f[out][0];
-        a.vxo = P->f[out][1];
-        a.vyo = P->f[out][2];
-        a.vzo = P->f[out][3];
+        set_io(P, a, P->cur);
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
         a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
-        const bool g = P->flags != nullptr;
-        int rc;
-        if (variant == 2) rc = sf_launch_step_march(a, P->src, g, ich, st);
-        else if (variant >= 3) rc = sf_launch_step_col(a, P->src, g, vec, ich, st);
-        else rc = sf_launch_step(a, P->src, P->poles, g, st);
-        if (rc) return rc;
-        P->cur = out;
+        if (int rc = launch_config(P, cfg, ich, a, P->src, st)) return rc;
+        P->cur = 1 - P->cur;
     }
     if (trace && P->n_probe > 0)
         return sf_launch_probe_gather(P->f[P->cur][0], P->probe_cells, P->n_probe,
                                       trace + (n_steps - 1) * P->n_probe, st);
+    return 0;
+}
+
+int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int* best_out) {
+    if (!P) return sf_fail("sf_plan_autotune: NULL plan");
+    if (!P->bound) return sf_fail("sf_plan_autotune: fields not bound");
+    if (launches < 1) launches = 1;
+    DeviceGuard g(P->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int count = SF_CFG_COL_FIRST + kSfColConfigCount;
+    if (ms_out)
+        for (int q = 0; q < count; ++q) ms_out[q] = -1.0f;
+    if (P->poles.n > 0) {  // ADE runs the per-cell kernel only
+        P->tuned = SF_CFG_CELL;
+        if (best_out) *best_out = SF_CFG_CELL;
+        return 0;
+    }
+    // Every trial reads the current set and writes the other one without
+    // swapping, with no sources and no probes: the state is untouched, and the
+    // next real step overwrites the other set entirely.
+    SfStepArgs a;
+    fill_args(P, a, false);
+    set_io(P, a, P->cur);
+    const SfSources none{};
+    cudaEvent_t e0, e1;
+    SF_CUDA_OK(cudaEventCreate(&e0));
+    SF_CUDA_OK(cudaEventCreate(&e1));
+    int best = 0;
+    float best_ms = 0.0f;
+    int rc = 0;
+    for (int cfg = SF_CFG_CELL; cfg < count && !rc; ++cfg) {
+        if (cfg >= SF_CFG_COL_FIRST && P->d.nz % kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec != 0)
+            continue;
+        const int ich = chunk_for(P, cfg);
+        if ((rc = launch_config(P, cfg, ich, a, none, st))) break;  // warm-up
+        if (cudaEventRecord(e0, st) != cudaSuccess) { rc = sf_fail("event record failed"); break; }
+        for (int q = 0; q < launches && !rc; ++q) rc = launch_config(P, cfg, ich, a, none, st);
+        if (rc) break;
+        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = sf_fail("sf_plan_autotune: timing failed");
+            break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= launches;
+        if (ms_out) ms_out[cfg] = ms;
+        if (best == 0 || ms < best_ms) {
+            best = cfg;
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    P->tuned = best;
+    if (best_out) *best_out = best;
     return 0;
 }
 

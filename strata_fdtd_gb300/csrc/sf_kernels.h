@@ -1,0 +1,36 @@
+// sf_kernels.h -- internal launcher declarations shared by the .cu files.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sf_common.cuh"
+
+// Step-kernel configuration indices used by sf_plan_set_kernel /
+// sf_plan_autotune: 0 = automatic, 1 = per-cell kernel, 2 = slab march,
+// SF_CFG_COL_FIRST + c = column kernel configuration c.
+enum { SF_CFG_AUTO = 0, SF_CFG_CELL = 1, SF_CFG_MARCH = 2, SF_CFG_COL_FIRST = 3 };
+
+struct SfColConfig {
+    int vec, by, minb, cs;
+    const char* name;
+};
+extern const SfColConfig kSfColConfigs[];
+extern const int kSfColConfigCount;
+
+int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, int nz,
+                          cudaStream_t st);
+int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& poles, bool geom,
+                   cudaStream_t st);
+int sf_launch_probe_gather(const float* p, const long long* cells, int n, float* out,
+                           cudaStream_t st);
+int sf_launch_step_march(const SfStepArgs& a, const SfSources& src, bool geom, int ich,
+                         cudaStream_t st);
+int sf_launch_step_col_cfg(const SfStepArgs& a, const SfSources& src, bool geom, int cfg, int ich,
+                           cudaStream_t st);
+long long sf_energy_blocks(long long n);
+int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,
+                     const uint8_t* flags, long long n, double* scratch, double* out2,
+                     cudaStream_t st);
+int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny, int nz,
+                       double res, int invert, uint8_t* out, int* err_dev, cudaStream_t st);
+int sf_launch_sdf_points(const sf_sdf_node* prog_dev, int n_nodes, const double* pts, long long n,
+                         double* out, int* err_dev, cudaStream_t st);

@@ -2,49 +2,35 @@
 //
 // Same per-cell arithmetic as k_step (sf_step.cu), which restates the
 // reference passes listed there.  Each thread owns VEC consecutive cells
-// along k (VEC = 4: one float4 per field, needs nz % 4 == 0) in one j row,
-// and walks a chunk of i planes with no block barrier:
-//   * p(i+1) and the plane-(i+1) velocities and flags are loaded one plane
+// along k (VEC = 2 / 4: one float2 / float4 per field, needs nz % VEC == 0)
+// in one j row, and walks a chunk of i planes with no block barrier:
+//   * the plane-(i+1) velocities and flags and p(i+2) are loaded one step
 //     ahead, so their latency overlaps the current plane's arithmetic;
 //   * the new x-face velocity and the pressure of plane i are carried in
 //     registers into plane i+1;
 //   * j +- 1 and k +- 1 neighbours are read straight from global memory and
-//     mostly hit L1 (the neighbouring threads of the block read the same
-//     lines in the same plane).
+//     mostly hit L1 (the block's other threads read the same lines).
 // DRAM traffic per cell and step: 17 bytes read (p, vx, vy, vz, flags) and
-// 16 written, plus one plane of re-reads per chunk.
+// 16 written, plus one plane of re-reads per chunk of i planes.
+//
+// The family is templated on the vector width, the block height (rows of 32
+// threads), a minimum resident-block count (register cap) and streaming
+// (evict-first) stores; sf_plan_autotune picks the fastest for a grid.
 #include <cuda_runtime.h>
 
 #include "sf_common.cuh"
+#include "sf_kernels.h"
 
 namespace {
-
-constexpr int CX = 32;  // threads along k
-constexpr int CY = 8;   // threads along j
-
-template <int VEC>
-struct VecT;
-template <>
-struct VecT<1> {
-    using F = float;
-    using B = uint8_t;
-};
-template <>
-struct VecT<4> {
-    using F = float4;
-    using B = uchar4;
-};
-
-__device__ __forceinline__ float ld(const float* p, long long i) { return __ldg(p + i); }
 
 template <int VEC>
 __device__ __forceinline__ void load_f(const float* __restrict__ base, long long c, float (&v)[VEC]) {
     if constexpr (VEC == 4) {
         const float4 t = __ldg(reinterpret_cast<const float4*>(base + c));
-        v[0] = t.x;
-        v[1] = t.y;
-        v[2] = t.z;
-        v[3] = t.w;
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (VEC == 2) {
+        const float2 t = __ldg(reinterpret_cast<const float2*>(base + c));
+        v[0] = t.x; v[1] = t.y;
     } else {
         v[0] = __ldg(base + c);
     }
@@ -55,34 +41,41 @@ __device__ __forceinline__ void load_b(const uint8_t* __restrict__ base, long lo
                                        uint8_t (&v)[VEC]) {
     if constexpr (VEC == 4) {
         const uchar4 t = __ldg(reinterpret_cast<const uchar4*>(base + c));
-        v[0] = t.x;
-        v[1] = t.y;
-        v[2] = t.z;
-        v[3] = t.w;
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (VEC == 2) {
+        const uchar2 t = __ldg(reinterpret_cast<const uchar2*>(base + c));
+        v[0] = t.x; v[1] = t.y;
     } else {
         v[0] = __ldg(base + c);
     }
 }
 
-template <int VEC>
+template <int VEC, bool CS>
 __device__ __forceinline__ void store_f(float* __restrict__ base, long long c, const float (&v)[VEC]) {
     if constexpr (VEC == 4) {
-        *reinterpret_cast<float4*>(base + c) = make_float4(v[0], v[1], v[2], v[3]);
+        const float4 t = make_float4(v[0], v[1], v[2], v[3]);
+        if (CS) __stcs(reinterpret_cast<float4*>(base + c), t);
+        else *reinterpret_cast<float4*>(base + c) = t;
+    } else if constexpr (VEC == 2) {
+        const float2 t = make_float2(v[0], v[1]);
+        if (CS) __stcs(reinterpret_cast<float2*>(base + c), t);
+        else *reinterpret_cast<float2*>(base + c) = t;
     } else {
-        base[c] = v[0];
+        if (CS) __stcs(base + c, v[0]);
+        else base[c] = v[0];
     }
 }
 
-template <bool GEOM, int VEC>
-__global__ void __launch_bounds__(CX* CY) k_step_col(SfStepArgs a, SfSources src, int ich) {
-    const int k = (blockIdx.x * CX + threadIdx.x) * VEC;
-    const int j = blockIdx.y * CY + threadIdx.y;
+template <bool GEOM, int VEC, int BY, int MINB, bool CS>
+__global__ void __launch_bounds__(32 * BY, MINB) k_step_col(SfStepArgs a, SfSources src, int ich) {
+    const int k = (blockIdx.x * 32 + threadIdx.x) * VEC;
+    const int j = blockIdx.y * BY + threadIdx.y;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int i0 = blockIdx.z * ich;
     const int i1 = min(i0 + ich, nx);
 
     if (a.trace_prev != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) {
-        for (int t = threadIdx.y * CX + threadIdx.x; t < a.n_probe; t += CX * CY)
+        for (int t = threadIdx.y * 32 + threadIdx.x; t < a.n_probe; t += 32 * BY)
             a.trace_prev[t] = a.p[a.probe_cells[t]];
     }
     if (k >= nz || j >= ny) return;
@@ -104,14 +97,18 @@ __global__ void __launch_bounds__(CX* CY) k_step_col(SfStepArgs a, SfSources src
         load_f<VEC>(a.vx, c, vx);
         load_f<VEC>(a.vy, c, vy);
         load_f<VEC>(a.vz, c, vz);
-        if (GEOM) load_b<VEC>(a.flags, c, fc);
-        else
+        if (GEOM) {
+            load_b<VEC>(a.flags, c, fc);
+        } else {
 #pragma unroll
             for (int e = 0; e < VEC; ++e) fc[e] = SF_ALL;
-        if (i0 + 1 < nx) load_f<VEC>(a.p, c + plane, pn);
-        else
+        }
+        if (i0 + 1 < nx) {
+            load_f<VEC>(a.p, c + plane, pn);
+        } else {
 #pragma unroll
             for (int e = 0; e < VEC; ++e) pn[e] = 0.0f;
+        }
 #pragma unroll
         for (int e = 0; e < VEC; ++e) vxm[e] = 0.0f;
         if (i0 > 0) {  // chunk start: low x face from plane i0-1
@@ -158,11 +155,11 @@ __global__ void __launch_bounds__(CX* CY) k_step_col(SfStepArgs a, SfSources src
         float pkm = 0.0f, vzkm = 0.0f, pkp = 0.0f;
         uint8_t fkm = SF_ALL;
         if (has_km) {
-            pkm = ld(a.p, c - 1);
-            vzkm = ld(a.vz, c - 1);
+            pkm = __ldg(a.p + c - 1);
+            vzkm = __ldg(a.vz + c - 1);
             if (GEOM) fkm = __ldg(a.flags + c - 1);
         }
-        if (has_kp) pkp = ld(a.p, c + VEC);
+        if (has_kp) pkp = __ldg(a.p + c + VEC);
 
         float ux[VEC], uy[VEC], uz[VEC], uym[VEC], uzm[VEC];
 #pragma unroll
@@ -222,10 +219,10 @@ __global__ void __launch_bounds__(CX* CY) k_step_col(SfStepArgs a, SfSources src
             }
             po[e] = pnew;
         }
-        store_f<VEC>(a.vxo, c, ox);
-        store_f<VEC>(a.vyo, c, oy);
-        store_f<VEC>(a.vzo, c, oz);
-        store_f<VEC>(a.po, c, po);
+        store_f<VEC, CS>(a.vxo, c, ox);
+        store_f<VEC, CS>(a.vyo, c, oy);
+        store_f<VEC, CS>(a.vzo, c, oz);
+        store_f<VEC, CS>(a.po, c, po);
 
 #pragma unroll
         for (int e = 0; e < VEC; ++e) {
@@ -240,21 +237,48 @@ __global__ void __launch_bounds__(CX* CY) k_step_col(SfStepArgs a, SfSources src
     }
 }
 
+template <int VEC, int BY, int MINB, bool CS>
+int launch(const SfStepArgs& a, const SfSources& src, bool geom, int ich, cudaStream_t st) {
+    const int kthreads = (a.nz + VEC - 1) / VEC;
+    dim3 blk(32, BY, 1);
+    dim3 grd((kthreads + 31) / 32, (a.ny + BY - 1) / BY, (a.nx + ich - 1) / ich);
+    if (geom) k_step_col<true, VEC, BY, MINB, CS><<<grd, blk, 0, st>>>(a, src, ich);
+    else k_step_col<false, VEC, BY, MINB, CS><<<grd, blk, 0, st>>>(a, src, ich);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step_col launch failed");
+}
+
 }  // namespace
 
-int sf_launch_step_col(const SfStepArgs& a, const SfSources& src, bool geom, int vec, int ich,
-                       cudaStream_t st) {
+// Column-kernel configurations (index = SF_CFG_COL_FIRST + position).
+const SfColConfig kSfColConfigs[] = {
+    // vec, by, minb, cs, name
+    {1, 8, 1, 0, "col1"},
+    {4, 8, 1, 0, "col4"},
+    {1, 8, 8, 1, "col1_b8_m8_cs"},
+    {1, 16, 4, 1, "col1_b16_m4_cs"},
+    {1, 4, 16, 1, "col1_b4_m16_cs"},
+    {2, 8, 6, 1, "col2_b8_m6_cs"},
+    {2, 4, 12, 1, "col2_b4_m12_cs"},
+    {4, 8, 4, 1, "col4_b8_m4_cs"},
+    {4, 4, 8, 1, "col4_b4_m8_cs"},
+};
+const int kSfColConfigCount = sizeof(kSfColConfigs) / sizeof(kSfColConfigs[0]);
+
+int sf_launch_step_col_cfg(const SfStepArgs& a, const SfSources& src, bool geom, int cfg, int ich,
+                           cudaStream_t st) {
     if (ich < 1) ich = 1;
-    if (vec == 4 && (a.nz % 4) != 0) return sf_fail("k_step_col<4> needs nz % 4 == 0");
-    const int kthreads = (a.nz + vec - 1) / vec;
-    dim3 blk(CX, CY, 1);
-    dim3 grd((kthreads + CX - 1) / CX, (a.ny + CY - 1) / CY, (a.nx + ich - 1) / ich);
-    if (vec == 4) {
-        if (geom) k_step_col<true, 4><<<grd, blk, 0, st>>>(a, src, ich);
-        else k_step_col<false, 4><<<grd, blk, 0, st>>>(a, src, ich);
-    } else {
-        if (geom) k_step_col<true, 1><<<grd, blk, 0, st>>>(a, src, ich);
-        else k_step_col<false, 1><<<grd, blk, 0, st>>>(a, src, ich);
+    if (cfg < 0 || cfg >= kSfColConfigCount) return sf_fail("k_step_col: bad configuration");
+    if (a.nz % kSfColConfigs[cfg].vec != 0) cfg = 0;  // vector width must divide nz
+    switch (cfg) {
+        case 0: return launch<1, 8, 1, false>(a, src, geom, ich, st);
+        case 1: return launch<4, 8, 1, false>(a, src, geom, ich, st);
+        case 2: return launch<1, 8, 8, true>(a, src, geom, ich, st);
+        case 3: return launch<1, 16, 4, true>(a, src, geom, ich, st);
+        case 4: return launch<1, 4, 16, true>(a, src, geom, ich, st);
+        case 5: return launch<2, 8, 6, true>(a, src, geom, ich, st);
+        case 6: return launch<2, 4, 12, true>(a, src, geom, ich, st);
+        case 7: return launch<4, 8, 4, true>(a, src, geom, ich, st);
+        case 8: return launch<4, 4, 8, true>(a, src, geom, ich, st);
     }
-    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step_col launch failed");
+    return sf_fail("k_step_col: bad configuration");
 }

@@ -100,6 +100,12 @@ def step_coefficients(grid, c: float, rho: float, courant: float):
     return dt, coeff_v, coeff_p
 
 
+def kernel_configs() -> list[str]:
+    """Names of the step-kernel configurations, by configuration index."""
+    lib = _native.load()
+    return [lib.sf_kernel_config_name(q).decode() for q in range(lib.sf_kernel_config_count())]
+
+
 def has_native_kernels() -> bool:
     """True when a CUDA device is present and the sm_103a library loads."""
     try:
@@ -633,14 +639,35 @@ class FDTDSolver:
                               UserWarning, stacklevel=2)
 
     def set_kernel(self, variant: str = "auto", i_chunk: int = 0) -> None:
-        """Choose the step kernel: "auto", "cell" (one thread per cell),
-        "march" (2.5-D slab march with shared-memory halos), "col" (thread
-        columns along i, float4 along k when nz % 4 == 0) or "col1" (thread
-        columns, scalar); ``i_chunk`` planes per block (0 = automatic).  ADE
-        materials always use "cell".  Results are identical."""
-        v = {"auto": 0, "cell": 1, "march": 2, "col": 3, "col1": 4}[variant]
-        _native.check(self._lib.sf_plan_set_kernel(self._plan, v, int(i_chunk)),
+        """Choose the step kernel by name: "auto", "cell" (one thread per
+        cell), "march" (2.5-D slab march with shared-memory halos), "col"
+        (thread columns along i, float4 along k when nz % 4 == 0), "col1"
+        (scalar columns) or any name from :func:`kernel_configs`;
+        ``i_chunk`` planes per block (0 = automatic).  ADE materials always
+        use "cell".  Results are identical."""
+        names = kernel_configs()
+        name = "col4" if variant == "col" else variant
+        if name not in names:
+            raise ValueError(f"unknown kernel {variant!r}; choose from {names}")
+        _native.check(self._lib.sf_plan_set_kernel(self._plan, names.index(name), int(i_chunk)),
                       "sf_plan_set_kernel")
+
+    def autotune(self, launches: int = 20) -> dict:
+        """Time every kernel configuration on this grid (the state is left
+        unchanged) and make the fastest the automatic choice.  Returns
+        {name: ms per step} and the chosen name under "best"."""
+        import ctypes as C
+
+        self._sync_tables()
+        self._upload_exposed()
+        names = kernel_configs()
+        ms = (C.c_float * len(names))()
+        best = C.c_int()
+        _native.check(self._lib.sf_plan_autotune(self._plan, int(launches), self._stream(),
+                                                 ms, C.byref(best)), "sf_plan_autotune")
+        out = {n: float(ms[q]) for q, n in enumerate(names) if ms[q] >= 0}
+        out["best"] = names[best.value]
+        return out
 
     def synchronize(self) -> None:
         self._torch.cuda.synchronize(self._device)

@@ -209,6 +209,41 @@ def test_col_float4_against_oracle(shape, ich):
         np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
 
 
+@pytest.mark.parametrize("config", S.solver.kernel_configs()[1:])
+def test_every_kernel_config_against_oracle(config):
+    """Each column-kernel configuration (vector width, rows, register cap,
+    streaming stores) on a float4-compatible grid and an odd one."""
+    for shape in ((20, 18, 36), (15, 13, 22)):
+        case = dict(shape=shape, res=1e-3, courant=0.55, pml=dict(depth=3),
+                    geometry=dict(kind="blocks", seed=shape[2], n_boxes=2, n_spheres=1),
+                    sources=[("point", (5, 6, 7), 25000.0, 1.0),
+                             ("plane", {"axis": 1, "index": 2}, 12000.0, 0.3)],
+                    probes=[("a", (10, 9, 11))], steps=45)
+        ref = C.build_case(ORACLE, case)
+        ref.run_steps(case["steps"])
+        s = C.build_case(API, case)
+        s.set_kernel(config, 3 if shape[0] == 15 else 0)
+        s.run_steps(case["steps"])
+        for f in ("p", "vx", "vy", "vz"):
+            np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f"{config} {f}")
+        np.testing.assert_array_equal(s.get_probe_data()["a"], ref.get_probe_data()["a"])
+
+
+def test_autotune_leaves_state_unchanged():
+    case = C.PLAIN_CASES["blocks_odd"]
+    a = C.build_case(API, case)
+    b = C.build_case(API, case)
+    a.run_steps(50)
+    b.run_steps(50)
+    table = a.autotune(launches=3)
+    assert table["best"] in S.solver.kernel_configs()
+    assert all(v > 0 for k, v in table.items() if k != "best")
+    a.run_steps(40)
+    b.run_steps(40)
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f))
+
+
 @pytest.mark.parametrize("variant", ["cell", "march", "col", "col1"])
 def test_c1_quick_start_both_kernels(variant, manifest):
     case = C.PLAIN_CASES["c1_full"]
