@@ -185,6 +185,19 @@ int64_t sf_energy_scratch_doubles(const sf_plan* plan);
 int sf_plan_energy(sf_plan* plan, double rho, double c, double dx, double* scratch_dev,
                    double* out_host, void* stream);
 
+/* The same energy for callers that cannot allocate device memory when they
+ * need the number (a process whose HBM another caching allocator holds, or
+ * a real-time loop that must not call cudaMalloc / cudaFree).  No
+ * counterpart in the reference.  It allocates nothing: its scratch is a
+ * fixed 4096-double (32 KiB) array in the library's device image, present
+ * on every GPU that loads the library until exit.  The first call on a
+ * device looks the array's device address up (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture
+ * begins.  Calls share the array: two calls whose work
+ * overlaps on the GPU race.  Refuses (nonzero status) a reduction that would
+ * need more than the 4096 doubles.  Synchronises the stream. */
+int sf_plan_energy_noalloc(sf_plan* plan, double rho, double c, double dx, double* out_host,
+                           void* stream);
 
 /* --- voxelisation -------------------------------------------------------- */
 /* mask[i,j,k] = sdf(cell centre) <= 0, cell centre = (i + 0.5)*res, as

@@ -118,6 +118,7 @@ SIGNATURES = {
     "sf_plan_step": (_I, [_P, _I64, _P, _P, _P]),
     "sf_energy_scratch_doubles": (_I64, [_P]),
     "sf_plan_energy": (_I, [_P, _D, _D, _D, _P, _P, _P]),
+    "sf_plan_energy_noalloc": (_I, [_P, _D, _D, _D, _P, _P]),
     "sf_voxelize": (_I, [_P, _I, _I, _I, _I, _D, _I, _P, _P]),
     "sf_sdf_eval": (_I, [_P, _I, _P, _I64, _P, _P]),
 }

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -522,3 +523,76 @@ int sf_sdf_eval(const sf_sdf_node* nodes, int n_nodes, const double* points_dev,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Energy without any device allocation.
+//
+// Some callers cannot allocate device memory at the moment they want an
+// energy reading: a host whose HBM is already reserved by another caching
+// allocator (a PyTorch process, say), where a fresh cudaMalloc can fail or
+// force that allocator to release its cache; or a real-time loop (an audio
+// or auralisation callback) that must not take cudaMalloc / cudaFree, which
+// can synchronise the whole device and stall for milliseconds.  For them the
+// energy reduction runs with its scratch in a fixed array that lives in the
+// library's device image: SF_NOALLOC_ENERGY_DOUBLES doubles (32 KiB), held by
+// every GPU that loads the library until the process exits.
+//
+// The reduction needs 2 partial sums per block plus 2 totals; its block
+// count is capped at 8 per SM (1216 on a 152-SM GB300), so every grid size
+// fits; a device with so many SMs that it would not fit is refused with an
+// error.  Every partial-sum slot is written before it is read, so nothing
+// has to be cleared between calls.  All calls share the one array per
+// device: calls whose kernels overlap on the GPU (two streams at once) race
+// and must not be issued.
+#define SF_NOALLOC_ENERGY_DOUBLES 4096
+#define SF_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) double g_sf_noalloc_energy[SF_NOALLOC_ENERGY_DOUBLES];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[SF_NOALLOC_MAX_DEVICES] = {nullptr};
+
+// Device address of the array on device `dev`, looked up once per device with
+// that device current, by the first sf_plan_energy_noalloc call on that
+// device (make that call before any stream capture begins).  In host code the
+// array's name is only a host-side stand-in; the kernel must be given this
+// address.
+int noalloc_scratch(int dev, double** out) {
+    if (dev < 0 || dev >= SF_NOALLOC_MAX_DEVICES)
+        return sf_fail("sf_plan_energy_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_sf_noalloc_energy);
+        if (e != cudaSuccess) return sf_fail_cuda(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
+        g_noalloc_addr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return 0;
+}
+}  // namespace
+
+extern "C" int sf_plan_energy_noalloc(sf_plan* P, double rho, double c, double dx,
+                                      double* out_host, void* stream) {
+    if (!P || !out_host) return sf_fail("sf_plan_energy_noalloc: NULL argument");
+    if (!P->bound) return sf_fail("sf_plan_energy_noalloc: fields not bound");
+    DeviceGuard g(P->device);
+    const long long nb = sf_energy_blocks(P->n);
+    if (2 * nb + 2 > SF_NOALLOC_ENERGY_DOUBLES)
+        return sf_fail("sf_plan_energy_noalloc: reduction needs more than the 4096-double "
+                       "fixed scratch");
+    double* scratch = nullptr;
+    if (int rc = noalloc_scratch(P->device, &scratch)) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float* const* f = P->f[P->cur];
+    if (int rc = sf_launch_energy(f[0], f[1], f[2], f[3], P->flags, P->n, scratch,
+                                  scratch + 2 * nb, st))
+        return rc;
+    double sums[2];
+    SF_CUDA_OK(cudaMemcpyAsync(sums, scratch + 2 * nb, sizeof(sums), cudaMemcpyDeviceToHost, st));
+    SF_CUDA_OK(cudaStreamSynchronize(st));
+    const double dV = dx * dx * dx;
+    *out_host = 0.5 * sums[0] / (rho * c * c) * dV + 0.5 * rho * sums[1] * dV;
+    return 0;
+}
