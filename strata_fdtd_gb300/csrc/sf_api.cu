@@ -60,6 +60,7 @@ struct sf_plan {
     int variant = 0;               // kernel configuration (SF_CFG_*), 0 = auto
     int i_chunk = 0;               // planes per block in march / column kernels (0 = auto)
     int tuned = 0;                 // configuration chosen by sf_plan_autotune (0 = none)
+    long long steps_done = 0;      // steps issued so far (alternates the chunk order)
 };
 
 // Planes per block for the slab march: enough (j,k)-tile x i-chunk blocks
@@ -386,8 +387,10 @@ int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* t
         set_io(P, a, P->cur);
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
         a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
+        a.reverse = (int)(P->steps_done & 1);
         if (int rc = launch_config(P, cfg, ich, a, P->src, st)) return rc;
         P->cur = 1 - P->cur;
+        ++P->steps_done;
     }
     if (trace && P->n_probe > 0)
         return sf_launch_probe_gather(P->f[P->cur][0], P->probe_cells, P->n_probe,

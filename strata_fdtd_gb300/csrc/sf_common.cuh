@@ -62,6 +62,7 @@ struct SfStepArgs {
     const long long* __restrict__ probe_cells;
     float* __restrict__ trace_prev;  // probe values of the input state, or null
     const uint8_t* __restrict__ mat;  // ADE material ids (ADE kernels only)
+    int reverse;                      // column kernels: dispatch i-chunks high to low
 };
 
 #define SF_CUDA_OK(expr)                                                   \

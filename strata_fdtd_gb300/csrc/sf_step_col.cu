@@ -71,7 +71,10 @@ __global__ void __launch_bounds__(32 * BY, MINB) k_step_col(SfStepArgs a, SfSour
     const int k = (blockIdx.x * 32 + threadIdx.x) * VEC;
     const int j = blockIdx.y * BY + threadIdx.y;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const int i0 = blockIdx.z * ich;
+    // On alternate steps the chunks are dispatched from high i to low i, so a
+    // step starts on the planes the previous step wrote last (still in L2).
+    const int chunk = a.reverse ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z;
+    const int i0 = chunk * ich;
     const int i1 = min(i0 + ich, nx);
 
     if (a.trace_prev != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) {
@@ -88,6 +91,19 @@ __global__ void __launch_bounds__(32 * BY, MINB) k_step_col(SfStepArgs a, SfSour
 #pragma unroll
     for (int e = 0; e < VEC; ++e) dk[e] = a.dz[k + e];
     const bool has_jm = j > 0, has_jp = j < ny - 1, has_km = k > 0, has_kp = k + VEC < nz;
+    // Sources that can reach this thread's column of cells, in source order:
+    // a point source in this (j, k) range, a plane across i, a plane at this
+    // j, or a plane at one of this thread's k.
+    unsigned smask = 0;
+    for (int q = 0; q < src.n; ++q) {
+        const sf_source& S = src.s[q];
+        bool can;
+        if (S.kind == 0) can = (S.b == j) && (S.c >= k) && (S.c < k + VEC);
+        else if (S.a == 0) can = true;
+        else if (S.a == 1) can = (S.b == j);
+        else can = (S.b >= k) && (S.b < k + VEC);
+        if (can) smask |= 1u << q;
+    }
 
     float pc[VEC], pn[VEC], vx[VEC], vy[VEC], vz[VEC], vxm[VEC];
     uint8_t fc[VEC];
@@ -207,15 +223,17 @@ __global__ void __launch_bounds__(32 * BY, MINB) k_step_col(SfStepArgs a, SfSour
             oy[e] = f_mul(uy[e], dj);
             oz[e] = f_mul(uz[e], dk[e]);
             pnew = f_mul(f_mul(f_mul(pnew, di), dj), dk[e]);
-#pragma unroll 1
-            for (int q = 0; q < src.n; ++q) {
-                const sf_source& S = src.s[q];
-                bool hit;
-                if (S.kind == 0)
-                    hit = (i == S.a) && (j == S.b) && (k + e == S.c);
-                else
-                    hit = (S.a == 0) ? (i == S.b) : ((S.a == 1) ? (j == S.b) : (k + e == S.b));
-                if (hit && air) pnew = __double2float_rn(d_add((double)pnew, a.src_val[q]));
+            if (smask != 0) {
+                for (unsigned m = smask; m != 0; m &= m - 1) {
+                    const int q = __ffs(m) - 1;
+                    const sf_source& S = src.s[q];
+                    bool hit;
+                    if (S.kind == 0)
+                        hit = (i == S.a) && (k + e == S.c);
+                    else
+                        hit = (S.a == 0) ? (i == S.b) : ((S.a == 1) ? true : (k + e == S.b));
+                    if (hit && air) pnew = __double2float_rn(d_add((double)pnew, a.src_val[q]));
+                }
             }
             po[e] = pnew;
         }
