@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--size", type=int, default=400, help="grid edge (400 = the workload)")
     ap.add_argument("--kernel", default="auto", help="auto (autotuned) or a kernel configuration name")
     ap.add_argument("--ichunk", type=int, default=0, help="planes per block (march)")
+    ap.add_argument("--workload", default="enclosure", choices=["enclosure", "batch"])
+    ap.add_argument("--batch-solves", type=int, default=64)
+    ap.add_argument("--graph-steps", type=int, default=50)
     return ap.parse_args()
 
 
@@ -348,10 +351,83 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_batch(args):
+    """The heterogeneous batch: 64 grids (edges 64-256), solids, a 2-pole
+    Debye block each, 500-3000 steps; batched persistent launches under CUDA
+    graphs vs the same solves one after another through the single-grid path.
+    Both produce bit-identical results (tests/test_gpu_batch.py)."""
+    import torch
+
+    from strata_fdtd_gb300.batch import BatchedSolver
+    from strata_fdtd_gb300.workloads import batch_workload
+
+    n = args.batch_solves
+    seq, steps, info = batch_workload(seed=0, n_solves=n)
+    cell_updates = sum(int(np.prod(s.shape)) * q for s, q in zip(seq, steps))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s, q in zip(seq, steps):
+        s.run_steps(q)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    traces_seq = [s.get_probe_data() for s in seq]
+    del seq
+    torch.cuda.empty_cache()
+    # second baseline: each solve alone through the batch tile kernel (a batch of one)
+    one, _, _ = batch_workload(seed=0, n_solves=n)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s, q in zip(one, steps):
+        BatchedSolver([s]).run_steps(q, graph_steps=args.graph_steps)
+    torch.cuda.synchronize()
+    t_one = time.perf_counter() - t0
+    del one
+    torch.cuda.empty_cache()
+    bat, _, _ = batch_workload(seed=0, n_solves=n)
+    b = BatchedSolver(bat)
+    tune = b.autotune(launches=2)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    start.record()
+    b.run_steps(steps, graph_steps=args.graph_steps)
+    end.record()
+    torch.cuda.synchronize()
+    t_bat_wall = time.perf_counter() - t0
+    t_bat = start.elapsed_time(end) / 1e3
+    same = all(
+        all(np.array_equal(bs.get_probe_data()[k], tr[k]) for k in tr)
+        for bs, tr in zip(bat, traces_seq))
+    line = {
+        "metric": "Gcell-updates/s (batched uneven grids)", "value": cell_updates / t_bat / 1e9,
+        "unit": "Gcell-updates/s", "n_gpus": 1, "steps": int(max(steps)), "warmup": 0,
+        "ms_per_step": t_bat / max(steps) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batch of {n} grids, edges log-U[64,256], PML 8, 1-6 solids, "
+                               "2-pole Debye block, 1-4 kHz pulse, 2 probes, 500-3000 steps",
+                   "cells": int(sum(np.prod(s.shape) for s in bat)),
+                   "cell_updates": cell_updates, "tiles": b.rows, "i_chunk": b.i_chunk,
+                   "graph_steps": args.graph_steps, "rejected_materials": info["rejected_materials"],
+                   "autotune_ms_per_step": {f"{k[0]}x{k[1]}": v for k, v in tune.items()
+                                            if k != "best"}},
+        "sequential": {"value": cell_updates / t_seq / 1e9, "seconds": t_seq,
+                       "path": "each solve alone through FDTDSolver.run_steps"},
+        "sequential_tile_kernel": {"value": cell_updates / t_one / 1e9, "seconds": t_one,
+                                   "path": "each solve alone as a batch of one (same tile kernel)"},
+        "speedup_vs_sequential_tile_kernel": t_one / t_bat,
+        "batched_wall_seconds": t_bat_wall,
+        "speedup_vs_sequential": t_seq / t_bat,
+        "traces_identical": bool(same),
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 

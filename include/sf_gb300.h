@@ -147,6 +147,11 @@ int sf_plan_set_probes(sf_plan* plan, int n, const int64_t* cells);
 int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const sf_pole* poles,
                     float inv_dx);
 
+/* Box [lo, hi) holding every cell with a nonzero material id; the batched
+ * density-pole pass walks only this box (default: the whole grid).  No
+ * counterpart in the reference (its ADE kernels sweep the whole grid). */
+int sf_plan_set_ade_box(sf_plan* plan, const int32_t* lo, const int32_t* hi);
+
 /* Step-kernel configuration.  config 0 = automatic (the autotuned
  * configuration if sf_plan_autotune ran, else the default), 1 = one thread
  * per cell, 2 = slab march along i with shared-memory halos, 3.. = thread
@@ -198,6 +203,75 @@ int sf_plan_energy(sf_plan* plan, double rho, double c, double dx, double* scrat
  * need more than the 4096 doubles.  Synchronises the stream. */
 int sf_plan_energy_noalloc(sf_plan* plan, double rho, double c, double dx, double* out_host,
                            void* stream);
+
+/* --- batches of independent grids ---------------------------------------- */
+/* A batch advances many plans (grids of any sizes, with or without
+ * geometry, PML, sources, probes, ADE) together: per time step one
+ * persistent launch whose blocks take (grid, i-chunk, row block, column
+ * block) tiles from a device work queue, plus the ADE density pass, the
+ * probe gather and a step-counter advance.  Results are identical to
+ * stepping each plan alone.  No counterpart in the reference (it steps one
+ * solver at a time on the CPU). */
+typedef struct sf_batch sf_batch;
+int sf_batch_create(sf_batch** out);
+int sf_batch_destroy(sf_batch* batch);
+/* Add a plan that will run n_steps (its own count; shorter members drop out
+ * of the queue).  src_values_dev: [n_steps][n_sources] doubles; trace_dev:
+ * [n_steps][n_probes] floats or NULL.  Pointers advance with each run. */
+int sf_batch_add(sf_batch* batch, sf_plan* plan, int64_t n_steps, const double* src_values_dev,
+                 float* trace_dev);
+int sf_batch_clear(sf_batch* batch);
+/* Tile shape: rows of 32 columns (4, 8 or 16) and i planes per tile (0 = 16). */
+int sf_batch_set_tiles(sf_batch* batch, int rows, int i_chunk);
+int sf_batch_tiles(const sf_batch* batch);
+/* Time the 9 tile shapes (rows 4/8/16 x i_chunk 8/16/32) on the members'
+ * current state without changing it and keep the fastest; ms_out[9] may be
+ * NULL. */
+int sf_batch_autotune(sf_batch* batch, int launches, void* stream, float* ms_out, int* best_rows,
+                      int* best_chunk);
+/* Advance every member by min(its remaining steps, n_steps).  graph_steps >
+ * 0 captures that many steps as one CUDA graph and replays it. */
+int sf_batch_run(sf_batch* batch, int64_t n_steps, int graph_steps, void* stream);
+
+/* --- differentiable solve (reverse-time adjoint) ------------------------- */
+/* A builder-defined extension with no counterpart in the reference (whose
+ * density is a scalar, core/solver.py:1584-1586): per-cell density
+ * rho = rho0 (1 + theta) with face coefficients
+ * cv = -(dt/dx) (1/rho_lo + 1/rho_hi) / 2, K = rho0 c^2 fixed, PML decays and
+ * a point source as the reference, no solids.  dtype 0 = float32, 1 =
+ * float64 for every array below.  decay[3]: device arrays of nx, ny, nz
+ * (1 where an axis has no PML).  src_cell < 0: no source. */
+typedef struct {
+    int32_t nx, ny, nz, dtype;
+    double cp;         /* -K dt / dx */
+    double dt_over_dx; /* dt / dx */
+    double rho0;
+    const void* decay[3];
+    int64_t src_cell;
+    int32_t n_probe, reserved;
+    const int64_t* probe_cells; /* device */
+} sf_diff_desc;
+/* cv arrays (3 x N) from theta (N). */
+int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, void* cvy, void* cvz,
+                         void* stream);
+/* n_steps forward steps between two state sets (4 pointers each: p, vx,
+ * vy, vz), starting from set `cur`; src_vals [n] (device, may be NULL);
+ * trace [n][n_probe] (may be NULL); p_store [n][N] receives each step's input
+ * pressure (may be NULL). */
+int sf_diff_forward(const sf_diff_desc* d, void* const* cv, void* const* set0, void* const* set1,
+                    int cur, int64_t n_steps, const void* src_vals, void* trace, void* p_store,
+                    void* stream);
+/* Reverse-time adjoint of the same n_steps: lambda sets (4 pointers each),
+ * starting from set `cur` holding lambda after the last step; p_store as
+ * written by the forward; the probe-loss gradient weight*2*(trace-target)
+ * is injected before each step's adjoint; dL/dcv accumulates into
+ * grad_cv[3]. */
+int sf_diff_adjoint(const sf_diff_desc* d, void* const* cv, void* const* lam0, void* const* lam1,
+                    int cur, int64_t n_steps, const void* p_store, const void* trace,
+                    const void* target, double weight, void* const* grad_cv, void* stream);
+/* dL/dtheta from dL/dcv. */
+int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* grad_cv, void* out,
+                       void* stream);
 
 /* --- voxelisation -------------------------------------------------------- */
 /* mask[i,j,k] = sdf(cell centre) <= 0, cell centre = (i + 0.5)*res, as

@@ -119,6 +119,19 @@ SIGNATURES = {
     "sf_energy_scratch_doubles": (_I64, [_P]),
     "sf_plan_energy": (_I, [_P, _D, _D, _D, _P, _P, _P]),
     "sf_plan_energy_noalloc": (_I, [_P, _D, _D, _D, _P, _P]),
+    "sf_plan_set_ade_box": (_I, [_P, _P, _P]),
+    "sf_diff_coefficients": (_I, [_P, _P, _P, _P, _P, _P]),
+    "sf_diff_forward": (_I, [_P, _P, _P, _P, _I, _I64, _P, _P, _P, _P]),
+    "sf_diff_adjoint": (_I, [_P, _P, _P, _P, _I, _I64, _P, _P, _P, _D, _P, _P]),
+    "sf_diff_grad_theta": (_I, [_P, _P, _P, _P, _P]),
+    "sf_batch_create": (_I, [ctypes.POINTER(_P)]),
+    "sf_batch_destroy": (_I, [_P]),
+    "sf_batch_add": (_I, [_P, _P, _I64, _P, _P]),
+    "sf_batch_clear": (_I, [_P]),
+    "sf_batch_set_tiles": (_I, [_P, _I, _I]),
+    "sf_batch_tiles": (_I, [_P]),
+    "sf_batch_autotune": (_I, [_P, _I, _P, _P, _P, _P]),
+    "sf_batch_run": (_I, [_P, _I64, _I, _P]),
     "sf_voxelize": (_I, [_P, _I, _I, _I, _I, _D, _I, _P, _P]),
     "sf_sdf_eval": (_I, [_P, _I, _P, _I64, _P, _P]),
 }

@@ -1,0 +1,255 @@
+"""Differentiable solve: probe-trace loss w.r.t. a per-cell density field.
+
+The forward model is the reference's staggered update (core/solver.py
+step order, PML decays, point GaussianPulse source, probes) with a per-cell
+density rho = rho0 * (1 + theta); every face velocity uses
+cv = -(dt/dx) (1/rho_lo + 1/rho_hi) / 2 while the bulk modulus K = rho0 c^2
+stays fixed.  The reference has a scalar density only
+(core/solver.py:1584-1586): the design field theta is an extension.
+
+Gradients come from hand-written reverse-time adjoint kernels
+(``sf_diff_*``, strata_fdtd_gb300/csrc/sf_adjoint.cu) behind a
+``torch.autograd.Function``.  The forward keeps a state checkpoint every K
+steps; the backward recomputes each K-step segment from its checkpoint
+(storing that segment's pressures) and runs the adjoint back through it, so
+memory is O(N * (steps/K + K)) instead of O(N * steps).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from .boundaries import PML
+from .grid import UniformGrid
+from .solver import GaussianPulse, step_coefficients
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("dtype", ctypes.c_int32), ("cp", ctypes.c_double), ("dt_over_dx", ctypes.c_double),
+                ("rho0", ctypes.c_double), ("decay", ctypes.c_void_p * 3),
+                ("src_cell", ctypes.c_int64), ("n_probe", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("probe_cells", ctypes.c_void_p)]
+
+
+def _ptrs(ts):
+    arr = (ctypes.c_void_p * len(ts))(*[t.data_ptr() for t in ts])
+    return arr
+
+
+class DifferentiableSolver:
+    """A fixed acoustic setup whose probe traces are differentiated w.r.t. a
+    density-scale field ``theta`` (shape = grid shape, values >= 0).
+
+    ``dtype``: torch.float32 (default) or torch.float64 working precision."""
+
+    def __init__(self, shape, resolution=1e-3, c=343.0, rho0=1.204, courant=0.5, pml_depth=10,
+                 source=None, frequency=1500.0, probes=(), dtype=None, checkpoint_every=100):
+        import torch
+
+        self.torch = torch
+        self.dtype = dtype or torch.float32
+        self.grid = UniformGrid(shape, resolution)
+        self.shape = tuple(self.grid.shape)
+        self.n = int(np.prod(self.shape))
+        self.c, self.rho0 = c, rho0
+        self.dt, _, _ = step_coefficients(self.grid, c, rho0, courant)
+        self.dx = self.grid.min_spacing
+        self.cp = -rho0 * c**2 * self.dt / self.dx  # core/solver.py:1585 with rho0
+        self.K = int(checkpoint_every)
+        dev = torch.device("cuda")
+        self.dev = dev
+        # PML decays exp(-sigma dt) in the working precision
+        pml = PML(depth=pml_depth)
+
+        class _S:
+            pass
+
+        stub = _S()
+        stub.shape, stub.c, stub.grid = self.shape, c, self.grid
+        pml.initialize(stub)
+        self.decay = []
+        for sig in pml.sigmas:
+            d = np.exp(-sig.astype(np.float64) * self.dt)
+            self.decay.append(torch.tensor(d, dtype=self.dtype, device=dev))
+        self.source = tuple(source) if source is not None else tuple(n // 2 for n in self.shape)
+        self.pulse = GaussianPulse(position=self.source, frequency=frequency)
+        self.probe_pos = [tuple(p) for p in probes]
+        cells = [int(np.ravel_multi_index(p, self.shape)) for p in self.probe_pos]
+        self.probe_cells = torch.tensor(cells or [0], dtype=torch.int64, device=dev)
+        self.lib = _native.load()
+
+    def _desc(self):
+        d = _Desc()
+        d.nx, d.ny, d.nz = self.shape
+        d.dtype = 1 if self.dtype == self.torch.float64 else 0
+        d.cp = self.cp
+        d.dt_over_dx = self.dt / self.dx
+        d.rho0 = self.rho0
+        for a in range(3):
+            d.decay[a] = self.decay[a].data_ptr()
+        d.src_cell = int(np.ravel_multi_index(self.source, self.shape))
+        d.n_probe = len(self.probe_pos)
+        d.probe_cells = self.probe_cells.data_ptr()
+        return d
+
+    def source_values(self, n_steps):
+        t, vals = 0.0, []
+        for _ in range(n_steps):
+            vals.append(self.pulse.waveform(np.array([t]), self.dt)[0])
+            t += self.dt
+        return self.torch.tensor(vals, dtype=self.dtype, device=self.dev)
+
+    def _stream(self):
+        return self.torch.cuda.current_stream().cuda_stream
+
+    def coefficients(self, theta):
+        torch = self.torch
+        cv = [torch.empty(self.shape, dtype=self.dtype, device=self.dev) for _ in range(3)]
+        _native.check(self.lib.sf_diff_coefficients(ctypes.byref(self._desc()), theta.data_ptr(),
+                                                    *[c.data_ptr() for c in cv], self._stream()),
+                      "sf_diff_coefficients")
+        return cv
+
+    def _zeros4(self):
+        return [self.torch.zeros(self.shape, dtype=self.dtype, device=self.dev) for _ in range(4)]
+
+    def forward(self, theta, n_steps, keep_checkpoints=True):
+        """Run n_steps from rest.  Returns (trace [n, n_probe], checkpoints)."""
+        torch = self.torch
+        theta = theta.to(self.dtype).contiguous()
+        cv = self.coefficients(theta)
+        sets = [self._zeros4(), self._zeros4()]
+        cur = 0
+        src = self.source_values(n_steps)
+        trace = torch.zeros((n_steps, max(1, len(self.probe_pos))), dtype=self.dtype,
+                            device=self.dev)
+        ckpts = []
+        desc = self._desc()
+        for s0 in range(0, n_steps, self.K):
+            n = min(self.K, n_steps - s0)
+            if keep_checkpoints:
+                ckpts.append([t.clone() for t in sets[cur]])
+            _native.check(self.lib.sf_diff_forward(
+                ctypes.byref(desc), _ptrs(cv), _ptrs(sets[0]), _ptrs(sets[1]), cur, n,
+                src[s0:].data_ptr(), trace[s0:].data_ptr(), None, self._stream()),
+                "sf_diff_forward")
+            cur = (cur + n) & 1
+        return trace[:, :len(self.probe_pos)], ckpts, cv, src
+
+    def gradient(self, theta, trace, target, ckpts, cv, src, weight=1.0):
+        """dL/dtheta of L = weight * sum((trace - target)^2) by checkpointed
+        recomputation and the reverse-time adjoint."""
+        torch = self.torch
+        n_steps = trace.shape[0]
+        theta = theta.to(self.dtype).contiguous()
+        full = torch.zeros((n_steps, max(1, len(self.probe_pos))), dtype=self.dtype, device=self.dev)
+        full[:, :trace.shape[1]] = trace
+        tgt = torch.zeros_like(full)
+        tgt[:, :target.shape[1]] = target.to(self.dtype)
+        lam = [self._zeros4(), self._zeros4()]
+        lcur = 0
+        grad_cv = [torch.zeros(self.shape, dtype=self.dtype, device=self.dev) for _ in range(3)]
+        desc = self._desc()
+        store = torch.empty((self.K,) + self.shape, dtype=self.dtype, device=self.dev)
+        seg_starts = list(range(0, n_steps, self.K))
+        for si in reversed(range(len(seg_starts))):
+            s0 = seg_starts[si]
+            n = min(self.K, n_steps - s0)
+            work = [[t.clone() for t in ckpts[si]], self._zeros4()]
+            _native.check(self.lib.sf_diff_forward(
+                ctypes.byref(desc), _ptrs(cv), _ptrs(work[0]), _ptrs(work[1]), 0, n,
+                src[s0:].data_ptr(), None, store.data_ptr(), self._stream()), "sf_diff_forward")
+            _native.check(self.lib.sf_diff_adjoint(
+                ctypes.byref(desc), _ptrs(cv), _ptrs(lam[0]), _ptrs(lam[1]), lcur, n,
+                store.data_ptr(), full[s0:].data_ptr(), tgt[s0:].data_ptr(), float(weight),
+                _ptrs(grad_cv), self._stream()), "sf_diff_adjoint")
+            lcur = (lcur + n) & 1
+        out = torch.empty(self.shape, dtype=self.dtype, device=self.dev)
+        _native.check(self.lib.sf_diff_grad_theta(ctypes.byref(desc), theta.data_ptr(),
+                                                  _ptrs(grad_cv), out.data_ptr(), self._stream()),
+                      "sf_diff_grad_theta")
+        return out
+
+    def loss(self, theta, target, n_steps):
+        """L2 loss of the probe traces against ``target`` [n_steps, n_probe],
+        differentiable w.r.t. ``theta`` through the adjoint kernels."""
+        return ProbeLoss.apply(theta, target, self, n_steps)
+
+
+def _make_function():
+    import torch
+
+    class ProbeLossFn(torch.autograd.Function):
+        """loss = sum((trace(theta) - target)^2); backward via the adjoint."""
+
+        @staticmethod
+        def forward(ctx, theta, target, solver, n_steps):
+            trace, ckpts, cv, src = solver.forward(theta.detach(), n_steps)
+            loss = ((trace - target.to(trace.dtype)) ** 2).sum()
+            ctx.solver = solver
+            ctx.saved = (trace, ckpts, cv, src)
+            ctx.save_for_backward(theta, target)
+            return loss.to(theta.dtype)
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            theta, target = ctx.saved_tensors
+            trace, ckpts, cv, src = ctx.saved
+            g = ctx.solver.gradient(theta.detach(), trace, target, ckpts, cv, src,
+                                    weight=float(grad_out))
+            return g.to(theta.dtype), None, None, None
+
+    return ProbeLossFn
+
+
+class _Lazy:
+    fn = None
+
+    @classmethod
+    def apply(cls, *a):
+        if cls.fn is None:
+            cls.fn = _make_function()
+        return cls.fn.apply(*a)
+
+
+ProbeLoss = _Lazy
+
+
+def reference_loss_torch(solver: DifferentiableSolver, theta, target, n_steps):
+    """The same scheme stepped with plain PyTorch tensor ops (for checking the
+    adjoint kernels with torch.autograd at small sizes).  Not used by the
+    GPU path."""
+    torch = solver.torch
+    dt_dx, rho0 = solver.dt / solver.dx, solver.rho0
+    rho = rho0 * (1 + theta)
+    b = 1.0 / rho
+    cvx = -dt_dx * 0.5 * (b[:-1] + b[1:])
+    cvy = -dt_dx * 0.5 * (b[:, :-1] + b[:, 1:])
+    cvz = -dt_dx * 0.5 * (b[:, :, :-1] + b[:, :, 1:])
+    dx, dy, dz = solver.decay
+    p = torch.zeros_like(theta)
+    vx, vy, vz = torch.zeros_like(theta), torch.zeros_like(theta), torch.zeros_like(theta)
+    src = solver.source_values(n_steps).to(theta.dtype)
+    si, sj, sk = solver.source
+    traces = []
+    for n in range(n_steps):
+        vx = torch.cat([vx[:-1] + cvx * (p[1:] - p[:-1]), vx[-1:]], 0)
+        vy = torch.cat([vy[:, :-1] + cvy * (p[:, 1:] - p[:, :-1]), vy[:, -1:]], 1)
+        vz = torch.cat([vz[:, :, :-1] + cvz * (p[:, :, 1:] - p[:, :, :-1]), vz[:, :, -1:]], 2)
+        div = (vx - torch.nn.functional.pad(vx, (0, 0, 0, 0, 1, 0))[:-1]
+               + vy - torch.nn.functional.pad(vy, (0, 0, 1, 0))[:, :-1]
+               + vz - torch.nn.functional.pad(vz, (1, 0))[:, :, :-1])
+        p = p + solver.cp * div
+        vx = vx * dx[:, None, None]
+        vy = vy * dy[None, :, None]
+        vz = vz * dz[None, None, :]
+        p = p * dx[:, None, None] * dy[None, :, None] * dz[None, None, :]
+        onehot = torch.zeros_like(p)
+        onehot[si, sj, sk] = 1.0
+        p = p + src[n] * onehot
+        traces.append(torch.stack([p[q] for q in solver.probe_pos]))
+    trace = torch.stack(traces)
+    return ((trace - target) ** 2).sum()

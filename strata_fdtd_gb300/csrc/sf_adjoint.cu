@@ -1,0 +1,323 @@
+// sf_adjoint.cu -- forward and reverse-time (adjoint) steps of the
+// differentiable solve.
+//
+// Scheme: the reference's staggered update (fdtd_step.cpp:15-212 order) with a
+// per-cell density rho = rho0 * (1 + theta) in place of the scalar rho of
+// core/solver.py:1584-1586: every face velocity uses its own coefficient
+//     cv_face = -(dt/dx) * (1/rho_lo + 1/rho_hi) / 2
+// while the pressure coefficient cp = -K dt/dx keeps K = rho0 c^2.  No solids;
+// PML decays and the point source as the reference (pml.cpp:47-149,
+// core/solver.py:2413-2421); probe samples after each step.  The per-cell
+// density is a builder-defined design field: the reference has only a scalar
+// rho.
+//
+// One step is linear in the state u = (p, v):
+//     v' = v + C G p          (C = diag(cv), G = face differences)
+//     p' = p + cp Div v'
+//     v'' = Dv v',  p'' = Dp p' + s
+// so its adjoint, with mu_p = Dp lambda_p'' and
+// mu_v = Dv lambda_v'' + cp Div^T mu_p, is
+//     lambda_v = mu_v,  lambda_p = mu_p + G^T C mu_v,
+//     dL/dcv_face += mu_v(face) * (G p^n)(face)
+// which k_dadj evaluates per cell (one fused stencil pass, reverse time).
+// Both directions are templated on the working precision (float / double).
+#include <cuda_runtime.h>
+
+#include "sf_common.cuh"
+#include "sf_gb300.h"
+
+namespace {
+
+template <typename T>
+struct DiffPtrs {
+    int nx, ny, nz;
+    long long plane;
+    T cp;
+    const T* cvx;
+    const T* cvy;
+    const T* cvz;
+    const T* dx;
+    const T* dy;
+    const T* dz;
+};
+
+// Coefficients from theta: cv_a(c) for the face between c and c + e_a
+// (zero on the last plane of each axis, which carries no face update).
+template <typename T>
+__global__ void k_dcoef(const T* __restrict__ theta, T* __restrict__ cvx, T* __restrict__ cvy,
+                        T* __restrict__ cvz, int nx, int ny, int nz, T dt_dx, T rho0) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    const long long plane = (long long)ny * nz;
+    const long long c = (long long)i * plane + (long long)j * nz + k;
+    const T b0 = T(1) / (rho0 * (T(1) + theta[c]));
+    auto face = [&](long long n) {
+        const T b1 = T(1) / (rho0 * (T(1) + theta[n]));
+        return -dt_dx * T(0.5) * (b0 + b1);
+    };
+    cvx[c] = (i < nx - 1) ? face(c + plane) : T(0);
+    cvy[c] = (j < ny - 1) ? face(c + nz) : T(0);
+    cvz[c] = (k < nz - 1) ? face(c + 1) : T(0);
+}
+
+// Forward step (per cell, ping-pong): out = step(in); records p at the probe
+// cells of the *input* into trace_prev (the previous step's samples).
+template <typename T>
+__global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restrict__ vx,
+                       const T* __restrict__ vy, const T* __restrict__ vz, T* __restrict__ po,
+                       T* __restrict__ vxo, T* __restrict__ vyo, T* __restrict__ vzo,
+                       long long src_cell, const T* __restrict__ src_val, T* __restrict__ p_store) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= g.nz || j >= g.ny) return;
+    const long long plane = g.plane;
+    const int nz = g.nz;
+    const long long c = (long long)i * plane + (long long)j * nz + k;
+    const T pc = p[c];
+    if (p_store) p_store[c] = pc;
+    T ux = vx[c], uy = vy[c], uz = vz[c];
+    if (i < g.nx - 1) ux = ux + g.cvx[c] * (p[c + plane] - pc);
+    if (j < g.ny - 1) uy = uy + g.cvy[c] * (p[c + nz] - pc);
+    if (k < nz - 1) uz = uz + g.cvz[c] * (p[c + 1] - pc);
+    T uxm = T(0), uym = T(0), uzm = T(0);
+    if (i > 0) uxm = vx[c - plane] + g.cvx[c - plane] * (pc - p[c - plane]);
+    if (j > 0) uym = vy[c - nz] + g.cvy[c - nz] * (pc - p[c - nz]);
+    if (k > 0) uzm = vz[c - 1] + g.cvz[c - 1] * (pc - p[c - 1]);
+    T pn = pc + g.cp * (((ux - uxm) + (uy - uym)) + (uz - uzm));
+    const T di = g.dx[i], dj = g.dy[j], dk = g.dz[k];
+    vxo[c] = ux * di;
+    vyo[c] = uy * dj;
+    vzo[c] = uz * dk;
+    pn = ((pn * di) * dj) * dk;
+    if (c == src_cell && src_val != nullptr) pn = pn + *src_val;
+    po[c] = pn;
+}
+
+template <typename T>
+__global__ void k_dprobe(const T* __restrict__ p, const int64_t* __restrict__ cells, int n,
+                         T* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = p[cells[t]];
+}
+
+// lambda_p(probe) += w * 2 (trace - target): the loss gradient at step n.
+template <typename T>
+__global__ void k_dinject(T* __restrict__ lp, const int64_t* __restrict__ cells, int n,
+                          const T* __restrict__ trace, const T* __restrict__ target, T w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) atomicAdd(&lp[cells[t]], w * T(2) * (trace[t] - target[t]));
+}
+
+// Adjoint of one step.  in: lambda after the step; out: lambda before it;
+// pst: p^n (the step's input pressure); g*: accumulated dL/dcv per face.
+template <typename T>
+__global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restrict__ lx,
+                       const T* __restrict__ ly, const T* __restrict__ lz, T* __restrict__ lpo,
+                       T* __restrict__ lxo, T* __restrict__ lyo, T* __restrict__ lzo,
+                       const T* __restrict__ pst, T* __restrict__ gx, T* __restrict__ gy,
+                       T* __restrict__ gz) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (k >= nz || j >= ny) return;
+    const long long plane = g.plane;
+    const long long c = (long long)i * plane + (long long)j * nz + k;
+    const T di = g.dx[i], dj = g.dy[j], dk = g.dz[k];
+    // mu_p = Dp lambda_p at this cell and its six neighbours
+    auto mup = [&](int ii, int jj, int kk, long long q) -> T {
+        return g.dx[ii] * g.dy[jj] * g.dz[kk] * lp[q];
+    };
+    const T m0 = di * dj * dk * lp[c];
+    const T mxp = (i < nx - 1) ? mup(i + 1, j, k, c + plane) : T(0);
+    const T myp = (j < ny - 1) ? mup(i, j + 1, k, c + nz) : T(0);
+    const T mzp = (k < nz - 1) ? mup(i, j, k + 1, c + 1) : T(0);
+    // mu_v on the cell's high faces (the last plane's face has no +1 cell)
+    const T vx_hi = di * lx[c] + g.cp * (m0 - mxp);
+    const T vy_hi = dj * ly[c] + g.cp * (m0 - myp);
+    const T vz_hi = dk * lz[c] + g.cp * (m0 - mzp);
+    // mu_v on the low faces (owned by the lower neighbour)
+    T vx_lo = T(0), vy_lo = T(0), vz_lo = T(0);
+    if (i > 0) vx_lo = g.dx[i - 1] * lx[c - plane] + g.cp * (mup(i - 1, j, k, c - plane) - m0);
+    if (j > 0) vy_lo = dj * ly[c - nz] + g.cp * (mup(i, j - 1, k, c - nz) - m0);
+    if (k > 0) vz_lo = g.dz[k - 1] * lz[c - 1] + g.cp * (mup(i, j, k - 1, c - 1) - m0);
+    lxo[c] = vx_hi;
+    lyo[c] = vy_hi;
+    lzo[c] = vz_hi;
+    // lambda_p = mu_p + G^T C mu_v
+    T acc = m0;
+    if (i > 0) acc += g.cvx[c - plane] * vx_lo;
+    if (j > 0) acc += g.cvy[c - nz] * vy_lo;
+    if (k > 0) acc += g.cvz[c - 1] * vz_lo;
+    acc -= g.cvx[c] * vx_hi + g.cvy[c] * vy_hi + g.cvz[c] * vz_hi;
+    lpo[c] = acc;
+    // dL/dcv on the high faces: mu_v * (p^n[hi] - p^n[lo])
+    const T p0 = pst[c];
+    if (i < nx - 1) gx[c] += vx_hi * (pst[c + plane] - p0);
+    if (j < ny - 1) gy[c] += vy_hi * (pst[c + nz] - p0);
+    if (k < nz - 1) gz[c] += vz_hi * (pst[c + 1] - p0);
+}
+
+// dL/dtheta(c) = (dt/dx) rho0 / (2 rho(c)^2) * sum of dL/dcv over its faces.
+template <typename T>
+__global__ void k_dgrad(const T* __restrict__ theta, const T* __restrict__ gx,
+                        const T* __restrict__ gy, const T* __restrict__ gz, T* __restrict__ out,
+                        int nx, int ny, int nz, T dt_dx, T rho0) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    const long long plane = (long long)ny * nz;
+    const long long c = (long long)i * plane + (long long)j * nz + k;
+    T s = gx[c] + gy[c] + gz[c];  // high faces (zero on the last plane)
+    if (i > 0) s += gx[c - plane];
+    if (j > 0) s += gy[c - nz];
+    if (k > 0) s += gz[c - 1];
+    const T rho = rho0 * (T(1) + theta[c]);
+    out[c] = s * dt_dx * rho0 / (T(2) * rho * rho);
+}
+
+template <typename T>
+DiffPtrs<T> ptrs(const sf_diff_desc* d, const void* const* cv) {
+    DiffPtrs<T> g;
+    g.nx = d->nx;
+    g.ny = d->ny;
+    g.nz = d->nz;
+    g.plane = (long long)d->ny * d->nz;
+    g.cp = (T)d->cp;
+    g.cvx = static_cast<const T*>(cv[0]);
+    g.cvy = static_cast<const T*>(cv[1]);
+    g.cvz = static_cast<const T*>(cv[2]);
+    g.dx = static_cast<const T*>(d->decay[0]);
+    g.dy = static_cast<const T*>(d->decay[1]);
+    g.dz = static_cast<const T*>(d->decay[2]);
+    return g;
+}
+
+dim3 grid_of(const sf_diff_desc* d) { return dim3((d->nz + 31) / 32, (d->ny + 7) / 8, d->nx); }
+
+template <typename T>
+int forward(const sf_diff_desc* d, const void* const* cv, void* const* set0, void* const* set1,
+            int cur, int64_t n, const void* src_vals, void* trace, void* p_store, cudaStream_t st) {
+    const DiffPtrs<T> g = ptrs<T>(d, cv);
+    const long long N = (long long)d->nx * d->ny * d->nz;
+    const T* sv = static_cast<const T*>(src_vals);
+    T* tr = static_cast<T*>(trace);
+    T* ps = static_cast<T*>(p_store);
+    for (int64_t s = 0; s < n; ++s) {
+        void* const* in = cur ? set1 : set0;
+        void* const* out = cur ? set0 : set1;
+        k_dfwd<T><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            g, (const T*)in[0], (const T*)in[1], (const T*)in[2], (const T*)in[3], (T*)out[0],
+            (T*)out[1], (T*)out[2], (T*)out[3], d->src_cell, sv ? sv + s : nullptr,
+            ps ? ps + s * N : nullptr);
+        if (tr && d->n_probe > 0)
+            k_dprobe<T><<<(d->n_probe + 127) / 128, 128, 0, st>>>((const T*)out[0], d->probe_cells,
+                                                                  d->n_probe, tr + s * d->n_probe);
+        cur = 1 - cur;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_forward: launch failed");
+}
+
+template <typename T>
+int adjoint(const sf_diff_desc* d, const void* const* cv, void* const* lam0, void* const* lam1,
+            int cur, int64_t n, const void* p_store, const void* trace, const void* target,
+            double weight, void* const* grad_cv, cudaStream_t st) {
+    const DiffPtrs<T> g = ptrs<T>(d, cv);
+    const long long N = (long long)d->nx * d->ny * d->nz;
+    const T* ps = static_cast<const T*>(p_store);
+    const T* tr = static_cast<const T*>(trace);
+    const T* tg = static_cast<const T*>(target);
+    for (int64_t s = n - 1; s >= 0; --s) {
+        void* const* in = cur ? lam1 : lam0;  // lambda after step s
+        void* const* out = cur ? lam0 : lam1;
+        if (tr && tg && d->n_probe > 0)
+            k_dinject<T><<<(d->n_probe + 127) / 128, 128, 0, st>>>(
+                (T*)in[0], d->probe_cells, d->n_probe, tr + s * d->n_probe, tg + s * d->n_probe,
+                (T)weight);
+        k_dadj<T><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            g, (const T*)in[0], (const T*)in[1], (const T*)in[2], (const T*)in[3], (T*)out[0],
+            (T*)out[1], (T*)out[2], (T*)out[3], ps + s * N, (T*)grad_cv[0], (T*)grad_cv[1],
+            (T*)grad_cv[2]);
+        cur = 1 - cur;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_adjoint: launch failed");
+}
+
+int check_desc(const sf_diff_desc* d) {
+    if (!d) return sf_fail("sf_diff: NULL descriptor");
+    if (d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nx > 65535)
+        return sf_fail("sf_diff: bad grid dimensions");
+    if (d->dtype != 0 && d->dtype != 1) return sf_fail("sf_diff: dtype must be 0 (f32) or 1 (f64)");
+    if (!d->decay[0] || !d->decay[1] || !d->decay[2]) return sf_fail("sf_diff: decay arrays required");
+    if (d->src_cell >= (long long)d->nx * d->ny * d->nz) return sf_fail("sf_diff: source outside");
+    if (d->n_probe < 0 || (d->n_probe > 0 && !d->probe_cells)) return sf_fail("sf_diff: bad probes");
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, void* cvy, void* cvz,
+                         void* stream) {
+    if (int rc = check_desc(d)) return rc;
+    if (!theta || !cvx || !cvy || !cvz) return sf_fail("sf_diff_coefficients: NULL buffer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (d->dtype == 1)
+        k_dcoef<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            (const double*)theta, (double*)cvx, (double*)cvy, (double*)cvz, d->nx, d->ny, d->nz,
+            d->dt_over_dx, d->rho0);
+    else
+        k_dcoef<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            (const float*)theta, (float*)cvx, (float*)cvy, (float*)cvz, d->nx, d->ny, d->nz,
+            (float)d->dt_over_dx, (float)d->rho0);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_coefficients: launch failed");
+}
+
+int sf_diff_forward(const sf_diff_desc* d, void* const* cv, void* const* set0, void* const* set1,
+                    int cur, int64_t n_steps, const void* src_vals, void* trace, void* p_store,
+                    void* stream) {
+    if (int rc = check_desc(d)) return rc;
+    if (!cv || !set0 || !set1 || (cur != 0 && cur != 1) || n_steps < 0)
+        return sf_fail("sf_diff_forward: bad arguments");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return d->dtype == 1
+               ? forward<double>(d, cv, set0, set1, cur, n_steps, src_vals, trace, p_store, st)
+               : forward<float>(d, cv, set0, set1, cur, n_steps, src_vals, trace, p_store, st);
+}
+
+int sf_diff_adjoint(const sf_diff_desc* d, void* const* cv, void* const* lam0, void* const* lam1,
+                    int cur, int64_t n_steps, const void* p_store, const void* trace,
+                    const void* target, double weight, void* const* grad_cv, void* stream) {
+    if (int rc = check_desc(d)) return rc;
+    if (!cv || !lam0 || !lam1 || !p_store || !grad_cv || (cur != 0 && cur != 1) || n_steps < 0)
+        return sf_fail("sf_diff_adjoint: bad arguments");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return d->dtype == 1 ? adjoint<double>(d, cv, lam0, lam1, cur, n_steps, p_store, trace, target,
+                                           weight, grad_cv, st)
+                         : adjoint<float>(d, cv, lam0, lam1, cur, n_steps, p_store, trace, target,
+                                          weight, grad_cv, st);
+}
+
+int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* grad_cv, void* out,
+                       void* stream) {
+    if (int rc = check_desc(d)) return rc;
+    if (!theta || !grad_cv || !out) return sf_fail("sf_diff_grad_theta: NULL buffer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (d->dtype == 1)
+        k_dgrad<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            (const double*)theta, (const double*)grad_cv[0], (const double*)grad_cv[1],
+            (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
+    else
+        k_dgrad<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            (const float*)theta, (const float*)grad_cv[0], (const float*)grad_cv[1],
+            (const float*)grad_cv[2], (float*)out, d->nx, d->ny, d->nz, (float)d->dt_over_dx,
+            (float)d->rho0);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_grad_theta: launch failed");
+}
+
+}  // extern "C"

@@ -43,40 +43,7 @@ int sf_fail_cuda(cudaError_t e, const char* what, const char* file, int line) {
     return 2;
 }
 
-struct sf_plan {
-    sf_grid_desc d{};
-    long long n = 0;
-    int device = 0;
-    float* f[2][4] = {{nullptr}};
-    int cur = 0;
-    bool bound = false;
-    uint8_t* flags = nullptr;  // owned; null = no geometry (all air)
-    float* decay[3] = {nullptr, nullptr, nullptr};  // owned, 1.0f where axis off
-    SfSources src{};
-    long long* probe_cells = nullptr;  // owned
-    int n_probe = 0;
-    SfPoles poles{};
-    const uint8_t* mat = nullptr;  // caller-owned
-    int variant = 0;               // kernel configuration (SF_CFG_*), 0 = auto
-    int i_chunk = 0;               // planes per block in march / column kernels (0 = auto)
-    int tuned = 0;                 // configuration chosen by sf_plan_autotune (0 = none)
-    long long steps_done = 0;      // steps issued so far (alternates the chunk order)
-};
-
-// Planes per block for the slab march: enough (j,k)-tile x i-chunk blocks
-// for about four waves of 8 resident blocks on each of the SMs.
-static int auto_chunk(const sf_plan* P, int kspan) {
-    int sms = 152;
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long tiles = (long long)((P->d.nz + kspan - 1) / kspan) * ((P->d.ny + 7) / 8);
-    long long chunks = (4LL * 8 * sms + tiles - 1) / tiles;
-    if (chunks < 1) chunks = 1;
-    long long ich = (P->d.nx + chunks - 1) / chunks;
-    if (ich < 4) ich = 4;
-    if (ich > P->d.nx) ich = P->d.nx;
-    return (int)ich;
-}
+#include "sf_plan_internal.h"
 
 namespace {
 
@@ -90,16 +57,7 @@ int set_decays(sf_plan* P, const float* host[3]) {
     return 0;
 }
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int now = -1;
-        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
-    }
-};
+
 
 }  // namespace
 
@@ -135,6 +93,9 @@ int sf_plan_create(const sf_grid_desc* desc, sf_plan** out) {
     auto* P = new sf_plan();
     P->d = *desc;
     P->n = (long long)desc->nx * desc->ny * desc->nz;
+    P->ade_hi[0] = desc->nx;
+    P->ade_hi[1] = desc->ny;
+    P->ade_hi[2] = desc->nz;
     cudaGetDevice(&P->device);
     const int n[3] = {desc->nx, desc->ny, desc->nz};
     for (int a = 0; a < 3; ++a) {
@@ -284,6 +245,19 @@ int sf_plan_set_ade(sf_plan* P, const uint8_t* mat, int n, const sf_pole* poles,
     return 0;
 }
 
+int sf_plan_set_ade_box(sf_plan* P, const int32_t* lo, const int32_t* hi) {
+    if (!P || !lo || !hi) return sf_fail("sf_plan_set_ade_box: NULL argument");
+    const int n[3] = {P->d.nx, P->d.ny, P->d.nz};
+    for (int a = 0; a < 3; ++a)
+        if (lo[a] < 0 || hi[a] > n[a] || lo[a] > hi[a])
+            return sf_fail("sf_plan_set_ade_box: box outside the grid");
+    for (int a = 0; a < 3; ++a) {
+        P->ade_lo[a] = lo[a];
+        P->ade_hi[a] = hi[a];
+    }
+    return 0;
+}
+
 int sf_plan_set_kernel(sf_plan* P, int config, int i_chunk) {
     if (!P) return sf_fail("sf_plan_set_kernel: NULL plan");
     if (config < 0 || config >= SF_CFG_COL_FIRST + kSfColConfigCount)
@@ -324,6 +298,10 @@ void fill_args(const sf_plan* P, SfStepArgs& a, bool with_trace) {
     a.n_probe = with_trace ? P->n_probe : 0;
     a.probe_cells = P->probe_cells;
     a.mat = P->mat;
+    for (int q = 0; q < 3; ++q) {
+        a.ade_lo[q] = P->ade_lo[q];
+        a.ade_hi[q] = P->ade_hi[q];
+    }
 }
 
 void set_io(const sf_plan* P, SfStepArgs& a, int in) {

@@ -1,0 +1,639 @@
+// sf_batch.cu -- many independent grids of different sizes, stepped together.
+//
+// A batch gathers plans (each a complete single-grid solve: fields, flags,
+// PML, sources, probes, ADE) and advances them with one persistent launch
+// per time step.  Every grid is cut into tiles (i-chunk x BY rows x 32
+// columns); a device-wide work queue (one atomic counter) hands tiles to the
+// resident blocks, so uneven grids load-balance across the SMs.  Each tile
+// is processed as thread columns along i, with the per-cell arithmetic of
+// k_step / k_step_col (and so of the reference passes they restate,
+// including the ADE order of core/solver.py:2135-2193): a grid's result is
+// bit-identical alone or in the batch.
+//
+// Per step the batch enqueues: the ADE density pre-pass over the material
+// boxes (if any grid has density poles), the step kernel, the probe gather,
+// and a one-thread kernel that advances the device step counter and resets
+// the queue.  The kernels read the step number from device memory, so a run
+// of steps can be captured once as a CUDA graph and replayed.  Grids drop out
+// of the queue's work when they reach their own step count.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sf_common.cuh"
+#include "sf_kernels.h"
+#include "sf_plan_internal.h"
+
+struct SfGridDev {
+    int nx, ny, nz, ich;
+    long long plane, n_steps;
+    float cv, cp;
+    int cur0, n_probe;
+    float* f[2][4];
+    const uint8_t* flags;
+    const float* dx;
+    const float* dy;
+    const float* dz;
+    const double* src_val;
+    const long long* probe_cells;
+    float* trace;
+    const uint8_t* mat;
+    int ade_lo[3], ade_hi[3];
+    SfSources src;
+    SfPoles poles;
+};
+
+namespace {
+
+__device__ __forceinline__ float ade_face_g(float v, const SfPoles& P, uint8_t m_lo, uint8_t m_hi,
+                                            long long lo, long long hi) {
+    if (m_lo == 0 || m_lo != m_hi) return v;
+    for (int q = 0; q < P.n; ++q) {
+        const sf_pole& pl = P.p[q];
+        if (pl.target == 0 && pl.material_id == m_lo)
+            v = f_add(v, f_mul(pl.corr, f_sub(pl.J[hi], pl.J[lo])));
+    }
+    return v;
+}
+
+// One tile: thread (tx, ty) walks cells (i0..i1-1, j, k) of grid g at step s.
+template <int BY, bool GEOM, bool ADE>
+__device__ void batch_column(const SfGridDev& g, long long s, int chunk, int jb, int kb, bool trial) {
+    const int k = kb * 32 + threadIdx.x;
+    const int j = jb * BY + threadIdx.y;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    if (k >= nz || j >= ny) return;
+    const int i0 = chunk * g.ich;
+    const int i1 = min(i0 + g.ich, nx);
+    const int in = (int)((g.cur0 + s) & 1);
+    const float* __restrict__ P = g.f[in][0];
+    const float* __restrict__ VX = g.f[in][1];
+    const float* __restrict__ VY = g.f[in][2];
+    const float* __restrict__ VZ = g.f[in][3];
+    float* __restrict__ PO = g.f[1 - in][0];
+    float* __restrict__ VXO = g.f[1 - in][1];
+    float* __restrict__ VYO = g.f[1 - in][2];
+    float* __restrict__ VZO = g.f[1 - in][3];
+    const uint8_t* __restrict__ F = g.flags;
+    const uint8_t* __restrict__ M = g.mat;
+    const float* __restrict__ DX = g.dx;
+    constexpr bool geom = GEOM;
+    constexpr bool ade = ADE;
+    const long long plane = g.plane;
+    const float cv = g.cv, cp = g.cp;
+    const float dj = g.dy[j], dk = g.dz[k];
+    const double* sv = g.src_val + s * g.src.n;
+
+    unsigned smask = 0;
+    for (int q = 0; q < g.src.n; ++q) {
+        const sf_source& S = g.src.s[q];
+        bool can;
+        if (S.kind == 0) can = (S.b == j) && (S.c == k);
+        else if (S.a == 0) can = true;
+        else if (S.a == 1) can = (S.b == j);
+        else can = (S.b == k);
+        if (can) smask |= 1u << q;
+    }
+
+    long long c = (long long)i0 * plane + (long long)j * nz + k;
+    float pc = P[c], vxc = VX[c], vyc = VY[c], vzc = VZ[c];
+    uint8_t fc = geom ? F[c] : (uint8_t)SF_ALL;
+    float pn = (i0 + 1 < nx) ? P[c + plane] : 0.0f;
+    float vxm = 0.0f;
+    if (i0 > 0) {
+        const long long m = c - plane;
+        vxm = face_update(VX[m], cv, pc, P[m]);
+        if (ade) vxm = ade_face_g(vxm, g.poles, M[m], M[c], m, c);
+        if (geom && !(F[m] & SF_OPX)) vxm = 0.0f;
+    }
+
+    for (int i = i0; i < i1; ++i, c += plane) {
+        float pnn = 0.0f, vxn = 0.0f, vyn = 0.0f, vzn = 0.0f;
+        uint8_t fnn = SF_ALL;
+        if (i + 1 < i1) {
+            vxn = VX[c + plane];
+            vyn = VY[c + plane];
+            vzn = VZ[c + plane];
+            if (geom) fnn = F[c + plane];
+            if (i + 2 < nx) pnn = P[c + 2 * plane];
+        }
+        const uint8_t mc = ade ? M[c] : (uint8_t)0;
+
+        float ux = vxc, uy = vyc, uz = vzc;
+        if (i < nx - 1) {
+            ux = face_update(vxc, cv, pn, pc);
+            if (ade) ux = ade_face_g(ux, g.poles, mc, M[c + plane], c, c + plane);
+            if (geom && !(fc & SF_OPX)) ux = 0.0f;
+        }
+        if (j < ny - 1) {
+            uy = face_update(vyc, cv, P[c + nz], pc);
+            if (ade) uy = ade_face_g(uy, g.poles, mc, M[c + nz], c, c + nz);
+            if (geom && !(fc & SF_OPY)) uy = 0.0f;
+        }
+        if (k < nz - 1) {
+            uz = face_update(vzc, cv, P[c + 1], pc);
+            if (ade) uz = ade_face_g(uz, g.poles, mc, M[c + 1], c, c + 1);
+            if (geom && !(fc & SF_OPZ)) uz = 0.0f;
+        }
+        float uym = 0.0f, uzm = 0.0f;
+        if (j > 0) {
+            const long long m = c - nz;
+            uym = face_update(VY[m], cv, pc, P[m]);
+            if (ade) uym = ade_face_g(uym, g.poles, M[m], mc, m, c);
+            if (geom && !(F[m] & SF_OPY)) uym = 0.0f;
+        }
+        if (k > 0) {
+            const long long m = c - 1;
+            uzm = face_update(VZ[m], cv, pc, P[m]);
+            if (ade) uzm = ade_face_g(uzm, g.poles, M[m], mc, m, c);
+            if (geom && !(F[m] & SF_OPZ)) uzm = 0.0f;
+        }
+
+        const bool air = (fc & SF_AIR) != 0;
+        const float ddx = f_sub(ux, vxm), ddy = f_sub(uy, uym), ddz = f_sub(uz, uzm);
+        float pnew = air ? f_add(pc, f_mul(cp, f_add(f_add(ddx, ddy), ddz))) : 0.0f;
+        if (ade && mc != 0 && g.poles.n_modulus > 0) {
+            const float sc = g.poles.inv_dx;
+            const float div = f_add(f_add(f_mul(ddx, sc), f_mul(ddy, sc)), f_mul(ddz, sc));
+            for (int q = 0; q < g.poles.n; ++q) {
+                const sf_pole& pl = g.poles.p[q];
+                if (pl.target != 1 || pl.material_id != mc) continue;
+                const float j0 = pl.J[c];
+                float jn;
+                if (pl.kind == 0) {
+                    jn = f_add(f_mul(pl.c0, j0), f_mul(pl.c1, div));
+                } else {
+                    const float jp = pl.J_prev[c];
+                    jn = f_add(f_add(f_mul(pl.c0, j0), f_mul(pl.c1, jp)), f_mul(pl.c2, div));
+                    if (!trial) pl.J_prev[c] = j0;
+                }
+                if (!trial) pl.J[c] = jn;
+                pnew = f_add(pnew, f_mul(pl.corr, jn));
+            }
+            if (!air) pnew = 0.0f;
+        }
+        const float di = DX[i];
+        VXO[c] = f_mul(ux, di);
+        VYO[c] = f_mul(uy, dj);
+        VZO[c] = f_mul(uz, dk);
+        pnew = f_mul(f_mul(f_mul(pnew, di), dj), dk);
+        for (unsigned mm = smask; mm != 0; mm &= mm - 1) {
+            const int q = __ffs(mm) - 1;
+            const sf_source& S = g.src.s[q];
+            const bool hit = (S.kind == 0) ? (i == S.a) : (S.a == 0 ? (i == S.b) : true);
+            if (hit && air) pnew = __double2float_rn(d_add((double)pnew, sv[q]));
+        }
+        PO[c] = pnew;
+
+        vxm = ux;
+        pc = pn;
+        pn = pnn;
+        vxc = vxn;
+        vyc = vyn;
+        vzc = vzn;
+        fc = fnn;
+    }
+}
+
+// Does the tile (with a one-cell margin, for the neighbours' faces) reach
+// the grid's material box?  Outside it every ADE term is absent.
+__device__ __forceinline__ bool tile_meets_box(const SfGridDev& g, int chunk, int jb, int kb, int by) {
+    const int i0 = chunk * g.ich - 1, i1 = chunk * g.ich + g.ich + 1;
+    const int j0 = jb * by - 1, j1 = jb * by + by + 1;
+    const int k0 = kb * 32 - 1, k1 = kb * 32 + 33;
+    return i1 > g.ade_lo[0] && i0 < g.ade_hi[0] && j1 > g.ade_lo[1] && j0 < g.ade_hi[1] &&
+           k1 > g.ade_lo[2] && k0 < g.ade_hi[2];
+}
+
+template <int BY>
+__global__ void __launch_bounds__(32 * BY) k_batch_step(const SfGridDev* __restrict__ grids,
+                                                        const int4* __restrict__ tiles, int n_tiles,
+                                                        int* __restrict__ queue,
+                                                        const long long* __restrict__ step_ptr,
+                                                        int trial) {
+    __shared__ int t_sh;
+    __shared__ SfGridDev g_sh;  // the tile's grid descriptor, with its pole table
+    const long long s = *step_ptr;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (;;) {
+        if (tid == 0) t_sh = atomicAdd(queue, 1);
+        __syncthreads();
+        const int t = t_sh;
+        if (t >= n_tiles) return;
+        const int4 T = tiles[t];  // grid, i-chunk, j-block, k-block
+        {   // stage the descriptor in shared memory (word by word)
+            const int* src = reinterpret_cast<const int*>(grids + T.x);
+            int* dst = reinterpret_cast<int*>(&g_sh);
+            for (int w = tid; w < (int)(sizeof(SfGridDev) / sizeof(int)); w += 32 * BY)
+                dst[w] = src[w];
+        }
+        __syncthreads();
+        if (s < g_sh.n_steps) {
+            const bool geom = g_sh.flags != nullptr;
+            const bool ade = g_sh.poles.n > 0 && tile_meets_box(g_sh, T.y, T.z, T.w, BY);
+            if (geom) {
+                if (ade) batch_column<BY, true, true>(g_sh, s, T.y, T.z, T.w, trial != 0);
+                else batch_column<BY, true, false>(g_sh, s, T.y, T.z, T.w, trial != 0);
+            } else {
+                if (ade) batch_column<BY, false, true>(g_sh, s, T.y, T.z, T.w, trial != 0);
+                else batch_column<BY, false, false>(g_sh, s, T.y, T.z, T.w, trial != 0);
+            }
+        }
+        __syncthreads();  // everyone is done with t_sh and g_sh
+    }
+}
+
+// ADE density poles of every grid that has them, over its material box
+// (ade.cpp:25-68 and 118-170), from the step's input pressure.
+__global__ void k_batch_ade_density(const SfGridDev* __restrict__ grids, const int* __restrict__ ids,
+                                    const long long* __restrict__ step_ptr) {
+    const long long s = *step_ptr;
+    const SfGridDev& g = grids[ids[blockIdx.y]];
+    if (s >= g.n_steps || g.poles.n_density == 0) return;
+    const float* __restrict__ P = g.f[(g.cur0 + s) & 1][0];
+    const int ex = g.ade_hi[0] - g.ade_lo[0], ey = g.ade_hi[1] - g.ade_lo[1],
+              ez = g.ade_hi[2] - g.ade_lo[2];
+    const long long total = (long long)ex * ey * ez;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = g.ade_lo[0] + (int)(t / ((long long)ey * ez));
+        const int r = (int)(t % ((long long)ey * ez));
+        const int j = g.ade_lo[1] + r / ez, k = g.ade_lo[2] + r % ez;
+        const long long c = (long long)i * g.plane + (long long)j * g.nz + k;
+        const uint8_t mc = g.mat[c];
+        if (mc == 0) continue;
+        const float pc = P[c];
+        for (int q = 0; q < g.poles.n; ++q) {
+            const sf_pole& pl = g.poles.p[q];
+            if (pl.target != 0 || pl.material_id != mc) continue;
+            const float j0 = pl.J[c];
+            if (pl.kind == 0) {
+                pl.J[c] = f_add(f_mul(pl.c0, j0), f_mul(pl.c1, pc));
+            } else {
+                const float jp = pl.J_prev[c];
+                pl.J[c] = f_add(f_add(f_mul(pl.c0, j0), f_mul(pl.c1, jp)), f_mul(pl.c2, pc));
+                pl.J_prev[c] = j0;
+            }
+        }
+    }
+}
+
+// Probe samples of every grid after the step (core/solver.py:2435-2439).
+__global__ void k_batch_post(const SfGridDev* __restrict__ grids, const long long* __restrict__ step_ptr) {
+    const long long s = *step_ptr;
+    const SfGridDev& g = grids[blockIdx.x];
+    if (s >= g.n_steps || g.n_probe == 0 || g.trace == nullptr) return;
+    const float* __restrict__ P = g.f[(g.cur0 + s + 1) & 1][0];
+    for (int t = threadIdx.x; t < g.n_probe; t += blockDim.x)
+        g.trace[s * g.n_probe + t] = P[g.probe_cells[t]];
+}
+
+__global__ void k_batch_advance(long long* step_ptr, int* queue) {
+    *step_ptr += 1;
+    *queue = 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+struct sf_batch {
+    struct Member {
+        sf_plan* plan;
+        long long steps;
+        const double* src;
+        float* trace;
+    };
+    std::vector<Member> members;
+    int rows = 8;
+    int i_chunk = 0;
+    int device = 0;
+    bool built = false;
+    SfGridDev* d_grids = nullptr;
+    int4* d_tiles = nullptr;
+    int n_tiles = 0;
+    int* d_ade_ids = nullptr;
+    int n_ade = 0;
+    int ade_blocks = 1;
+    int* d_queue = nullptr;
+    long long* d_step = nullptr;
+    int blocks = 0;  // persistent grid size
+    long long max_steps = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_steps = 0;
+};
+
+namespace {
+
+void free_device(sf_batch* B) {
+    if (B->graph_exec) cudaGraphExecDestroy(B->graph_exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    B->graph_exec = nullptr;
+    B->graph = nullptr;
+    B->graph_steps = 0;
+    cudaFree(B->d_grids);
+    cudaFree(B->d_tiles);
+    cudaFree(B->d_ade_ids);
+    cudaFree(B->d_queue);
+    cudaFree(B->d_step);
+    B->d_grids = nullptr;
+    B->d_tiles = nullptr;
+    B->d_ade_ids = nullptr;
+    B->d_queue = nullptr;
+    B->d_step = nullptr;
+    B->built = false;
+}
+
+int chunk_for_grid(const sf_batch* B, const sf_plan* P) {
+    if (B->i_chunk > 0) return B->i_chunk;
+    // about 16 planes per tile, fewer for thin grids
+    return P->d.nx < 32 ? (P->d.nx + 1) / 2 : 16;
+}
+
+template <int BY>
+int occupancy_blocks(int* out) {
+    int dev = 0, sms = 0, per = 0;
+    SF_CUDA_OK(cudaGetDevice(&dev));
+    SF_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SF_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<BY>, 32 * BY, 0));
+    *out = sms * (per > 0 ? per : 1);
+    return 0;
+}
+
+int build(sf_batch* B) {
+    free_device(B);
+    if (B->members.empty()) return sf_fail("sf_batch: no members");
+    std::vector<SfGridDev> grids;
+    std::vector<int4> tiles;
+    std::vector<int> ade_ids;
+    // largest grids first, so the queue hands out the long work early
+    std::vector<int> order(B->members.size());
+    for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return B->members[a].plan->n * B->members[a].steps > B->members[b].plan->n * B->members[b].steps;
+    });
+    B->max_steps = 0;
+    long long ade_cells = 0;
+    for (int q : order) {
+        const auto& m = B->members[q];
+        const sf_plan* P = m.plan;
+        SfGridDev g{};
+        g.nx = P->d.nx;
+        g.ny = P->d.ny;
+        g.nz = P->d.nz;
+        g.ich = chunk_for_grid(B, P);
+        g.plane = (long long)P->d.ny * P->d.nz;
+        g.n_steps = m.steps;
+        g.cv = P->d.coeff_v;
+        g.cp = P->d.coeff_p;
+        g.cur0 = P->cur;
+        g.n_probe = m.trace ? P->n_probe : 0;
+        for (int a = 0; a < 2; ++a)
+            for (int f = 0; f < 4; ++f) g.f[a][f] = P->f[a][f];
+        g.flags = P->flags;
+        g.dx = P->decay[0];
+        g.dy = P->decay[1];
+        g.dz = P->decay[2];
+        g.src_val = m.src;
+        g.probe_cells = P->probe_cells;
+        g.trace = m.trace;
+        g.mat = P->mat;
+        for (int a = 0; a < 3; ++a) {
+            g.ade_lo[a] = P->ade_lo[a];
+            g.ade_hi[a] = P->ade_hi[a];
+        }
+        g.src = P->src;
+        g.poles = P->poles;
+        const int gi = (int)grids.size();
+        grids.push_back(g);
+        if (g.poles.n > 0 && g.poles.n_density > 0) {
+            ade_ids.push_back(gi);
+            ade_cells = std::max(ade_cells, (long long)(g.ade_hi[0] - g.ade_lo[0]) *
+                                                (g.ade_hi[1] - g.ade_lo[1]) * (g.ade_hi[2] - g.ade_lo[2]));
+        }
+        B->max_steps = std::max(B->max_steps, m.steps);
+        const int nch = (g.nx + g.ich - 1) / g.ich, njb = (g.ny + B->rows - 1) / B->rows,
+                  nkb = (g.nz + 31) / 32;
+        for (int ch = 0; ch < nch; ++ch)
+            for (int jb = 0; jb < njb; ++jb)
+                for (int kb = 0; kb < nkb; ++kb) tiles.push_back(make_int4(gi, ch, jb, kb));
+    }
+    if (tiles.size() > 0x7fffffff) return sf_fail("sf_batch: too many tiles");
+    B->n_tiles = (int)tiles.size();
+    B->n_ade = (int)ade_ids.size();
+    B->ade_blocks = (int)std::min<long long>(std::max<long long>(1, (ade_cells + 255) / 256), 512);
+    SF_CUDA_OK(cudaMalloc(&B->d_grids, sizeof(SfGridDev) * grids.size()));
+    SF_CUDA_OK(cudaMemcpy(B->d_grids, grids.data(), sizeof(SfGridDev) * grids.size(),
+                          cudaMemcpyHostToDevice));
+    SF_CUDA_OK(cudaMalloc(&B->d_tiles, sizeof(int4) * tiles.size()));
+    SF_CUDA_OK(cudaMemcpy(B->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice));
+    if (!ade_ids.empty()) {
+        SF_CUDA_OK(cudaMalloc(&B->d_ade_ids, sizeof(int) * ade_ids.size()));
+        SF_CUDA_OK(cudaMemcpy(B->d_ade_ids, ade_ids.data(), sizeof(int) * ade_ids.size(),
+                              cudaMemcpyHostToDevice));
+    }
+    SF_CUDA_OK(cudaMalloc(&B->d_queue, sizeof(int)));
+    SF_CUDA_OK(cudaMalloc(&B->d_step, sizeof(long long)));
+    int rc = 0;
+    switch (B->rows) {
+        case 4: rc = occupancy_blocks<4>(&B->blocks); break;
+        case 16: rc = occupancy_blocks<16>(&B->blocks); break;
+        default: rc = occupancy_blocks<8>(&B->blocks); break;
+    }
+    if (rc) return rc;
+    B->built = true;
+    return 0;
+}
+
+int launch_step_kernel(sf_batch* B, cudaStream_t st, int trial) {
+    switch (B->rows) {
+        case 4:
+            k_batch_step<4><<<B->blocks, dim3(32, 4), 0, st>>>(B->d_grids, B->d_tiles, B->n_tiles,
+                                                                B->d_queue, B->d_step, trial);
+            break;
+        case 16:
+            k_batch_step<16><<<B->blocks, dim3(32, 16), 0, st>>>(B->d_grids, B->d_tiles, B->n_tiles,
+                                                                  B->d_queue, B->d_step, trial);
+            break;
+        default:
+            k_batch_step<8><<<B->blocks, dim3(32, 8), 0, st>>>(B->d_grids, B->d_tiles, B->n_tiles,
+                                                                B->d_queue, B->d_step, trial);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_batch_step launch failed");
+}
+
+// One batch step: ADE density pass, step, probes, advance.
+int enqueue_step(sf_batch* B, cudaStream_t st) {
+    if (B->n_ade > 0)
+        k_batch_ade_density<<<dim3(B->ade_blocks, B->n_ade), 256, 0, st>>>(B->d_grids, B->d_ade_ids,
+                                                                           B->d_step);
+    if (int rc = launch_step_kernel(B, st, 0)) return rc;
+    k_batch_post<<<(int)B->members.size(), 64, 0, st>>>(B->d_grids, B->d_step);
+    k_batch_advance<<<1, 1, 0, st>>>(B->d_step, B->d_queue);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_batch: launch failed");
+}
+
+}  // namespace
+
+extern "C" {
+
+int sf_batch_create(sf_batch** out) {
+    if (!out) return sf_fail("sf_batch_create: NULL argument");
+    auto* B = new sf_batch();
+    cudaGetDevice(&B->device);
+    *out = B;
+    return 0;
+}
+
+int sf_batch_destroy(sf_batch* B) {
+    if (!B) return 0;
+    DeviceGuard g(B->device);
+    free_device(B);
+    delete B;
+    return 0;
+}
+
+int sf_batch_add(sf_batch* B, sf_plan* P, int64_t n_steps, const double* src_values_dev,
+                 float* trace_dev) {
+    if (!B || !P) return sf_fail("sf_batch_add: NULL argument");
+    if (!P->bound) return sf_fail("sf_batch_add: plan fields not bound");
+    if (P->device != B->device) return sf_fail("sf_batch_add: plan on another device");
+    if (n_steps < 0) return sf_fail("sf_batch_add: negative step count");
+    if (P->src.n > 0 && n_steps > 0 && !src_values_dev)
+        return sf_fail("sf_batch_add: sources need src_values");
+    B->members.push_back({P, n_steps, src_values_dev, trace_dev});
+    B->built = false;
+    return 0;
+}
+
+int sf_batch_clear(sf_batch* B) {
+    if (!B) return sf_fail("sf_batch_clear: NULL batch");
+    DeviceGuard g(B->device);
+    free_device(B);
+    B->members.clear();
+    return 0;
+}
+
+int sf_batch_set_tiles(sf_batch* B, int rows, int i_chunk) {
+    if (!B) return sf_fail("sf_batch_set_tiles: NULL batch");
+    if (rows != 4 && rows != 8 && rows != 16) return sf_fail("sf_batch_set_tiles: rows must be 4, 8 or 16");
+    if (i_chunk < 0) return sf_fail("sf_batch_set_tiles: negative i_chunk");
+    B->rows = rows;
+    B->i_chunk = i_chunk;
+    B->built = false;
+    return 0;
+}
+
+int sf_batch_tiles(const sf_batch* B) { return B ? B->n_tiles : -1; }
+
+int sf_batch_run(sf_batch* B, int64_t n_steps, int graph_steps, void* stream) {
+    if (!B) return sf_fail("sf_batch_run: NULL batch");
+    DeviceGuard g(B->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!B->built)
+        if (int rc = build(B)) return rc;
+    if (n_steps <= 0) return 0;
+    SF_CUDA_OK(cudaMemsetAsync(B->d_step, 0, sizeof(long long), st));
+    SF_CUDA_OK(cudaMemsetAsync(B->d_queue, 0, sizeof(int), st));
+    int64_t done = 0;
+    if (graph_steps > 0 && n_steps >= graph_steps) {
+        if (!B->graph_exec || B->graph_steps != graph_steps) {
+            if (B->graph_exec) cudaGraphExecDestroy(B->graph_exec);
+            if (B->graph) cudaGraphDestroy(B->graph);
+            B->graph_exec = nullptr;
+            B->graph = nullptr;
+            cudaStream_t cap;
+            SF_CUDA_OK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            int rc = 0;
+            if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                rc = sf_fail("sf_batch_run: stream capture failed to begin");
+            } else {
+                for (int q = 0; q < graph_steps && !rc; ++q) rc = enqueue_step(B, cap);
+                if (cudaStreamEndCapture(cap, &B->graph) != cudaSuccess && !rc)
+                    rc = sf_fail("sf_batch_run: stream capture failed");
+            }
+            cudaStreamDestroy(cap);
+            if (rc) return rc;
+            SF_CUDA_OK(cudaGraphInstantiate(&B->graph_exec, B->graph, 0));
+            B->graph_steps = graph_steps;
+        }
+        while (n_steps - done >= graph_steps) {
+            SF_CUDA_OK(cudaGraphLaunch(B->graph_exec, st));
+            done += graph_steps;
+        }
+    }
+    for (; done < n_steps; ++done)
+        if (int rc = enqueue_step(B, st)) return rc;
+    // the members' current sets and step counts move with the batch
+    for (auto& m : B->members) {
+        const long long ran = std::min<long long>(m.steps, n_steps);
+        m.plan->cur = (int)((m.plan->cur + ran) & 1);
+        m.plan->steps_done += ran;
+        m.steps -= ran;
+        if (m.src) m.src += ran * m.plan->src.n;
+        if (m.trace) m.trace += ran * m.plan->n_probe;
+    }
+    B->built = false;  // descriptors carry cur0 / remaining steps
+    return 0;
+}
+
+int sf_batch_autotune(sf_batch* B, int launches, void* stream, float* ms_out, int* best_rows,
+                      int* best_chunk) {
+    if (!B) return sf_fail("sf_batch_autotune: NULL batch");
+    if (launches < 1) launches = 1;
+    DeviceGuard g(B->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int rows_c[3] = {4, 8, 16};
+    const int chunk_c[3] = {8, 16, 32};
+    cudaEvent_t e0, e1;
+    SF_CUDA_OK(cudaEventCreate(&e0));
+    SF_CUDA_OK(cudaEventCreate(&e1));
+    float best = -1.0f;
+    int br = B->rows, bc = B->i_chunk;
+    int rc = 0;
+    for (int a = 0; a < 3 && !rc; ++a)
+        for (int b = 0; b < 3 && !rc; ++b) {
+            B->rows = rows_c[a];
+            B->i_chunk = chunk_c[b];
+            if ((rc = build(B))) break;
+            // trial launches: step 0 of every member, out of place, no J writes,
+            // no probes and no step advance -- the members' state is untouched
+            if (cudaMemsetAsync(B->d_step, 0, sizeof(long long), st) != cudaSuccess) {
+                rc = sf_fail("sf_batch_autotune: memset failed");
+                break;
+            }
+            float ms = 0.0f;
+            for (int q = 0; q <= launches && !rc; ++q) {
+                if (q == 1) cudaEventRecord(e0, st);
+                cudaMemsetAsync(B->d_queue, 0, sizeof(int), st);
+                rc = launch_step_kernel(B, st, 1);
+            }
+            if (rc) break;
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = sf_fail("sf_batch_autotune: timing failed");
+                break;
+            }
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= launches;
+            if (ms_out) ms_out[a * 3 + b] = ms;
+            if (best < 0 || ms < best) {
+                best = ms;
+                br = rows_c[a];
+                bc = chunk_c[b];
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    B->rows = br;
+    B->i_chunk = bc;
+    B->built = false;
+    if (rc) return rc;
+    if (best_rows) *best_rows = br;
+    if (best_chunk) *best_chunk = bc;
+    return 0;
+}
+
+}  // extern "C"

@@ -63,6 +63,7 @@ struct SfStepArgs {
     float* __restrict__ trace_prev;  // probe values of the input state, or null
     const uint8_t* __restrict__ mat;  // ADE material ids (ADE kernels only)
     int reverse;                      // column kernels: dispatch i-chunks high to low
+    int ade_lo[3], ade_hi[3];         // box holding every material cell
 };
 
 #define SF_CUDA_OK(expr)                                                   \

@@ -1,0 +1,56 @@
+// sf_plan_internal.h -- the plan object behind the sf_plan handle, shared by
+// the host-side translation units (sf_api.cu, sf_batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sf_common.cuh"
+
+struct sf_plan {
+    sf_grid_desc d{};
+    long long n = 0;
+    int device = 0;
+    float* f[2][4] = {{nullptr}};
+    int cur = 0;
+    bool bound = false;
+    uint8_t* flags = nullptr;  // owned; null = no geometry (all air)
+    float* decay[3] = {nullptr, nullptr, nullptr};  // owned, 1.0f where axis off
+    SfSources src{};
+    long long* probe_cells = nullptr;  // owned
+    int n_probe = 0;
+    SfPoles poles{};
+    const uint8_t* mat = nullptr;  // caller-owned
+    int variant = 0;               // kernel configuration (SF_CFG_*), 0 = auto
+    int i_chunk = 0;               // planes per block in march / column kernels (0 = auto)
+    int tuned = 0;                 // configuration chosen by sf_plan_autotune (0 = none)
+    long long steps_done = 0;      // steps issued so far (alternates the chunk order)
+    int ade_lo[3] = {0, 0, 0};     // box holding every material cell (density pre-pass)
+    int ade_hi[3] = {0, 0, 0};
+};
+
+// Planes per block for the slab march: enough (j,k)-tile x i-chunk blocks
+// for about four waves of 8 resident blocks on each of the SMs.
+inline int auto_chunk(const sf_plan* P, int kspan) {
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long tiles = (long long)((P->d.nz + kspan - 1) / kspan) * ((P->d.ny + 7) / 8);
+    long long chunks = (4LL * 8 * sms + tiles - 1) / tiles;
+    if (chunks < 1) chunks = 1;
+    long long ich = (P->d.nx + chunks - 1) / chunks;
+    if (ich < 4) ich = 4;
+    if (ich > P->d.nx) ich = P->d.nx;
+    return (int)ich;
+}
+
+
+// Makes the plan's device current for the scope of a call.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+};

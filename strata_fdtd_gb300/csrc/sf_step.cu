@@ -165,9 +165,15 @@ __global__ void __launch_bounds__(BX* BY) k_step(SfStepArgs a, SfSources src, Sf
 
 // Density-pole recursions from the old pressure, before the step kernel
 // reads the updated J (ade.cpp:25-68 Debye, 118-170 Lorentz).
+// Walks only the box that holds every material cell.
 __global__ void k_ade_density(SfStepArgs a, SfPoles poles, long long n) {
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n;
-         c += (long long)gridDim.x * blockDim.x) {
+    const int ey = a.ade_hi[1] - a.ade_lo[1], ez = a.ade_hi[2] - a.ade_lo[2];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = a.ade_lo[0] + (int)(t / ((long long)ey * ez));
+        const int r = (int)(t % ((long long)ey * ez));
+        const long long c = (long long)i * a.plane + (long long)(a.ade_lo[1] + r / ez) * a.nz +
+                            (a.ade_lo[2] + r % ez);
         const uint8_t mc = a.mat[c];
         if (mc == 0) continue;
         const float pc = a.p[c];
@@ -280,9 +286,10 @@ int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& pol
     dim3 blk(BX, BY, 1), grd((a.nz + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nx);
     const bool ade = poles.n > 0;
     if (ade && poles.n_density > 0) {
-        const long long n = (long long)a.nx * a.plane;
+        const long long n = (long long)(a.ade_hi[0] - a.ade_lo[0]) * (a.ade_hi[1] - a.ade_lo[1]) *
+                            (a.ade_hi[2] - a.ade_lo[2]);
         const int blocks = (int)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16);
-        k_ade_density<<<blocks, 256, 0, st>>>(a, poles, n);
+        if (n > 0) k_ade_density<<<blocks, 256, 0, st>>>(a, poles, n);
     }
     if (geom) {
         if (ade)

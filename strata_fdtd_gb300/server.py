@@ -1,0 +1,280 @@
+"""A served stream of independent solves with continuous batching.
+
+Requests (each a fully configured FDTD solve and a step count) arrive over
+time.  The server keeps every admitted solve's fields, flags, PML tables and
+ADE state resident in HBM and advances all of them together in step groups
+(one batched persistent launch per time step, see batch.py).  At every group
+boundary it retires finished solves (freeing their memory) and admits the
+requests that have arrived, first come first served, as long as the sum of
+their exact device footprints stays within the HBM budget.  A solve's result
+is bit-identical whether it ran alone or in the mix.
+
+The scheduling logic is independent of the GPU: it drives an *executor*
+(``GPUExecutor`` here; tests substitute a fake one to exercise admission,
+failures and cancellation on the CPU).
+
+Failure handling (no GPU fault is involved in any of it): a request whose
+footprint exceeds the whole budget is rejected at submission; a request whose
+construction raises (malformed spec, failed allocation) is marked failed and
+the server carries on; a request can be cancelled before or while it runs;
+a solve whose pressure turns non-finite is stopped and marked failed.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+from typing import Any, Callable
+
+import numpy as np
+
+
+@dataclass
+class Request:
+    """One solve: ``build()`` returns a configured solver (it is called only
+    when the request is admitted), ``steps`` time steps, ``arrival`` seconds
+    after the stream starts, ``nbytes`` its device footprint."""
+
+    rid: int
+    build: Callable[[], Any]
+    steps: int
+    arrival: float = 0.0
+    nbytes: int = 0
+    status: str = "queued"
+    error: str | None = None
+    t_admit: float | None = None
+    t_done: float | None = None
+    result: dict | None = None
+    remaining: int = 0
+    handle: Any = None
+    cancel_requested: bool = False
+    cell_updates: int = 0
+
+    @property
+    def latency(self) -> float | None:
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+def solve_bytes(shape, geometry=True, debye_poles=0, lorentz_poles=0, probes=2, sources=1) -> int:
+    """Exact device bytes one solve holds: two ping-pong sets of p, vx, vy,
+    vz (32 B/cell), the geometry mask and the flag byte (2 B/cell with a
+    geometry), material ids (1 B/cell with ADE), 4 B/cell per Debye and
+    8 B/cell per Lorentz auxiliary field, plus PML decays, probe cells and
+    the energy scratch."""
+    nx, ny, nz = shape
+    n = nx * ny * nz
+    b = 32 * n + (2 * n if geometry else 0)
+    if debye_poles or lorentz_poles:
+        b += n + 4 * n * debye_poles + 8 * n * lorentz_poles
+    b += 4 * (nx + ny + nz) + 8 * probes + 8 * sources
+    return b
+
+
+class SolveServer:
+    """Continuous-batching request loop over ``executor``.
+
+    ``hbm_budget``: bytes of device memory the resident solves may hold;
+    ``step_group``: time steps between admission points;
+    ``max_active``: cap on concurrently resident solves."""
+
+    def __init__(self, executor, hbm_budget: float = 160e9, step_group: int = 100,
+                 max_active: int = 512, clock=time.perf_counter):
+        self.ex = executor
+        self.budget = int(hbm_budget)
+        self.step_group = int(step_group)
+        self.max_active = int(max_active)
+        self.clock = clock
+        self.queue: list[Request] = []
+        self.active: list[Request] = []
+        self.finished: list[Request] = []
+        self.in_use = 0
+        self.peak_in_use = 0
+        self.peak_active = 0
+        self.groups = 0
+
+    # -- submission ----------------------------------------------------------
+    def submit(self, req: Request) -> Request:
+        if req.nbytes > self.budget:
+            req.status, req.error = "rejected", (
+                f"needs {req.nbytes} bytes, above the {self.budget}-byte budget")
+            self.finished.append(req)
+            return req
+        req.remaining = int(req.steps)
+        self.queue.append(req)
+        return req
+
+    def cancel(self, rid: int) -> bool:
+        for r in self.queue + self.active:
+            if r.rid == rid:
+                r.cancel_requested = True
+                return True
+        return False
+
+    # -- scheduling ----------------------------------------------------------
+    def _admit(self, now: float) -> None:
+        keep = []
+        for r in self.queue:
+            if r.cancel_requested:
+                r.status, r.t_done = "cancelled", now
+                self.finished.append(r)
+                continue
+            if (r.arrival <= now and len(self.active) < self.max_active
+                    and self.in_use + r.nbytes <= self.budget
+                    and not keep):  # first come, first served: no overtaking
+                try:
+                    r.handle = self.ex.start(r)
+                except Exception as e:  # malformed request or failed allocation
+                    r.status, r.error, r.t_done = "failed", f"{type(e).__name__}: {e}", now
+                    self.finished.append(r)
+                    continue
+                r.status, r.t_admit = "running", now
+                self.in_use += r.nbytes
+                self.active.append(r)
+            else:
+                keep.append(r)
+        self.queue = keep
+        self.peak_in_use = max(self.peak_in_use, self.in_use)
+        self.peak_active = max(self.peak_active, len(self.active))
+
+    def _retire(self, now: float) -> None:
+        still = []
+        for r in self.active:
+            done = r.remaining <= 0
+            bad = self.ex.failed(r.handle)
+            if done or bad or r.cancel_requested:
+                if bad:
+                    r.status, r.error = "failed", bad
+                elif r.cancel_requested and not done:
+                    r.status = "cancelled"
+                else:
+                    r.status = "done"
+                    r.result = self.ex.finish(r.handle)
+                self.ex.release(r.handle)
+                r.handle = None
+                r.t_done = now
+                self.in_use -= r.nbytes
+                self.finished.append(r)
+            else:
+                still.append(r)
+        self.active = still
+
+    def run(self, requests=(), realtime: bool = True) -> dict:
+        """Serve ``requests`` (plus anything submitted before) to completion.
+        With ``realtime`` the arrival times are honoured against the clock;
+        otherwise every request counts as arrived at the start."""
+        for r in requests:
+            self.submit(r)
+        t0 = self.clock()
+        self.t0 = t0
+
+        def now():
+            return self.clock() - t0
+
+        while self.queue or self.active:
+            self._admit(now() if realtime else float("inf"))
+            if not self.active:
+                if not self.queue:
+                    break
+                wait = min(r.arrival for r in self.queue) - now()
+                if realtime and wait > 0:
+                    time.sleep(min(wait, 0.01))
+                continue
+            members = list(self.active)
+            counts = [min(self.step_group, r.remaining) for r in members]
+            self.ex.advance([r.handle for r in members], counts)
+            # requests that arrived meanwhile are set up while the GPU works;
+            # they join from the next group
+            if realtime:
+                self._admit(now())
+            self.ex.wait()
+            for r, n in zip(members, counts):
+                r.remaining -= n
+                r.cell_updates += n * self.ex.cells(r.handle)
+            self.groups += 1
+            self._retire(now())
+        return self.stats()
+
+    def stats(self) -> dict:
+        done = [r for r in self.finished if r.status == "done"]
+        lat = np.array([r.latency for r in done]) if done else np.zeros(0)
+        span = max((r.t_done for r in done), default=0.0)
+        cu = sum(r.cell_updates for r in done)
+        return {
+            "requests": len(self.finished), "done": len(done),
+            "failed": sum(r.status == "failed" for r in self.finished),
+            "rejected": sum(r.status == "rejected" for r in self.finished),
+            "cancelled": sum(r.status == "cancelled" for r in self.finished),
+            "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "mean_latency_s": float(lat.mean()) if lat.size else None,
+            "makespan_s": span, "cell_updates": cu,
+            "gcell_updates_per_s": cu / span / 1e9 if span > 0 else None,
+            "peak_hbm_bytes": self.peak_in_use, "peak_active": self.peak_active,
+            "step_groups": self.groups,
+        }
+
+
+class GPUExecutor:
+    """Runs the admitted solves on the GPU: construction on a side stream
+    (overlapping the running group), each group as one batched run."""
+
+    def __init__(self, graph_steps: int = 0, autotune: bool = False):
+        import torch
+
+        from .batch import BatchedSolver
+
+        self.torch = torch
+        self.Batched = BatchedSolver
+        self.graph_steps = graph_steps
+        self.side = torch.cuda.Stream()
+        self.main = torch.cuda.current_stream()
+        self._pending = None
+        self._new: list = []
+
+    def start(self, req):
+        with self.torch.cuda.stream(self.side):
+            s = req.build()
+        self._new.append(s)
+        return {"solver": s, "bad": None}
+
+    def advance(self, handles, counts):
+        if self._new:
+            self.main.wait_stream(self.side)
+            self._new = []
+        solvers = [h["solver"] for h in handles]
+        b = self.Batched(solvers)
+        b.run_steps(counts, graph_steps=self.graph_steps)
+        self._pending = (b, handles)
+
+    def wait(self):
+        self.torch.cuda.current_stream().synchronize()
+        if self._pending is not None:
+            _, handles = self._pending
+            for h in handles:
+                traces = h["solver"].get_probe_data()
+                if any(len(t) and not np.all(np.isfinite(t[-1:])) for t in traces.values()):
+                    h["bad"] = "pressure became non-finite at a probe"
+            self._pending = None
+
+    def failed(self, h):
+        return h["bad"]
+
+    def cells(self, h):
+        return int(np.prod(h["solver"].shape))
+
+    def finish(self, h):
+        return h["solver"].get_probe_data()
+
+    def release(self, h):
+        h["solver"] = None
+
+
+class SequentialExecutor(GPUExecutor):
+    """The baseline: one solve at a time through the single-grid path."""
+
+    def advance(self, handles, counts):
+        if self._new:
+            self.main.wait_stream(self.side)
+            self._new = []
+        for h, n in zip(handles, counts):
+            h["solver"].run_steps(n)
+        self._pending = (None, handles)

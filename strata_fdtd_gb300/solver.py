@@ -479,6 +479,12 @@ class FDTDSolver:
         _native.check(self._lib.sf_plan_set_ade(self._plan, self._mat_dev.data_ptr(), n,
                                                 ctypes.addressof(poles), float(inv_dx)),
                       "sf_plan_set_ade")
+        where = np.nonzero(self._material_id)
+        lo = [int(w.min()) for w in where] if where[0].size else [0, 0, 0]
+        hi = [int(w.max()) + 1 for w in where] if where[0].size else [0, 0, 0]
+        _native.check(self._lib.sf_plan_set_ade_box(self._plan, (ctypes.c_int32 * 3)(*lo),
+                                                    (ctypes.c_int32 * 3)(*hi)),
+                      "sf_plan_set_ade_box")
         self._ade_initialized = True
 
     @property

@@ -16,6 +16,7 @@ import numpy as np
 
 from .boundaries import PML
 from .grid import UniformGrid
+from .materials import Pole, PoleType, SimpleMaterial
 from .sdf import Box, Cylinder, Difference
 from .solver import FDTDSolver, GaussianPulse
 
@@ -66,6 +67,107 @@ def enclosure(n=400, amplitude=1.0, **kw) -> FDTDSolver:
 
 def enclosure_400(amplitude=1.0, **kw) -> FDTDSolver:
     return enclosure(400, amplitude, **kw)
+
+
+def random_debye_material(rng):
+    """Two Debye poles: tau log-uniform in [1e-5, 1e-3] s, delta_chi uniform
+    in [0.1, 1.0], each pole's target drawn (density or modulus)."""
+    poles = []
+    for _ in range(2):
+        tau = float(np.exp(rng.uniform(np.log(1e-5), np.log(1e-3))))
+        chi = float(rng.uniform(0.1, 1.0))
+        target = "density" if rng.random() < 0.5 else "modulus"
+        poles.append(Pole(PoleType.DEBYE, delta_chi=chi, target=target, tau=tau))
+    return SimpleMaterial(name="debye2", _rho=RHO_AIR, _c=C_AIR, _poles=poles)
+
+
+def material_is_stable(material, n=24, steps=1500):
+    """Stability screen for a dispersive material: a unit pressure impulse in
+    an n^3 grid filled with the material, stepped on the GPU; the material is
+    rejected when |p| ever exceeds 10 (the reference's ADE recursion diverges
+    for short relaxation times and large strengths)."""
+    s = FDTDSolver(grid=UniformGrid((n, n, n), 1e-3), c=C_AIR, rho=RHO_AIR, courant=0.5)
+    mid = s.register_material(material)
+    s.set_material_box(mid, (0, n), (0, n), (0, n))
+    c = n // 2
+    s.p[c, c, c] = 1.0
+    s.add_probe("c", (c, c, c))
+    s.run_steps(steps)
+    peak = max(float(np.nanmax(np.abs(s.get_probe_data()["c"]))), float(np.abs(s.p).max()))
+    return bool(np.isfinite(peak) and peak <= 10.0), peak
+
+
+def _place(rng, n, r, pml):
+    lo, hi = pml + r, n - pml - r
+    if hi <= lo:
+        lo, hi = pml, max(pml + 1, n - pml)
+    return int(rng.integers(lo, hi))
+
+
+def batch_workload(seed=0, n_solves=64, screen=True, pml=8):
+    """The heterogeneous batch: n_solves grids with edges log-uniform in
+    [64, 256] per axis, 1 mm cells, PML 8, 1-6 rigid spheres or boxes
+    (radius / half-edge 5-30 cells) in the non-PML interior, one box of a
+    2-pole Debye material, a 1-4 kHz pulse at a random air cell, 2 probes,
+    500-3000 steps.  Unstable material draws are redrawn (``screen``).
+    Returns (solvers, steps, info)."""
+    rng = np.random.default_rng(seed)
+    solvers, steps, rejected = [], [], 0
+    for _ in range(n_solves):
+        shape = tuple(int(round(np.exp(rng.uniform(np.log(64), np.log(256))))) for _ in range(3))
+        geom = np.ones(shape, dtype=bool)
+        for _ in range(int(rng.integers(1, 7))):
+            r = int(rng.integers(5, 31))
+            cen = [_place(rng, n, r, pml) for n in shape]
+            lo = [max(0, c - r) for c in cen]
+            hi = [min(n, c + r + 1) for c, n in zip(cen, shape)]
+            if rng.random() < 0.5:  # sphere
+                ii, jj, kk = np.ogrid[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]
+                ball = (ii - cen[0]) ** 2 + (jj - cen[1]) ** 2 + (kk - cen[2]) ** 2 <= r * r
+                geom[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] &= ~ball
+            else:
+                geom[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] = False
+        s = FDTDSolver(grid=UniformGrid(shape, 1e-3), c=C_AIR, rho=RHO_AIR, courant=0.5)
+        s.add_boundary(PML(depth=pml))
+        s.set_geometry(geom)
+        while True:
+            mat = random_debye_material(rng)
+            if not screen or material_is_stable(mat)[0]:
+                break
+            rejected += 1
+        mid = s.register_material(mat)
+        half = [int(rng.integers(5, 21)) for _ in range(3)]
+        cen = [_place(rng, n, h, pml) for n, h in zip(shape, half)]
+        s.set_material_box(mid, *[(max(0, c - h), min(n, c + h)) for c, h, n in zip(cen, half, shape)])
+
+        def air_cell():
+            while True:
+                c = tuple(int(rng.integers(pml, n - pml)) for n in shape)
+                if geom[c]:
+                    return c
+
+        s.add_source(GaussianPulse(position=air_cell(), frequency=float(rng.uniform(1000, 4000))))
+        s.add_probe("p0", air_cell())
+        s.add_probe("p1", air_cell())
+        solvers.append(s)
+        steps.append(int(rng.integers(500, 3001)))
+    return solvers, steps, {"rejected_materials": rejected, "seed": seed}
+
+
+def design_field(shape, region=64, seed=0, sigma=4.0):
+    """Seeded smooth density-scale field: uniform noise on a central
+    region^3 box, Gaussian-filtered (sigma cells), renormalised to [0, 1];
+    zero outside the box."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    theta = np.zeros(shape, dtype=np.float64)
+    r = [min(region, n) for n in shape]
+    lo = [(n - m) // 2 for n, m in zip(shape, r)]
+    box = gaussian_filter(rng.uniform(0.0, 1.0, size=r), sigma=sigma, mode="reflect")
+    box = (box - box.min()) / max(box.max() - box.min(), 1e-300)
+    theta[lo[0]:lo[0] + r[0], lo[1]:lo[1] + r[1], lo[2]:lo[2] + r[2]] = box
+    return theta
 
 
 def quick_start_100(**kw) -> FDTDSolver:

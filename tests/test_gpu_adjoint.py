@@ -1,0 +1,83 @@
+"""The reverse-time adjoint (sf_diff_*): gradients of the probe-trace loss
+w.r.t. the density field, checked against torch.autograd through a plain
+PyTorch stepping of the same scheme and against central finite differences.
+
+Tolerances: FP64 adjoint vs FP64 autograd, rel 1e-9 (same arithmetic up to
+summation order); FP64 adjoint vs central differences (h = 1e-3), rel 1e-5
+(O(h^2) truncation); the FP32 adjoint vs FP64 central differences at the
+128^3 x 2000-step workload, rel 1e-4 on 16 random design cells."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from strata_fdtd_gb300.adjoint import DifferentiableSolver, reference_loss_torch  # noqa: E402
+from strata_fdtd_gb300.workloads import design_field  # noqa: E402
+
+
+def _small(dtype, K=25):
+    return DifferentiableSolver((16, 14, 18), pml_depth=3, frequency=20000.0, source=(5, 7, 9),
+                                probes=[(12, 7, 9), (8, 3, 14)], dtype=dtype,
+                                checkpoint_every=K)
+
+
+def test_adjoint_matches_autograd_fp64():
+    s = _small(torch.float64)
+    theta = torch.tensor(design_field(s.shape, region=8, seed=1, sigma=1.5), device="cuda")
+    target = s.forward(torch.tensor(design_field(s.shape, region=8, seed=2, sigma=1.5),
+                                    device="cuda"), 60)[0]
+    th = theta.clone().requires_grad_(True)
+    loss = s.loss(th, target, 60)
+    loss.backward()
+    ref_th = theta.clone().requires_grad_(True)
+    ref = reference_loss_torch(s, ref_th, target, 60)
+    ref.backward()
+    assert float(loss) == pytest.approx(float(ref), rel=1e-12)
+    g, r = th.grad.cpu().numpy(), ref_th.grad.cpu().numpy()
+    assert np.abs(r).max() > 0
+    np.testing.assert_allclose(g, r, rtol=1e-9, atol=1e-12 * np.abs(r).max())
+
+
+def test_adjoint_matches_central_differences_fp64():
+    s = _small(torch.float64, K=16)
+    theta = torch.tensor(design_field(s.shape, region=8, seed=3, sigma=1.5), device="cuda")
+    target = s.forward(torch.zeros_like(theta), 50)[0] * 0.5
+    th = theta.clone().requires_grad_(True)
+    s.loss(th, target, 50).backward()
+    rng = np.random.default_rng(0)
+    h = 1e-3
+    for _ in range(6):
+        c = tuple(int(rng.integers(4, n - 4)) for n in s.shape)
+        tp, tm = theta.clone(), theta.clone()
+        tp[c] += h
+        tm[c] -= h
+        fd = (float(s.loss(tp, target, 50)) - float(s.loss(tm, target, 50))) / (2 * h)
+        assert float(th.grad[c]) == pytest.approx(fd, rel=1e-5, abs=1e-14)
+
+
+def test_differentiable_workload_fp32_against_fd():
+    """The 128^3 workload: 10-cell PML, design field on the central 64^3,
+    1.5 kHz source, 2000 steps, checkpoints every 100 steps; FP32 adjoint
+    gradient vs FP64 central differences (h = 1e-3) on 16 random cells."""
+    shape = (128, 128, 128)
+    probes = [(100, 64, 64), (64, 100, 40)]
+    s32 = DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
+                               probes=probes, dtype=torch.float32, checkpoint_every=100)
+    s64 = DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
+                               probes=probes, dtype=torch.float64, checkpoint_every=100)
+    theta = torch.tensor(design_field(shape, 64, seed=0), device="cuda")
+    target = s64.forward(torch.tensor(design_field(shape, 64, seed=1), device="cuda"), 2000)[0]
+    th = theta.clone().to(torch.float32).requires_grad_(True)
+    s32.loss(th, target.to(torch.float32), 2000).backward()
+    rng = np.random.default_rng(5)
+    h = 1e-3
+    worst = 0.0
+    for _ in range(16):
+        c = tuple(int(v) for v in rng.integers(32, 96, size=3))
+        tp, tm = theta.clone(), theta.clone()
+        tp[c] += h
+        tm[c] -= h
+        fd = (float(s64.loss(tp, target, 2000)) - float(s64.loss(tm, target, 2000))) / (2 * h)
+        worst = max(worst, abs(float(th.grad[c]) - fd) / abs(fd))
+    assert worst < 1e-4, worst

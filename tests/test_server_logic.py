@@ -1,0 +1,114 @@
+"""The serving loop's scheduling on the CPU, with a fake executor: FIFO
+admission against the HBM budget, continuous batching (arrivals join at
+group boundaries while others run), rejection of oversized requests, failed
+construction, cancellation and non-finite detection.  No GPU involved."""
+import numpy as np
+
+from strata_fdtd_gb300.server import Request, SolveServer, solve_bytes
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+
+class FakeExecutor:
+    """Each advanced step costs 1 ms of fake time; records group membership."""
+
+    def __init__(self, clock, fail_build=(), nan_after=None):
+        self.clock = clock
+        self.groups = []
+        self.fail_build = set(fail_build)
+        self.nan_after = nan_after or {}
+        self.done_steps = {}
+
+    def start(self, req):
+        if req.rid in self.fail_build:
+            raise MemoryError("simulated allocation failure")
+        self.done_steps[req.rid] = 0
+        return {"rid": req.rid, "bad": None}
+
+    def advance(self, handles, counts):
+        self.groups.append(sorted(h["rid"] for h in handles))
+        for h, n in zip(handles, counts):
+            self.done_steps[h["rid"]] += n
+            lim = self.nan_after.get(h["rid"])
+            if lim is not None and self.done_steps[h["rid"]] >= lim:
+                h["bad"] = "pressure became non-finite at a probe"
+        self.clock.t += 1e-3 * max(counts)
+
+    def wait(self):
+        pass
+
+    def failed(self, h):
+        return h["bad"]
+
+    def cells(self, h):
+        return 1000
+
+    def finish(self, h):
+        return {"steps": self.done_steps[h["rid"]]}
+
+    def release(self, h):
+        pass
+
+
+def _req(rid, steps, arrival=0.0, nbytes=10):
+    return Request(rid=rid, build=lambda: None, steps=steps, arrival=arrival, nbytes=nbytes)
+
+
+def test_budget_limits_residency_and_fifo_order():
+    clock = FakeClock()
+    ex = FakeExecutor(clock)
+    srv = SolveServer(ex, hbm_budget=30, step_group=10, clock=clock)
+    reqs = [_req(q, 25, nbytes=10) for q in range(6)]
+    stats = srv.run(reqs, realtime=False)
+    assert stats["done"] == 6 and stats["peak_hbm_bytes"] <= 30
+    assert max(len(g) for g in ex.groups) == 3
+    assert ex.groups[0] == [0, 1, 2]
+    # FIFO: request 3 only runs after one of the first three finished
+    first_with_3 = next(i for i, g in enumerate(ex.groups) if 3 in g)
+    assert all(len(g) == 3 for g in ex.groups[:first_with_3])
+    assert all(r.result["steps"] == 25 for r in srv.finished)
+
+
+def test_continuous_batching_admits_arrivals_between_groups():
+    clock = FakeClock()
+    ex = FakeExecutor(clock)
+    srv = SolveServer(ex, hbm_budget=1000, step_group=10, clock=clock)
+    reqs = [_req(0, 100, arrival=0.0), _req(1, 30, arrival=0.025), _req(2, 10, arrival=0.05)]
+    srv.run(reqs, realtime=True)
+    joined = {rid: next(i for i, g in enumerate(ex.groups) if rid in g) for rid in (0, 1, 2)}
+    assert joined[0] == 0 and 0 < joined[1] < joined[2]
+    # request 1 overlapped with request 0 (same groups), not queued behind it
+    assert any(set(g) >= {0, 1} for g in ex.groups)
+    done = {r.rid: r for r in srv.finished}
+    assert all(done[q].status == "done" for q in (0, 1, 2))
+    assert done[2].latency < done[0].latency
+
+
+def test_rejection_failure_cancel_and_nonfinite():
+    clock = FakeClock()
+    ex = FakeExecutor(clock, fail_build={2}, nan_after={3: 20})
+    srv = SolveServer(ex, hbm_budget=100, step_group=10, clock=clock)
+    reqs = [_req(0, 40), _req(1, 40, nbytes=500), _req(2, 40), _req(3, 60), _req(4, 80)]
+    for r in reqs:
+        srv.submit(r)
+    srv.cancel(4)
+    stats = srv.run(realtime=False)
+    st = {r.rid: r.status for r in srv.finished}
+    assert st == {0: "done", 1: "rejected", 2: "failed", 3: "failed", 4: "cancelled"}
+    errs = {r.rid: r.error for r in srv.finished}
+    assert "budget" in errs[1] and "MemoryError" in errs[2] and "non-finite" in errs[3]
+    assert stats["done"] == 1 and stats["failed"] == 2
+
+
+def test_solve_bytes_counts_every_buffer():
+    n = 40 * 50 * 60
+    assert solve_bytes((40, 50, 60), geometry=False, probes=0, sources=0) == 32 * n + 4 * 150
+    assert solve_bytes((40, 50, 60), geometry=True, debye_poles=2, probes=2, sources=1) == (
+        32 * n + 2 * n + n + 8 * n + 4 * 150 + 16 + 8)
+    assert np.isclose(solve_bytes((320, 320, 320)) / 1e9, 1.11, atol=0.02)
