@@ -56,7 +56,9 @@ def parse():
     ap.add_argument("--size", type=int, default=400, help="grid edge (400 = the workload)")
     ap.add_argument("--kernel", default="auto", help="auto (autotuned) or a kernel configuration name")
     ap.add_argument("--ichunk", type=int, default=0, help="planes per block (march)")
-    ap.add_argument("--workload", default="enclosure", choices=["enclosure", "batch"])
+    ap.add_argument("--workload", default="enclosure", choices=["enclosure", "batch", "serve"])
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--step-group", type=int, default=100)
     ap.add_argument("--batch-solves", type=int, default=64)
     ap.add_argument("--graph-steps", type=int, default=50)
     return ap.parse_args()
@@ -422,12 +424,49 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def run_serve(args):
+    """The served stream: Poisson arrivals at 200/s, edges 48-320, 500-5000
+    steps, mixed geometry, optional Debye region, 160 GB budget; continuous
+    batching vs one solve at a time on the same GPU, same requests."""
+    import torch
+
+    from strata_fdtd_gb300.server import GPUExecutor, SequentialExecutor, SolveServer
+    from strata_fdtd_gb300.workloads import served_stream
+
+    n = args.requests
+    srv = SolveServer(GPUExecutor(graph_steps=0), hbm_budget=160e9, step_group=args.step_group)
+    st = srv.run(served_stream(seed=0, n_requests=n), realtime=True)
+    res = {r.rid: r.result for r in srv.finished if r.status == "done"}
+    del srv
+    torch.cuda.empty_cache()
+    seq = SolveServer(SequentialExecutor(), hbm_budget=160e9, step_group=10**9, max_active=1)
+    st2 = seq.run(served_stream(seed=0, n_requests=n), realtime=True)
+    same = all(all(np.array_equal(res[r.rid][k], r.result[k]) for k in r.result)
+               for r in seq.finished if r.status == "done" and r.rid in res)
+    line = {
+        "metric": "Gcell-updates/s (served stream)", "value": st["gcell_updates_per_s"],
+        "unit": "Gcell-updates/s", "n_gpus": 1, "steps": st["step_groups"], "warmup": 0,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n} requests, Poisson 200/s, edges log-U[48,320], steps "
+                               "U[500,5000], PML 8-16, free/box/Helmholtz-array geometry, "
+                               "50% with a 1-2 pole Debye region, 160 GB budget",
+                   "step_group": args.step_group},
+        "served": st, "sequential": st2,
+        "throughput_ratio": (st["gcell_updates_per_s"] or 0) / (st2["gcell_updates_per_s"] or 1),
+        "results_identical": bool(same),
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 

@@ -59,8 +59,7 @@ class BatchedSolver:
         for s, n in zip(self.solvers, counts):
             s._sync_tables()
             s._upload_exposed()
-            vals = s._source_values(n)
-            src = torch.from_numpy(vals).to(s._device) if s._sources else None
+            src = s.source_table(n) if s._sources else None
             n_probe = len(s._probe_order)
             trace = (torch.empty((n, n_probe), dtype=torch.float32, device=s._device)
                      if n_probe and n else None)

@@ -361,6 +361,7 @@ class FDTDSolver:
         if len(self._sources) >= 16:
             raise ValueError("at most 16 sources are supported")
         self._sources.append(source)
+        self._src_cache = None
         self._src_dirty = True
 
     def add_probe(self, name: str, position) -> None:
@@ -538,6 +539,23 @@ class FDTDSolver:
             t += self.dt
         return vals
 
+    def precompute_sources(self, n: int) -> None:
+        """Evaluate the waveform for the next n steps now and keep it on the
+        device (a served request does this once at admission)."""
+        vals = self._source_values(n)
+        self._src_cache = (self._step_count, self._torch.from_numpy(vals).to(self._device))
+
+    def source_table(self, n: int):
+        """Device tensor [n, n_sources] of waveform values for the next n
+        steps (from the precomputed table when it covers them)."""
+        cache = getattr(self, "_src_cache", None)
+        if cache is not None:
+            start, tab = cache
+            off = self._step_count - start
+            if 0 <= off and off + n <= tab.shape[0]:
+                return tab[off:off + n]
+        return self._torch.from_numpy(self._source_values(n)).to(self._device)
+
     def _advance(self, n: int) -> None:
         """Run n time steps through one sf_plan_step call."""
         torch = self._torch
@@ -545,8 +563,7 @@ class FDTDSolver:
             return
         self._sync_tables()
         self._upload_exposed()
-        vals = self._source_values(n)
-        src_dev = torch.from_numpy(vals).to(self._device) if self._sources else None
+        src_dev = self.source_table(n) if self._sources else None
         n_probe = len(self._probe_order)
         trace = (torch.empty((n, n_probe), dtype=torch.float32, device=self._device)
                  if n_probe else None)
@@ -733,6 +750,7 @@ class FDTDSolver:
             self._host_exposed[f] = False
         self._step_count = 0
         self._time = 0.0
+        self._src_cache = None
         self._snapshots.clear()
         self._energy_history.clear()
         self._track_energy = False

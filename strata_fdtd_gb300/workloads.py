@@ -154,6 +154,100 @@ def batch_workload(seed=0, n_solves=64, screen=True, pml=8):
     return solvers, steps, {"rejected_materials": rejected, "seed": seed}
 
 
+def served_stream(seed=0, n_requests=1000, rate=200.0, edges=(48, 320), steps=(500, 5000),
+                  pml=(8, 16), ade_fraction=0.5, screen=True):
+    """The request stream: Poisson arrivals (``rate`` per second), grid
+    edges log-uniform in ``edges`` per axis, steps uniform in ``steps``, PML
+    uniform in ``pml``, geometry drawn from free field / a sealed box / a
+    block of 4-32 Helmholtz resonators (neck radius 3-8 cells, cavity 10-20
+    cells), an optional 1-2 pole Debye region.  Returns a list of
+    server.Request whose ``build`` constructs the solver on admission."""
+    from .resonator import HelmholtzResonator
+    from .sdf import Union
+    from .server import Request, solve_bytes
+
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for rid in range(n_requests):
+        t += float(rng.exponential(1.0 / rate))
+        shape = tuple(int(round(np.exp(rng.uniform(np.log(edges[0]), np.log(edges[1])))))
+                      for _ in range(3))
+        n_steps = int(rng.integers(steps[0], steps[1] + 1))
+        depth = int(rng.integers(pml[0], pml[1] + 1))
+        kind = ["free", "box", "helmholtz"][int(rng.integers(0, 3))]
+        res = 1e-3
+        spec = dict(shape=shape, depth=depth, kind=kind, seed=int(rng.integers(0, 2**31)))
+        n_poles = 0
+        if rng.random() < ade_fraction:
+            n_poles = int(rng.integers(1, 3))
+        spec["n_poles"] = n_poles
+        nbytes = solve_bytes(shape, geometry=kind != "free", debye_poles=n_poles)
+
+        def build(spec=spec, res=res):
+            r = np.random.default_rng(spec["seed"])
+            shp, d = spec["shape"], spec["depth"]
+            s = FDTDSolver(grid=UniformGrid(shp, res), c=C_AIR, rho=RHO_AIR, courant=0.5)
+            s.add_boundary(PML(depth=d))
+            inner_lo = [d + 2 for _ in shp]
+            inner_hi = [n - d - 2 for n in shp]
+            src = tuple((lo + hi) // 2 for lo, hi in zip(inner_lo, inner_hi))
+            if spec["kind"] == "box":
+                # sealed box: 3-cell walls around a cavity holding the source
+                half = [max(4, (hi - lo) // 3) for lo, hi in zip(inner_lo, inner_hi)]
+                ctr = [(c + 0.5) * res for c in src]
+                outer = Box(center=ctr, size=[2 * (h + 3) * res for h in half])
+                cav = Box(center=ctr, size=[2 * h * res for h in half])
+                s.set_geometry_sdf(Difference(outer, cav))
+            elif spec["kind"] == "helmholtz":
+                # a block of resonators on the low-x side, necks opening to +x
+                span = [hi - lo for lo, hi in zip(inner_lo, inner_hi)]
+                nres = int(r.integers(4, 33))
+                cav = int(r.integers(10, 21))
+                neck_r = int(r.integers(3, 9))
+                per = max(1, int(np.ceil(np.sqrt(nres))))
+                bx = inner_lo[0] + cav + 6
+                res_list = []
+                for q in range(nres):
+                    a, b = q % per, q // per
+                    cy = inner_lo[1] + (a + 0.5) * span[1] / per
+                    cz = inner_lo[2] + (b + 0.5) * span[2] / per
+                    res_list.append(HelmholtzResonator(
+                        position=(inner_lo[0] * res + cav * res / 2 + 2 * res, cy * res, cz * res),
+                        cavity_shape="box", cavity_size=(cav * res,) * 3, neck_length=4 * res,
+                        neck_radius=neck_r * res, neck_direction=(1, 0, 0)))
+                block = Box(min_corner=(inner_lo[0] * res, inner_lo[1] * res, inner_lo[2] * res),
+                            max_corner=(bx * res, inner_hi[1] * res, inner_hi[2] * res))
+                s.set_geometry_sdf(Difference(block, Union(*res_list)))
+                src = (min(inner_hi[0] - 1, bx + 4), src[1], src[2])
+            if spec["n_poles"]:
+                while True:
+                    mat = random_debye_material(r)
+                    mat._poles = mat._poles[: spec["n_poles"]]
+                    if not screen or material_is_stable(mat)[0]:
+                        break
+                mid = s.register_material(mat)
+                half = [int(r.integers(3, 9)) for _ in shp]
+                cen = [int(r.integers(lo + h, max(lo + h + 1, hi - h)))
+                       for lo, hi, h in zip(inner_lo, inner_hi, half)]
+                s.set_material_box(mid, *[(c - h, c + h) for c, h in zip(cen, half)])
+            geom = s.geometry
+            if not geom[src]:
+                air = np.argwhere(geom[inner_lo[0]:inner_hi[0], inner_lo[1]:inner_hi[1],
+                                       inner_lo[2]:inner_hi[2]])
+                if len(air):
+                    src = tuple(int(v) + lo for v, lo in zip(air[len(air) // 2], inner_lo))
+            s.add_source(GaussianPulse(position=src, frequency=float(r.uniform(1000, 4000))))
+            s.add_probe("near", src)
+            s.add_probe("far", tuple(hi - 1 for hi in inner_hi))
+            s.precompute_sources(spec["steps"])
+            return s
+
+        spec["steps"] = n_steps
+        out.append(Request(rid=rid, build=build, steps=n_steps, arrival=t, nbytes=nbytes))
+    return out
+
+
 def design_field(shape, region=64, seed=0, sigma=4.0):
     """Seeded smooth density-scale field: uniform noise on a central
     region^3 box, Gaussian-filtered (sigma cells), renormalised to [0, 1];
