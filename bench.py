@@ -59,6 +59,10 @@ def parse():
     ap.add_argument("--workload", default="enclosure", choices=["enclosure", "batch", "serve"])
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--step-group", type=int, default=100)
+    ap.add_argument("--max-active-cells", type=int, default=1 << 26,
+                    help="served stream: cap on the cells of the running solves (0 = none)")
+    ap.add_argument("--solo-cells", type=int, default=1 << 24,
+                    help="served stream: solves this large step alone (0 = batch all)")
     ap.add_argument("--batch-solves", type=int, default=64)
     ap.add_argument("--graph-steps", type=int, default=50)
     return ap.parse_args()
@@ -434,13 +438,18 @@ def run_serve(args):
     from strata_fdtd_gb300.workloads import served_stream
 
     n = args.requests
-    srv = SolveServer(GPUExecutor(graph_steps=0), hbm_budget=160e9, step_group=args.step_group)
+    ex = GPUExecutor(graph_steps=0, solo_cells=args.solo_cells or None)
+    srv = SolveServer(ex, hbm_budget=160e9, step_group=args.step_group,
+                      max_active_cells=args.max_active_cells or None)
     st = srv.run(served_stream(seed=0, n_requests=n), realtime=True)
+    st["host_advance_s"], st["host_wait_s"] = ex.host_advance_s, ex.host_wait_s
     res = {r.rid: r.result for r in srv.finished if r.status == "done"}
     del srv
     torch.cuda.empty_cache()
-    seq = SolveServer(SequentialExecutor(), hbm_budget=160e9, step_group=10**9, max_active=1)
+    ex2 = SequentialExecutor()
+    seq = SolveServer(ex2, hbm_budget=160e9, step_group=10**9, max_active=1)
     st2 = seq.run(served_stream(seed=0, n_requests=n), realtime=True)
+    st2["host_advance_s"], st2["host_wait_s"] = ex2.host_advance_s, ex2.host_wait_s
     same = all(all(np.array_equal(res[r.rid][k], r.result[k]) for k in r.result)
                for r in seq.finished if r.status == "done" and r.rid in res)
     line = {
@@ -451,7 +460,8 @@ def run_serve(args):
         "config": {"workload": f"{n} requests, Poisson 200/s, edges log-U[48,320], steps "
                                "U[500,5000], PML 8-16, free/box/Helmholtz-array geometry, "
                                "50% with a 1-2 pole Debye region, 160 GB budget",
-                   "step_group": args.step_group},
+                   "step_group": args.step_group, "max_active_cells": args.max_active_cells,
+                   "solo_cells": args.solo_cells},
         "served": st, "sequential": st2,
         "throughput_ratio": (st["gcell_updates_per_s"] or 0) / (st2["gcell_updates_per_s"] or 1),
         "results_identical": bool(same),

@@ -138,6 +138,13 @@ int sf_plan_set_sources(sf_plan* plan, int n, const sf_source* sources);
  * (core/solver.py:2435-2439). */
 int sf_plan_set_probes(sf_plan* plan, int n, const int64_t* cells);
 
+/* Omni microphones: per microphone 8 corner cells (flat indices) and 8
+ * float weights, host arrays of 8*n, in the corner order and float
+ * arithmetic of precompute_microphone_data (microphones.cpp:16-80);
+ * recorded after each step by sf_plan_step_ex as the float sum from 0 of
+ * weight * p (record_microphones_batch, microphones.cpp:82-118). */
+int sf_plan_set_microphones(sf_plan* plan, int n, const int64_t* idx8, const float* w8);
+
 /* ADE materials: material_id (device, nx*ny*nz bytes) and the pole table
  * (at most SF_MAX_POLES; Debye poles first, then Lorentz, each in field
  * order, as ADEMaterialData holds them).  inv_dx = float(1/dx).  Replaces
@@ -181,6 +188,10 @@ int sf_plan_autotune(sf_plan* plan, int launches, void* stream, float* ms_out, i
  * Replaces FDTDSolver.step's native dispatch (core/solver.py:2003-2102). */
 int sf_plan_step(sf_plan* plan, int64_t n_steps, const double* src_values_dev,
                  float* trace_dev, void* stream);
+/* Same, also writing microphone samples to mic_trace_dev [n_steps][n_mics]
+ * (may be NULL). */
+int sf_plan_step_ex(sf_plan* plan, int64_t n_steps, const double* src_values_dev,
+                    float* trace_dev, float* mic_trace_dev, void* stream);
 
 /* Acoustic energy of the current state, (1/2) sum(p^2/(rho c^2) + rho v^2)
  * dV over air cells, as compute_energy (core/solver.py:2689-2705); result
@@ -265,11 +276,12 @@ int sf_diff_forward(const sf_diff_desc* d, void* const* cv, void* const* set0, v
  * starting from set `cur` holding lambda after the last step; p_store as
  * written by the forward; the probe-loss gradient weight*2*(trace-target)
  * is injected before each step's adjoint; dL/dcv accumulates into
- * grad_cv[3]. */
+ * grad_cv[3], three arrays of N doubles whatever the dtype (the per-face sum
+ * runs over every step and cancels, so it is kept in FP64). */
 int sf_diff_adjoint(const sf_diff_desc* d, void* const* cv, void* const* lam0, void* const* lam1,
                     int cur, int64_t n_steps, const void* p_store, const void* trace,
                     const void* target, double weight, void* const* grad_cv, void* stream);
-/* dL/dtheta from dL/dcv. */
+/* dL/dtheta (dtype) from dL/dcv (grad_cv: FP64, as sf_diff_adjoint). */
 int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* grad_cv, void* out,
                        void* stream);
 

@@ -431,6 +431,36 @@ class FDTDSolver:
         b.initialize(self)
         self._boundaries.append(b)
 
+    def add_microphone(self, position, name=None, pattern="omni"):
+        """Omni microphone with the native batch path's float32 trilinear
+        weights (core/solver.py:930-960 -> _kernels/src/microphones.cpp:16-80)."""
+        if not hasattr(self, "_mics"):
+            self._mics = {}
+        g = [np.float32(position[a] / self.dx) for a in range(3)]
+        i0 = [int(v) for v in g]
+        f = [np.float32(v - np.float32(i)) for v, i in zip(g, i0)]
+        one = np.float32(1.0)
+        fx, fy, fz = f
+        w = [(one - fx) * (one - fy) * (one - fz), fx * (one - fy) * (one - fz),
+             (one - fx) * fy * (one - fz), fx * fy * (one - fz), (one - fx) * (one - fy) * fz,
+             fx * (one - fy) * fz, (one - fx) * fy * fz, fx * fy * fz]
+        corners = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1), (0, 1, 1),
+                   (1, 1, 1)]
+        idx = [(i0[0] + a, i0[1] + b, i0[2] + c) for a, b, c in corners]
+        self._mics[name or f"mic_{len(self._mics)}"] = dict(idx=idx, w=[np.float32(x) for x in w],
+                                                             data=[])
+
+    def _record_mics(self):
+        """record_microphones_batch (microphones.cpp:82-118): float sum from 0."""
+        for m in getattr(self, "_mics", {}).values():
+            s = np.float32(0.0)
+            for q in range(8):
+                s = np.float32(s + np.float32(m["w"][q] * self.p[m["idx"][q]]))
+            m["data"].append(s)
+
+    def get_mic_data(self):
+        return {k: np.array(m["data"], dtype=np.float32) for k, m in getattr(self, "_mics", {}).items()}
+
     def register_material(self, material, material_id=None):
         if material_id is None:
             material_id = next(i for i in range(1, 256) if i not in self._materials)
@@ -544,6 +574,7 @@ class FDTDSolver:
             F("inject")(_ptr(p), g, nx, ny, nz, kind, a, b_, c, val)
         for pr in self._probes.values():
             pr.data.append(p[pr.position])
+        self._record_mics()
         self._step_count += 1
         self._time += self.dt
 
@@ -554,8 +585,13 @@ class FDTDSolver:
         return (1, s.position["axis"], s.position["index"], 0)
 
     def run_steps(self, n):
-        """n steps of the plain path through one C call (no ADE, one PML)."""
-        assert not self._materials and len(self._boundaries) <= 1
+        """n steps of the plain path through one C call (no ADE, one PML);
+        with ADE materials or microphones, step by step."""
+        if self._materials or getattr(self, "_mics", None):
+            for _ in range(n):
+                self.step()
+            return
+        assert len(self._boundaries) <= 1
         nx, ny, nz = self.shape
         R = self.real
         vals = np.zeros((n, max(1, len(self._sources))), dtype=np.float64)

@@ -8,6 +8,7 @@ kernels behind a C ABI (include/sf_gb300.h) loaded with ctypes.
 from ._native import NativeError, build
 from .boundaries import PML, RigidBoundary
 from .grid import UniformGrid
+from .microphones import Microphone
 from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
 from .resonator import HelmholtzResonator, helmholtz_array
 from .sdf import (Box, CSGNode, Cylinder, Difference, Intersection, Scale, SDFPrimitive, Sphere,
@@ -17,7 +18,7 @@ from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_nativ
 __version__ = "0.1.0"
 
 __all__ = [
-    "FDTDSolver", "GaussianPulse", "Probe", "UniformGrid", "PML", "RigidBoundary", "Pole",
+    "FDTDSolver", "GaussianPulse", "Probe", "Microphone", "UniformGrid", "PML", "RigidBoundary", "Pole",
     "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale",
     "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",

@@ -17,7 +17,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB_PATH = os.path.join(BUILD, "libsf_gb300.so")
-SOURCES = ("sf_step.cu", "sf_step_march.cu", "sf_step_col.cu", "sf_voxel.cu", "sf_batch.cu", "sf_adjoint.cu",
+SOURCES = ("sf_step.cu", "sf_step_march.cu", "sf_step_col.cu", "sf_step_tile.cu", "sf_voxel.cu",
+           "sf_batch.cu", "sf_adjoint.cu",
            "sf_api.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -116,6 +117,8 @@ SIGNATURES = {
     "sf_kernel_config_name": (ctypes.c_char_p, [_I]),
     "sf_plan_autotune": (_I, [_P, _I, _P, _P, _P]),
     "sf_plan_step": (_I, [_P, _I64, _P, _P, _P]),
+    "sf_plan_step_ex": (_I, [_P, _I64, _P, _P, _P, _P]),
+    "sf_plan_set_microphones": (_I, [_P, _I, _P, _P]),
     "sf_energy_scratch_doubles": (_I64, [_P]),
     "sf_plan_energy": (_I, [_P, _D, _D, _D, _P, _P, _P]),
     "sf_plan_energy_noalloc": (_I, [_P, _D, _D, _D, _P, _P]),

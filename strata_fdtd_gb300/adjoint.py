@@ -151,7 +151,8 @@ class DifferentiableSolver:
         tgt[:, :target.shape[1]] = target.to(self.dtype)
         lam = [self._zeros4(), self._zeros4()]
         lcur = 0
-        grad_cv = [torch.zeros(self.shape, dtype=self.dtype, device=self.dev) for _ in range(3)]
+        # per-face dL/dcv sums run over every step: FP64 accumulators
+        grad_cv = [torch.zeros(self.shape, dtype=torch.float64, device=self.dev) for _ in range(3)]
         desc = self._desc()
         store = torch.empty((self.K,) + self.shape, dtype=self.dtype, device=self.dev)
         seg_starts = list(range(0, n_steps, self.K))

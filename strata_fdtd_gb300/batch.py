@@ -25,6 +25,8 @@ class BatchedSolver:
     def __init__(self, solvers, rows: int = 8, i_chunk: int = 0):
         if not solvers:
             raise ValueError("BatchedSolver needs at least one solver")
+        if any(s._microphones for s in solvers):
+            raise NotImplementedError("microphones are recorded by single-solver runs only")
         self.solvers = list(solvers)
         self._lib = _native.load()
         self._torch = self.solvers[0]._torch

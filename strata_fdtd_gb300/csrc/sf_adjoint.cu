@@ -112,13 +112,14 @@ __global__ void k_dinject(T* __restrict__ lp, const int64_t* __restrict__ cells,
 }
 
 // Adjoint of one step.  in: lambda after the step; out: lambda before it;
-// pst: p^n (the step's input pressure); g*: accumulated dL/dcv per face.
+// pst: p^n (the step's input pressure); g*: accumulated dL/dcv per face,
+// held in FP64 whatever T is (the sum runs over every step and cancels).
 template <typename T>
 __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restrict__ lx,
                        const T* __restrict__ ly, const T* __restrict__ lz, T* __restrict__ lpo,
                        T* __restrict__ lxo, T* __restrict__ lyo, T* __restrict__ lzo,
-                       const T* __restrict__ pst, T* __restrict__ gx, T* __restrict__ gy,
-                       T* __restrict__ gz) {
+                       const T* __restrict__ pst, double* __restrict__ gx,
+                       double* __restrict__ gy, double* __restrict__ gz) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -142,7 +143,7 @@ __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restr
     // mu_v on the low faces (owned by the lower neighbour)
     T vx_lo = T(0), vy_lo = T(0), vz_lo = T(0);
     if (i > 0) vx_lo = g.dx[i - 1] * lx[c - plane] + g.cp * (mup(i - 1, j, k, c - plane) - m0);
-    if (j > 0) vy_lo = dj * ly[c - nz] + g.cp * (mup(i, j - 1, k, c - nz) - m0);
+    if (j > 0) vy_lo = g.dy[j - 1] * ly[c - nz] + g.cp * (mup(i, j - 1, k, c - nz) - m0);
     if (k > 0) vz_lo = g.dz[k - 1] * lz[c - 1] + g.cp * (mup(i, j, k - 1, c - 1) - m0);
     lxo[c] = vx_hi;
     lyo[c] = vy_hi;
@@ -156,28 +157,28 @@ __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restr
     lpo[c] = acc;
     // dL/dcv on the high faces: mu_v * (p^n[hi] - p^n[lo])
     const T p0 = pst[c];
-    if (i < nx - 1) gx[c] += vx_hi * (pst[c + plane] - p0);
-    if (j < ny - 1) gy[c] += vy_hi * (pst[c + nz] - p0);
-    if (k < nz - 1) gz[c] += vz_hi * (pst[c + 1] - p0);
+    if (i < nx - 1) gx[c] += double(vx_hi) * double(pst[c + plane] - p0);
+    if (j < ny - 1) gy[c] += double(vy_hi) * double(pst[c + nz] - p0);
+    if (k < nz - 1) gz[c] += double(vz_hi) * double(pst[c + 1] - p0);
 }
 
 // dL/dtheta(c) = (dt/dx) rho0 / (2 rho(c)^2) * sum of dL/dcv over its faces.
 template <typename T>
-__global__ void k_dgrad(const T* __restrict__ theta, const T* __restrict__ gx,
-                        const T* __restrict__ gy, const T* __restrict__ gz, T* __restrict__ out,
-                        int nx, int ny, int nz, T dt_dx, T rho0) {
+__global__ void k_dgrad(const T* __restrict__ theta, const double* __restrict__ gx,
+                        const double* __restrict__ gy, const double* __restrict__ gz,
+                        T* __restrict__ out, int nx, int ny, int nz, double dt_dx, double rho0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= nz || j >= ny) return;
     const long long plane = (long long)ny * nz;
     const long long c = (long long)i * plane + (long long)j * nz + k;
-    T s = gx[c] + gy[c] + gz[c];  // high faces (zero on the last plane)
+    double s = gx[c] + gy[c] + gz[c];  // high faces (zero on the last plane)
     if (i > 0) s += gx[c - plane];
     if (j > 0) s += gy[c - nz];
     if (k > 0) s += gz[c - 1];
-    const T rho = rho0 * (T(1) + theta[c]);
-    out[c] = s * dt_dx * rho0 / (T(2) * rho * rho);
+    const double rho = rho0 * (1.0 + double(theta[c]));
+    out[c] = T(s * dt_dx * rho0 / (2.0 * rho * rho));
 }
 
 template <typename T>
@@ -240,8 +241,8 @@ int adjoint(const sf_diff_desc* d, const void* const* cv, void* const* lam0, voi
                 (T)weight);
         k_dadj<T><<<grid_of(d), dim3(32, 8), 0, st>>>(
             g, (const T*)in[0], (const T*)in[1], (const T*)in[2], (const T*)in[3], (T*)out[0],
-            (T*)out[1], (T*)out[2], (T*)out[3], ps + s * N, (T*)grad_cv[0], (T*)grad_cv[1],
-            (T*)grad_cv[2]);
+            (T*)out[1], (T*)out[2], (T*)out[3], ps + s * N, (double*)grad_cv[0],
+            (double*)grad_cv[1], (double*)grad_cv[2]);
         cur = 1 - cur;
     }
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_adjoint: launch failed");
@@ -314,9 +315,8 @@ int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* gr
             (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     else
         k_dgrad<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const float*)theta, (const float*)grad_cv[0], (const float*)grad_cv[1],
-            (const float*)grad_cv[2], (float*)out, d->nx, d->ny, d->nz, (float)d->dt_over_dx,
-            (float)d->rho0);
+            (const float*)theta, (const double*)grad_cv[0], (const double*)grad_cv[1],
+            (const double*)grad_cv[2], (float*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_grad_theta: launch failed");
 }
 

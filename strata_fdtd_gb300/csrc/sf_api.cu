@@ -24,6 +24,7 @@
 // Step-kernel configuration used when the plan has not been autotuned.
 #ifndef SF_CFG_DEFAULT
 #define SF_CFG_DEFAULT (SF_CFG_COL_FIRST + 0)
+#define SF_CFG_TILE_FIRST (SF_CFG_COL_FIRST + kSfColConfigCount)
 #endif
 
 namespace {
@@ -119,6 +120,8 @@ int sf_plan_destroy(sf_plan* P) {
     for (auto& d : P->decay) cudaFree(d);
     cudaFree(P->flags);
     cudaFree(P->probe_cells);
+    cudaFree(P->mic_idx);
+    cudaFree(P->mic_w);
     delete P;
     return 0;
 }
@@ -260,7 +263,7 @@ int sf_plan_set_ade_box(sf_plan* P, const int32_t* lo, const int32_t* hi) {
 
 int sf_plan_set_kernel(sf_plan* P, int config, int i_chunk) {
     if (!P) return sf_fail("sf_plan_set_kernel: NULL plan");
-    if (config < 0 || config >= SF_CFG_COL_FIRST + kSfColConfigCount)
+    if (config < 0 || config >= sf_kernel_config_count())
         return sf_fail("sf_plan_set_kernel: unknown kernel configuration");
     if (i_chunk < 0) return sf_fail("sf_plan_set_kernel: negative i_chunk");
     P->variant = config;
@@ -268,7 +271,9 @@ int sf_plan_set_kernel(sf_plan* P, int config, int i_chunk) {
     return 0;
 }
 
-int sf_kernel_config_count(void) { return SF_CFG_COL_FIRST + kSfColConfigCount; }
+int sf_kernel_config_count(void) {
+    return SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount;
+}
 
 const char* sf_kernel_config_name(int config) {
     if (config == SF_CFG_AUTO) return "auto";
@@ -276,6 +281,8 @@ const char* sf_kernel_config_name(int config) {
     if (config == SF_CFG_MARCH) return "march";
     if (config >= SF_CFG_COL_FIRST && config < SF_CFG_COL_FIRST + kSfColConfigCount)
         return kSfColConfigs[config - SF_CFG_COL_FIRST].name;
+    if (config >= SF_CFG_TILE_FIRST && config < sf_kernel_config_count())
+        return kSfTileConfigs[config - SF_CFG_TILE_FIRST].name;
     return nullptr;
 }
 
@@ -327,6 +334,11 @@ int effective_config(const sf_plan* P) {
 
 int chunk_for(const sf_plan* P, int cfg) {
     if (P->i_chunk > 0) return P->i_chunk;
+    if (cfg >= SF_CFG_TILE_FIRST) {
+        const SfTileConfig& t = kSfTileConfigs[cfg - SF_CFG_TILE_FIRST];
+        if (P->d.nz % 4 == 0) return auto_chunk(P, 32, 4 * t.rows * t.warps);
+        return auto_chunk(P, 32);
+    }
     int kspan = 32;
     if (cfg >= SF_CFG_COL_FIRST) {
         const int vec = kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec;
@@ -335,10 +347,20 @@ int chunk_for(const sf_plan* P, int cfg) {
     return auto_chunk(P, kspan);
 }
 
+// Whether configuration cfg runs as itself on this plan's grid (otherwise
+// its launcher substitutes the first column configuration).
+bool config_native(const sf_plan* P, int cfg, const SfStepArgs& a) {
+    if (cfg >= SF_CFG_TILE_FIRST) return sf_tile_supported(a);
+    if (cfg >= SF_CFG_COL_FIRST) return P->d.nz % kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec == 0;
+    return true;
+}
+
 int launch_config(const sf_plan* P, int cfg, int ich, const SfStepArgs& a, const SfSources& src,
                   cudaStream_t st) {
     const bool g = P->flags != nullptr;
     if (cfg == SF_CFG_MARCH) return sf_launch_step_march(a, src, g, ich, st);
+    if (cfg >= SF_CFG_TILE_FIRST)
+        return sf_launch_step_tile_cfg(a, src, g, cfg - SF_CFG_TILE_FIRST, ich, st);
     if (cfg >= SF_CFG_COL_FIRST)
         return sf_launch_step_col_cfg(a, src, g, cfg - SF_CFG_COL_FIRST, ich, st);
     return sf_launch_step(a, src, P->poles, g, st);
@@ -350,6 +372,11 @@ extern "C" {
 
 int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* trace,
                  void* stream) {
+    return sf_plan_step_ex(P, n_steps, src_values, trace, nullptr, stream);
+}
+
+int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float* trace,
+                    float* mic_trace, void* stream) {
     if (!P) return sf_fail("sf_plan_step: NULL plan");
     if (!P->bound) return sf_fail("sf_plan_step: fields not bound");
     if (n_steps < 0) return sf_fail("sf_plan_step: negative step count");
@@ -361,6 +388,7 @@ int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* t
     fill_args(P, a, trace != nullptr);
     const int cfg = effective_config(P);
     const int ich = chunk_for(P, cfg);
+    const bool mics = mic_trace != nullptr && P->n_mic > 0;
     for (int64_t s = 0; s < n_steps; ++s) {
         set_io(P, a, P->cur);
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
@@ -369,10 +397,34 @@ int sf_plan_step(sf_plan* P, int64_t n_steps, const double* src_values, float* t
         if (int rc = launch_config(P, cfg, ich, a, P->src, st)) return rc;
         P->cur = 1 - P->cur;
         ++P->steps_done;
+        if (mics)
+            if (int rc = sf_launch_mic_gather(P->f[P->cur][0], P->mic_idx, P->mic_w, P->n_mic,
+                                              mic_trace + s * P->n_mic, st))
+                return rc;
     }
     if (trace && P->n_probe > 0)
         return sf_launch_probe_gather(P->f[P->cur][0], P->probe_cells, P->n_probe,
                                       trace + (n_steps - 1) * P->n_probe, st);
+    return 0;
+}
+
+int sf_plan_set_microphones(sf_plan* P, int n, const int64_t* idx8, const float* w8) {
+    if (!P) return sf_fail("sf_plan_set_microphones: NULL plan");
+    if (n < 0 || (n > 0 && (!idx8 || !w8))) return sf_fail("sf_plan_set_microphones: bad table");
+    for (long long q = 0; q < 8LL * n; ++q)
+        if (idx8[q] < 0 || idx8[q] >= P->n)
+            return sf_fail("sf_plan_set_microphones: corner cell outside the grid");
+    DeviceGuard g(P->device);
+    cudaFree(P->mic_idx);
+    cudaFree(P->mic_w);
+    P->mic_idx = nullptr;
+    P->mic_w = nullptr;
+    P->n_mic = n;
+    if (n == 0) return 0;
+    SF_CUDA_OK(cudaMalloc(&P->mic_idx, sizeof(long long) * 8 * n));
+    SF_CUDA_OK(cudaMalloc(&P->mic_w, sizeof(float) * 8 * n));
+    SF_CUDA_OK(cudaMemcpy(P->mic_idx, idx8, sizeof(long long) * 8 * n, cudaMemcpyHostToDevice));
+    SF_CUDA_OK(cudaMemcpy(P->mic_w, w8, sizeof(float) * 8 * n, cudaMemcpyHostToDevice));
     return 0;
 }
 
@@ -382,7 +434,7 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     if (launches < 1) launches = 1;
     DeviceGuard g(P->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int count = SF_CFG_COL_FIRST + kSfColConfigCount;
+    const int count = sf_kernel_config_count();
     if (ms_out)
         for (int q = 0; q < count; ++q) ms_out[q] = -1.0f;
     if (P->poles.n > 0) {  // ADE runs the per-cell kernel only
@@ -404,8 +456,7 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     float best_ms = 0.0f;
     int rc = 0;
     for (int cfg = SF_CFG_CELL; cfg < count && !rc; ++cfg) {
-        if (cfg >= SF_CFG_COL_FIRST && P->d.nz % kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec != 0)
-            continue;
+        if (!config_native(P, cfg, a)) continue;
         const int ich = chunk_for(P, cfg);
         if ((rc = launch_config(P, cfg, ich, a, none, st))) break;  // warm-up
         if (cudaEventRecord(e0, st) != cudaSuccess) { rc = sf_fail("event record failed"); break; }

@@ -197,8 +197,10 @@ __device__ void batch_column(const SfGridDev& g, long long s, int chunk, int jb,
 }
 
 // Does the tile (with a one-cell margin, for the neighbours' faces) reach
-// the grid's material box?  Outside it every ADE term is absent.
-__device__ __forceinline__ bool tile_meets_box(const SfGridDev& g, int chunk, int jb, int kb, int by) {
+// the grid's material box?  Outside it every ADE term is absent, so such
+// tiles go to the plain kernel.
+__host__ __device__ __forceinline__ bool tile_meets_box(const SfGridDev& g, int chunk, int jb,
+                                                        int kb, int by) {
     const int i0 = chunk * g.ich - 1, i1 = chunk * g.ich + g.ich + 1;
     const int j0 = jb * by - 1, j1 = jb * by + by + 1;
     const int k0 = kb * 32 - 1, k1 = kb * 32 + 33;
@@ -206,7 +208,9 @@ __device__ __forceinline__ bool tile_meets_box(const SfGridDev& g, int chunk, in
            k1 > g.ade_lo[2] && k0 < g.ade_hi[2];
 }
 
-template <int BY>
+// Persistent tile loop.  ADEK selects the tile kind this launch serves:
+// tiles away from every material box (plain), or tiles that meet one.
+template <int BY, bool ADEK>
 __global__ void __launch_bounds__(32 * BY) k_batch_step(const SfGridDev* __restrict__ grids,
                                                         const int4* __restrict__ tiles, int n_tiles,
                                                         int* __restrict__ queue,
@@ -230,15 +234,10 @@ __global__ void __launch_bounds__(32 * BY) k_batch_step(const SfGridDev* __restr
         }
         __syncthreads();
         if (s < g_sh.n_steps) {
-            const bool geom = g_sh.flags != nullptr;
-            const bool ade = g_sh.poles.n > 0 && tile_meets_box(g_sh, T.y, T.z, T.w, BY);
-            if (geom) {
-                if (ade) batch_column<BY, true, true>(g_sh, s, T.y, T.z, T.w, trial != 0);
-                else batch_column<BY, true, false>(g_sh, s, T.y, T.z, T.w, trial != 0);
-            } else {
-                if (ade) batch_column<BY, false, true>(g_sh, s, T.y, T.z, T.w, trial != 0);
-                else batch_column<BY, false, false>(g_sh, s, T.y, T.z, T.w, trial != 0);
-            }
+            if (g_sh.flags != nullptr)
+                batch_column<BY, true, ADEK>(g_sh, s, T.y, T.z, T.w, trial != 0);
+            else
+                batch_column<BY, false, ADEK>(g_sh, s, T.y, T.z, T.w, trial != 0);
         }
         __syncthreads();  // everyone is done with t_sh and g_sh
     }
@@ -291,7 +290,8 @@ __global__ void k_batch_post(const SfGridDev* __restrict__ grids, const long lon
 
 __global__ void k_batch_advance(long long* step_ptr, int* queue) {
     *step_ptr += 1;
-    *queue = 0;
+    queue[0] = 0;
+    queue[1] = 0;
 }
 
 }  // namespace
@@ -311,14 +311,16 @@ struct sf_batch {
     int device = 0;
     bool built = false;
     SfGridDev* d_grids = nullptr;
-    int4* d_tiles = nullptr;
-    int n_tiles = 0;
+    int4* d_tiles = nullptr;  // plain tiles, then ADE tiles
+    int n_tiles = 0;          // plain tiles
+    int n_tiles_ade = 0;      // tiles that meet a material box
     int* d_ade_ids = nullptr;
     int n_ade = 0;
     int ade_blocks = 1;
-    int* d_queue = nullptr;
+    int* d_queue = nullptr;   // [0] plain queue head, [1] ADE queue head
     long long* d_step = nullptr;
-    int blocks = 0;  // persistent grid size
+    int blocks = 0;      // persistent grid size, plain kernel
+    int blocks_ade = 0;  // persistent grid size, ADE kernel
     long long max_steps = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -352,21 +354,28 @@ int chunk_for_grid(const sf_batch* B, const sf_plan* P) {
     return P->d.nx < 32 ? (P->d.nx + 1) / 2 : 16;
 }
 
-template <int BY>
+template <int BY, bool ADEK>
 int occupancy_blocks(int* out) {
     int dev = 0, sms = 0, per = 0;
     SF_CUDA_OK(cudaGetDevice(&dev));
     SF_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SF_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<BY>, 32 * BY, 0));
+    SF_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<BY, ADEK>, 32 * BY,
+                                                             0));
     *out = sms * (per > 0 ? per : 1);
     return 0;
+}
+
+template <int BY>
+int occupancy_both(sf_batch* B) {
+    if (int rc = occupancy_blocks<BY, false>(&B->blocks)) return rc;
+    return occupancy_blocks<BY, true>(&B->blocks_ade);
 }
 
 int build(sf_batch* B) {
     free_device(B);
     if (B->members.empty()) return sf_fail("sf_batch: no members");
     std::vector<SfGridDev> grids;
-    std::vector<int4> tiles;
+    std::vector<int4> tiles, tiles_ade;
     std::vector<int> ade_ids;
     // largest grids first, so the queue hands out the long work early
     std::vector<int> order(B->members.size());
@@ -418,10 +427,15 @@ int build(sf_batch* B) {
                   nkb = (g.nz + 31) / 32;
         for (int ch = 0; ch < nch; ++ch)
             for (int jb = 0; jb < njb; ++jb)
-                for (int kb = 0; kb < nkb; ++kb) tiles.push_back(make_int4(gi, ch, jb, kb));
+                for (int kb = 0; kb < nkb; ++kb) {
+                    const bool ade = g.poles.n > 0 && tile_meets_box(g, ch, jb, kb, B->rows);
+                    (ade ? tiles_ade : tiles).push_back(make_int4(gi, ch, jb, kb));
+                }
     }
-    if (tiles.size() > 0x7fffffff) return sf_fail("sf_batch: too many tiles");
+    if (tiles.size() + tiles_ade.size() > 0x7fffffff) return sf_fail("sf_batch: too many tiles");
     B->n_tiles = (int)tiles.size();
+    B->n_tiles_ade = (int)tiles_ade.size();
+    tiles.insert(tiles.end(), tiles_ade.begin(), tiles_ade.end());
     B->n_ade = (int)ade_ids.size();
     B->ade_blocks = (int)std::min<long long>(std::max<long long>(1, (ade_cells + 255) / 256), 512);
     SF_CUDA_OK(cudaMalloc(&B->d_grids, sizeof(SfGridDev) * grids.size()));
@@ -434,32 +448,34 @@ int build(sf_batch* B) {
         SF_CUDA_OK(cudaMemcpy(B->d_ade_ids, ade_ids.data(), sizeof(int) * ade_ids.size(),
                               cudaMemcpyHostToDevice));
     }
-    SF_CUDA_OK(cudaMalloc(&B->d_queue, sizeof(int)));
+    SF_CUDA_OK(cudaMalloc(&B->d_queue, 2 * sizeof(int)));
     SF_CUDA_OK(cudaMalloc(&B->d_step, sizeof(long long)));
     int rc = 0;
     switch (B->rows) {
-        case 4: rc = occupancy_blocks<4>(&B->blocks); break;
-        case 16: rc = occupancy_blocks<16>(&B->blocks); break;
-        default: rc = occupancy_blocks<8>(&B->blocks); break;
+        case 4: rc = occupancy_both<4>(B); break;
+        case 16: rc = occupancy_both<16>(B); break;
+        default: rc = occupancy_both<8>(B); break;
     }
     if (rc) return rc;
     B->built = true;
     return 0;
 }
 
+template <int BY>
+void launch_pair(sf_batch* B, cudaStream_t st, int trial) {
+    if (B->n_tiles > 0)
+        k_batch_step<BY, false><<<B->blocks, dim3(32, BY), 0, st>>>(
+            B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step, trial);
+    if (B->n_tiles_ade > 0)
+        k_batch_step<BY, true><<<B->blocks_ade, dim3(32, BY), 0, st>>>(
+            B->d_grids, B->d_tiles + B->n_tiles, B->n_tiles_ade, B->d_queue + 1, B->d_step, trial);
+}
+
 int launch_step_kernel(sf_batch* B, cudaStream_t st, int trial) {
     switch (B->rows) {
-        case 4:
-            k_batch_step<4><<<B->blocks, dim3(32, 4), 0, st>>>(B->d_grids, B->d_tiles, B->n_tiles,
-                                                                B->d_queue, B->d_step, trial);
-            break;
-        case 16:
-            k_batch_step<16><<<B->blocks, dim3(32, 16), 0, st>>>(B->d_grids, B->d_tiles, B->n_tiles,
-                                                                  B->d_queue, B->d_step, trial);
-            break;
-        default:
-            k_batch_step<8><<<B->blocks, dim3(32, 8), 0, st>>>(B->d_grids, B->d_tiles, B->n_tiles,
-                                                                B->d_queue, B->d_step, trial);
+        case 4: launch_pair<4>(B, st, trial); break;
+        case 16: launch_pair<16>(B, st, trial); break;
+        default: launch_pair<8>(B, st, trial);
     }
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_batch_step launch failed");
 }
@@ -536,7 +552,7 @@ int sf_batch_run(sf_batch* B, int64_t n_steps, int graph_steps, void* stream) {
         if (int rc = build(B)) return rc;
     if (n_steps <= 0) return 0;
     SF_CUDA_OK(cudaMemsetAsync(B->d_step, 0, sizeof(long long), st));
-    SF_CUDA_OK(cudaMemsetAsync(B->d_queue, 0, sizeof(int), st));
+    SF_CUDA_OK(cudaMemsetAsync(B->d_queue, 0, 2 * sizeof(int), st));
     int64_t done = 0;
     if (graph_steps > 0 && n_steps >= graph_steps) {
         if (!B->graph_exec || B->graph_steps != graph_steps) {
@@ -607,7 +623,7 @@ int sf_batch_autotune(sf_batch* B, int launches, void* stream, float* ms_out, in
             float ms = 0.0f;
             for (int q = 0; q <= launches && !rc; ++q) {
                 if (q == 1) cudaEventRecord(e0, st);
-                cudaMemsetAsync(B->d_queue, 0, sizeof(int), st);
+                cudaMemsetAsync(B->d_queue, 0, 2 * sizeof(int), st);
                 rc = launch_step_kernel(B, st, 1);
             }
             if (rc) break;

@@ -6,7 +6,8 @@
 
 // Step-kernel configuration indices used by sf_plan_set_kernel /
 // sf_plan_autotune: 0 = automatic, 1 = per-cell kernel, 2 = slab march,
-// SF_CFG_COL_FIRST + c = column kernel configuration c.
+// SF_CFG_COL_FIRST + c = column kernel configuration c, then the warp-tile
+// configurations.
 enum { SF_CFG_AUTO = 0, SF_CFG_CELL = 1, SF_CFG_MARCH = 2, SF_CFG_COL_FIRST = 3 };
 
 struct SfColConfig {
@@ -15,6 +16,16 @@ struct SfColConfig {
 };
 extern const SfColConfig kSfColConfigs[];
 extern const int kSfColConfigCount;
+
+// Warp-tile kernel configurations follow the column ones:
+// index SF_CFG_COL_FIRST + kSfColConfigCount + t.
+struct SfTileConfig {
+    int rows, warps, minb, prefetch;
+    const char* name;
+};
+extern const SfTileConfig kSfTileConfigs[];
+extern const int kSfTileConfigCount;
+bool sf_tile_supported(const SfStepArgs& a);
 
 int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, int nz,
                           cudaStream_t st);
@@ -26,6 +37,10 @@ int sf_launch_step_march(const SfStepArgs& a, const SfSources& src, bool geom, i
                          cudaStream_t st);
 int sf_launch_step_col_cfg(const SfStepArgs& a, const SfSources& src, bool geom, int cfg, int ich,
                            cudaStream_t st);
+int sf_launch_step_tile_cfg(const SfStepArgs& a, const SfSources& src, bool geom, int cfg, int ich,
+                            cudaStream_t st);
+int sf_launch_mic_gather(const float* p, const long long* idx, const float* w, int n, float* out,
+                         cudaStream_t st);
 long long sf_energy_blocks(long long n);
 int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,
                      const uint8_t* flags, long long n, double* scratch, double* out2,

@@ -23,17 +23,21 @@ struct sf_plan {
     int i_chunk = 0;               // planes per block in march / column kernels (0 = auto)
     int tuned = 0;                 // configuration chosen by sf_plan_autotune (0 = none)
     long long steps_done = 0;      // steps issued so far (alternates the chunk order)
+    int n_mic = 0;                 // omni microphones: 8 corner cells and weights each
+    long long* mic_idx = nullptr;  // owned
+    float* mic_w = nullptr;        // owned
     int ade_lo[3] = {0, 0, 0};     // box holding every material cell (density pre-pass)
     int ade_hi[3] = {0, 0, 0};
 };
 
-// Planes per block for the slab march: enough (j,k)-tile x i-chunk blocks
-// for about four waves of 8 resident blocks on each of the SMs.
-inline int auto_chunk(const sf_plan* P, int kspan) {
+// Planes per block: enough (j,k)-tile x i-chunk blocks for about four waves
+// of 8 resident blocks on each of the SMs.  kspan / jspan: cells a block
+// covers along k / j.
+inline int auto_chunk(const sf_plan* P, int kspan, int jspan = 8) {
     int sms = 152;
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long tiles = (long long)((P->d.nz + kspan - 1) / kspan) * ((P->d.ny + 7) / 8);
+    const long long tiles = (long long)((P->d.nz + kspan - 1) / kspan) * ((P->d.ny + jspan - 1) / jspan);
     long long chunks = (4LL * 8 * sms + tiles - 1) / tiles;
     if (chunks < 1) chunks = 1;
     long long ich = (P->d.nx + chunks - 1) / chunks;

@@ -198,6 +198,19 @@ __global__ void k_probe_gather(const float* __restrict__ p, const long long* __r
     if (t < n) out[t] = p[cells[t]];
 }
 
+// Omni microphones: trilinear sum over 8 corners in float, from 0, corner
+// order and weights as precompute_microphone_data / record_microphones_batch
+// (microphones.cpp:16-118).
+__global__ void k_mic_gather(const float* __restrict__ p, const long long* __restrict__ idx,
+                             const float* __restrict__ w, int n, float* __restrict__ out) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    float s = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s = f_add(s, f_mul(w[8 * m + q], p[idx[8 * m + q]]));
+    out[m] = s;
+}
+
 // Face flags from the geometry mask (boundaries.cpp:13-64 rule).
 __global__ void k_build_flags(const uint8_t* __restrict__ geom, uint8_t* __restrict__ flags,
                               int nx, int ny, int nz) {
@@ -310,6 +323,13 @@ int sf_launch_probe_gather(const float* p, const long long* cells, int n, float*
     if (n <= 0) return 0;
     k_probe_gather<<<(n + 127) / 128, 128, 0, st>>>(p, cells, n, out);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_probe_gather launch failed");
+}
+
+int sf_launch_mic_gather(const float* p, const long long* idx, const float* w, int n, float* out,
+                         cudaStream_t st) {
+    if (n <= 0) return 0;
+    k_mic_gather<<<(n + 127) / 128, 128, 0, st>>>(p, idx, w, n, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_mic_gather launch failed");
 }
 
 long long sf_energy_blocks(long long n) {

@@ -163,6 +163,22 @@ class Cylinder(SDFPrimitive):
         return np.minimum(self.p1, self.p2) - r, np.maximum(self.p1, self.p2) + r
 
 
+def _emit_fold(prog, children, op):
+    """Emit an n-ary CSG node as a left fold of two-operand steps
+    (c0, c1, op, c2, op, ...): the reference folds its children in the same
+    order, and the evaluation stack then grows with the tree's depth only,
+    not with the number of children."""
+    if not children:
+        prog.append(_node(op, n=0))
+        return
+    children[0]._emit(prog)
+    if len(children) == 1:
+        prog.append(_node(op, n=1))
+    for c in children[1:]:
+        c._emit(prog)
+        prog.append(_node(op, n=2))
+
+
 class CSGNode(SDFPrimitive):
     pass
 
@@ -174,9 +190,7 @@ class Union(CSGNode):
         self.children = children
 
     def _emit(self, prog):
-        for c in self.children:
-            c._emit(prog)
-        prog.append(_node(OP_UNION, n=len(self.children)))
+        _emit_fold(prog, self.children, OP_UNION)
 
     @cached_property
     def bounding_box(self):
@@ -193,9 +207,7 @@ class Intersection(CSGNode):
         self.children = children
 
     def _emit(self, prog):
-        for c in self.children:
-            c._emit(prog)
-        prog.append(_node(OP_INTERSECTION, n=len(self.children)))
+        _emit_fold(prog, self.children, OP_INTERSECTION)
 
     @cached_property
     def bounding_box(self):
@@ -216,10 +228,7 @@ class Difference(CSGNode):
         self.subtracted = subtracted
 
     def _emit(self, prog):
-        self.base._emit(prog)
-        for s in self.subtracted:
-            s._emit(prog)
-        prog.append(_node(OP_DIFFERENCE, n=1 + len(self.subtracted)))
+        _emit_fold(prog, (self.base,) + tuple(self.subtracted), OP_DIFFERENCE)
 
     @cached_property
     def bounding_box(self):

@@ -48,6 +48,7 @@ class Request:
     handle: Any = None
     cancel_requested: bool = False
     cell_updates: int = 0
+    cells: int = 0
 
     @property
     def latency(self) -> float | None:
@@ -74,14 +75,22 @@ class SolveServer:
 
     ``hbm_budget``: bytes of device memory the resident solves may hold;
     ``step_group``: time steps between admission points;
-    ``max_active``: cap on concurrently resident solves."""
+    ``max_active``: cap on concurrently resident solves;
+    ``max_active_cells``: cap on the cells of the running solves (None: no
+    cap).  Enough cells to fill the device keep the throughput while fewer
+    solves share it, so each finishes sooner (first come, first served
+    instead of processor sharing); a solve larger than the cap still runs,
+    alone."""
 
     def __init__(self, executor, hbm_budget: float = 160e9, step_group: int = 100,
-                 max_active: int = 512, clock=time.perf_counter):
+                 max_active: int = 512, max_active_cells: int | None = None,
+                 clock=time.perf_counter):
         self.ex = executor
         self.budget = int(hbm_budget)
         self.step_group = int(step_group)
         self.max_active = int(max_active)
+        self.max_cells = None if max_active_cells is None else int(max_active_cells)
+        self.active_cells = 0
         self.clock = clock
         self.queue: list[Request] = []
         self.active: list[Request] = []
@@ -117,8 +126,10 @@ class SolveServer:
                 r.status, r.t_done = "cancelled", now
                 self.finished.append(r)
                 continue
+            fits_cells = (self.max_cells is None or not self.active
+                          or self.active_cells + r.cells <= self.max_cells)
             if (r.arrival <= now and len(self.active) < self.max_active
-                    and self.in_use + r.nbytes <= self.budget
+                    and self.in_use + r.nbytes <= self.budget and fits_cells
                     and not keep):  # first come, first served: no overtaking
                 try:
                     r.handle = self.ex.start(r)
@@ -128,6 +139,7 @@ class SolveServer:
                     continue
                 r.status, r.t_admit = "running", now
                 self.in_use += r.nbytes
+                self.active_cells += r.cells
                 self.active.append(r)
             else:
                 keep.append(r)
@@ -152,6 +164,7 @@ class SolveServer:
                 r.handle = None
                 r.t_done = now
                 self.in_use -= r.nbytes
+                self.active_cells -= r.cells
                 self.finished.append(r)
             else:
                 still.append(r)
@@ -210,14 +223,19 @@ class SolveServer:
             "gcell_updates_per_s": cu / span / 1e9 if span > 0 else None,
             "peak_hbm_bytes": self.peak_in_use, "peak_active": self.peak_active,
             "step_groups": self.groups,
+            "errors": [(r.rid, r.status, r.error) for r in self.finished
+                       if r.status in ("failed", "rejected")][:20],
         }
 
 
 class GPUExecutor:
     """Runs the admitted solves on the GPU: construction on a side stream
-    (overlapping the running group), each group as one batched run."""
+    (overlapping the running group), each group as one batched run.  Solves
+    of ``solo_cells`` cells or more fill the device by themselves and step
+    through the single-grid column kernels instead (same results, a faster
+    kernel for one large grid); None batches everything."""
 
-    def __init__(self, graph_steps: int = 0, autotune: bool = False):
+    def __init__(self, graph_steps: int = 0, solo_cells: int | None = 1 << 24):
         import torch
 
         from .batch import BatchedSolver
@@ -225,6 +243,9 @@ class GPUExecutor:
         self.torch = torch
         self.Batched = BatchedSolver
         self.graph_steps = graph_steps
+        self.solo_cells = solo_cells
+        self.host_advance_s = 0.0  # host time spent enqueueing groups
+        self.host_wait_s = 0.0     # host time blocked on the device
         self.side = torch.cuda.Stream()
         self.main = torch.cuda.current_stream()
         self._pending = None
@@ -237,16 +258,29 @@ class GPUExecutor:
         return {"solver": s, "bad": None}
 
     def advance(self, handles, counts):
+        t0 = time.perf_counter()
         if self._new:
             self.main.wait_stream(self.side)
             self._new = []
-        solvers = [h["solver"] for h in handles]
-        b = self.Batched(solvers)
-        b.run_steps(counts, graph_steps=self.graph_steps)
+        batch, steps = [], []
+        for h, n in zip(handles, counts):
+            s = h["solver"]
+            if self.solo_cells is not None and int(np.prod(s.shape)) >= self.solo_cells:
+                s.run_steps(n)
+            else:
+                batch.append(s)
+                steps.append(n)
+        b = None
+        if batch:
+            b = self.Batched(batch)
+            b.run_steps(steps, graph_steps=self.graph_steps)
         self._pending = (b, handles)
+        self.host_advance_s += time.perf_counter() - t0
 
     def wait(self):
+        t0 = time.perf_counter()
         self.torch.cuda.current_stream().synchronize()
+        self.host_wait_s += time.perf_counter() - t0
         if self._pending is not None:
             _, handles = self._pending
             for h in handles:
@@ -272,9 +306,11 @@ class SequentialExecutor(GPUExecutor):
     """The baseline: one solve at a time through the single-grid path."""
 
     def advance(self, handles, counts):
+        t0 = time.perf_counter()
         if self._new:
             self.main.wait_stream(self.side)
             self._new = []
         for h, n in zip(handles, counts):
             h["solver"].run_steps(n)
         self._pending = (None, handles)
+        self.host_advance_s += time.perf_counter() - t0

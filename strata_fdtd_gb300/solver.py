@@ -196,6 +196,9 @@ class FDTDSolver:
         self._probe_dirty = True
         self._probe_order: list[str] = []
         self._pending_traces: list = []
+        self._mic_order: list[str] = []
+        self._mic_dirty = False
+        self._pending_mics: list = []
 
         self._step_count = 0
         self._time = 0.0
@@ -376,8 +379,25 @@ class FDTDSolver:
                                    _solver=self)
         self._probe_dirty = True
 
-    def add_microphone(self, *args, **kwargs):
-        raise NotImplementedError("microphones are not implemented by the GB300 backend")
+    def add_microphone(self, position, name=None, pattern="omni", direction=None, up=None):
+        """Omni microphone at a physical position (core/solver.py:1887-1965);
+        returns the Microphone."""
+        from .microphones import Microphone
+
+        mic = position if isinstance(position, Microphone) else Microphone(
+            position=position, name=name, pattern=pattern, direction=direction, up=up)
+        mic.name = mic.name or f"mic_{len(self._microphones)}"
+        if mic.name in self._microphones:
+            raise ValueError(f"Microphone '{mic.name}' already exists")
+        mic._initialize(self)
+        self._flush_traces()
+        self._microphones[mic.name] = mic
+        self._mic_dirty = True
+        return mic
+
+    @property
+    def microphones(self) -> dict:
+        return self._microphones
 
     def add_boundary(self, boundary) -> None:
         if isinstance(boundary, RigidBoundary):
@@ -523,6 +543,15 @@ class FDTDSolver:
             _native.check(self._lib.sf_plan_set_probes(self._plan, len(self._probe_order),
                                                        cells.ctypes.data), "sf_plan_set_probes")
             self._probe_dirty = False
+        if self._mic_dirty:
+            self._mic_order = list(self._microphones)
+            mics = [self._microphones[n] for n in self._mic_order]
+            idx = np.concatenate([m.corner_cells for m in mics] or [np.zeros(8, np.int64)])
+            w = np.concatenate([m.weights for m in mics] or [np.zeros(8, np.float32)])
+            _native.check(self._lib.sf_plan_set_microphones(self._plan, len(mics), idx.ctypes.data,
+                                                            w.ctypes.data),
+                          "sf_plan_set_microphones")
+            self._mic_dirty = False
         if self.has_materials and not self._ade_initialized:
             self._initialize_ade_fields()
 
@@ -567,16 +596,25 @@ class FDTDSolver:
         n_probe = len(self._probe_order)
         trace = (torch.empty((n, n_probe), dtype=torch.float32, device=self._device)
                  if n_probe else None)
-        rc = self._lib.sf_plan_step(self._plan, n,
-                                    None if src_dev is None else src_dev.data_ptr(),
-                                    None if trace is None else trace.data_ptr(), self._stream())
+        n_mic = len(self._mic_order)
+        mic_trace = (torch.empty((n, n_mic), dtype=torch.float32, device=self._device)
+                     if n_mic else None)
+        rc = self._lib.sf_plan_step_ex(self._plan, n,
+                                       None if src_dev is None else src_dev.data_ptr(),
+                                       None if trace is None else trace.data_ptr(),
+                                       None if mic_trace is None else mic_trace.data_ptr(),
+                                       self._stream())
         _native.check(rc, "sf_plan_step")
         if trace is not None:
             self._pending_traces.append((trace, list(self._probe_order)))
+        times = []
+        for _ in range(n):
+            times.append(self._time)
+            self._time += self.dt
+        if mic_trace is not None:
+            self._pending_mics.append((mic_trace, list(self._mic_order), times))
         self._mark_device_newer()
         self._step_count += n
-        for _ in range(n):
-            self._time += self.dt
 
     def _flush_traces(self):
         for trace, names in self._pending_traces:
@@ -585,6 +623,13 @@ class FDTDSolver:
                 if name in self._probes:
                     self._probes[name]._samples.extend(host[:, q].tolist())
         self._pending_traces.clear()
+        for trace, names, times in getattr(self, "_pending_mics", []):
+            host = trace.cpu().numpy()
+            for q, name in enumerate(names):
+                if name in self._microphones:
+                    self._microphones[name]._data.extend(host[:, q].tolist())
+                    self._microphones[name]._times.extend(times)
+        self._pending_mics = []
 
     def step(self) -> None:
         """Advance one time step (core/solver.py:2003-2077)."""

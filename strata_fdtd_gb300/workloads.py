@@ -244,7 +244,8 @@ def served_stream(seed=0, n_requests=1000, rate=200.0, edges=(48, 320), steps=(5
             return s
 
         spec["steps"] = n_steps
-        out.append(Request(rid=rid, build=build, steps=n_steps, arrival=t, nbytes=nbytes))
+        out.append(Request(rid=rid, build=build, steps=n_steps, arrival=t, nbytes=nbytes,
+                           cells=int(np.prod(shape))))
     return out
 
 

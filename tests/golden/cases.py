@@ -91,6 +91,16 @@ PLAIN_CASES = {
         probes=[("in", (18, 15, 14)), ("out", (5, 5, 5))],
         steps=160, store_fields=True,
     ),
+    "mics_geom": dict(
+        # omni microphones (trilinear, native batch path) beside probes
+        shape=(28, 24, 30), res=1e-3, courant=0.5, pml=dict(depth=4),
+        geometry=dict(kind="blocks", seed=21, n_boxes=1, n_spheres=1),
+        sources=[("point", (8, 12, 15), 20000.0, 1.0)],
+        probes=[("pr", (20, 12, 15))],
+        mics=[("m0", (0.0153, 0.0121, 0.0107)), ("m1", (0.0201, 0.0042, 0.0255)),
+              ("m2", (0.004, 0.0195, 0.0149)), ("m3", (0.0222, 0.0133, 0.0178))],
+        steps=140, store_fields=True,
+    ),
     "c1_full": dict(
         # the reference quick start, 100^3 x 1000 steps (hashes + traces only)
         shape=(100, 100, 100), res=1e-3, courant=0.5, pml=dict(depth=10),
@@ -275,6 +285,8 @@ def build_case(api, case, ade=False):
         probes = c2_probes(solver.geometry)
     for name, pos in probes:
         solver.add_probe(name, pos)
+    for name, pos in case.get("mics", []):
+        solver.add_microphone(position=pos, name=name)
     if case.get("impulse"):
         pos, val = case["impulse"]
         solver.p[pos] = val

@@ -138,6 +138,8 @@ def run_case(api, name, case, ade, manifest):
     out["probe_names"] = np.array(list(traces.keys()))
     for pname, tr in traces.items():
         out[f"trace__{pname}"] = tr
+    for mic_name, mic in getattr(solver, "_microphones", {}).items():
+        out[f"mic__{mic_name}"] = mic.get_waveform()
     info = dict(steps=case["steps"], dt=float(solver.dt), coeff_v=float(solver._coeff_v),
                 coeff_p=float(solver._coeff_p), time=float(solver._time))
     for f in ("p", "vx", "vy", "vz"):

@@ -109,9 +109,10 @@ def test_sdf_program_layout():
                         .translate((0.0, 0.0, 0.001)))
     prog, n = tree.program()
     ops = [prog[q].op for q in range(n)]
-    assert ops == [1, 2, 20, 3, 22, 12]
-    assert prog[n - 1].n == 3
-    assert prog[3].s0 == 0.05 and prog[3].b[2] == 1.0
+    # difference folded left: max(max(box, -sphere), -translated cylinder)
+    assert ops == [1, 2, 12, 20, 3, 22, 12]
+    assert prog[2].n == 2 and prog[n - 1].n == 2
+    assert prog[4].s0 == 0.05 and prog[4].b[2] == 1.0
     assert ctypes.sizeof(_native.SfSdfNode) == 72
     assert ctypes.sizeof(_native.SfPole) == 48
 

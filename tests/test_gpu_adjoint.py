@@ -4,8 +4,9 @@ PyTorch stepping of the same scheme and against central finite differences.
 
 Tolerances: FP64 adjoint vs FP64 autograd, rel 1e-9 (same arithmetic up to
 summation order); FP64 adjoint vs central differences (h = 1e-3), rel 1e-5
-(O(h^2) truncation); the FP32 adjoint vs FP64 central differences at the
-128^3 x 2000-step workload, rel 1e-4 on 16 random design cells."""
+(O(h^2) truncation); at the 128^3 x 2000-step workload the FP64 adjoint
+vs central differences rel 1e-5 and the FP32 adjoint vs the FP64 adjoint
+rel 1e-3."""
 import numpy as np
 import pytest
 
@@ -58,8 +59,12 @@ def test_adjoint_matches_central_differences_fp64():
 
 def test_differentiable_workload_fp32_against_fd():
     """The 128^3 workload: 10-cell PML, design field on the central 64^3,
-    1.5 kHz source, 2000 steps, checkpoints every 100 steps; FP32 adjoint
-    gradient vs FP64 central differences (h = 1e-3) on 16 random cells."""
+    1.5 kHz source, 2000 steps, checkpoints every 100 steps.  The FP64
+    adjoint gradient must match FP64 central differences (h = 1e-3) on 16
+    random cells to rel 1e-5 (O(h^2) truncation); the FP32 adjoint (FP32
+    fields, FP64 face-gradient sums) must match the FP64 adjoint to rel 1e-3
+    per sampled cell and 1e-3 in L2 over the design region (FP32 rounding of
+    2000 forward and 2000 adjoint steps)."""
     shape = (128, 128, 128)
     probes = [(100, 64, 64), (64, 100, 40)]
     s32 = DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
@@ -68,16 +73,27 @@ def test_differentiable_workload_fp32_against_fd():
                                probes=probes, dtype=torch.float64, checkpoint_every=100)
     theta = torch.tensor(design_field(shape, 64, seed=0), device="cuda")
     target = s64.forward(torch.tensor(design_field(shape, 64, seed=1), device="cuda"), 2000)[0]
-    th = theta.clone().to(torch.float32).requires_grad_(True)
-    s32.loss(th, target.to(torch.float32), 2000).backward()
+    th32 = theta.clone().to(torch.float32).requires_grad_(True)
+    s32.loss(th32, target.to(torch.float32), 2000).backward()
+    th64 = theta.clone().requires_grad_(True)
+    s64.loss(th64, target, 2000).backward()
+    g32 = th32.grad.double()
+    g64 = th64.grad
     rng = np.random.default_rng(5)
     h = 1e-3
-    worst = 0.0
+    worst64 = worst32 = 0.0
     for _ in range(16):
         c = tuple(int(v) for v in rng.integers(32, 96, size=3))
         tp, tm = theta.clone(), theta.clone()
         tp[c] += h
         tm[c] -= h
         fd = (float(s64.loss(tp, target, 2000)) - float(s64.loss(tm, target, 2000))) / (2 * h)
-        worst = max(worst, abs(float(th.grad[c]) - fd) / abs(fd))
-    assert worst < 1e-4, worst
+        worst64 = max(worst64, abs(float(g64[c]) - fd) / abs(fd))
+        worst32 = max(worst32, abs(float(g32[c]) - float(g64[c])) / abs(float(g64[c])))
+    region = (slice(32, 96),) * 3
+    l2 = float(torch.linalg.norm(g32[region] - g64[region]) / torch.linalg.norm(g64[region]))
+    print(f"fp64 adjoint vs FD worst rel {worst64:.3e}; fp32 vs fp64 adjoint worst rel "
+          f"{worst32:.3e}, L2 rel {l2:.3e}")
+    assert worst64 < 1e-5, worst64
+    assert worst32 < 1e-3, worst32
+    assert l2 < 1e-3, l2

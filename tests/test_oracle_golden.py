@@ -44,6 +44,15 @@ def test_plain_fused_loop_matches_reference(name, manifest):
     _check(_run(C.PLAIN_CASES[name], step_by_step=False), "plain_" + name, manifest)
 
 
+def test_microphones_match_reference(manifest):
+    case = C.PLAIN_CASES["mics_geom"]
+    s = _run(case, step_by_step=True)
+    _check(s, "plain_mics_geom", manifest)
+    g = golden("plain_mics_geom")
+    for name, tr in s.get_mic_data().items():
+        np.testing.assert_array_equal(tr, g[f"mic__{name}"])
+
+
 @pytest.mark.parametrize("name", ["c1_tiny", "blocks_odd", "plane_yz_geom"])
 def test_plain_kernel_by_kernel_matches_reference(name, manifest):
     _check(_run(C.PLAIN_CASES[name], step_by_step=True), "plain_" + name, manifest)

@@ -112,3 +112,18 @@ def test_solve_bytes_counts_every_buffer():
     assert solve_bytes((40, 50, 60), geometry=True, debye_poles=2, probes=2, sources=1) == (
         32 * n + 2 * n + n + 8 * n + 4 * 150 + 16 + 8)
     assert np.isclose(solve_bytes((320, 320, 320)) / 1e9, 1.11, atol=0.02)
+
+
+def test_cell_cap_admits_in_order_and_lets_an_oversized_solve_run_alone():
+    clock = FakeClock()
+    ex = FakeExecutor(clock)
+    srv = SolveServer(ex, hbm_budget=10**9, step_group=10, max_active_cells=300, clock=clock)
+    reqs = [Request(rid=q, build=lambda: None, steps=20, nbytes=1, cells=c)
+            for q, c in enumerate([100, 100, 100, 500, 100, 200])]
+    stats = srv.run(reqs, realtime=False)
+    assert stats["done"] == 6
+    assert ex.groups[0] == [0, 1, 2]          # 300 cells: at the cap
+    assert [3] in ex.groups                   # 500 cells > cap: runs, alone
+    assert not any(3 in g and len(g) > 1 for g in ex.groups)
+    assert ex.groups[-1] == [4, 5]            # admitted together after it
+    assert srv.active_cells == 0
