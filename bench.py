@@ -412,9 +412,10 @@ def run_batch(args):
         "config": {"workload": f"batch of {n} grids, edges log-U[64,256], PML 8, 1-6 solids, "
                                "2-pole Debye block, 1-4 kHz pulse, 2 probes, 500-3000 steps",
                    "cells": int(sum(np.prod(s.shape) for s in bat)),
-                   "cell_updates": cell_updates, "tiles": b.rows, "i_chunk": b.i_chunk,
+                   "cell_updates": cell_updates, "plain_kernel": b.kernel, "tile_rows": b.rows,
+                   "i_chunk": b.i_chunk,
                    "graph_steps": args.graph_steps, "rejected_materials": info["rejected_materials"],
-                   "autotune_ms_per_step": {f"{k[0]}x{k[1]}": v for k, v in tune.items()
+                   "autotune_ms_per_step": {f"{k[0]}:{k[1]}x{k[2]}": v for k, v in tune.items()
                                             if k != "best"}},
         "sequential": {"value": cell_updates / t_seq / 1e9, "seconds": t_seq,
                        "path": "each solve alone through FDTDSolver.run_steps"},

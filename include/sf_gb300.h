@@ -144,6 +144,15 @@ int sf_plan_set_probes(sf_plan* plan, int n, const int64_t* cells);
  * recorded after each step by sf_plan_step_ex as the float sum from 0 of
  * weight * p (record_microphones_batch, microphones.cpp:82-118). */
 int sf_plan_set_microphones(sf_plan* plan, int n, const int64_t* idx8, const float* w8);
+/* Microphone rows of any field: field[n] selects what row q interpolates
+ * (0 p, 1 vx, 2 vy, 3 vz; NULL = all p).  A directional microphone of the
+ * reference (Microphone.record with velocities, core/solver.py:1004-1118)
+ * is four rows -- p at its grid position, vx/vy/vz at the staggered,
+ * clamped positions of _interpolate_velocity -- with float32 weights, the
+ * same float products and float sum from 0; the polar-pattern combination
+ * of the four samples (core/solver.py:1120-1179) runs on the host. */
+int sf_plan_set_microphones_ex(sf_plan* plan, int n, const int32_t* field, const int64_t* idx8,
+                               const float* w8);
 
 /* ADE materials: material_id (device, nx*ny*nz bytes) and the pole table
  * (at most SF_MAX_POLES; Debye poles first, then Lorentz, each in field
@@ -235,6 +244,11 @@ int sf_batch_clear(sf_batch* batch);
 /* Tile shape: rows of 32 columns (4, 8 or 16) and i planes per tile (0 = 16). */
 int sf_batch_set_tiles(sf_batch* batch, int rows, int i_chunk);
 int sf_batch_tiles(const sf_batch* batch);
+/* Kernel for the tiles away from every material box: 0 thread columns
+ * (default), 1 scalar warp tiles (lane-shuffled neighbours), 2 the same with
+ * the next plane loaded ahead.  Tiles that meet a material box always run
+ * the ADE column kernel. */
+int sf_batch_set_kernel(sf_batch* batch, int kind);
 /* Time the 9 tile shapes (rows 4/8/16 x i_chunk 8/16/32) on the members'
  * current state without changing it and keep the fastest; ms_out[9] may be
  * NULL. */

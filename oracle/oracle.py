@@ -431,32 +431,85 @@ class FDTDSolver:
         b.initialize(self)
         self._boundaries.append(b)
 
-    def add_microphone(self, position, name=None, pattern="omni"):
-        """Omni microphone with the native batch path's float32 trilinear
-        weights (core/solver.py:930-960 -> _kernels/src/microphones.cpp:16-80)."""
+    _PATTERNS = {"omni": 0.0, "subcardioid": 0.3, "cardioid": 0.5, "supercardioid": 0.63,
+                 "hypercardioid": 0.75, "figure8": 1.0}  # core/solver.py:787-794
+    _CORNERS = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1), (0, 1, 1),
+                (1, 1, 1)]
+
+    def add_microphone(self, position, name=None, pattern="omni", direction=None, up=None):
+        """Microphone at a physical position (core/solver.py:853-963,
+        1887-1965): grid position = position / dx; pattern coefficient or a
+        custom gain(theta); unit direction."""
         if not hasattr(self, "_mics"):
             self._mics = {}
-        g = [np.float32(position[a] / self.dx) for a in range(3)]
-        i0 = [int(v) for v in g]
-        f = [np.float32(v - np.float32(i)) for v, i in zip(g, i0)]
-        one = np.float32(1.0)
-        fx, fy, fz = f
-        w = [(one - fx) * (one - fy) * (one - fz), fx * (one - fy) * (one - fz),
-             (one - fx) * fy * (one - fz), fx * fy * (one - fz), (one - fx) * (one - fy) * fz,
-             fx * (one - fy) * fz, (one - fx) * fy * fz, fx * fy * fz]
-        corners = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1), (0, 1, 1),
-                   (1, 1, 1)]
-        idx = [(i0[0] + a, i0[1] + b, i0[2] + c) for a, b, c in corners]
-        self._mics[name or f"mic_{len(self._mics)}"] = dict(idx=idx, w=[np.float32(x) for x in w],
-                                                             data=[])
+        d = np.array((1.0, 0.0, 0.0) if direction is None else direction, dtype=np.float64)
+        d = d / np.linalg.norm(d)
+        g = tuple(position[a] / self.dx for a in range(3))
+        if not all(0 <= g[a] < self.shape[a] - 1 for a in range(3)):
+            raise ValueError("microphone outside the domain")
+        self._mics[name or f"mic_{len(self._mics)}"] = dict(
+            g=g, direction=d, data=[],
+            k=self._PATTERNS[pattern] if isinstance(pattern, str) else None,
+            custom=None if isinstance(pattern, str) else pattern)
+
+    def _trilinear_fp64(self, gx, gy, gz):
+        """Microphone._compute_trilinear_weights (core/solver.py:965-1002)."""
+        i0, j0, k0 = int(gx), int(gy), int(gz)
+        fx, fy, fz = gx - i0, gy - j0, gz - k0
+        w = [(1 - fx) * (1 - fy) * (1 - fz), fx * (1 - fy) * (1 - fz), (1 - fx) * fy * (1 - fz),
+             fx * fy * (1 - fz), (1 - fx) * (1 - fy) * fz, fx * (1 - fy) * fz,
+             (1 - fx) * fy * fz, fx * fy * fz]
+        return [(i0 + a, j0 + b, k0 + c) for a, b, c in self._CORNERS], w
 
     def _record_mics(self):
-        """record_microphones_batch (microphones.cpp:82-118): float sum from 0."""
-        for m in getattr(self, "_mics", {}).values():
-            s = np.float32(0.0)
-            for q in range(8):
-                s = np.float32(s + np.float32(m["w"][q] * self.p[m["idx"][q]]))
-            m["data"].append(s)
+        """FDTDSolver._record_microphones (core/solver.py:2441-2518): the
+        native batch kernel when every microphone is omni, else
+        Microphone.record for each (core/solver.py:1004-1179)."""
+        mics = getattr(self, "_mics", {})
+        directional = any(m["k"] != 0.0 for m in mics.values())
+        one = np.float32(1.0)
+        for m in mics.values():
+            if not directional:  # microphones.cpp:16-118, float32 throughout
+                gf = [np.float32(v) for v in m["g"]]
+                i0 = [int(v) for v in gf]
+                fx, fy, fz = (np.float32(v - np.float32(i)) for v, i in zip(gf, i0))
+                w = [(one - fx) * (one - fy) * (one - fz), fx * (one - fy) * (one - fz),
+                     (one - fx) * fy * (one - fz), fx * fy * (one - fz),
+                     (one - fx) * (one - fy) * fz, fx * (one - fy) * fz, (one - fx) * fy * fz,
+                     fx * fy * fz]
+                s = np.float32(0.0)
+                for q, (a, b, c) in enumerate(self._CORNERS):
+                    s = np.float32(s + np.float32(w[q] * self.p[i0[0] + a, i0[1] + b, i0[2] + c]))
+                m["data"].append(s)
+                continue
+            cells, w = self._trilinear_fp64(*m["g"])
+            pressure = 0.0
+            for cell, wq in zip(cells, w):
+                pressure += wq * self.p[cell]
+            if m["k"] == 0.0:
+                m["data"].append(pressure)
+                continue
+            vel = []
+            for axis, field in enumerate((self.vx, self.vy, self.vz)):
+                g = list(m["g"])
+                g[axis] -= 0.5
+                n = field.shape
+                g = [max(0.0, min(g[a], n[a] - 1.001)) for a in range(3)]
+                vc, vw = self._trilinear_fp64(*g)
+                v = 0.0
+                for (i, j, k), wq in zip(vc, vw):
+                    v += wq * field[min(i, n[0] - 1), min(j, n[1] - 1), min(k, n[2] - 1)]
+                vel.append(v)
+            d = m["direction"]
+            Z = self.rho * self.c
+            vd = vel[0] * d[0] + vel[1] * d[1] + vel[2] * d[2]
+            if m["custom"] is not None:
+                v_mag = np.sqrt(vel[0] ** 2 + vel[1] ** 2 + vel[2] ** 2)
+                theta = np.arccos(np.clip(vd / v_mag, -1.0, 1.0)) if v_mag > 1e-20 else 0.0
+                m["data"].append(pressure * m["custom"](theta))
+            else:
+                k = m["k"]
+                m["data"].append((1 - k) * pressure + k * Z * vd)
 
     def get_mic_data(self):
         return {k: np.array(m["data"], dtype=np.float32) for k, m in getattr(self, "_mics", {}).items()}

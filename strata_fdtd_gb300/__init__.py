@@ -2,10 +2,16 @@
 
 A drop-in for ``FDTDSolver(backend="native")`` of rjwalters/strata-fdtd:
 same classes and arguments, with the per-step stencil, rigid walls, PML, ADE
-materials, sources, probes and SDF voxelisation running as hand-written CUDA
-kernels behind a C ABI (include/sf_gb300.h) loaded with ctypes.
+materials, sources, probes, microphones and SDF voxelisation running as
+hand-written CUDA kernels behind a C ABI (include/sf_gb300.h) loaded with
+ctypes.  ``BatchedSolver`` steps many solvers in one persistent launch,
+``server.SolveServer`` serves a stream of solves with continuous batching,
+and ``DifferentiableSolver`` differentiates a probe loss with respect to a
+per-cell density field by a reverse-time adjoint.
 """
 from ._native import NativeError, build
+from .adjoint import DifferentiableSolver
+from .batch import BatchedSolver
 from .boundaries import PML, RigidBoundary
 from .grid import UniformGrid
 from .microphones import Microphone
@@ -22,5 +28,5 @@ __all__ = [
     "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale",
     "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",
-    "NativeError",
+    "NativeError", "BatchedSolver", "DifferentiableSolver",
 ]

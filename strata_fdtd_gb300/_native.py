@@ -119,6 +119,7 @@ SIGNATURES = {
     "sf_plan_step": (_I, [_P, _I64, _P, _P, _P]),
     "sf_plan_step_ex": (_I, [_P, _I64, _P, _P, _P, _P]),
     "sf_plan_set_microphones": (_I, [_P, _I, _P, _P]),
+    "sf_plan_set_microphones_ex": (_I, [_P, _I, _P, _P, _P]),
     "sf_energy_scratch_doubles": (_I64, [_P]),
     "sf_plan_energy": (_I, [_P, _D, _D, _D, _P, _P, _P]),
     "sf_plan_energy_noalloc": (_I, [_P, _D, _D, _D, _P, _P]),
@@ -133,6 +134,7 @@ SIGNATURES = {
     "sf_batch_clear": (_I, [_P]),
     "sf_batch_set_tiles": (_I, [_P, _I, _I]),
     "sf_batch_tiles": (_I, [_P]),
+    "sf_batch_set_kernel": (_I, [_P, _I]),
     "sf_batch_autotune": (_I, [_P, _I, _P, _P, _P, _P]),
     "sf_batch_run": (_I, [_P, _I64, _I, _P]),
     "sf_voxelize": (_I, [_P, _I, _I, _I, _I, _D, _I, _P, _P]),

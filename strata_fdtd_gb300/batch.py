@@ -18,11 +18,16 @@ import numpy as np
 from . import _native
 
 
+PLAIN_KERNELS = ("column", "warp", "warp_prefetch")
+
+
 class BatchedSolver:
     """Steps ``solvers`` together.  ``rows`` (4, 8, 16) and ``i_chunk``
-    (planes per tile, 0 = 16) set the tile shape; :meth:`autotune` picks them."""
+    (planes per tile, 0 = 16) set the tile shape and ``kernel`` (one of
+    PLAIN_KERNELS) the kernel of the tiles away from material boxes;
+    :meth:`autotune` picks all three."""
 
-    def __init__(self, solvers, rows: int = 8, i_chunk: int = 0):
+    def __init__(self, solvers, rows: int = 8, i_chunk: int = 0, kernel: str = "column"):
         if not solvers:
             raise ValueError("BatchedSolver needs at least one solver")
         if any(s._microphones for s in solvers):
@@ -31,6 +36,9 @@ class BatchedSolver:
         self._lib = _native.load()
         self._torch = self.solvers[0]._torch
         self.rows, self.i_chunk = rows, i_chunk
+        if kernel not in PLAIN_KERNELS:
+            raise ValueError(f"kernel must be one of {PLAIN_KERNELS}")
+        self.kernel = kernel
         h = ctypes.c_void_p()
         _native.check(self._lib.sf_batch_create(ctypes.byref(h)), "sf_batch_create")
         self._batch = h
@@ -54,6 +62,8 @@ class BatchedSolver:
         _native.check(lib.sf_batch_clear(self._batch), "sf_batch_clear")
         _native.check(lib.sf_batch_set_tiles(self._batch, self.rows, self.i_chunk),
                       "sf_batch_set_tiles")
+        _native.check(lib.sf_batch_set_kernel(self._batch, PLAIN_KERNELS.index(self.kernel)),
+                      "sf_batch_set_kernel")
         counts = [int(steps)] * len(self.solvers) if np.isscalar(steps) else [int(n) for n in steps]
         if len(counts) != len(self.solvers):
             raise ValueError("one step count per solver")
@@ -73,18 +83,27 @@ class BatchedSolver:
         return keep
 
     def autotune(self, launches: int = 3) -> dict:
-        """Time the 9 tile shapes on the members' current state (unchanged)
-        and keep the fastest.  Returns {(rows, i_chunk): ms per step, "best": ...}."""
-        self._load(1)
-        ms = (ctypes.c_float * 9)()
-        br, bc = ctypes.c_int(), ctypes.c_int()
-        _native.check(self._lib.sf_batch_autotune(self._batch, int(launches), self._stream(), ms,
-                                                  ctypes.byref(br), ctypes.byref(bc)),
-                      "sf_batch_autotune")
-        self.rows, self.i_chunk = br.value, bc.value
-        out = {(r, c): float(ms[a * 3 + b]) for a, r in enumerate((4, 8, 16))
-               for b, c in enumerate((8, 16, 32))}
-        out["best"] = (self.rows, self.i_chunk)
+        """Time the 9 tile shapes with each plain-tile kernel on the members'
+        current state (unchanged) and keep the fastest.  Returns
+        {(kernel, rows, i_chunk): ms per step, "best": (kernel, rows, i_chunk)}."""
+        out = {}
+        best = None
+        for kernel in PLAIN_KERNELS:
+            self.kernel = kernel
+            self._load(1)
+            ms = (ctypes.c_float * 9)()
+            br, bc = ctypes.c_int(), ctypes.c_int()
+            _native.check(self._lib.sf_batch_autotune(self._batch, int(launches), self._stream(),
+                                                      ms, ctypes.byref(br), ctypes.byref(bc)),
+                          "sf_batch_autotune")
+            for a, r in enumerate((4, 8, 16)):
+                for b, c in enumerate((8, 16, 32)):
+                    t = float(ms[a * 3 + b])
+                    out[(kernel, r, c)] = t
+                    if t > 0 and (best is None or t < out[best]):
+                        best = (kernel, r, c)
+        self.kernel, self.rows, self.i_chunk = best
+        out["best"] = best
         return out
 
     def run_steps(self, steps, graph_steps: int = 50) -> None:

@@ -25,6 +25,8 @@
 #ifndef SF_CFG_DEFAULT
 #define SF_CFG_DEFAULT (SF_CFG_COL_FIRST + 0)
 #define SF_CFG_TILE_FIRST (SF_CFG_COL_FIRST + kSfColConfigCount)
+#define SF_CFG_TILE_DEFAULT (SF_CFG_TILE_FIRST + 2)
+#define SF_CFG_TILE1_DEFAULT (SF_CFG_TILE_FIRST + 11)
 #endif
 
 namespace {
@@ -122,6 +124,7 @@ int sf_plan_destroy(sf_plan* P) {
     cudaFree(P->probe_cells);
     cudaFree(P->mic_idx);
     cudaFree(P->mic_w);
+    cudaFree(P->mic_field);
     delete P;
     return 0;
 }
@@ -325,17 +328,21 @@ void set_io(const sf_plan* P, SfStepArgs& a, int in) {
 
 // The configuration a step of this plan runs: ADE poles need the per-cell
 // kernel; otherwise the explicit choice, else the autotuned one, else the
-// default.
-int effective_config(const sf_plan* P) {
+// default warp-tile configuration where the grid allows it (nz % 4 == 0,
+// aligned fields, 32-bit offsets), else the first column configuration.
+int effective_config(const sf_plan* P, const SfStepArgs& a) {
     if (P->poles.n > 0) return SF_CFG_CELL;
     if (P->variant != SF_CFG_AUTO) return P->variant;
-    return P->tuned > 0 ? P->tuned : SF_CFG_DEFAULT;
+    if (P->tuned > 0) return P->tuned;
+    if (sf_tile_supported(a, 4)) return SF_CFG_TILE_DEFAULT;
+    return sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT;
 }
 
 int chunk_for(const sf_plan* P, int cfg) {
     if (P->i_chunk > 0) return P->i_chunk;
     if (cfg >= SF_CFG_TILE_FIRST) {
         const SfTileConfig& t = kSfTileConfigs[cfg - SF_CFG_TILE_FIRST];
+        if (t.vec == 1) return auto_chunk(P, 32, t.rows * t.warps);
         if (P->d.nz % 4 == 0) return auto_chunk(P, 32, 4 * t.rows * t.warps);
         return auto_chunk(P, 32);
     }
@@ -350,7 +357,8 @@ int chunk_for(const sf_plan* P, int cfg) {
 // Whether configuration cfg runs as itself on this plan's grid (otherwise
 // its launcher substitutes the first column configuration).
 bool config_native(const sf_plan* P, int cfg, const SfStepArgs& a) {
-    if (cfg >= SF_CFG_TILE_FIRST) return sf_tile_supported(a);
+    if (cfg >= SF_CFG_TILE_FIRST)
+        return sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec);
     if (cfg >= SF_CFG_COL_FIRST) return P->d.nz % kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec == 0;
     return true;
 }
@@ -386,7 +394,8 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     SfStepArgs a;
     fill_args(P, a, trace != nullptr);
-    const int cfg = effective_config(P);
+    set_io(P, a, P->cur);  // both sets: the alignment check covers every field
+    const int cfg = effective_config(P, a);
     const int ich = chunk_for(P, cfg);
     const bool mics = mic_trace != nullptr && P->n_mic > 0;
     for (int64_t s = 0; s < n_steps; ++s) {
@@ -398,8 +407,9 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
         P->cur = 1 - P->cur;
         ++P->steps_done;
         if (mics)
-            if (int rc = sf_launch_mic_gather(P->f[P->cur][0], P->mic_idx, P->mic_w, P->n_mic,
-                                              mic_trace + s * P->n_mic, st))
+            if (int rc = sf_launch_mic_gather(P->f[P->cur][0], P->f[P->cur][1], P->f[P->cur][2],
+                                              P->f[P->cur][3], P->mic_field, P->mic_idx,
+                                              P->mic_w, P->n_mic, mic_trace + s * P->n_mic, st))
                 return rc;
     }
     if (trace && P->n_probe > 0)
@@ -409,22 +419,37 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
 }
 
 int sf_plan_set_microphones(sf_plan* P, int n, const int64_t* idx8, const float* w8) {
+    return sf_plan_set_microphones_ex(P, n, nullptr, idx8, w8);
+}
+
+int sf_plan_set_microphones_ex(sf_plan* P, int n, const int32_t* field, const int64_t* idx8,
+                               const float* w8) {
     if (!P) return sf_fail("sf_plan_set_microphones: NULL plan");
     if (n < 0 || (n > 0 && (!idx8 || !w8))) return sf_fail("sf_plan_set_microphones: bad table");
+    if (field)
+        for (int q = 0; q < n; ++q)
+            if (field[q] < 0 || field[q] > 3)
+                return sf_fail("sf_plan_set_microphones: field must be 0 (p) .. 3 (vz)");
     for (long long q = 0; q < 8LL * n; ++q)
         if (idx8[q] < 0 || idx8[q] >= P->n)
             return sf_fail("sf_plan_set_microphones: corner cell outside the grid");
     DeviceGuard g(P->device);
     cudaFree(P->mic_idx);
     cudaFree(P->mic_w);
+    cudaFree(P->mic_field);
     P->mic_idx = nullptr;
     P->mic_w = nullptr;
+    P->mic_field = nullptr;
     P->n_mic = n;
     if (n == 0) return 0;
     SF_CUDA_OK(cudaMalloc(&P->mic_idx, sizeof(long long) * 8 * n));
     SF_CUDA_OK(cudaMalloc(&P->mic_w, sizeof(float) * 8 * n));
     SF_CUDA_OK(cudaMemcpy(P->mic_idx, idx8, sizeof(long long) * 8 * n, cudaMemcpyHostToDevice));
     SF_CUDA_OK(cudaMemcpy(P->mic_w, w8, sizeof(float) * 8 * n, cudaMemcpyHostToDevice));
+    if (field) {
+        SF_CUDA_OK(cudaMalloc(&P->mic_field, sizeof(int) * n));
+        SF_CUDA_OK(cudaMemcpy(P->mic_field, field, sizeof(int) * n, cudaMemcpyHostToDevice));
+    }
     return 0;
 }
 

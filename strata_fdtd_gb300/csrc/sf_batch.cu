@@ -24,6 +24,7 @@
 #include "sf_common.cuh"
 #include "sf_kernels.h"
 #include "sf_plan_internal.h"
+#include "sf_tile1.cuh"
 
 struct SfGridDev {
     int nx, ny, nz, ich;
@@ -243,6 +244,70 @@ __global__ void __launch_bounds__(32 * BY) k_batch_step(const SfGridDev* __restr
     }
 }
 
+// Persistent loop over the plain tiles (away from every material box): each
+// warp takes R of the tile's R*W rows and runs them as a scalar warp tile
+// (sf_tile1.cuh: k neighbours by lane shuffles, j neighbours in registers).
+template <int R, int W, bool PF>
+__global__ void __launch_bounds__(32 * W, (PF ? 20 : 24) / W) k_batch_plain(const SfGridDev* __restrict__ grids,
+                                                        const int4* __restrict__ tiles, int n_tiles,
+                                                        int* __restrict__ queue,
+                                                        const long long* __restrict__ step_ptr) {
+    __shared__ int t_sh;
+    __shared__ SfGridDev g_sh;
+    const long long s = *step_ptr;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (;;) {
+        if (tid == 0) t_sh = atomicAdd(queue, 1);
+        __syncthreads();
+        const int t = t_sh;
+        if (t >= n_tiles) return;
+        const int4 T = tiles[t];  // grid, i-chunk, j-block, k-block
+        {
+            const int* src = reinterpret_cast<const int*>(grids + T.x);
+            int* dst = reinterpret_cast<int*>(&g_sh);
+            for (int w = tid; w < (int)(sizeof(SfGridDev) / sizeof(int)); w += 32 * W)
+                dst[w] = src[w];
+        }
+        __syncthreads();
+        const int jb = T.z * (R * W) + threadIdx.y * R;
+        if (s < g_sh.n_steps && jb < g_sh.ny) {  // warp-uniform
+            const int in = (int)((g_sh.cur0 + s) & 1);
+            Tile1Io io;
+            io.nx = g_sh.nx;
+            io.ny = g_sh.ny;
+            io.nz = g_sh.nz;
+            io.plane = g_sh.plane;
+            io.cv = g_sh.cv;
+            io.cp = g_sh.cp;
+            io.p = g_sh.f[in][0];
+            io.vx = g_sh.f[in][1];
+            io.vy = g_sh.f[in][2];
+            io.vz = g_sh.f[in][3];
+            io.po = g_sh.f[1 - in][0];
+            io.vxo = g_sh.f[1 - in][1];
+            io.vyo = g_sh.f[1 - in][2];
+            io.vzo = g_sh.f[1 - in][3];
+            io.flags = g_sh.flags;
+            io.dx = g_sh.dx;
+            io.dy = g_sh.dy;
+            io.dz = g_sh.dz;
+            io.src_val = g_sh.src_val + s * g_sh.src.n;
+            const int i0 = T.y * g_sh.ich;
+            const int i1 = min(i0 + g_sh.ich, g_sh.nx);
+            const int k = T.w * 32 + threadIdx.x;
+            if (g_sh.flags != nullptr) tile1_run<true, R, PF>(io, g_sh.src, i0, i1, jb, k);
+            else tile1_run<false, R, PF>(io, g_sh.src, i0, i1, jb, k);
+        }
+        __syncthreads();  // everyone is done with t_sh and g_sh
+    }
+}
+
+// Scalar-tile shape for a tile height: rows = R * W.
+template <int ROWS> struct PlainShape;
+template <> struct PlainShape<4> { static constexpr int R = 2, W = 2; };
+template <> struct PlainShape<8> { static constexpr int R = 2, W = 4; };
+template <> struct PlainShape<16> { static constexpr int R = 2, W = 8; };
+
 // ADE density poles of every grid that has them, over its material box
 // (ade.cpp:25-68 and 118-170), from the step's input pressure.
 __global__ void k_batch_ade_density(const SfGridDev* __restrict__ grids, const int* __restrict__ ids,
@@ -307,6 +372,7 @@ struct sf_batch {
     };
     std::vector<Member> members;
     int rows = 8;
+    int plain_kernel = 0;  // plain tiles: 0 thread columns, 1 warp tiles, 2 warp tiles + prefetch
     int i_chunk = 0;
     int device = 0;
     bool built = false;
@@ -354,21 +420,28 @@ int chunk_for_grid(const sf_batch* B, const sf_plan* P) {
     return P->d.nx < 32 ? (P->d.nx + 1) / 2 : 16;
 }
 
-template <int BY, bool ADEK>
-int occupancy_blocks(int* out) {
+template <typename K>
+int occupancy_blocks(K kernel, int threads, int* out) {
     int dev = 0, sms = 0, per = 0;
     SF_CUDA_OK(cudaGetDevice(&dev));
     SF_CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SF_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<BY, ADEK>, 32 * BY,
-                                                             0));
+    SF_CUDA_OK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0));
     *out = sms * (per > 0 ? per : 1);
     return 0;
 }
 
 template <int BY>
 int occupancy_both(sf_batch* B) {
-    if (int rc = occupancy_blocks<BY, false>(&B->blocks)) return rc;
-    return occupancy_blocks<BY, true>(&B->blocks_ade);
+    using S = PlainShape<BY>;
+    int rc = 0;
+    if (B->plain_kernel == 1)
+        rc = occupancy_blocks(k_batch_plain<S::R, S::W, false>, 32 * S::W, &B->blocks);
+    else if (B->plain_kernel == 2)
+        rc = occupancy_blocks(k_batch_plain<S::R, S::W, true>, 32 * S::W, &B->blocks);
+    else
+        rc = occupancy_blocks(k_batch_step<BY, false>, 32 * BY, &B->blocks);
+    if (rc) return rc;
+    return occupancy_blocks(k_batch_step<BY, true>, 32 * BY, &B->blocks_ade);
 }
 
 int build(sf_batch* B) {
@@ -463,9 +536,18 @@ int build(sf_batch* B) {
 
 template <int BY>
 void launch_pair(sf_batch* B, cudaStream_t st, int trial) {
-    if (B->n_tiles > 0)
-        k_batch_step<BY, false><<<B->blocks, dim3(32, BY), 0, st>>>(
-            B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step, trial);
+    using S = PlainShape<BY>;
+    if (B->n_tiles > 0) {
+        if (B->plain_kernel == 1)
+            k_batch_plain<S::R, S::W, false><<<B->blocks, dim3(32, S::W), 0, st>>>(
+                B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step);
+        else if (B->plain_kernel == 2)
+            k_batch_plain<S::R, S::W, true><<<B->blocks, dim3(32, S::W), 0, st>>>(
+                B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step);
+        else
+            k_batch_step<BY, false><<<B->blocks, dim3(32, BY), 0, st>>>(
+                B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step, trial);
+    }
     if (B->n_tiles_ade > 0)
         k_batch_step<BY, true><<<B->blocks_ade, dim3(32, BY), 0, st>>>(
             B->d_grids, B->d_tiles + B->n_tiles, B->n_tiles_ade, B->d_queue + 1, B->d_step, trial);
@@ -542,7 +624,15 @@ int sf_batch_set_tiles(sf_batch* B, int rows, int i_chunk) {
     return 0;
 }
 
-int sf_batch_tiles(const sf_batch* B) { return B ? B->n_tiles : -1; }
+int sf_batch_tiles(const sf_batch* B) { return B ? B->n_tiles + B->n_tiles_ade : -1; }
+
+int sf_batch_set_kernel(sf_batch* B, int kind) {
+    if (!B) return sf_fail("sf_batch_set_kernel: NULL batch");
+    if (kind < 0 || kind > 2) return sf_fail("sf_batch_set_kernel: kind must be 0, 1 or 2");
+    B->plain_kernel = kind;
+    B->built = false;
+    return 0;
+}
 
 int sf_batch_run(sf_batch* B, int64_t n_steps, int graph_steps, void* stream) {
     if (!B) return sf_fail("sf_batch_run: NULL batch");

@@ -20,12 +20,13 @@ extern const int kSfColConfigCount;
 // Warp-tile kernel configurations follow the column ones:
 // index SF_CFG_COL_FIRST + kSfColConfigCount + t.
 struct SfTileConfig {
-    int rows, warps, minb, prefetch;
+    int vec, rows, warps, minb, prefetch;
     const char* name;
 };
 extern const SfTileConfig kSfTileConfigs[];
 extern const int kSfTileConfigCount;
-bool sf_tile_supported(const SfStepArgs& a);
+// Whether a warp-tile kernel with `vec` cells per lane runs on this grid.
+bool sf_tile_supported(const SfStepArgs& a, int vec);
 
 int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, int nz,
                           cudaStream_t st);
@@ -39,7 +40,8 @@ int sf_launch_step_col_cfg(const SfStepArgs& a, const SfSources& src, bool geom,
                            cudaStream_t st);
 int sf_launch_step_tile_cfg(const SfStepArgs& a, const SfSources& src, bool geom, int cfg, int ich,
                             cudaStream_t st);
-int sf_launch_mic_gather(const float* p, const long long* idx, const float* w, int n, float* out,
+int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const float* vz,
+                         const int* field, const long long* idx, const float* w, int n, float* out,
                          cudaStream_t st);
 long long sf_energy_blocks(long long n);
 int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,

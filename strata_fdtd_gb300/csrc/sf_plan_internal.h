@@ -23,9 +23,10 @@ struct sf_plan {
     int i_chunk = 0;               // planes per block in march / column kernels (0 = auto)
     int tuned = 0;                 // configuration chosen by sf_plan_autotune (0 = none)
     long long steps_done = 0;      // steps issued so far (alternates the chunk order)
-    int n_mic = 0;                 // omni microphones: 8 corner cells and weights each
+    int n_mic = 0;                 // microphone rows: 8 corner cells and weights each
     long long* mic_idx = nullptr;  // owned
     float* mic_w = nullptr;        // owned
+    int* mic_field = nullptr;      // owned: field per row (0 p, 1 vx, 2 vy, 3 vz)
     int ade_lo[3] = {0, 0, 0};     // box holding every material cell (density pre-pass)
     int ade_hi[3] = {0, 0, 0};
 };

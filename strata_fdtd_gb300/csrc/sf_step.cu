@@ -198,16 +198,22 @@ __global__ void k_probe_gather(const float* __restrict__ p, const long long* __r
     if (t < n) out[t] = p[cells[t]];
 }
 
-// Omni microphones: trilinear sum over 8 corners in float, from 0, corner
-// order and weights as precompute_microphone_data / record_microphones_batch
-// (microphones.cpp:16-118).
-__global__ void k_mic_gather(const float* __restrict__ p, const long long* __restrict__ idx,
+// Microphone rows: trilinear sum over 8 corners in float, from 0, of one
+// field (field[m]: 0 p, 1 vx, 2 vy, 3 vz; null = all p).  Corner order and
+// the float sum are those of record_microphones_batch (microphones.cpp:82-118)
+// and of Microphone.record / _interpolate_velocity (core/solver.py:1004-1118),
+// whose float32 products and sums are the same operations.
+__global__ void k_mic_gather(const float* __restrict__ p, const float* __restrict__ vx,
+                             const float* __restrict__ vy, const float* __restrict__ vz,
+                             const int* __restrict__ field, const long long* __restrict__ idx,
                              const float* __restrict__ w, int n, float* __restrict__ out) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n) return;
+    const int f = field ? field[m] : 0;
+    const float* __restrict__ src = f == 1 ? vx : (f == 2 ? vy : (f == 3 ? vz : p));
     float s = 0.0f;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s = f_add(s, f_mul(w[8 * m + q], p[idx[8 * m + q]]));
+    for (int q = 0; q < 8; ++q) s = f_add(s, f_mul(w[8 * m + q], src[idx[8 * m + q]]));
     out[m] = s;
 }
 
@@ -325,10 +331,11 @@ int sf_launch_probe_gather(const float* p, const long long* cells, int n, float*
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_probe_gather launch failed");
 }
 
-int sf_launch_mic_gather(const float* p, const long long* idx, const float* w, int n, float* out,
+int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const float* vz,
+                         const int* field, const long long* idx, const float* w, int n, float* out,
                          cudaStream_t st) {
     if (n <= 0) return 0;
-    k_mic_gather<<<(n + 127) / 128, 128, 0, st>>>(p, idx, w, n, out);
+    k_mic_gather<<<(n + 127) / 128, 128, 0, st>>>(p, vx, vy, vz, field, idx, w, n, out);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_mic_gather launch failed");
 }
 

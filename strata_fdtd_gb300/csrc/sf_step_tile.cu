@@ -21,13 +21,15 @@
 //
 // Needs nz % 4 == 0, 16-byte aligned fields and nx*ny*nz + 2*ny*nz < 2^31
 // (32-bit cell offsets); the launcher falls back to the first column
-// configuration otherwise.
+// configuration otherwise.  The scalar form (k_step_tile1, one cell per lane,
+// sf_tile1.cuh) has no such needs beyond ny*nz < 2^31.
 #include <cuda_runtime.h>
 
 #include <climits>
 
 #include "sf_common.cuh"
 #include "sf_kernels.h"
+#include "sf_tile1.cuh"
 
 namespace {
 
@@ -328,6 +330,51 @@ __global__ void __launch_bounds__(32 * W, MINB) k_step_tile(SfStepArgs a, SfSour
     }
 }
 
+// Scalar warp tiles: 32 lanes along k, R rows per lane, W warps along j.
+template <bool GEOM, int R, int W, int MINB, bool PF>
+__global__ void __launch_bounds__(32 * W, MINB) k_step_tile1(SfStepArgs a, SfSources src, int ich) {
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int jb = (blockIdx.y * W + threadIdx.y) * R;
+    const int chunk = a.reverse ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z;
+    const int i0 = chunk * ich;
+    const int i1 = min(i0 + ich, a.nx);
+    if (a.trace_prev != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) {
+        for (int t = threadIdx.y * 32 + threadIdx.x; t < a.n_probe; t += 32 * W)
+            a.trace_prev[t] = a.p[a.probe_cells[t]];
+    }
+    if (jb >= a.ny) return;  // the whole warp is past the grid
+    Tile1Io io;
+    io.nx = a.nx;
+    io.ny = a.ny;
+    io.nz = a.nz;
+    io.plane = a.plane;
+    io.cv = a.cv;
+    io.cp = a.cp;
+    io.p = a.p;
+    io.vx = a.vx;
+    io.vy = a.vy;
+    io.vz = a.vz;
+    io.po = a.po;
+    io.vxo = a.vxo;
+    io.vyo = a.vyo;
+    io.vzo = a.vzo;
+    io.flags = a.flags;
+    io.dx = a.dx;
+    io.dy = a.dy;
+    io.dz = a.dz;
+    io.src_val = a.src_val;
+    tile1_run<GEOM, R, PF>(io, src, i0, i1, jb, k);
+}
+
+template <int R, int W, int MINB, bool PF>
+int launch1(const SfStepArgs& a, const SfSources& src, bool geom, int ich, cudaStream_t st) {
+    dim3 blk(32, W, 1);
+    dim3 grd((a.nz + 31) / 32, (a.ny + R * W - 1) / (R * W), (a.nx + ich - 1) / ich);
+    if (geom) k_step_tile1<true, R, W, MINB, PF><<<grd, blk, 0, st>>>(a, src, ich);
+    else k_step_tile1<false, R, W, MINB, PF><<<grd, blk, 0, st>>>(a, src, ich);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step_tile1 launch failed");
+}
+
 template <int R, int W, int MINB, bool PF>
 int launch(const SfStepArgs& a, const SfSources& src, bool geom, int ich, cudaStream_t st) {
     dim3 blk(32, W, 1);
@@ -344,16 +391,26 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 
 // Warp-tile configurations (index = SF_CFG_COL_FIRST + kSfColConfigCount + position).
 const SfTileConfig kSfTileConfigs[] = {
-    // rows per lane, warps per block, min blocks, prefetch, name
-    {1, 4, 6, 1, "tile_r1_w4_pf"},
-    {1, 8, 3, 1, "tile_r1_w8_pf"},
-    {1, 4, 8, 0, "tile_r1_w4"},
-    {2, 4, 4, 0, "tile_r2_w4"},
-    {2, 2, 8, 0, "tile_r2_w2"},
+    // cells per lane along k, rows per lane, warps per block, min blocks, prefetch, name
+    {4, 1, 4, 6, 1, "tile_r1_w4_pf"},
+    {4, 1, 8, 3, 1, "tile_r1_w8_pf"},
+    {4, 1, 4, 8, 0, "tile_r1_w4"},
+    {4, 2, 4, 4, 0, "tile_r2_w4"},
+    {4, 2, 2, 8, 0, "tile_r2_w2"},
+    {4, 1, 2, 16, 0, "tile_r1_w2"},
+    {4, 1, 8, 4, 0, "tile_r1_w8"},
+    {4, 1, 4, 6, 0, "tile_r1_w4_m6"},
+    {1, 4, 4, 4, 0, "tile1_r4_w4"},
+    {1, 2, 8, 3, 1, "tile1_r2_w8_pf"},
+    {1, 2, 4, 8, 0, "tile1_r2_w4"},
+    {1, 2, 8, 4, 0, "tile1_r2_w8"},
+    {1, 1, 8, 4, 1, "tile1_r1_w8_pf"},
+    {1, 2, 4, 6, 1, "tile1_r2_w4_pf"},
 };
 const int kSfTileConfigCount = sizeof(kSfTileConfigs) / sizeof(kSfTileConfigs[0]);
 
-bool sf_tile_supported(const SfStepArgs& a) {
+bool sf_tile_supported(const SfStepArgs& a, int vec) {
+    if (vec == 1) return (long long)a.ny * a.nz + a.nz + 64 < (long long)INT_MAX;
     const long long n = (long long)a.nx * a.ny * a.nz;
     if (a.nz % 4 != 0 || n + 2LL * a.ny * a.nz + 8 >= (long long)INT_MAX) return false;
     return aligned16(a.p) && aligned16(a.vx) && aligned16(a.vy) && aligned16(a.vz) &&
@@ -365,13 +422,23 @@ int sf_launch_step_tile_cfg(const SfStepArgs& a, const SfSources& src, bool geom
                             cudaStream_t st) {
     if (ich < 1) ich = 1;
     if (cfg < 0 || cfg >= kSfTileConfigCount) return sf_fail("k_step_tile: bad configuration");
-    if (!sf_tile_supported(a)) return sf_launch_step_col_cfg(a, src, geom, 0, ich, st);
+    if (!sf_tile_supported(a, kSfTileConfigs[cfg].vec))
+        return sf_launch_step_col_cfg(a, src, geom, 0, ich, st);
     switch (cfg) {
         case 0: return launch<1, 4, 6, true>(a, src, geom, ich, st);
         case 1: return launch<1, 8, 3, true>(a, src, geom, ich, st);
         case 2: return launch<1, 4, 8, false>(a, src, geom, ich, st);
         case 3: return launch<2, 4, 4, false>(a, src, geom, ich, st);
         case 4: return launch<2, 2, 8, false>(a, src, geom, ich, st);
+        case 5: return launch<1, 2, 16, false>(a, src, geom, ich, st);
+        case 6: return launch<1, 8, 4, false>(a, src, geom, ich, st);
+        case 7: return launch<1, 4, 6, false>(a, src, geom, ich, st);
+        case 8: return launch1<4, 4, 4, false>(a, src, geom, ich, st);
+        case 9: return launch1<2, 8, 3, true>(a, src, geom, ich, st);
+        case 10: return launch1<2, 4, 8, false>(a, src, geom, ich, st);
+        case 11: return launch1<2, 8, 4, false>(a, src, geom, ich, st);
+        case 12: return launch1<1, 8, 4, true>(a, src, geom, ich, st);
+        case 13: return launch1<2, 4, 6, true>(a, src, geom, ich, st);
     }
     return sf_fail("k_step_tile: bad configuration");
 }

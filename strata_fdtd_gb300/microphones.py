@@ -1,64 +1,184 @@
-"""Virtual microphones at physical positions (core/solver.py:797-1438 of
-rjwalters/strata-fdtd), omnidirectional, recorded on the GPU.
+"""Virtual microphones at physical positions (core/solver.py:786-1438 of
+rjwalters/strata-fdtd), recorded on the GPU.
 
-The reference records omni microphones through its native batch kernel:
-grid positions as float32, corner weights formed in float
-(``_kernels/src/microphones.cpp:16-80``) and the float sum from zero of
-weight x pressure over the 8 corners after each step (``:82-118``).  The
-weights here are formed with the same float32 arithmetic on the host and the
-sum runs in ``k_mic_gather``, so the waveforms are bit-identical.
-Directional patterns (which the reference evaluates in its Python path from
-interpolated velocities) are not part of the GB300 path.
+Every microphone is one or four *rows* of the plan's microphone table
+(``sf_plan_set_microphones_ex``): 8 corner cells, 8 float32 weights and the
+field they read.  ``k_mic_gather`` forms the float sum from 0 of weight x
+field over the corners after each step.
+
+The reference has two recording paths, and the weights follow whichever one
+it would take (``FDTDSolver._record_microphones``, core/solver.py:2441-2461):
+
+* all microphones omnidirectional -> its native batch kernel: grid positions
+  as float32 and corner weights in float arithmetic
+  (``_kernels/src/microphones.cpp:16-80``), sum as ``:82-118``;
+* any microphone directional -> ``Microphone.record`` for every microphone:
+  FP64 weights (``_compute_trilinear_weights``, core/solver.py:965-1002)
+  which NumPy rounds to float32 when it multiplies them with the float32
+  field, and float32 sums.  A directional microphone adds three rows: vx, vy
+  and vz at its position shifted half a cell back along the component's axis
+  and clamped (``_interpolate_velocity``, :1060-1118).
+
+The polar-pattern combination (``_compute_directional_output``,
+:1120-1179) runs on the host over the recorded rows with the reference's own
+NumPy scalar types, so standard and custom patterns give the reference's
+samples bit for bit.
 """
 from __future__ import annotations
+
+from typing import Callable
 
 import numpy as np
 
 _CORNERS = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0), (0, 0, 1), (1, 0, 1), (0, 1, 1),
             (1, 1, 1)]
 
+# pattern coefficient k of output = (1 - k) p + k rho c (v . d)  (core/solver.py:787-794)
+POLAR_PATTERNS: dict[str, float] = {
+    "omni": 0.0,
+    "subcardioid": 0.3,
+    "cardioid": 0.5,
+    "supercardioid": 0.63,
+    "hypercardioid": 0.75,
+    "figure8": 1.0,
+}
+
+
+def _weights_fp64(gx: float, gy: float, gz: float):
+    """Corner cells and FP64 weights of Microphone._compute_trilinear_weights."""
+    i0, j0, k0 = int(gx), int(gy), int(gz)
+    fx, fy, fz = gx - i0, gy - j0, gz - k0
+    w = [(1 - fx) * (1 - fy) * (1 - fz), fx * (1 - fy) * (1 - fz), (1 - fx) * fy * (1 - fz),
+         fx * fy * (1 - fz), (1 - fx) * (1 - fy) * fz, fx * (1 - fy) * fz, (1 - fx) * fy * fz,
+         fx * fy * fz]
+    cells = [(i0 + a, j0 + b, k0 + c) for a, b, c in _CORNERS]
+    return cells, w
+
 
 class Microphone:
-    """Omnidirectional microphone at ``position`` (metres)."""
+    """Microphone at ``position`` (metres) with a polar ``pattern`` (a name of
+    POLAR_PATTERNS or a callable gain(theta)), pointing along ``direction``."""
 
-    def __init__(self, position, name=None, pattern="omni", direction=None, up=None):
-        if pattern != "omni":
-            raise NotImplementedError(
-                "directional microphone patterns are not implemented by the GB300 backend")
-        self.position = tuple(float(v) for v in position)
+    def __init__(self, position, name=None, pattern: str | Callable[[float], float] = "omni",
+                 direction=None, up=None):
+        self.position = position
         self.name = name
-        self.pattern = "omni"
-        self._data: list[float] = []
+        if isinstance(pattern, str):
+            if pattern not in POLAR_PATTERNS:
+                raise ValueError(f"Unknown pattern '{pattern}'. "
+                                 f"Valid patterns: {list(POLAR_PATTERNS.keys())}")
+            self._pattern_name = pattern
+            self._pattern_k = POLAR_PATTERNS[pattern]
+            self._custom_pattern = None
+        elif callable(pattern):
+            self._pattern_name = "custom"
+            self._pattern_k = None
+            self._custom_pattern = pattern
+        else:
+            raise TypeError(f"pattern must be str or callable, got {type(pattern).__name__}")
+        self.pattern = pattern
+        d = np.array((1.0, 0.0, 0.0) if direction is None else direction, dtype=np.float64)
+        dn = np.linalg.norm(d)
+        if dn < 1e-10:
+            raise ValueError("direction vector cannot be zero")
+        self._direction = d / dn
+        u = np.array((0.0, 0.0, 1.0) if up is None else up, dtype=np.float64)
+        un = np.linalg.norm(u)
+        if un < 1e-10:
+            raise ValueError("up vector cannot be zero")
+        self._up = u / un
+        if abs(np.dot(self._direction, self._up)) > 0.999:
+            raise ValueError("direction and up vectors cannot be parallel")
+        self._data: list = []
         self._times: list[float] = []
         self._solver = None
+        self._solver_dt = None
+        self._solver_rho = None
+        self._solver_c = None
         self._grid_position = None
-        self.corner_cells = None
-        self.weights = None
+
+    @property
+    def direction(self):
+        return tuple(self._direction)
 
     def is_directional(self) -> bool:
-        return False
+        return self._pattern_name != "omni"
 
     def _initialize(self, solver) -> None:
-        """core/solver.py:930-960: grid position = position / dx, inside the
-        domain; corner cells and float32 weights as microphones.cpp:16-80."""
-        gx, gy, gz = (p / solver.dx for p in self.position)
+        """core/solver.py:930-963: grid position = position / dx, strictly
+        inside the domain."""
+        self._solver_dt = solver.dt
+        self._solver_rho = solver.rho
+        self._solver_c = solver.c
+        gx = self.position[0] / solver.dx
+        gy = self.position[1] / solver.dx
+        gz = self.position[2] / solver.dx
+        self._grid_position = (gx, gy, gz)
         if not (0 <= gx < solver.shape[0] - 1 and 0 <= gy < solver.shape[1] - 1
                 and 0 <= gz < solver.shape[2] - 1):
             raise ValueError(f"Microphone position {self.position} is outside simulation domain.")
-        self._grid_position = (gx, gy, gz)
-        g = [np.float32(v) for v in self._grid_position]
-        i0 = [int(v) for v in g]
-        fx, fy, fz = (np.float32(v - np.float32(i)) for v, i in zip(g, i0))
-        one = np.float32(1.0)
-        w = [(one - fx) * (one - fy) * (one - fz), fx * (one - fy) * (one - fz),
-             (one - fx) * fy * (one - fz), fx * fy * (one - fz), (one - fx) * (one - fy) * fz,
-             fx * (one - fy) * fz, (one - fx) * fy * fz, fx * fy * fz]
-        self.weights = np.array(w, dtype=np.float32)
-        self.corner_cells = np.array(
-            [np.ravel_multi_index((i0[0] + a, i0[1] + b, i0[2] + c), solver.shape)
-             for a, b, c in _CORNERS], dtype=np.int64)
         self._solver = solver
 
+    # -- rows of the device table --------------------------------------------
+    def _rows(self, shape, python_path: bool):
+        """[(field, 8 flat cells, 8 float32 weights)] this microphone records."""
+        gx, gy, gz = self._grid_position
+        if not python_path:  # native batch kernel (microphones.cpp:16-80)
+            g = [np.float32(v) for v in self._grid_position]
+            i0 = [int(v) for v in g]
+            fx, fy, fz = (np.float32(v - np.float32(i)) for v, i in zip(g, i0))
+            one = np.float32(1.0)
+            w = [(one - fx) * (one - fy) * (one - fz), fx * (one - fy) * (one - fz),
+                 (one - fx) * fy * (one - fz), fx * fy * (one - fz), (one - fx) * (one - fy) * fz,
+                 fx * (one - fy) * fz, (one - fx) * fy * fz, fx * fy * fz]
+            cells = [np.ravel_multi_index((i0[0] + a, i0[1] + b, i0[2] + c), shape)
+                     for a, b, c in _CORNERS]
+            return [(0, np.array(cells, np.int64), np.array(w, np.float32))]
+        cells, w = _weights_fp64(gx, gy, gz)
+        rows = [(0, np.array([np.ravel_multi_index(c, shape) for c in cells], np.int64),
+                 np.array(w, dtype=np.float64).astype(np.float32))]
+        if self.is_directional():
+            nx, ny, nz = shape
+            for axis in range(3):  # _interpolate_velocity (core/solver.py:1060-1118)
+                g = [gx, gy, gz]
+                g[axis] -= 0.5
+                g[0] = max(0.0, min(g[0], nx - 1.001))
+                g[1] = max(0.0, min(g[1], ny - 1.001))
+                g[2] = max(0.0, min(g[2], nz - 1.001))
+                vc, vw = _weights_fp64(*g)
+                flat = [np.ravel_multi_index((min(i, nx - 1), min(j, ny - 1), min(k, nz - 1)),
+                                             shape) for i, j, k in vc]
+                rows.append((1 + axis, np.array(flat, np.int64),
+                             np.array(vw, dtype=np.float64).astype(np.float32)))
+        return rows
+
+    def _append(self, samples: np.ndarray, times) -> None:
+        """Add recorded rows (float32 [steps, rows]) as output samples."""
+        if not self.is_directional():
+            self._data.extend(samples[:, 0].tolist())
+            self._times.extend(times)
+            return
+        p, vx, vy, vz = (samples[:, q] for q in range(4))
+        d0, d1, d2 = self._direction[0], self._direction[1], self._direction[2]
+        Z = self._solver_rho * self._solver_c
+        if self._custom_pattern is None:
+            k = self._pattern_k
+            vd = vx * d0 + vy * d1 + vz * d2            # float64 (float32 x np.float64)
+            out = (1 - k) * p + k * Z * vd               # float32 term + float64 term
+            self._data.extend(out.tolist())
+        else:  # per sample, with the reference's scalar types (core/solver.py:1160-1174)
+            for t in range(samples.shape[0]):
+                px, ux, uy, uz = (np.float32(samples[t, q]) for q in range(4))
+                vd = ux * d0 + uy * d1 + uz * d2
+                v_mag = np.sqrt(ux ** 2 + uy ** 2 + uz ** 2)
+                if v_mag > 1e-20:
+                    theta = np.arccos(np.clip(vd / v_mag, -1.0, 1.0))
+                else:
+                    theta = 0.0
+                self._data.append(px * self._custom_pattern(theta))
+        self._times.extend(times)
+
+    # -- reference accessors ---------------------------------------------------
     @property
     def data(self) -> list:
         if self._solver is not None:
@@ -75,7 +195,9 @@ class Microphone:
         return np.array(self._times, dtype=np.float64)
 
     def get_sample_rate(self) -> float:
-        return 1.0 / self._solver.dt
+        if self._solver_dt is None:
+            raise RuntimeError("Microphone not initialized. Add to solver first.")
+        return 1.0 / self._solver_dt
 
     def clear(self) -> None:
         self.data  # noqa: B018

@@ -196,7 +196,8 @@ class FDTDSolver:
         self._probe_dirty = True
         self._probe_order: list[str] = []
         self._pending_traces: list = []
-        self._mic_order: list[str] = []
+        self._mic_order: list = []  # (name, rows) per microphone
+        self._mic_rows = 0
         self._mic_dirty = False
         self._pending_mics: list = []
 
@@ -380,8 +381,8 @@ class FDTDSolver:
         self._probe_dirty = True
 
     def add_microphone(self, position, name=None, pattern="omni", direction=None, up=None):
-        """Omni microphone at a physical position (core/solver.py:1887-1965);
-        returns the Microphone."""
+        """Microphone at a physical position, omnidirectional or with a polar
+        pattern (core/solver.py:1887-1965); returns the Microphone."""
         from .microphones import Microphone
 
         mic = position if isinstance(position, Microphone) else Microphone(
@@ -544,13 +545,23 @@ class FDTDSolver:
                                                        cells.ctypes.data), "sf_plan_set_probes")
             self._probe_dirty = False
         if self._mic_dirty:
-            self._mic_order = list(self._microphones)
-            mics = [self._microphones[n] for n in self._mic_order]
-            idx = np.concatenate([m.corner_cells for m in mics] or [np.zeros(8, np.int64)])
-            w = np.concatenate([m.weights for m in mics] or [np.zeros(8, np.float32)])
-            _native.check(self._lib.sf_plan_set_microphones(self._plan, len(mics), idx.ctypes.data,
-                                                            w.ctypes.data),
-                          "sf_plan_set_microphones")
+            # the reference's Python recording path (FP64 weights) as soon as
+            # one microphone is directional, else its native batch kernel
+            # (core/solver.py:2441-2461)
+            python_path = any(m.is_directional() for m in self._microphones.values())
+            self._mic_order = []
+            rows = []
+            for name, m in self._microphones.items():
+                r = m._rows(self.shape, python_path)
+                self._mic_order.append((name, len(r)))
+                rows.extend(r)
+            field = np.array([f for f, _, _ in rows] or [0], dtype=np.int32)
+            idx = np.concatenate([c for _, c, _ in rows] or [np.zeros(8, np.int64)])
+            w = np.concatenate([x for _, _, x in rows] or [np.zeros(8, np.float32)])
+            _native.check(self._lib.sf_plan_set_microphones_ex(
+                self._plan, len(rows), field.ctypes.data, idx.ctypes.data, w.ctypes.data),
+                "sf_plan_set_microphones")
+            self._mic_rows = len(rows)
             self._mic_dirty = False
         if self.has_materials and not self._ade_initialized:
             self._initialize_ade_fields()
@@ -596,7 +607,7 @@ class FDTDSolver:
         n_probe = len(self._probe_order)
         trace = (torch.empty((n, n_probe), dtype=torch.float32, device=self._device)
                  if n_probe else None)
-        n_mic = len(self._mic_order)
+        n_mic = getattr(self, "_mic_rows", 0)
         mic_trace = (torch.empty((n, n_mic), dtype=torch.float32, device=self._device)
                      if n_mic else None)
         rc = self._lib.sf_plan_step_ex(self._plan, n,
@@ -623,12 +634,13 @@ class FDTDSolver:
                 if name in self._probes:
                     self._probes[name]._samples.extend(host[:, q].tolist())
         self._pending_traces.clear()
-        for trace, names, times in getattr(self, "_pending_mics", []):
+        for trace, layout, times in getattr(self, "_pending_mics", []):
             host = trace.cpu().numpy()
-            for q, name in enumerate(names):
+            q = 0
+            for name, n_rows in layout:
                 if name in self._microphones:
-                    self._microphones[name]._data.extend(host[:, q].tolist())
-                    self._microphones[name]._times.extend(times)
+                    self._microphones[name]._append(host[:, q:q + n_rows], times)
+                q += n_rows
         self._pending_mics = []
 
     def step(self) -> None:

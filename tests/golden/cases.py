@@ -38,6 +38,11 @@ def _mask_blocks(shape, seed, n_boxes=2, n_spheres=1):
     return g
 
 
+def gain_07_03(theta):
+    """Custom microphone pattern of the directional golden case."""
+    return 0.7 + 0.3 * np.cos(theta)
+
+
 # --------------------------------------------------------------------------
 # Plain path: reference FDTDSolver(backend="native") step for step.
 # source tuple: (kind, position, frequency, amplitude); a plane position is a
@@ -100,6 +105,27 @@ PLAIN_CASES = {
         mics=[("m0", (0.0153, 0.0121, 0.0107)), ("m1", (0.0201, 0.0042, 0.0255)),
               ("m2", (0.004, 0.0195, 0.0149)), ("m3", (0.0222, 0.0133, 0.0178))],
         steps=140, store_fields=True,
+    ),
+    "mics_directional": dict(
+        # directional microphones (the reference's Python recording path for
+        # every microphone): omni, cardioid, figure-8, supercardioid on an
+        # oblique axis, a custom gain(theta); positions at the low and high
+        # clamps of the staggered velocity interpolation
+        shape=(26, 22, 30), res=1e-3, courant=0.5, pml=dict(depth=4),
+        geometry=dict(kind="blocks", seed=33, n_boxes=1, n_spheres=1),
+        sources=[("point", (9, 11, 15), 18000.0, 1.0)],
+        probes=[("pr", (18, 11, 15))],
+        mics=[("om", (0.0153, 0.0121, 0.0107)),
+              ("card", (0.0131, 0.0072, 0.0146), dict(pattern="cardioid", direction=(1, 0, 0))),
+              ("fig8", (0.0124, 0.0143, 0.0181), dict(pattern="figure8", direction=(0, 1, 0),
+                                                      up=(1, 0, 0))),
+              ("super", (0.0003, 0.0209996, 0.0066),
+               dict(pattern="supercardioid", direction=(0.3, -0.5, 0.8))),
+              ("hyper", (0.0247, 0.0004, 0.0288), dict(pattern="hypercardioid",
+                                                       direction=(-1, 0.2, 0.1))),
+              ("custom", (0.0171, 0.0113, 0.0139), dict(pattern="gain_07_03",
+                                                        direction=(0, 0.6, 0.8)))],
+        steps=120, store_fields=True,
     ),
     "c1_full": dict(
         # the reference quick start, 100^3 x 1000 steps (hashes + traces only)
@@ -285,8 +311,12 @@ def build_case(api, case, ade=False):
         probes = c2_probes(solver.geometry)
     for name, pos in probes:
         solver.add_probe(name, pos)
-    for name, pos in case.get("mics", []):
-        solver.add_microphone(position=pos, name=name)
+    for mic in case.get("mics", []):
+        name, pos = mic[0], mic[1]
+        opts = dict(mic[2]) if len(mic) > 2 else {}
+        if opts.get("pattern") == "gain_07_03":
+            opts["pattern"] = gain_07_03
+        solver.add_microphone(position=pos, name=name, **opts)
     if case.get("impulse"):
         pos, val = case["impulse"]
         solver.p[pos] = val

@@ -54,8 +54,9 @@ def test_batch_matches_reference_goldens(graph_steps, manifest):
             np.testing.assert_array_equal(s._ade_J_debye, g["ade_ade_J_debye"])
 
 
-@pytest.mark.parametrize("rows,i_chunk", [(4, 8), (16, 32), (8, 0)])
-def test_batch_equals_alone_in_two_runs(rows, i_chunk):
+@pytest.mark.parametrize("kernel", ["column", "warp", "warp_prefetch"])
+@pytest.mark.parametrize("rows,i_chunk", [(4, 8), (16, 32), (8, 0), (8, 3)])
+def test_batch_equals_alone_in_two_runs(rows, i_chunk, kernel):
     """Members run in two batched runs (continuing state) equal the solves run
     alone with the default kernel."""
     alone = [C.build_case(API, _case(k, n)) for k, n in MIX]
@@ -65,7 +66,7 @@ def test_batch_equals_alone_in_two_runs(rows, i_chunk):
     for s, a, b_ in zip(alone, first, second):
         s.run_steps(a)
         s.run_steps(b_)
-    b = BatchedSolver(mixed, rows=rows, i_chunk=i_chunk)
+    b = BatchedSolver(mixed, rows=rows, i_chunk=i_chunk, kernel=kernel)
     b.run_steps(first, graph_steps=8)
     b.run_steps(second, graph_steps=0)
     for s, t in zip(mixed, alone):
@@ -83,7 +84,8 @@ def test_batch_autotune_leaves_state_unchanged():
     BatchedSolver(b).run_steps(20)
     bs = BatchedSolver(a)
     table = bs.autotune(launches=2)
-    assert table["best"][0] in (4, 8, 16)
+    assert table["best"][0] in ("column", "warp", "warp_prefetch")
+    assert table["best"][1] in (4, 8, 16)
     bs.run_steps(30)
     BatchedSolver(b).run_steps(30)
     for x, y in zip(a, b):

@@ -57,7 +57,7 @@ def test_plain_cases_one_call(name, manifest):
         assert sha256(s.geometry) == manifest["plain_" + name]["sha_geometry"]
 
 
-@pytest.mark.parametrize("name", ["c1_tiny", "blocks_odd", "plane_yz_geom"])
+@pytest.mark.parametrize("name", ["c1_tiny", "blocks_odd", "plane_yz_geom", "mics_directional"])
 def test_plain_cases_step_by_step(name, manifest):
     case = C.PLAIN_CASES[name]
     s = C.build_case(API, case)
@@ -392,7 +392,10 @@ def test_errors_are_loud():
     s = S.FDTDSolver(shape=(8, 8, 8), resolution=1e-3)
     with pytest.raises(ValueError):
         s.add_source(S.GaussianPulse(position=(9, 0, 0), frequency=1000.0))
-    with pytest.raises(NotImplementedError):
-        s.add_microphone(position=(0.001, 0.001, 0.001), name="card", pattern="cardioid")
+    with pytest.raises(ValueError):
+        s.add_microphone(position=(0.001, 0.001, 0.001), name="card", pattern="cardioid5")
+    with pytest.raises(ValueError):
+        s.add_microphone(position=(0.001, 0.001, 0.001), name="par", pattern="figure8",
+                         direction=(0, 0, 2))
     with pytest.raises(ValueError):
         s.add_microphone(position=(0.0079, 0.001, 0.001), name="outside")

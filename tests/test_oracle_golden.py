@@ -44,13 +44,20 @@ def test_plain_fused_loop_matches_reference(name, manifest):
     _check(_run(C.PLAIN_CASES[name], step_by_step=False), "plain_" + name, manifest)
 
 
-def test_microphones_match_reference(manifest):
-    case = C.PLAIN_CASES["mics_geom"]
+@pytest.mark.parametrize("name", ["mics_geom", "mics_directional"])
+def test_microphones_match_reference(name, manifest):
+    """Omni microphones through the native batch kernel's float32 weights;
+    with directional ones present, every microphone through the reference's
+    Python path (FP64 weights, staggered clamped velocity interpolation,
+    pattern combination, a custom gain)."""
+    case = C.PLAIN_CASES[name]
     s = _run(case, step_by_step=True)
-    _check(s, "plain_mics_geom", manifest)
-    g = golden("plain_mics_geom")
-    for name, tr in s.get_mic_data().items():
-        np.testing.assert_array_equal(tr, g[f"mic__{name}"])
+    _check(s, "plain_" + name, manifest)
+    g = golden("plain_" + name)
+    mics = s.get_mic_data()
+    assert len(mics) == len(case["mics"])
+    for mic, tr in mics.items():
+        np.testing.assert_array_equal(tr, g[f"mic__{mic}"])
 
 
 @pytest.mark.parametrize("name", ["c1_tiny", "blocks_odd", "plane_yz_geom"])
