@@ -163,20 +163,27 @@ int sf_plan_set_microphones_ex(sf_plan* plan, int n, const int32_t* field, const
 int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const sf_pole* poles,
                     float inv_dx);
 
-/* Box [lo, hi) holding every cell with a nonzero material id; the batched
- * density-pole pass walks only this box (default: the whole grid).  No
- * counterpart in the reference (its ADE kernels sweep the whole grid). */
+/* Box [lo, hi) holding every cell with a nonzero material id; the
+ * density-pole pass walks only this box, and an ADE step on a warp-tile
+ * configuration gives the box (grown by one cell, rounded out to whole
+ * tiles) to the per-cell ADE kernel and the rest of the grid to the
+ * warp-tile kernel.  No counterpart in the reference (its ADE kernels sweep
+ * the whole grid). */
 int sf_plan_set_ade_box(sf_plan* plan, const int32_t* lo, const int32_t* hi);
 
 /* Step-kernel configuration.  config 0 = automatic (the autotuned
- * configuration if sf_plan_autotune ran, else the default), 1 = one thread
- * per cell, 2 = slab march along i with shared-memory halos, 3.. = thread
- * columns along i in the variants named by sf_kernel_config_name (vector
- * width, block rows, register cap, streaming stores; a vector width that
- * does not divide nz falls back to scalar columns).  i_chunk = planes per
- * block (0 = automatic).  ADE poles always run the per-cell kernel.  Every
- * configuration gives identical results.  No counterpart in the reference
- * (its kernels are CPU loops). */
+ * configuration if sf_plan_autotune ran, else the default warp tiles), 1 =
+ * one thread per cell, 2 = slab march along i with shared-memory halos,
+ * then thread columns along i ("col*": vector width, block rows, register
+ * cap, streaming stores) and warp tiles with lane-shuffled neighbours
+ * ("tile_*": float4 lanes, needs nz % 4 == 0 and 16-byte aligned fields;
+ * "tile1_*": one cell per lane), as named by sf_kernel_config_name.  A
+ * configuration the grid cannot take falls back to scalar columns.  i_chunk
+ * = planes per block (0 = automatic).  With ADE poles the warp-tile
+ * configurations split each step with the per-cell kernel (see
+ * sf_plan_set_ade_box); any other configuration runs the per-cell kernel.
+ * Every configuration gives identical results.  No counterpart in the
+ * reference (its kernels are CPU loops). */
 int sf_plan_set_kernel(sf_plan* plan, int config, int i_chunk);
 int sf_kernel_config_count(void);
 const char* sf_kernel_config_name(int config);
@@ -184,7 +191,8 @@ const char* sf_kernel_config_name(int config);
 /* Autotuner: times every configuration that fits the grid for `launches`
  * step launches each (reading the current state and writing the other set
  * without swapping, no sources, no probes -- the state is unchanged) and
- * makes the fastest the plan's automatic choice.  ms_out (host, may be NULL)
+ * makes the fastest the plan's automatic choice; with ADE poles only the
+ * warp-tile configurations, timed outside their ADE region.  ms_out (host, may be NULL)
  * receives sf_kernel_config_count() per-launch times (-1 = not run);
  * best_out (may be NULL) the chosen configuration.  Synchronises the stream.
  * No counterpart in the reference. */

@@ -308,9 +308,13 @@ void fill_args(const sf_plan* P, SfStepArgs& a, bool with_trace) {
     a.n_probe = with_trace ? P->n_probe : 0;
     a.probe_cells = P->probe_cells;
     a.mat = P->mat;
+    const int n3[3] = {P->d.nx, P->d.ny, P->d.nz};
     for (int q = 0; q < 3; ++q) {
         a.ade_lo[q] = P->ade_lo[q];
         a.ade_hi[q] = P->ade_hi[q];
+        a.reg_lo[q] = 0;  // the per-cell kernel covers the grid
+        a.reg_hi[q] = n3[q];
+        a.skip_lo[q] = a.skip_hi[q] = 0;  // the warp-tile kernels skip nothing
     }
 }
 
@@ -326,17 +330,50 @@ void set_io(const sf_plan* P, SfStepArgs& a, int in) {
     a.vzo = P->f[out][3];
 }
 
-// The configuration a step of this plan runs: ADE poles need the per-cell
-// kernel; otherwise the explicit choice, else the autotuned one, else the
-// default warp-tile configuration where the grid allows it (nz % 4 == 0,
-// aligned fields, 32-bit offsets), else the first column configuration.
+// The configuration a step of this plan runs: the explicit choice, else the
+// autotuned one, else the default warp-tile configuration where the grid
+// allows it (nz % 4 == 0, aligned fields, 32-bit offsets), else the first
+// column configuration.  With ADE poles only the warp-tile configurations
+// (which then leave the material box to the per-cell kernel, see
+// ade_region) and the per-cell kernel itself are used.
 int effective_config(const sf_plan* P, const SfStepArgs& a) {
-    if (P->poles.n > 0) return SF_CFG_CELL;
-    if (P->variant != SF_CFG_AUTO) return P->variant;
-    if (P->tuned > 0) return P->tuned;
-    if (sf_tile_supported(a, 4)) return SF_CFG_TILE_DEFAULT;
-    return sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT;
+    int cfg;
+    if (P->variant != SF_CFG_AUTO) cfg = P->variant;
+    else if (P->tuned > 0) cfg = P->tuned;
+    else if (sf_tile_supported(a, 4)) cfg = SF_CFG_TILE_DEFAULT;
+    else cfg = sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT;
+    if (P->poles.n > 0 &&
+        !(cfg >= SF_CFG_TILE_FIRST && sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec)))
+        cfg = SF_CFG_CELL;
+    return cfg;
 }
+
+// The cells an ADE step gives to the per-cell kernel when warp-tile
+// configuration cfg (i-chunk ich) runs the rest: the material box grown by
+// one cell (the faces the ADE terms touch) and rounded out to whole tiles of
+// that configuration.  Outside it no cell and no face carries an ADE term
+// (both cells of a corrected face lie in one material), so the warp-tile
+// kernel's plain arithmetic is the reference's there.  Empty when the plan
+// has no material cells.
+void ade_region(const sf_plan* P, int cfg, int ich, int lo[3], int hi[3]) {
+    const SfTileConfig& t = kSfTileConfigs[cfg - SF_CFG_TILE_FIRST];
+    const int n3[3] = {P->d.nx, P->d.ny, P->d.nz};
+    const int span[3] = {ich, t.vec == 4 ? 4 * t.rows * t.warps : t.rows * t.warps, 32};
+    bool empty = false;
+    for (int q = 0; q < 3; ++q) empty = empty || P->ade_hi[q] <= P->ade_lo[q];
+    for (int q = 0; q < 3; ++q) {
+        if (empty) {
+            lo[q] = hi[q] = 0;
+            continue;
+        }
+        const int l = P->ade_lo[q] > 0 ? P->ade_lo[q] - 1 : 0;
+        const int h = P->ade_hi[q] < n3[q] ? P->ade_hi[q] + 1 : n3[q];
+        lo[q] = l / span[q] * span[q];
+        hi[q] = (h + span[q] - 1) / span[q] * span[q];
+        if (hi[q] > n3[q]) hi[q] = n3[q];
+    }
+}
+
 
 int chunk_for(const sf_plan* P, int cfg) {
     if (P->i_chunk > 0) return P->i_chunk;
@@ -374,6 +411,31 @@ int launch_config(const sf_plan* P, int cfg, int ich, const SfStepArgs& a, const
     return sf_launch_step(a, src, P->poles, g, st);
 }
 
+// One step of configuration cfg: a single launch, or for an ADE plan on a
+// warp-tile configuration the warp-tile kernel outside the ADE region and
+// the per-cell kernel (with the density pre-pass) inside it.  Both read
+// only the input set and write disjoint cells of the output set.
+int launch_step_split(const sf_plan* P, int cfg, int ich, SfStepArgs& a, const SfSources& src,
+                      cudaStream_t st) {
+    if (P->poles.n == 0 || cfg < SF_CFG_TILE_FIRST) return launch_config(P, cfg, ich, a, src, st);
+    int lo[3], hi[3];
+    ade_region(P, cfg, ich, lo, hi);
+    SfStepArgs t = a;
+    for (int q = 0; q < 3; ++q) {
+        t.skip_lo[q] = lo[q];
+        t.skip_hi[q] = hi[q];
+    }
+    if (int rc = launch_config(P, cfg, ich, t, src, st)) return rc;
+    if (hi[0] <= lo[0]) return 0;
+    SfStepArgs c = a;
+    c.trace_prev = nullptr;  // sampled by the warp-tile kernel
+    for (int q = 0; q < 3; ++q) {
+        c.reg_lo[q] = lo[q];
+        c.reg_hi[q] = hi[q];
+    }
+    return sf_launch_step(c, src, P->poles, P->flags != nullptr, st);
+}
+
 }  // namespace
 
 extern "C" {
@@ -403,7 +465,7 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
         a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
         a.reverse = (int)(P->steps_done & 1);
-        if (int rc = launch_config(P, cfg, ich, a, P->src, st)) return rc;
+        if (int rc = launch_step_split(P, cfg, ich, a, P->src, st)) return rc;
         P->cur = 1 - P->cur;
         ++P->steps_done;
         if (mics)
@@ -462,11 +524,10 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     const int count = sf_kernel_config_count();
     if (ms_out)
         for (int q = 0; q < count; ++q) ms_out[q] = -1.0f;
-    if (P->poles.n > 0) {  // ADE runs the per-cell kernel only
-        P->tuned = SF_CFG_CELL;
-        if (best_out) *best_out = SF_CFG_CELL;
-        return 0;
-    }
+    // With ADE poles only the warp-tile configurations are candidates; each
+    // is timed on the cells outside its ADE region (the per-cell kernel's
+    // share inside it is the same for all of them).
+    const bool ade = P->poles.n > 0;
     // Every trial reads the current set and writes the other one without
     // swapping, with no sources and no probes: the state is untouched, and the
     // next real step overwrites the other set entirely.
@@ -481,11 +542,13 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     float best_ms = 0.0f;
     int rc = 0;
     for (int cfg = SF_CFG_CELL; cfg < count && !rc; ++cfg) {
-        if (!config_native(P, cfg, a)) continue;
+        if (!config_native(P, cfg, a) || (ade && cfg < SF_CFG_TILE_FIRST)) continue;
         const int ich = chunk_for(P, cfg);
-        if ((rc = launch_config(P, cfg, ich, a, none, st))) break;  // warm-up
+        SfStepArgs t = a;
+        if (ade) ade_region(P, cfg, ich, t.skip_lo, t.skip_hi);
+        if ((rc = launch_config(P, cfg, ich, t, none, st))) break;  // warm-up
         if (cudaEventRecord(e0, st) != cudaSuccess) { rc = sf_fail("event record failed"); break; }
-        for (int q = 0; q < launches && !rc; ++q) rc = launch_config(P, cfg, ich, a, none, st);
+        for (int q = 0; q < launches && !rc; ++q) rc = launch_config(P, cfg, ich, t, none, st);
         if (rc) break;
         if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
             rc = sf_fail("sf_plan_autotune: timing failed");
@@ -503,6 +566,7 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
+    if (best == 0) best = SF_CFG_CELL;  // ADE on a grid no warp-tile kernel takes
     P->tuned = best;
     if (best_out) *best_out = best;
     return 0;

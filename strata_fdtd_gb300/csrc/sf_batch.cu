@@ -24,10 +24,12 @@
 #include "sf_common.cuh"
 #include "sf_kernels.h"
 #include "sf_plan_internal.h"
-#include "sf_tile1.cuh"
+#include "sf_tile.cuh"
 
 struct SfGridDev {
     int nx, ny, nz, ich;
+    int jspan;  // rows per tile
+    int vec4;   // plain tiles run as float4 warp tiles (nz % 4 == 0, aligned, 32-bit offsets)
     long long plane, n_steps;
     float cv, cp;
     int cur0, n_probe;
@@ -58,13 +60,15 @@ __device__ __forceinline__ float ade_face_g(float v, const SfPoles& P, uint8_t m
     return v;
 }
 
-// One tile: thread (tx, ty) walks cells (i0..i1-1, j, k) of grid g at step s.
+// Rows j0 .. j0+BY-1 (below j_end) of a tile: thread (tx, ty) walks cells
+// (i0..i1-1, j0 + ty, kb*32 + tx) of grid g at step s.
 template <int BY, bool GEOM, bool ADE>
-__device__ void batch_column(const SfGridDev& g, long long s, int chunk, int jb, int kb, bool trial) {
+__device__ void batch_column(const SfGridDev& g, long long s, int chunk, int j0, int j_end, int kb,
+                             bool trial) {
     const int k = kb * 32 + threadIdx.x;
-    const int j = jb * BY + threadIdx.y;
+    const int j = j0 + threadIdx.y;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    if (k >= nz || j >= ny) return;
+    if (k >= nz || j >= ny || j >= j_end) return;
     const int i0 = chunk * g.ich;
     const int i1 = min(i0 + g.ich, nx);
     const int in = (int)((g.cur0 + s) & 1);
@@ -201,7 +205,8 @@ __device__ void batch_column(const SfGridDev& g, long long s, int chunk, int jb,
 // the grid's material box?  Outside it every ADE term is absent, so such
 // tiles go to the plain kernel.
 __host__ __device__ __forceinline__ bool tile_meets_box(const SfGridDev& g, int chunk, int jb,
-                                                        int kb, int by) {
+                                                        int kb) {
+    const int by = g.jspan;
     const int i0 = chunk * g.ich - 1, i1 = chunk * g.ich + g.ich + 1;
     const int j0 = jb * by - 1, j1 = jb * by + by + 1;
     const int k0 = kb * 32 - 1, k1 = kb * 32 + 33;
@@ -234,24 +239,28 @@ __global__ void __launch_bounds__(32 * BY) k_batch_step(const SfGridDev* __restr
                 dst[w] = src[w];
         }
         __syncthreads();
-        if (s < g_sh.n_steps) {
-            if (g_sh.flags != nullptr)
-                batch_column<BY, true, ADEK>(g_sh, s, T.y, T.z, T.w, trial != 0);
-            else
-                batch_column<BY, false, ADEK>(g_sh, s, T.y, T.z, T.w, trial != 0);
+        if (s < g_sh.n_steps) {  // the tile's rows, BY at a time
+            const int j_end = min((T.z + 1) * g_sh.jspan, g_sh.ny);
+#pragma unroll 1
+            for (int j0 = T.z * g_sh.jspan; j0 < j_end; j0 += BY) {
+                if (g_sh.flags != nullptr)
+                    batch_column<BY, true, ADEK>(g_sh, s, T.y, j0, j_end, T.w, trial != 0);
+                else
+                    batch_column<BY, false, ADEK>(g_sh, s, T.y, j0, j_end, T.w, trial != 0);
+            }
         }
         __syncthreads();  // everyone is done with t_sh and g_sh
     }
 }
 
-// Persistent loop over the plain tiles (away from every material box): each
-// warp takes R of the tile's R*W rows and runs them as a scalar warp tile
-// (sf_tile1.cuh: k neighbours by lane shuffles, j neighbours in registers).
-template <int R, int W, bool PF>
-__global__ void __launch_bounds__(32 * W, (PF ? 20 : 24) / W) k_batch_plain(const SfGridDev* __restrict__ grids,
-                                                        const int4* __restrict__ tiles, int n_tiles,
-                                                        int* __restrict__ queue,
-                                                        const long long* __restrict__ step_ptr) {
+// Persistent loop over the plain tiles (away from every material box) as
+// warp tiles (sf_tile.cuh): a grid whose fields allow it runs float4 tiles,
+// 4 rows per warp (a tile is 32 k x 4W rows), any other scalar tiles, 2 rows
+// per warp (32 k x 2W rows).
+template <int W, bool PF>
+__global__ void __launch_bounds__(32 * W, (PF ? 12 : 16) / W) k_batch_plain(
+    const SfGridDev* __restrict__ grids, const int4* __restrict__ tiles, int n_tiles,
+    int* __restrict__ queue, const long long* __restrict__ step_ptr) {
     __shared__ int t_sh;
     __shared__ SfGridDev g_sh;
     const long long s = *step_ptr;
@@ -269,10 +278,11 @@ __global__ void __launch_bounds__(32 * W, (PF ? 20 : 24) / W) k_batch_plain(cons
                 dst[w] = src[w];
         }
         __syncthreads();
-        const int jb = T.z * (R * W) + threadIdx.y * R;
-        if (s < g_sh.n_steps && jb < g_sh.ny) {  // warp-uniform
+        const int rpw = g_sh.vec4 ? 4 : 2;  // rows per warp
+        const int jw = T.z * g_sh.jspan + threadIdx.y * rpw;
+        if (s < g_sh.n_steps && jw < g_sh.ny) {  // warp-uniform
             const int in = (int)((g_sh.cur0 + s) & 1);
-            Tile1Io io;
+            SfTileIo io;
             io.nx = g_sh.nx;
             io.ny = g_sh.ny;
             io.nz = g_sh.nz;
@@ -294,19 +304,21 @@ __global__ void __launch_bounds__(32 * W, (PF ? 20 : 24) / W) k_batch_plain(cons
             io.src_val = g_sh.src_val + s * g_sh.src.n;
             const int i0 = T.y * g_sh.ich;
             const int i1 = min(i0 + g_sh.ich, g_sh.nx);
-            const int k = T.w * 32 + threadIdx.x;
-            if (g_sh.flags != nullptr) tile1_run<true, R, PF>(io, g_sh.src, i0, i1, jb, k);
-            else tile1_run<false, R, PF>(io, g_sh.src, i0, i1, jb, k);
+            const bool geom = g_sh.flags != nullptr;
+            if (g_sh.vec4) {
+                if (geom) tile4_run<true, 1, PF>(io, g_sh.src, i0, i1, jw, T.w * 32);
+                else tile4_run<false, 1, PF>(io, g_sh.src, i0, i1, jw, T.w * 32);
+            } else {
+                const int k = T.w * 32 + threadIdx.x;
+                if (geom) tile1_run<true, 2, PF>(io, g_sh.src, i0, i1, jw, k);
+                else tile1_run<false, 2, PF>(io, g_sh.src, i0, i1, jw, k);
+            }
         }
         __syncthreads();  // everyone is done with t_sh and g_sh
     }
 }
 
-// Scalar-tile shape for a tile height: rows = R * W.
-template <int ROWS> struct PlainShape;
-template <> struct PlainShape<4> { static constexpr int R = 2, W = 2; };
-template <> struct PlainShape<8> { static constexpr int R = 2, W = 4; };
-template <> struct PlainShape<16> { static constexpr int R = 2, W = 8; };
+constexpr int kPlainWarps = 4;  // warps per block of the warp-tile plain kernel
 
 // ADE density poles of every grid that has them, over its material box
 // (ade.cpp:25-68 and 118-170), from the step's input pressure.
@@ -432,12 +444,12 @@ int occupancy_blocks(K kernel, int threads, int* out) {
 
 template <int BY>
 int occupancy_both(sf_batch* B) {
-    using S = PlainShape<BY>;
+    constexpr int W = kPlainWarps;
     int rc = 0;
     if (B->plain_kernel == 1)
-        rc = occupancy_blocks(k_batch_plain<S::R, S::W, false>, 32 * S::W, &B->blocks);
+        rc = occupancy_blocks(k_batch_plain<W, false>, 32 * W, &B->blocks);
     else if (B->plain_kernel == 2)
-        rc = occupancy_blocks(k_batch_plain<S::R, S::W, true>, 32 * S::W, &B->blocks);
+        rc = occupancy_blocks(k_batch_plain<W, true>, 32 * W, &B->blocks);
     else
         rc = occupancy_blocks(k_batch_step<BY, false>, 32 * BY, &B->blocks);
     if (rc) return rc;
@@ -466,6 +478,16 @@ int build(sf_batch* B) {
         g.ny = P->d.ny;
         g.nz = P->d.nz;
         g.ich = chunk_for_grid(B, P);
+        // warp-tile plain kernels: float4 tiles where the fields allow them
+        const long long n_cells = (long long)P->d.nx * P->d.ny * P->d.nz;
+        bool aligned = true;
+        for (int a = 0; a < 2; ++a)
+            for (int f = 0; f < 4; ++f)
+                aligned = aligned && (reinterpret_cast<uintptr_t>(P->f[a][f]) & 15u) == 0;
+        g.vec4 = B->plain_kernel != 0 && P->d.nz % 4 == 0 && aligned &&
+                 (P->flags == nullptr || (reinterpret_cast<uintptr_t>(P->flags) & 3u) == 0) &&
+                 n_cells + 2LL * P->d.ny * P->d.nz + 8 < 0x7fffffffLL;
+        g.jspan = B->plain_kernel == 0 ? B->rows : (g.vec4 ? 4 : 2) * kPlainWarps;
         g.plane = (long long)P->d.ny * P->d.nz;
         g.n_steps = m.steps;
         g.cv = P->d.coeff_v;
@@ -496,12 +518,12 @@ int build(sf_batch* B) {
                                                 (g.ade_hi[1] - g.ade_lo[1]) * (g.ade_hi[2] - g.ade_lo[2]));
         }
         B->max_steps = std::max(B->max_steps, m.steps);
-        const int nch = (g.nx + g.ich - 1) / g.ich, njb = (g.ny + B->rows - 1) / B->rows,
+        const int nch = (g.nx + g.ich - 1) / g.ich, njb = (g.ny + g.jspan - 1) / g.jspan,
                   nkb = (g.nz + 31) / 32;
         for (int ch = 0; ch < nch; ++ch)
             for (int jb = 0; jb < njb; ++jb)
                 for (int kb = 0; kb < nkb; ++kb) {
-                    const bool ade = g.poles.n > 0 && tile_meets_box(g, ch, jb, kb, B->rows);
+                    const bool ade = g.poles.n > 0 && tile_meets_box(g, ch, jb, kb);
                     (ade ? tiles_ade : tiles).push_back(make_int4(gi, ch, jb, kb));
                 }
     }
@@ -536,13 +558,13 @@ int build(sf_batch* B) {
 
 template <int BY>
 void launch_pair(sf_batch* B, cudaStream_t st, int trial) {
-    using S = PlainShape<BY>;
+    constexpr int W = kPlainWarps;
     if (B->n_tiles > 0) {
         if (B->plain_kernel == 1)
-            k_batch_plain<S::R, S::W, false><<<B->blocks, dim3(32, S::W), 0, st>>>(
+            k_batch_plain<W, false><<<B->blocks, dim3(32, W), 0, st>>>(
                 B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step);
         else if (B->plain_kernel == 2)
-            k_batch_plain<S::R, S::W, true><<<B->blocks, dim3(32, S::W), 0, st>>>(
+            k_batch_plain<W, true><<<B->blocks, dim3(32, W), 0, st>>>(
                 B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step);
         else
             k_batch_step<BY, false><<<B->blocks, dim3(32, BY), 0, st>>>(

@@ -64,6 +64,8 @@ struct SfStepArgs {
     const uint8_t* __restrict__ mat;  // ADE material ids (ADE kernels only)
     int reverse;                      // column kernels: dispatch i-chunks high to low
     int ade_lo[3], ade_hi[3];         // box holding every material cell
+    int reg_lo[3], reg_hi[3];         // per-cell kernel: the cells it updates
+    int skip_lo[3], skip_hi[3];       // warp-tile kernels: tile-aligned cells they leave out
 };
 
 #define SF_CUDA_OK(expr)                                                   \

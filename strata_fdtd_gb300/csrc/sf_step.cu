@@ -50,16 +50,16 @@ __device__ __forceinline__ float ade_face(float v, const SfPoles& P, uint8_t m_l
 
 template <bool GEOM, bool ADE>
 __global__ void __launch_bounds__(BX* BY) k_step(SfStepArgs a, SfSources src, SfPoles poles) {
-    const int k = blockIdx.x * BX + threadIdx.x;
-    const int j = blockIdx.y * BY + threadIdx.y;
-    const int i = blockIdx.z;
+    const int k = a.reg_lo[2] + blockIdx.x * BX + threadIdx.x;
+    const int j = a.reg_lo[1] + blockIdx.y * BY + threadIdx.y;
+    const int i = a.reg_lo[0] + blockIdx.z;
 
     // Probe values of the input state are the previous step's samples.
     if (a.trace_prev != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) {
         for (int t = threadIdx.y * BX + threadIdx.x; t < a.n_probe; t += BX * BY)
             a.trace_prev[t] = a.p[a.probe_cells[t]];
     }
-    if (k >= a.nz || j >= a.ny) return;
+    if (k >= a.reg_hi[2] || j >= a.reg_hi[1]) return;
 
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const long long plane = a.plane;
@@ -302,7 +302,12 @@ int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, i
 
 int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& poles, bool geom,
                    cudaStream_t st) {
-    dim3 blk(BX, BY, 1), grd((a.nz + BX - 1) / BX, (a.ny + BY - 1) / BY, a.nx);
+    // the cells of a.reg_lo .. a.reg_hi (the whole grid unless the plan
+    // splits an ADE step between a warp-tile kernel and this one)
+    const int ex = a.reg_hi[0] - a.reg_lo[0], ey = a.reg_hi[1] - a.reg_lo[1],
+              ez = a.reg_hi[2] - a.reg_lo[2];
+    if (ex <= 0 || ey <= 0 || ez <= 0) return 0;
+    dim3 blk(BX, BY, 1), grd((ez + BX - 1) / BX, (ey + BY - 1) / BY, ex);
     const bool ade = poles.n > 0;
     if (ade && poles.n_density > 0) {
         const long long n = (long long)(a.ade_hi[0] - a.ade_lo[0]) * (a.ade_hi[1] - a.ade_lo[1]) *

@@ -175,6 +175,23 @@ ADE_CASES = {
         probes=[("x", (8, 6, 10)), ("y", (16, 13, 18))],
         steps=120, store_fields=True,
     ),
+    "split_boxes_geom": dict(
+        # material boxes small against the grid, with solids: the GPU splits
+        # each step between a warp-tile kernel and the per-cell ADE kernel
+        shape=(70, 45, 76), res=1e-3, courant=0.5, pml=dict(depth=5),
+        geometry=dict(kind="blocks", seed=8, n_boxes=2, n_spheres=1),
+        materials=[
+            dict(id=2, rho=1.3, c=330.0,
+                 poles=[("debye", "density", 0.35, 3e-4), ("debye", "modulus", 0.3, 4e-4)],
+                 box=((29, 41), (13, 27), (33, 47))),
+            dict(id=5, rho=1.1, c=355.0,
+                 poles=[("lorentz", "density", 0.15, 2 * np.pi * 9000.0, 4000.0)],
+                 box=((40, 47), (20, 31), (45, 52))),
+        ],
+        sources=[("point", (20, 22, 38), 15000.0, 1.0), ("point", (50, 30, 60), 11000.0, 0.6)],
+        probes=[("mid", (35, 20, 40)), ("far", (60, 35, 20))],
+        steps=140, store_fields=False,
+    ),
 }
 
 # --------------------------------------------------------------------------

@@ -187,7 +187,8 @@ def python_backend_run(api, name, case, manifest):
         solver._record_probes()
         solver._time += solver.dt
     out = {f"trace__{k}": v for k, v in solver.get_probe_data().items()}
-    out["field__p"] = solver.p
+    if case.get("store_fields"):
+        out["field__p"] = solver.p
     np.savez_compressed(os.path.join(HERE, f"pyade_{name}.npz"), **out)
 
 

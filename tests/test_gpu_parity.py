@@ -82,6 +82,41 @@ def test_ade_cases(name, manifest):
         np.testing.assert_array_equal(s._ade_J_lorentz_prev, g["ade_ade_J_lorentz_prev"])
 
 
+def _check_ade(s, name, manifest):
+    _compare(s, "ade_" + name, manifest)
+    g = golden("ade_" + name)
+    if s._ade_debye:
+        np.testing.assert_array_equal(s._ade_J_debye, g["ade_ade_J_debye"])
+    if s._ade_lorentz:
+        np.testing.assert_array_equal(s._ade_J_lorentz, g["ade_ade_J_lorentz"])
+        np.testing.assert_array_equal(s._ade_J_lorentz_prev, g["ade_ade_J_lorentz_prev"])
+
+
+@pytest.mark.parametrize("config", ["cell"] + [c for c in S.solver.kernel_configs()
+                                               if c.startswith("tile")])
+@pytest.mark.parametrize("name", ["split_boxes_geom", "lorentz_mixed_geom"])
+def test_ade_split_step_every_tile_config(name, config, manifest):
+    """ADE steps split between a warp-tile kernel (outside the material
+    boxes, rounded out to its tiles) and the per-cell ADE kernel (inside):
+    fields, traces and J equal the reference's for every configuration."""
+    case = C.ADE_CASES[name]
+    s = C.build_case(API, case)
+    s.set_kernel(config, 3 if config.startswith("tile1") else 0)
+    s.run_steps(case["steps"] // 2)
+    s.run_steps(case["steps"] - case["steps"] // 2)
+    _check_ade(s, name, manifest)
+
+
+def test_ade_autotune_then_steps(manifest):
+    case = C.ADE_CASES["split_boxes_geom"]
+    s = C.build_case(API, case)
+    s.run_steps(10)
+    table = s.autotune(launches=2)
+    assert table["best"].startswith("tile")
+    s.run_steps(case["steps"] - 10)
+    _check_ade(s, "split_boxes_geom", manifest)
+
+
 def test_c1_quick_start_1000_steps(manifest):
     """The reference quick start, 100^3 x 1000 steps, through run(duration)."""
     case = C.PLAIN_CASES["c1_full"]
