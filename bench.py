@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--solo-cells", type=int, default=1 << 24,
                     help="served stream: solves this large step alone (0 = batch all)")
     ap.add_argument("--batch-solves", type=int, default=64)
+    ap.add_argument("--batch-config", default="auto",
+                    help="batch: auto (autotuned) or kernel:ROWSxICHUNK, e.g. column:16x16")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="batch: skip the sequential baselines (profiling runs)")
     ap.add_argument("--graph-steps", type=int, default=50)
     return ap.parse_args()
 
@@ -370,28 +374,38 @@ def run_batch(args):
     n = args.batch_solves
     seq, steps, info = batch_workload(seed=0, n_solves=n)
     cell_updates = sum(int(np.prod(s.shape)) * q for s, q in zip(seq, steps))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s, q in zip(seq, steps):
-        s.run_steps(q)
-    torch.cuda.synchronize()
-    t_seq = time.perf_counter() - t0
-    traces_seq = [s.get_probe_data() for s in seq]
+    t_seq = t_one = float("nan")
+    traces_seq = None
+    if not args.batch_only:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s, q in zip(seq, steps):
+            s.run_steps(q)
+        torch.cuda.synchronize()
+        t_seq = time.perf_counter() - t0
+        traces_seq = [s.get_probe_data() for s in seq]
     del seq
     torch.cuda.empty_cache()
-    # second baseline: each solve alone through the batch tile kernel (a batch of one)
-    one, _, _ = batch_workload(seed=0, n_solves=n)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s, q in zip(one, steps):
-        BatchedSolver([s]).run_steps(q, graph_steps=args.graph_steps)
-    torch.cuda.synchronize()
-    t_one = time.perf_counter() - t0
-    del one
-    torch.cuda.empty_cache()
+    if not args.batch_only:
+        # second baseline: each solve alone through the batch tile kernel (a batch of one)
+        one, _, _ = batch_workload(seed=0, n_solves=n)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s, q in zip(one, steps):
+            BatchedSolver([s]).run_steps(q, graph_steps=args.graph_steps)
+        torch.cuda.synchronize()
+        t_one = time.perf_counter() - t0
+        del one
+        torch.cuda.empty_cache()
     bat, _, _ = batch_workload(seed=0, n_solves=n)
     b = BatchedSolver(bat)
-    tune = b.autotune(launches=2)
+    if args.batch_config == "auto":
+        tune = b.autotune(launches=2)
+    else:
+        kernel, shape = args.batch_config.split(":")
+        rows, ich = (int(v) for v in shape.split("x"))
+        b.kernel, b.rows, b.i_chunk = kernel, rows, ich
+        tune = {}
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
@@ -401,7 +415,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     t_bat_wall = time.perf_counter() - t0
     t_bat = start.elapsed_time(end) / 1e3
-    same = all(
+    same = traces_seq is not None and all(
         all(np.array_equal(bs.get_probe_data()[k], tr[k]) for k in tr)
         for bs, tr in zip(bat, traces_seq))
     line = {

@@ -235,9 +235,9 @@ int sf_plan_energy_noalloc(sf_plan* plan, double rho, double c, double dx, doubl
 /* --- batches of independent grids ---------------------------------------- */
 /* A batch advances many plans (grids of any sizes, with or without
  * geometry, PML, sources, probes, ADE) together: per time step one
- * persistent launch whose blocks take (grid, i-chunk, row block, column
- * block) tiles from a device work queue, plus the ADE density pass, the
- * probe gather and a step-counter advance.  Results are identical to
+ * persistent launch whose warps take (grid, i-chunk, row block, column
+ * block) work items from a device work queue, plus the ADE density pass,
+ * the probe gather and a step-counter advance.  Results are identical to
  * stepping each plan alone.  No counterpart in the reference (it steps one
  * solver at a time on the CPU). */
 typedef struct sf_batch sf_batch;
@@ -249,17 +249,20 @@ int sf_batch_destroy(sf_batch* batch);
 int sf_batch_add(sf_batch* batch, sf_plan* plan, int64_t n_steps, const double* src_values_dev,
                  float* trace_dev);
 int sf_batch_clear(sf_batch* batch);
-/* Tile shape: rows of 32 columns (4, 8 or 16) and i planes per tile (0 = 16). */
+/* Work-item shape: rows of 32 columns (4, 8 or 16; the thread-column path
+ * only -- warp tiles take 4 rows with float4 lanes, else 2) and i planes per
+ * item (0 = 16).  sf_batch_tiles: the number of items of the last build. */
 int sf_batch_set_tiles(sf_batch* batch, int rows, int i_chunk);
 int sf_batch_tiles(const sf_batch* batch);
-/* Kernel for the tiles away from every material box: 0 thread columns
- * (default), 1 scalar warp tiles (lane-shuffled neighbours), 2 the same with
- * the next plane loaded ahead.  Tiles that meet a material box always run
- * the ADE column kernel. */
+/* Path of the items away from every material box: 0 thread columns
+ * (default), 1 warp tiles (lane-shuffled neighbours; float4 lanes where nz %
+ * 4 == 0 and the fields are 16-byte aligned), 2 the same with the next plane
+ * loaded ahead.  Items that meet a material box always run the ADE column
+ * path. */
 int sf_batch_set_kernel(sf_batch* batch, int kind);
-/* Time the 9 tile shapes (rows 4/8/16 x i_chunk 8/16/32) on the members'
- * current state without changing it and keep the fastest; ms_out[9] may be
- * NULL. */
+/* Time the 9 item shapes (rows 4/8/16 x i_chunk 8/16/32) of the current
+ * path on the members' current state without changing it and keep the
+ * fastest; ms_out[9] may be NULL. */
 int sf_batch_autotune(sf_batch* batch, int launches, void* stream, float* ms_out, int* best_rows,
                       int* best_chunk);
 /* Advance every member by min(its remaining steps, n_steps).  graph_steps >

@@ -2,20 +2,22 @@
 //
 // A batch gathers plans (each a complete single-grid solve: fields, flags,
 // PML, sources, probes, ADE) and advances them with one persistent launch
-// per time step.  Every grid is cut into tiles (i-chunk x BY rows x 32
-// columns); a device-wide work queue (one atomic counter) hands tiles to the
-// resident blocks, so uneven grids load-balance across the SMs.  Each tile
-// is processed as thread columns along i, with the per-cell arithmetic of
-// k_step / k_step_col (and so of the reference passes they restate,
-// including the ADE order of core/solver.py:2135-2193): a grid's result is
-// bit-identical alone or in the batch.
+// per time step.  Every grid is cut into work items (i-chunk x a block of
+// rows x 32 columns); the warps of the persistent kernel claim items one at a
+// time from a device-wide work queue (one atomic counter, no block
+// barriers), so uneven grids load-balance across the SMs.  Items that meet a
+// grid's material box run the ADE column path (the arithmetic and order of
+// core/solver.py:2135-2193 and ade.cpp); the others run the batch's plain
+// path: thread columns or warp tiles (sf_tile.cuh).  Every path is the
+// per-cell arithmetic of k_step, so a grid's result is bit-identical alone
+// or in the batch.
 //
 // Per step the batch enqueues: the ADE density pre-pass over the material
-// boxes (if any grid has density poles), the step kernel, the probe gather,
-// and a one-thread kernel that advances the device step counter and resets
-// the queue.  The kernels read the step number from device memory, so a run
-// of steps can be captured once as a CUDA graph and replayed.  Grids drop out
-// of the queue's work when they reach their own step count.
+// boxes (if any grid has density poles), the persistent kernel, the probe
+// gather, and a one-thread kernel that advances the device step counter and
+// resets the queue.  The kernels read the step number from device memory, so
+// a run of steps can be captured once as a CUDA graph and replayed.  Grids
+// drop out of the work when they reach their own step count.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -60,15 +62,14 @@ __device__ __forceinline__ float ade_face_g(float v, const SfPoles& P, uint8_t m
     return v;
 }
 
-// Rows j0 .. j0+BY-1 (below j_end) of a tile: thread (tx, ty) walks cells
-// (i0..i1-1, j0 + ty, kb*32 + tx) of grid g at step s.
-template <int BY, bool GEOM, bool ADE>
-__device__ void batch_column(const SfGridDev& g, long long s, int chunk, int j0, int j_end, int kb,
+// One row of an item: lane l of the warp walks cells (i0..i1-1, j, kb*32 + l)
+// of grid g at step s, as k_step_col does.
+template <bool GEOM, bool ADE>
+__device__ void batch_column(const SfGridDev& g, long long s, int chunk, int j, int kb,
                              bool trial) {
-    const int k = kb * 32 + threadIdx.x;
-    const int j = j0 + threadIdx.y;
+    const int k = kb * 32 + (threadIdx.x & 31);
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    if (k >= nz || j >= ny || j >= j_end) return;
+    if (k >= nz || j >= ny) return;
     const int i0 = chunk * g.ich;
     const int i1 = min(i0 + g.ich, nx);
     const int in = (int)((g.cur0 + s) & 1);
@@ -214,111 +215,82 @@ __host__ __device__ __forceinline__ bool tile_meets_box(const SfGridDev& g, int 
            k1 > g.ade_lo[2] && k0 < g.ade_hi[2];
 }
 
-// Persistent tile loop.  ADEK selects the tile kind this launch serves:
-// tiles away from every material box (plain), or tiles that meet one.
-template <int BY, bool ADEK>
-__global__ void __launch_bounds__(32 * BY) k_batch_step(const SfGridDev* __restrict__ grids,
-                                                        const int4* __restrict__ tiles, int n_tiles,
-                                                        int* __restrict__ queue,
-                                                        const long long* __restrict__ step_ptr,
-                                                        int trial) {
-    __shared__ int t_sh;
-    __shared__ SfGridDev g_sh;  // the tile's grid descriptor, with its pole table
+// Persistent warp loop over the step's work items (grid, i-chunk, row block,
+// k block).  Every warp claims items on its own -- one atomic per item, no
+// block barrier -- so items of all sizes and kinds balance across the SMs.
+// Items that meet a grid's material box come first in the list and run the
+// ADE column path; the others run the batch's plain path: thread columns
+// (KIND 0) or warp tiles (sf_tile.cuh; KIND 1, and 2 with the next plane
+// loaded ahead), float4 tiles where the grid's fields allow them.  The grid
+// descriptor is read in place (global memory, L1-resident while a warp
+// works through its items).
+template <int W, int MINB, int KIND>
+__global__ void __launch_bounds__(32 * W, MINB) k_batch_warp(
+    const SfGridDev* __restrict__ grids, const int4* __restrict__ items, int n_items, int n_ade,
+    int* __restrict__ queue, const long long* __restrict__ step_ptr, int trial) {
+    constexpr bool PF = KIND == 2;
+    const int lane = threadIdx.x;
     const long long s = *step_ptr;
-    const int tid = threadIdx.y * 32 + threadIdx.x;
     for (;;) {
-        if (tid == 0) t_sh = atomicAdd(queue, 1);
-        __syncthreads();
-        const int t = t_sh;
-        if (t >= n_tiles) return;
-        const int4 T = tiles[t];  // grid, i-chunk, j-block, k-block
-        {   // stage the descriptor in shared memory (word by word)
-            const int* src = reinterpret_cast<const int*>(grids + T.x);
-            int* dst = reinterpret_cast<int*>(&g_sh);
-            for (int w = tid; w < (int)(sizeof(SfGridDev) / sizeof(int)); w += 32 * BY)
-                dst[w] = src[w];
-        }
-        __syncthreads();
-        if (s < g_sh.n_steps) {  // the tile's rows, BY at a time
-            const int j_end = min((T.z + 1) * g_sh.jspan, g_sh.ny);
+        int it = 0;
+        if (lane == 0) it = atomicAdd(queue, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= n_items) return;  // warp-uniform
+        const int4 T = items[it];   // grid, i-chunk, row block, k block
+        const SfGridDev& g = grids[T.x];
+        if (s >= g.n_steps) continue;
+        const bool geom = g.flags != nullptr;
+        const int j0 = T.z * g.jspan;
+        if (it < n_ade || KIND == 0) {
+            const int j_end = min(j0 + g.jspan, g.ny);
+            const bool ade = it < n_ade;
 #pragma unroll 1
-            for (int j0 = T.z * g_sh.jspan; j0 < j_end; j0 += BY) {
-                if (g_sh.flags != nullptr)
-                    batch_column<BY, true, ADEK>(g_sh, s, T.y, j0, j_end, T.w, trial != 0);
-                else
-                    batch_column<BY, false, ADEK>(g_sh, s, T.y, j0, j_end, T.w, trial != 0);
+            for (int j = j0; j < j_end; ++j) {
+                if (geom) {
+                    if (ade) batch_column<true, true>(g, s, T.y, j, T.w, trial != 0);
+                    else batch_column<true, false>(g, s, T.y, j, T.w, trial != 0);
+                } else {
+                    if (ade) batch_column<false, true>(g, s, T.y, j, T.w, trial != 0);
+                    else batch_column<false, false>(g, s, T.y, j, T.w, trial != 0);
+                }
             }
+            continue;
         }
-        __syncthreads();  // everyone is done with t_sh and g_sh
+        const int in = (int)((g.cur0 + s) & 1);
+        SfTileIo io;
+        io.nx = g.nx;
+        io.ny = g.ny;
+        io.nz = g.nz;
+        io.plane = g.plane;
+        io.cv = g.cv;
+        io.cp = g.cp;
+        io.p = g.f[in][0];
+        io.vx = g.f[in][1];
+        io.vy = g.f[in][2];
+        io.vz = g.f[in][3];
+        io.po = g.f[1 - in][0];
+        io.vxo = g.f[1 - in][1];
+        io.vyo = g.f[1 - in][2];
+        io.vzo = g.f[1 - in][3];
+        io.flags = g.flags;
+        io.dx = g.dx;
+        io.dy = g.dy;
+        io.dz = g.dz;
+        io.src_val = g.src_val + s * g.src.n;
+        const int i0 = T.y * g.ich;
+        const int i1 = min(i0 + g.ich, g.nx);
+        if (g.vec4) {
+            if (geom) tile4_run<true, 1, PF>(io, g.src, i0, i1, j0, T.w * 32);
+            else tile4_run<false, 1, PF>(io, g.src, i0, i1, j0, T.w * 32);
+        } else {
+            const int k = T.w * 32 + lane;
+            if (geom) tile1_run<true, 2, PF>(io, g.src, i0, i1, j0, k);
+            else tile1_run<false, 2, PF>(io, g.src, i0, i1, j0, k);
+        }
     }
 }
 
-// Persistent loop over the plain tiles (away from every material box) as
-// warp tiles (sf_tile.cuh): a grid whose fields allow it runs float4 tiles,
-// 4 rows per warp (a tile is 32 k x 4W rows), any other scalar tiles, 2 rows
-// per warp (32 k x 2W rows).
-template <int W, bool PF>
-__global__ void __launch_bounds__(32 * W, (PF ? 12 : 16) / W) k_batch_plain(
-    const SfGridDev* __restrict__ grids, const int4* __restrict__ tiles, int n_tiles,
-    int* __restrict__ queue, const long long* __restrict__ step_ptr) {
-    __shared__ int t_sh;
-    __shared__ SfGridDev g_sh;
-    const long long s = *step_ptr;
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    for (;;) {
-        if (tid == 0) t_sh = atomicAdd(queue, 1);
-        __syncthreads();
-        const int t = t_sh;
-        if (t >= n_tiles) return;
-        const int4 T = tiles[t];  // grid, i-chunk, j-block, k-block
-        {
-            const int* src = reinterpret_cast<const int*>(grids + T.x);
-            int* dst = reinterpret_cast<int*>(&g_sh);
-            for (int w = tid; w < (int)(sizeof(SfGridDev) / sizeof(int)); w += 32 * W)
-                dst[w] = src[w];
-        }
-        __syncthreads();
-        const int rpw = g_sh.vec4 ? 4 : 2;  // rows per warp
-        const int jw = T.z * g_sh.jspan + threadIdx.y * rpw;
-        if (s < g_sh.n_steps && jw < g_sh.ny) {  // warp-uniform
-            const int in = (int)((g_sh.cur0 + s) & 1);
-            SfTileIo io;
-            io.nx = g_sh.nx;
-            io.ny = g_sh.ny;
-            io.nz = g_sh.nz;
-            io.plane = g_sh.plane;
-            io.cv = g_sh.cv;
-            io.cp = g_sh.cp;
-            io.p = g_sh.f[in][0];
-            io.vx = g_sh.f[in][1];
-            io.vy = g_sh.f[in][2];
-            io.vz = g_sh.f[in][3];
-            io.po = g_sh.f[1 - in][0];
-            io.vxo = g_sh.f[1 - in][1];
-            io.vyo = g_sh.f[1 - in][2];
-            io.vzo = g_sh.f[1 - in][3];
-            io.flags = g_sh.flags;
-            io.dx = g_sh.dx;
-            io.dy = g_sh.dy;
-            io.dz = g_sh.dz;
-            io.src_val = g_sh.src_val + s * g_sh.src.n;
-            const int i0 = T.y * g_sh.ich;
-            const int i1 = min(i0 + g_sh.ich, g_sh.nx);
-            const bool geom = g_sh.flags != nullptr;
-            if (g_sh.vec4) {
-                if (geom) tile4_run<true, 1, PF>(io, g_sh.src, i0, i1, jw, T.w * 32);
-                else tile4_run<false, 1, PF>(io, g_sh.src, i0, i1, jw, T.w * 32);
-            } else {
-                const int k = T.w * 32 + threadIdx.x;
-                if (geom) tile1_run<true, 2, PF>(io, g_sh.src, i0, i1, jw, k);
-                else tile1_run<false, 2, PF>(io, g_sh.src, i0, i1, jw, k);
-            }
-        }
-        __syncthreads();  // everyone is done with t_sh and g_sh
-    }
-}
-
-constexpr int kPlainWarps = 4;  // warps per block of the warp-tile plain kernel
+constexpr int kBatchWarps = 4;  // warps per block of the persistent kernel
 
 // ADE density poles of every grid that has them, over its material box
 // (ade.cpp:25-68 and 118-170), from the step's input pressure.
@@ -384,21 +356,20 @@ struct sf_batch {
     };
     std::vector<Member> members;
     int rows = 8;
-    int plain_kernel = 0;  // plain tiles: 0 thread columns, 1 warp tiles, 2 warp tiles + prefetch
+    int plain_kernel = 0;  // plain items: 0 thread columns, 1 warp tiles, 2 warp tiles + prefetch
     int i_chunk = 0;
     int device = 0;
     bool built = false;
     SfGridDev* d_grids = nullptr;
-    int4* d_tiles = nullptr;  // plain tiles, then ADE tiles
-    int n_tiles = 0;          // plain tiles
-    int n_tiles_ade = 0;      // tiles that meet a material box
+    int4* d_tiles = nullptr;  // work items: those meeting a material box first
+    int n_tiles = 0;          // all work items
+    int n_tiles_ade = 0;      // items that meet a material box
     int* d_ade_ids = nullptr;
     int n_ade = 0;
     int ade_blocks = 1;
-    int* d_queue = nullptr;   // [0] plain queue head, [1] ADE queue head
+    int* d_queue = nullptr;   // [0] work-queue head ([1] spare)
     long long* d_step = nullptr;
-    int blocks = 0;      // persistent grid size, plain kernel
-    int blocks_ade = 0;  // persistent grid size, ADE kernel
+    int blocks = 0;      // persistent grid size
     long long max_steps = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -442,18 +413,17 @@ int occupancy_blocks(K kernel, int threads, int* out) {
     return 0;
 }
 
-template <int BY>
-int occupancy_both(sf_batch* B) {
-    constexpr int W = kPlainWarps;
-    int rc = 0;
+// Resident blocks of 4 warps asked of the compiler: 6 caps registers at 85
+// per thread (24 warps per SM).
+constexpr int kMinBlocksColumn = 6, kMinBlocksTile = 6;
+
+int occupancy_warp(sf_batch* B) {
+    constexpr int W = kBatchWarps;
     if (B->plain_kernel == 1)
-        rc = occupancy_blocks(k_batch_plain<W, false>, 32 * W, &B->blocks);
-    else if (B->plain_kernel == 2)
-        rc = occupancy_blocks(k_batch_plain<W, true>, 32 * W, &B->blocks);
-    else
-        rc = occupancy_blocks(k_batch_step<BY, false>, 32 * BY, &B->blocks);
-    if (rc) return rc;
-    return occupancy_blocks(k_batch_step<BY, true>, 32 * BY, &B->blocks_ade);
+        return occupancy_blocks(k_batch_warp<W, kMinBlocksTile, 1>, 32 * W, &B->blocks);
+    if (B->plain_kernel == 2)
+        return occupancy_blocks(k_batch_warp<W, kMinBlocksTile, 2>, 32 * W, &B->blocks);
+    return occupancy_blocks(k_batch_warp<W, kMinBlocksColumn, 0>, 32 * W, &B->blocks);
 }
 
 int build(sf_batch* B) {
@@ -487,7 +457,7 @@ int build(sf_batch* B) {
         g.vec4 = B->plain_kernel != 0 && P->d.nz % 4 == 0 && aligned &&
                  (P->flags == nullptr || (reinterpret_cast<uintptr_t>(P->flags) & 3u) == 0) &&
                  n_cells + 2LL * P->d.ny * P->d.nz + 8 < 0x7fffffffLL;
-        g.jspan = B->plain_kernel == 0 ? B->rows : (g.vec4 ? 4 : 2) * kPlainWarps;
+        g.jspan = B->plain_kernel == 0 ? B->rows : (g.vec4 ? 4 : 2);  // rows per item
         g.plane = (long long)P->d.ny * P->d.nz;
         g.n_steps = m.steps;
         g.cv = P->d.coeff_v;
@@ -528,9 +498,12 @@ int build(sf_batch* B) {
                 }
     }
     if (tiles.size() + tiles_ade.size() > 0x7fffffff) return sf_fail("sf_batch: too many tiles");
-    B->n_tiles = (int)tiles.size();
+    // items meeting a material box first: they are the slowest, so they
+    // start early and the step ends on short plain items
     B->n_tiles_ade = (int)tiles_ade.size();
-    tiles.insert(tiles.end(), tiles_ade.begin(), tiles_ade.end());
+    tiles_ade.insert(tiles_ade.end(), tiles.begin(), tiles.end());
+    tiles.swap(tiles_ade);
+    B->n_tiles = (int)tiles.size();
     B->n_ade = (int)ade_ids.size();
     B->ade_blocks = (int)std::min<long long>(std::max<long long>(1, (ade_cells + 255) / 256), 512);
     SF_CUDA_OK(cudaMalloc(&B->d_grids, sizeof(SfGridDev) * grids.size()));
@@ -545,43 +518,25 @@ int build(sf_batch* B) {
     }
     SF_CUDA_OK(cudaMalloc(&B->d_queue, 2 * sizeof(int)));
     SF_CUDA_OK(cudaMalloc(&B->d_step, sizeof(long long)));
-    int rc = 0;
-    switch (B->rows) {
-        case 4: rc = occupancy_both<4>(B); break;
-        case 16: rc = occupancy_both<16>(B); break;
-        default: rc = occupancy_both<8>(B); break;
-    }
-    if (rc) return rc;
+    if (int rc = occupancy_warp(B)) return rc;
     B->built = true;
     return 0;
 }
 
-template <int BY>
-void launch_pair(sf_batch* B, cudaStream_t st, int trial) {
-    constexpr int W = kPlainWarps;
-    if (B->n_tiles > 0) {
-        if (B->plain_kernel == 1)
-            k_batch_plain<W, false><<<B->blocks, dim3(32, W), 0, st>>>(
-                B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step);
-        else if (B->plain_kernel == 2)
-            k_batch_plain<W, true><<<B->blocks, dim3(32, W), 0, st>>>(
-                B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step);
-        else
-            k_batch_step<BY, false><<<B->blocks, dim3(32, BY), 0, st>>>(
-                B->d_grids, B->d_tiles, B->n_tiles, B->d_queue, B->d_step, trial);
-    }
-    if (B->n_tiles_ade > 0)
-        k_batch_step<BY, true><<<B->blocks_ade, dim3(32, BY), 0, st>>>(
-            B->d_grids, B->d_tiles + B->n_tiles, B->n_tiles_ade, B->d_queue + 1, B->d_step, trial);
-}
-
 int launch_step_kernel(sf_batch* B, cudaStream_t st, int trial) {
-    switch (B->rows) {
-        case 4: launch_pair<4>(B, st, trial); break;
-        case 16: launch_pair<16>(B, st, trial); break;
-        default: launch_pair<8>(B, st, trial);
-    }
-    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_batch_step launch failed");
+    constexpr int W = kBatchWarps;
+    if (B->n_tiles == 0) return 0;
+    const dim3 blk(32, W);
+    if (B->plain_kernel == 1)
+        k_batch_warp<W, kMinBlocksTile, 1><<<B->blocks, blk, 0, st>>>(
+            B->d_grids, B->d_tiles, B->n_tiles, B->n_tiles_ade, B->d_queue, B->d_step, trial);
+    else if (B->plain_kernel == 2)
+        k_batch_warp<W, kMinBlocksTile, 2><<<B->blocks, blk, 0, st>>>(
+            B->d_grids, B->d_tiles, B->n_tiles, B->n_tiles_ade, B->d_queue, B->d_step, trial);
+    else
+        k_batch_warp<W, kMinBlocksColumn, 0><<<B->blocks, blk, 0, st>>>(
+            B->d_grids, B->d_tiles, B->n_tiles, B->n_tiles_ade, B->d_queue, B->d_step, trial);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_batch_warp launch failed");
 }
 
 // One batch step: ADE density pass, step, probes, advance.
@@ -646,7 +601,7 @@ int sf_batch_set_tiles(sf_batch* B, int rows, int i_chunk) {
     return 0;
 }
 
-int sf_batch_tiles(const sf_batch* B) { return B ? B->n_tiles + B->n_tiles_ade : -1; }
+int sf_batch_tiles(const sf_batch* B) { return B ? B->n_tiles : -1; }
 
 int sf_batch_set_kernel(sf_batch* B, int kind) {
     if (!B) return sf_fail("sf_batch_set_kernel: NULL batch");
