@@ -254,10 +254,10 @@ int sf_batch_clear(sf_batch* batch);
  * item (0 = 16).  sf_batch_tiles: the number of items of the last build. */
 int sf_batch_set_tiles(sf_batch* batch, int rows, int i_chunk);
 int sf_batch_tiles(const sf_batch* batch);
-/* Path of the items away from every material box: 0 thread columns
- * (default), 1 warp tiles (lane-shuffled neighbours; float4 lanes where nz %
- * 4 == 0 and the fields are 16-byte aligned), 2 the same with the next plane
- * loaded ahead.  Items that meet a material box always run the ADE column
+/* Path of the items away from every material box: 0 thread columns, 1
+ * warp tiles (lane-shuffled neighbours; float4 lanes where nz % 4 == 0 and
+ * the fields are 16-byte aligned), 2 (default) the same with the next plane
+ * loaded ahead, 3 as 2 with a 64-register cap (more resident warps).  Items that meet a material box always run the ADE column
  * path. */
 int sf_batch_set_kernel(sf_batch* batch, int kind);
 /* Time the 9 item shapes (rows 4/8/16 x i_chunk 8/16/32) of the current

@@ -18,7 +18,7 @@ import numpy as np
 from . import _native
 
 
-PLAIN_KERNELS = ("column", "warp", "warp_prefetch")
+PLAIN_KERNELS = ("column", "warp", "warp_prefetch", "warp_prefetch_m8")
 
 
 class BatchedSolver:
@@ -27,7 +27,7 @@ class BatchedSolver:
     PLAIN_KERNELS) the kernel of the tiles away from material boxes;
     :meth:`autotune` picks all three."""
 
-    def __init__(self, solvers, rows: int = 8, i_chunk: int = 0, kernel: str = "column"):
+    def __init__(self, solvers, rows: int = 8, i_chunk: int = 0, kernel: str = "warp_prefetch"):
         if not solvers:
             raise ValueError("BatchedSolver needs at least one solver")
         if any(s._microphones for s in solvers):

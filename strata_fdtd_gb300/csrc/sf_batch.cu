@@ -221,14 +221,15 @@ __host__ __device__ __forceinline__ bool tile_meets_box(const SfGridDev& g, int 
 // Items that meet a grid's material box come first in the list and run the
 // ADE column path; the others run the batch's plain path: thread columns
 // (KIND 0) or warp tiles (sf_tile.cuh; KIND 1, and 2 with the next plane
-// loaded ahead), float4 tiles where the grid's fields allow them.  The grid
+// loaded ahead; 3 the same with fewer registers and more resident warps),
+// float4 tiles where the grid's fields allow them.  The grid
 // descriptor is read in place (global memory, L1-resident while a warp
 // works through its items).
 template <int W, int MINB, int KIND>
 __global__ void __launch_bounds__(32 * W, MINB) k_batch_warp(
     const SfGridDev* __restrict__ grids, const int4* __restrict__ items, int n_items, int n_ade,
     int* __restrict__ queue, const long long* __restrict__ step_ptr, int trial) {
-    constexpr bool PF = KIND == 2;
+    constexpr bool PF = KIND >= 2;
     const int lane = threadIdx.x;
     const long long s = *step_ptr;
     for (;;) {
@@ -356,7 +357,7 @@ struct sf_batch {
     };
     std::vector<Member> members;
     int rows = 8;
-    int plain_kernel = 0;  // plain items: 0 thread columns, 1 warp tiles, 2 warp tiles + prefetch
+    int plain_kernel = 2;  // plain items: 0 thread columns, 1 warp tiles, 2 warp tiles + prefetch
     int i_chunk = 0;
     int device = 0;
     bool built = false;
@@ -414,8 +415,8 @@ int occupancy_blocks(K kernel, int threads, int* out) {
 }
 
 // Resident blocks of 4 warps asked of the compiler: 6 caps registers at 85
-// per thread (24 warps per SM).
-constexpr int kMinBlocksColumn = 6, kMinBlocksTile = 6;
+// per thread (24 warps per SM), 8 at 64 (32 warps).
+constexpr int kMinBlocksColumn = 6, kMinBlocksTile = 6, kMinBlocksLean = 8;
 
 int occupancy_warp(sf_batch* B) {
     constexpr int W = kBatchWarps;
@@ -423,6 +424,8 @@ int occupancy_warp(sf_batch* B) {
         return occupancy_blocks(k_batch_warp<W, kMinBlocksTile, 1>, 32 * W, &B->blocks);
     if (B->plain_kernel == 2)
         return occupancy_blocks(k_batch_warp<W, kMinBlocksTile, 2>, 32 * W, &B->blocks);
+    if (B->plain_kernel == 3)
+        return occupancy_blocks(k_batch_warp<W, kMinBlocksLean, 3>, 32 * W, &B->blocks);
     return occupancy_blocks(k_batch_warp<W, kMinBlocksColumn, 0>, 32 * W, &B->blocks);
 }
 
@@ -533,6 +536,9 @@ int launch_step_kernel(sf_batch* B, cudaStream_t st, int trial) {
     else if (B->plain_kernel == 2)
         k_batch_warp<W, kMinBlocksTile, 2><<<B->blocks, blk, 0, st>>>(
             B->d_grids, B->d_tiles, B->n_tiles, B->n_tiles_ade, B->d_queue, B->d_step, trial);
+    else if (B->plain_kernel == 3)
+        k_batch_warp<W, kMinBlocksLean, 3><<<B->blocks, blk, 0, st>>>(
+            B->d_grids, B->d_tiles, B->n_tiles, B->n_tiles_ade, B->d_queue, B->d_step, trial);
     else
         k_batch_warp<W, kMinBlocksColumn, 0><<<B->blocks, blk, 0, st>>>(
             B->d_grids, B->d_tiles, B->n_tiles, B->n_tiles_ade, B->d_queue, B->d_step, trial);
@@ -605,7 +611,7 @@ int sf_batch_tiles(const sf_batch* B) { return B ? B->n_tiles : -1; }
 
 int sf_batch_set_kernel(sf_batch* B, int kind) {
     if (!B) return sf_fail("sf_batch_set_kernel: NULL batch");
-    if (kind < 0 || kind > 2) return sf_fail("sf_batch_set_kernel: kind must be 0, 1 or 2");
+    if (kind < 0 || kind > 3) return sf_fail("sf_batch_set_kernel: kind must be 0 .. 3");
     B->plain_kernel = kind;
     B->built = false;
     return 0;

@@ -54,7 +54,7 @@ def test_batch_matches_reference_goldens(graph_steps, manifest):
             np.testing.assert_array_equal(s._ade_J_debye, g["ade_ade_J_debye"])
 
 
-@pytest.mark.parametrize("kernel", ["column", "warp", "warp_prefetch"])
+@pytest.mark.parametrize("kernel", ["column", "warp", "warp_prefetch", "warp_prefetch_m8"])
 @pytest.mark.parametrize("rows,i_chunk", [(4, 8), (16, 32), (8, 0), (8, 3)])
 def test_batch_equals_alone_in_two_runs(rows, i_chunk, kernel):
     """Members run in two batched runs (continuing state) equal the solves run
@@ -84,7 +84,7 @@ def test_batch_autotune_leaves_state_unchanged():
     BatchedSolver(b).run_steps(20)
     bs = BatchedSolver(a)
     table = bs.autotune(launches=2)
-    assert table["best"][0] in ("column", "warp", "warp_prefetch")
+    assert table["best"][0] in S.batch.PLAIN_KERNELS
     assert table["best"][1] in (4, 8, 16)
     bs.run_steps(30)
     BatchedSolver(b).run_steps(30)
