@@ -81,6 +81,23 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The slowest rank's time: every rank's replica must finish."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, cell_updates_per_rank: int, seconds: float) -> float:
+    """Whole-job Gcell-updates/s of `world` replicas that each did the same
+    work in (at most) `seconds`: weak scaling, no collective on the data path."""
+    return world * cell_updates_per_rank / seconds / 1e9
+
+
 def profiled_traffic():
     """DRAM bytes per launch of the step kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_step_enclosure_400.md")
@@ -287,13 +304,9 @@ def run_gpu(args):
     end.record(stream)
     barrier()
     clk = clocks.stop()
-    ms = start.elapsed_time(end)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(start.elapsed_time(end), dist, "cuda")
     launches = K * (inner + 1)
-    value = world * cells * inner * K / (ms / 1e3) / 1e9
+    value = replica_rate(world, cells * inner * K, ms / 1e3)
     kernel_ms = ms / (K * inner)  # every timed launch attributed to the step kernel
     hbm, peak_kind = peaks()
     achieved = BYTES_PER_CELL * cells / (kernel_ms / 1e3) / 1e9
@@ -318,12 +331,8 @@ def run_gpu(args):
             _ = s.p
             _ = s.get_probe_data()
         torch.cuda.synchronize()
-        el = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([el], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
-        e2e = {"value": world * cells * inner * Ke / el / 1e9, "unit": METRIC,
+        el = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+        e2e = {"value": replica_rate(world, cells * inner * Ke, el), "unit": METRIC,
                "h2d_bytes_per_step": 4 * cells * 4 + inner * n_src * 8,
                "d2h_bytes_per_step": cells * 4 + inner * n_probe * 4,
                "steps": Ke, "path": "FDTDSolver fields assigned from pinned host arrays, "

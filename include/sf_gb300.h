@@ -191,8 +191,10 @@ const char* sf_kernel_config_name(int config);
 /* Autotuner: times every configuration that fits the grid for `launches`
  * step launches each (reading the current state and writing the other set
  * without swapping, no sources, no probes -- the state is unchanged) and
- * makes the fastest the plan's automatic choice; with ADE poles only the
- * warp-tile configurations, timed outside their ADE region.  ms_out (host, may be NULL)
+ * makes the fastest the plan's automatic choice, then times that one with
+ * 8-48 planes per block (unless sf_plan_set_kernel fixed i_chunk) and keeps
+ * the fastest chunk; with ADE poles only the warp-tile configurations, timed
+ * outside their ADE region.  ms_out (host, may be NULL)
  * receives sf_kernel_config_count() per-launch times (-1 = not run);
  * best_out (may be NULL) the chosen configuration.  Synchronises the stream.
  * No counterpart in the reference. */

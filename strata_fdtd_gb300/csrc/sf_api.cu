@@ -377,6 +377,7 @@ void ade_region(const sf_plan* P, int cfg, int ich, int lo[3], int hi[3]) {
 
 int chunk_for(const sf_plan* P, int cfg) {
     if (P->i_chunk > 0) return P->i_chunk;
+    if (cfg == P->tuned && P->tuned_ich > 0) return P->tuned_ich;
     if (cfg >= SF_CFG_TILE_FIRST) {
         const SfTileConfig& t = kSfTileConfigs[cfg - SF_CFG_TILE_FIRST];
         if (t.vec == 1) return auto_chunk(P, 32, t.rows * t.warps);
@@ -528,6 +529,7 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     // is timed on the cells outside its ADE region (the per-cell kernel's
     // share inside it is the same for all of them).
     const bool ade = P->poles.n > 0;
+    P->tuned_ich = 0;
     // Every trial reads the current set and writes the other one without
     // swapping, with no sources and no probes: the state is untouched, and the
     // next real step overwrites the other set entirely.
@@ -562,6 +564,33 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
             best = cfg;
             best_ms = ms;
         }
+    }
+    // then the planes per block of the winner (unless the caller fixed them)
+    if (!rc && best >= SF_CFG_COL_FIRST && P->i_chunk == 0) {
+        const int auto_ich = chunk_for(P, best);
+        int best_ich = auto_ich;
+        const int cand[] = {8, 12, 16, 20, 24, 32, 48};
+        for (int ich : cand) {
+            if (ich == auto_ich || ich > P->d.nx || rc) continue;
+            SfStepArgs t = a;
+            if (ade) ade_region(P, best, ich, t.skip_lo, t.skip_hi);
+            if ((rc = launch_config(P, best, ich, t, none, st))) break;
+            if (cudaEventRecord(e0, st) != cudaSuccess) { rc = sf_fail("event record failed"); break; }
+            for (int q = 0; q < launches && !rc; ++q) rc = launch_config(P, best, ich, t, none, st);
+            if (rc) break;
+            if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = sf_fail("sf_plan_autotune: timing failed");
+                break;
+            }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= launches;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_ich = ich;
+            }
+        }
+        if (!rc && best_ich != auto_ich) P->tuned_ich = best_ich;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -22,6 +22,7 @@ struct sf_plan {
     int variant = 0;               // kernel configuration (SF_CFG_*), 0 = auto
     int i_chunk = 0;               // planes per block in march / column kernels (0 = auto)
     int tuned = 0;                 // configuration chosen by sf_plan_autotune (0 = none)
+    int tuned_ich = 0;             // its planes per block, when the autotuner chose them
     long long steps_done = 0;      // steps issued so far (alternates the chunk order)
     int n_mic = 0;                 // microphone rows: 8 corner cells and weights each
     long long* mic_idx = nullptr;  // owned
