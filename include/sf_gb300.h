@@ -32,6 +32,7 @@ extern "C" {
 #define SF_ABI_VERSION 1
 #define SF_MAX_SOURCES 16
 #define SF_MAX_POLES 16
+#define SF_MAX_PLANE_OPS 8
 
 typedef struct sf_plan sf_plan;
 
@@ -83,6 +84,19 @@ typedef struct {
     double a[3], b[3];
     double s0, s1;
 } sf_sdf_node;
+
+/* Pressure-plane boundary operation, applied after the PML in list order
+ * (the reference's boundary loop, core/solver.py:2040-2047).  kind 0 = Mur
+ * first-order ABC on both ends of `axis` (_boundaries.py:420-527): p_b =
+ * float(double(prev) + coeff * double(p_i - p_b)), prev = p_i, low end then
+ * high end; kind 1 = radiation impedance on one end (side 0 low, 1 high;
+ * _boundaries.py:529-793): p_b = float(double(float(R) * p_i) + (1 - R) *
+ * (double(prev) + coeff * double(p_i - p_b))), prev = p_i.  coeff is the
+ * Mur coefficient (c dt - dx)/(c dt + dx) in FP64, R the reflection. */
+typedef struct {
+    int32_t kind, axis, side, reserved;
+    double coeff, reflection;
+} sf_plane_bc;
 
 typedef struct {
     int32_t device, sm_count, cc_major, cc_minor;
@@ -162,6 +176,26 @@ int sf_plan_set_microphones_ex(sf_plan* plan, int n, const int32_t* field, const
  * core/solver.py:2135-2193. n = 0 turns ADE off. */
 int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const sf_pole* poles,
                     float inv_dx);
+
+/* Nonuniform grid (core/grid.py:148-532; replaces create_nonuniform_grid_data
+ * and update_velocity/pressure_nonuniform, fdtd_step.cpp:235-456).
+ * cv_face[a]: n_a floats, cv_face[a][i] = float(coeff_v_base) *
+ * inv_face[a][i] formed in float by the caller (the last entry is unused);
+ * inv_cell[a]: n_a cell inverse spacings.  The grid descriptor's coeff_p is
+ * then coeff_p_base = -rho c^2 dt and coeff_v is unused: the velocity update
+ * is v += cv_face[i] * (p[i+1] - p[i]) and the pressure update p +=
+ * coeff_p_base * ((inv_x (dvx) + inv_y (dvy)) + inv_z (dvz)), each term
+ * scaled before the sum.  Steps run the warp-tile kernels; no ADE.  Both
+ * NULL returns the plan to a uniform grid. */
+int sf_plan_set_nonuniform(sf_plan* plan, const float* const* cv_face, const float* const* inv_cell);
+
+/* Plane boundary operations (at most SF_MAX_PLANE_OPS; n = 0 removes them)
+ * and their stored planes, zeroed.  With any of them a step runs: the fused
+ * update with the PML, the operations in order, then the sources, as the
+ * reference's step does (core/solver.py:2040-2052).  Each axis an
+ * operation touches needs at least 2 cells.  Replaces ABCFirstOrder /
+ * RadiationImpedance.apply_pressure. */
+int sf_plan_set_plane_boundaries(sf_plan* plan, int n, const sf_plane_bc* ops);
 
 /* Box [lo, hi) holding every cell with a nonzero material id; the
  * density-pole pass walks only this box, and an ADE step on a warp-tile
@@ -319,6 +353,10 @@ int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* gr
  * complement (air = outside a solid).  out_dev: nx*ny*nz bytes. */
 int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, double res,
                 int invert, uint8_t* out_dev, void* stream);
+/* Same at the cell centres of a nonuniform grid: coords[3] host arrays of
+ * nx, ny, nz doubles (NonuniformGrid.x/y/z_coords, core/grid.py:148-532). */
+int sf_voxelize_coords(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz,
+                       const double* const* coords, int invert, uint8_t* out_dev, void* stream);
 
 /* Signed distance of the same program at n points (device doubles, n x 3,
  * row major) into out_dev[n]; replaces SDFPrimitive.sdf

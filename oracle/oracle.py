@@ -49,6 +49,8 @@ def _declare(L):
         sig = {
             "update_velocity": [P, P, P, P, I, I, I, R],
             "update_pressure": [P, P, P, P, P, I, I, I, R],
+            "update_velocity_nu": [P, P, P, P, I, I, I, R, P, P, P],
+            "update_pressure_nu": [P, P, P, P, P, I, I, I, R, P, P, P],
             "apply_rigid": [P, P, P, P, I, I, I],
             "boundary_faces": [P, I, I, I, I, P],
             "pml_decay": [P, I, R, P],
@@ -110,6 +112,80 @@ class UniformGrid:
         self.z_coords = np.arange(self.shape[2]) * r + r / 2
         self.min_spacing = r
         self.is_uniform = True
+
+
+class NonuniformGrid:
+    """core/grid.py:148-532: cell centres per axis, spacing (x[i+1]-x[i-1])/2
+    inside and the neighbour distance at the ends, from_stretch and
+    from_regions coordinate generators, float32 inverse spacings."""
+
+    def __init__(self, x_coords, y_coords, z_coords):
+        self.x_coords, self.y_coords, self.z_coords = (
+            np.asarray(c, dtype=np.float64).ravel() for c in (x_coords, y_coords, z_coords))
+        self.dx, self.dy, self.dz = (self._spacing(c) for c in
+                                     (self.x_coords, self.y_coords, self.z_coords))
+        self.shape = (len(self.x_coords), len(self.y_coords), len(self.z_coords))
+        self.min_spacing = float(min(np.min(self.dx), np.min(self.dy), np.min(self.dz)))
+        self.is_uniform = False
+
+    @staticmethod
+    def _spacing(c):
+        s = np.zeros(len(c), dtype=np.float64)
+        for i in range(1, len(c) - 1):
+            s[i] = (c[i + 1] - c[i - 1]) / 2
+        s[0] = c[1] - c[0]
+        s[-1] = c[-1] - c[-2]
+        return s
+
+    @classmethod
+    def from_stretch(cls, shape, base_resolution, stretch_x=1.0, stretch_y=1.0, stretch_z=1.0,
+                     center_fine=True):
+        return cls(*(cls._stretched(n, base_resolution, st, center_fine)
+                     for n, st in zip(shape, (stretch_x, stretch_y, stretch_z))))
+
+    @staticmethod
+    def _stretched(n, b, st, center_fine):
+        if st == 1.0:
+            return np.arange(n, dtype=np.float64) * b + b / 2
+        if not center_fine:
+            sizes = b * (st ** np.arange(n, dtype=np.float64))
+            return np.cumsum(sizes) - sizes / 2
+        h = n // 2
+        sizes = b * (st ** np.arange(h, dtype=np.float64))
+        pos = np.cumsum(sizes) - sizes[0] / 2
+        left = -pos[::-1] - sizes[::-1] / 2
+        if n % 2 == 0:
+            coords = np.concatenate([left, pos + sizes / 2])
+        else:
+            right = pos[1:] + sizes[1:] / 2 if h > 0 else np.array([])
+            coords = np.concatenate([left, np.array([0.0]), right])
+        return coords - coords[0] + b / 2
+
+    @classmethod
+    def from_regions(cls, x_regions, y_regions=None, z_regions=None):
+        return cls(*(cls._regions(r) for r in (x_regions, y_regions or x_regions,
+                                                z_regions or x_regions)))
+
+    @staticmethod
+    def _regions(regions):
+        out = []
+        for start, end, res in regions:
+            n = max(1, int(round((end - start) / res)))
+            step = (end - start) / n
+            rc = start + (np.arange(n) + 0.5) * step
+            if out and len(rc) > 0 and abs(rc[0] - out[-1]) < step / 2:
+                rc = rc[1:]
+            out.extend(rc.tolist())
+        return np.array(out, dtype=np.float64)
+
+    def get_spacing_arrays_for_stencil(self):
+        f = np.float32
+        return {"inv_dx_face": (1.0 / np.diff(self.x_coords)).astype(f),
+                "inv_dx_cell": (1.0 / self.dx).astype(f),
+                "inv_dy_face": (1.0 / np.diff(self.y_coords)).astype(f),
+                "inv_dy_cell": (1.0 / self.dy).astype(f),
+                "inv_dz_face": (1.0 / np.diff(self.z_coords)).astype(f),
+                "inv_dz_cell": (1.0 / self.dz).astype(f)}
 
 
 # ---------------------------------------------------------------------------
@@ -204,8 +280,14 @@ class PML:
             d = self.depth * solver.grid.min_spacing
             self._max_sigma = -(self.order + 1) * solver.c * np.log(R_target) / (2 * d)
         dtype = np.float64 if solver.precision == "f64" else np.float32
-        sig = [self._profile(n, dtype) if a in self.axes else None
-               for n, a in zip((nx, ny, nz), ("x", "y", "z"))]
+        g = solver.grid
+        if g.is_uniform:
+            sig = [self._profile(n, dtype) if a in self.axes else None
+                   for n, a in zip((nx, ny, nz), ("x", "y", "z"))]
+        else:
+            sig = [self._profile_nu(c, s, dtype) if a in self.axes else None
+                   for c, s, a in zip((g.x_coords, g.y_coords, g.z_coords), (g.dx, g.dy, g.dz),
+                                      ("x", "y", "z"))]
         self._sigma_x, self._sigma_y, self._sigma_z = sig
         self.decay = []
         for s in sig:
@@ -219,6 +301,23 @@ class PML:
                                         out.ctypes.data)
                 self.decay.append(out)
 
+    def _profile_nu(self, coords, sp, dtype):
+        """_boundaries.py:257-315: physical distance from the PML interface
+        over the PML thickness."""
+        n = len(coords)
+        sigma = np.zeros(n, dtype=dtype)
+        d = self.depth if self.depth < n // 2 else max(1, n // 4)
+        lt, rt = float(np.sum(sp[:d])), float(np.sum(sp[-d:]))
+        li = coords[d] - sp[d] / 2 if d < n else coords[-1]
+        ri = coords[n - d - 1] + sp[n - d - 1] / 2 if n - d > 0 else coords[0]
+        for i in range(d):
+            nd = min(1.0, (li - coords[i]) / lt) if lt > 0 else 0.0
+            sigma[i] = self._max_sigma * (nd ** self.order)
+        for i in range(n - d, n):
+            nd = min(1.0, (coords[i] - ri) / rt) if rt > 0 else 0.0
+            sigma[i] = self._max_sigma * (nd ** self.order)
+        return sigma
+
     def _profile(self, n, dtype):
         sigma = np.zeros(n, dtype=dtype)
         d = self.depth
@@ -227,6 +326,62 @@ class PML:
         for i in range(n - d, n):
             sigma[i] = self._max_sigma * (((i - (n - d - 1)) / d) ** self.order)
         return sigma
+
+
+class ABCFirstOrder:
+    """_boundaries.py:420-527, the same NumPy operations (the Mur
+    coefficient is a NumPy float64, so each plane update runs in FP64 and is
+    rounded into the float32 field)."""
+
+    def __init__(self, axis="all"):
+        self.axes = ("x", "y", "z") if axis == "all" else ((axis,) if isinstance(axis, str)
+                                                           else tuple(axis))
+
+    def initialize(self, solver):
+        nx, ny, nz = solver.shape
+        self._coeff = (solver.c * solver.dt - solver.dx) / (solver.c * solver.dt + solver.dx)
+        z = np.float32
+        self.prev = {a: [np.zeros(s, dtype=z), np.zeros(s, dtype=z)]
+                     for a, s in (("x", (ny, nz)), ("y", (nx, nz)), ("z", (nx, ny)))
+                     if a in self.axes}
+
+    def apply_pressure(self, solver):
+        p, c = solver.p, self._coeff
+        for a, ax in (("x", 0), ("y", 1), ("z", 2)):
+            if a not in self.prev:
+                continue
+            pm = np.moveaxis(p, ax, 0)  # a view: writes land in p
+            lo, hi = self.prev[a]
+            pm[0] = lo + c * (pm[1] - pm[0])
+            self.prev[a][0] = pm[1].copy()
+            pm[-1] = hi + c * (pm[-2] - pm[-1])
+            self.prev[a][1] = pm[-2].copy()
+
+
+class RadiationImpedance:
+    """_boundaries.py:529-793 with constant reflection or from a pipe radius."""
+
+    def __init__(self, axis, side, reflection_coeff=None, pipe_radius=None):
+        self.axis, self.side = axis, side
+        self.R, self.radius = reflection_coeff, pipe_radius
+
+    def initialize(self, solver):
+        nx, ny, nz = solver.shape
+        if self.R is None:
+            ka = (2 * np.pi * 1000 / solver.c) * self.radius
+            z = (ka ** 2) / 4
+            self.R = min(abs((z - 1) / (z + 1)), 0.95)
+        shape = {"x": (ny, nz), "y": (nx, nz), "z": (nx, ny)}[self.axis]
+        self.prev = np.zeros(shape, dtype=np.float32)
+
+    def apply_pressure(self, solver):
+        p, R = solver.p, self.R
+        mur = (solver.c * solver.dt - solver.dx) / (solver.c * solver.dt + solver.dx)
+        pm = np.moveaxis(p, "xyz".index(self.axis), 0)
+        b, i = (0, 1) if self.side == "low" else (-1, -2)
+        abc = self.prev + mur * (pm[i] - pm[b])
+        pm[b] = R * pm[i] + (1 - R) * abc
+        self.prev[:] = pm[i]
 
 
 # ---------------------------------------------------------------------------
@@ -391,8 +546,14 @@ class FDTDSolver:
         self.c, self.rho, self.precision = c, rho, precision
         dt_max = self.grid.min_spacing / (self.c * np.sqrt(3))
         self.dt = courant * dt_max
-        self._coeff_p = -self.rho * self.c**2 * self.dt / self.dx
-        self._coeff_v = -self.dt / (self.rho * self.dx)
+        self._nu = None
+        if getattr(self.grid, "is_uniform", True):
+            self._coeff_p = -self.rho * self.c**2 * self.dt / self.dx
+            self._coeff_v = -self.dt / (self.rho * self.dx)
+        else:  # base coefficients and float32 spacing arrays (solver.py:1587-1602)
+            self._coeff_p = -self.rho * self.c**2 * self.dt
+            self._coeff_v = -self.dt / self.rho
+            self._nu = self.grid.get_spacing_arrays_for_stencil()
         self.real = np.float64 if precision == "f64" else np.float32
         self.p = np.zeros(self.shape, dtype=self.real)
         self.vx = np.zeros(self.shape, dtype=self.real)
@@ -587,7 +748,15 @@ class FDTDSolver:
                 if e["target"] == 0:
                     F("ade_lorentz")(_ptr(e["J"]), _ptr(e["Jp"]), _ptr(p), _ptr(mat), e["mid"],
                                      *e["co"], ncell)
-        F("update_velocity")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz, cv)
+        nu = None
+        if self._nu is not None:
+            nu = {k: np.ascontiguousarray(v, dtype=R) for k, v in self._nu.items()}
+        if nu is not None:  # _step_native_nonuniform (solver.py:2104-2126)
+            F("update_velocity_nu")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz, cv,
+                                    _ptr(nu["inv_dx_face"]), _ptr(nu["inv_dy_face"]),
+                                    _ptr(nu["inv_dz_face"]))
+        else:
+            F("update_velocity")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz, cv)
         if ade:
             for e in ade["debye"] + ade["lorentz"]:
                 if e["target"] == 0:
@@ -607,19 +776,29 @@ class FDTDSolver:
                 if e["target"] == 1:
                     F("ade_lorentz")(_ptr(e["J"]), _ptr(e["Jp"]), _ptr(ade["div"]), _ptr(mat),
                                      e["mid"], *e["co"], ncell)
-        F("update_pressure")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz),
-                             _ptr(self.geometry.view(np.uint8)), nx, ny, nz, cp)
+        if nu is not None:
+            F("update_pressure_nu")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz),
+                                    _ptr(self.geometry.view(np.uint8)), nx, ny, nz, cp,
+                                    _ptr(nu["inv_dx_cell"]), _ptr(nu["inv_dy_cell"]),
+                                    _ptr(nu["inv_dz_cell"]))
+        else:
+            F("update_pressure")(_ptr(p), _ptr(vx), _ptr(vy), _ptr(vz),
+                                 _ptr(self.geometry.view(np.uint8)), nx, ny, nz, cp)
         if ade:
             for e in ade["debye"] + ade["lorentz"]:
                 if e["target"] == 1:
                     F("ade_pressure_correction")(_ptr(p), _ptr(e["J"]), _ptr(mat), e["mid"],
                                                  e["cpre"], ncell)
             p[~self.geometry] = 0.0
+        for b in self._boundaries:  # boundary loops in order (solver.py:2040-2047)
+            if isinstance(b, PML):
+                F("pml_velocity")(_ptr(vx), _ptr(vy), _ptr(vz), *(_ptr(d) for d in b.decay),
+                                  nx, ny, nz)
         for b in self._boundaries:
-            F("pml_velocity")(_ptr(vx), _ptr(vy), _ptr(vz), *(_ptr(d) for d in b.decay),
-                              nx, ny, nz)
-        for b in self._boundaries:
-            F("pml_pressure")(_ptr(p), *(_ptr(d) for d in b.decay), nx, ny, nz)
+            if isinstance(b, PML):
+                F("pml_pressure")(_ptr(p), *(_ptr(d) for d in b.decay), nx, ny, nz)
+            else:
+                b.apply_pressure(self)
         g = _ptr(self.geometry.view(np.uint8))
         for s in self._sources:
             val = float(s.waveform(np.array([self._time]), self.dt)[0])
@@ -640,7 +819,8 @@ class FDTDSolver:
     def run_steps(self, n):
         """n steps of the plain path through one C call (no ADE, one PML);
         with ADE materials or microphones, step by step."""
-        if self._materials or getattr(self, "_mics", None):
+        if (self._materials or getattr(self, "_mics", None) or self._nu is not None
+                or any(not isinstance(b, PML) for b in self._boundaries)):
             for _ in range(n):
                 self.step()
             return
@@ -696,7 +876,9 @@ def make_api():
     """Namespace with the reference API names, for tests/golden/cases.py."""
     import types
     return types.SimpleNamespace(
-        FDTDSolver=FDTDSolver, UniformGrid=UniformGrid, PML=PML, GaussianPulse=GaussianPulse,
+        FDTDSolver=FDTDSolver, UniformGrid=UniformGrid, NonuniformGrid=NonuniformGrid, PML=PML,
+        ABCFirstOrder=ABCFirstOrder, RadiationImpedance=RadiationImpedance,
+        GaussianPulse=GaussianPulse,
         Box=Box, Sphere=Sphere, Cylinder=Cylinder, Union=Union, Intersection=Intersection,
         Difference=Difference, HelmholtzResonator=HelmholtzResonator, Pole=Pole,
         PoleType=PoleType, SimpleMaterial=SimpleMaterial)

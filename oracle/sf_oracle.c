@@ -82,6 +82,58 @@ void FN(update_pressure)(real* p, const real* vx, const real* vy, const real* vz
     }
 }
 
+/* _kernels/src/fdtd_step.cpp:235-305 (update_velocity_nonuniform): the face
+ * coefficient is formed per face as coeff_v_base * inv_face[i] (a rounded
+ * product), then v += coeff * (p[a+1] - p[a]) for a < n_a - 1. */
+void FN(update_velocity_nu)(const real* p, real* vx, real* vy, real* vz, int nx, int ny, int nz,
+                            real cvb, const real* ifx, const real* ify, const real* ifz) {
+    OMP_FOR
+    for (int i = 0; i < nx; i++) {
+        for (int j = 0; j < ny; j++) {
+            for (int k = 0; k < nz; k++) {
+                const int64_t c = IDX(i, j, k);
+                if (i < nx - 1) {
+                    const real cf = cvb * ifx[i];
+                    vx[c] += cf * (p[IDX(i + 1, j, k)] - p[c]);
+                }
+                if (j < ny - 1) {
+                    const real cf = cvb * ify[j];
+                    vy[c] += cf * (p[IDX(i, j + 1, k)] - p[c]);
+                }
+                if (k < nz - 1) {
+                    const real cf = cvb * ifz[k];
+                    vz[c] += cf * (p[c + 1] - p[c]);
+                }
+            }
+        }
+    }
+}
+
+/* _kernels/src/fdtd_step.cpp:307-439 (update_pressure_nonuniform): each
+ * difference scaled by the cell's inverse spacing before the sum, v[-1] = 0
+ * on the low faces, p = 0 in solids:
+ * p += cpb * ((icx (dvx) + icy (dvy)) + icz (dvz)). */
+void FN(update_pressure_nu)(real* p, const real* vx, const real* vy, const real* vz,
+                            const uint8_t* geom, int nx, int ny, int nz, real cpb,
+                            const real* icx, const real* icy, const real* icz) {
+    OMP_FOR
+    for (int i = 0; i < nx; i++) {
+        for (int j = 0; j < ny; j++) {
+            for (int k = 0; k < nz; k++) {
+                const int64_t c = IDX(i, j, k);
+                if (geom && !geom[c]) {
+                    p[c] = (real)0;
+                    continue;
+                }
+                const real dx = icx[i] * ((i > 0) ? (vx[c] - vx[IDX(i - 1, j, k)]) : vx[c]);
+                const real dy = icy[j] * ((j > 0) ? (vy[c] - vy[IDX(i, j - 1, k)]) : vy[c]);
+                const real dz = icz[k] * ((k > 0) ? (vz[c] - vz[c - 1]) : vz[c]);
+                p[c] += cpb * (dx + dy + dz);
+            }
+        }
+    }
+}
+
 /* _kernels/src/boundaries.cpp:13-64 + 66-89 (precompute_boundary_cells and
  * apply_rigid_boundaries): a face velocity is zeroed when either cell that it
  * separates is solid.  The last plane along each axis carries no face. */

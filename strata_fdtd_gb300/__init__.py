@@ -12,8 +12,8 @@ per-cell density field by a reverse-time adjoint.
 from ._native import NativeError, build
 from .adjoint import DifferentiableSolver
 from .batch import BatchedSolver
-from .boundaries import PML, RigidBoundary
-from .grid import UniformGrid
+from .boundaries import PML, ABCFirstOrder, RadiationImpedance, RigidBoundary
+from .grid import NonuniformGrid, UniformGrid
 from .microphones import Microphone
 from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
 from .resonator import HelmholtzResonator, helmholtz_array
@@ -24,7 +24,8 @@ from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_nativ
 __version__ = "0.1.0"
 
 __all__ = [
-    "FDTDSolver", "GaussianPulse", "Probe", "Microphone", "UniformGrid", "PML", "RigidBoundary", "Pole",
+    "FDTDSolver", "GaussianPulse", "Probe", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
+    "RigidBoundary", "ABCFirstOrder", "RadiationImpedance", "Pole",
     "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale",
     "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",

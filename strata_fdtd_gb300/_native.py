@@ -83,6 +83,12 @@ class SfPole(ctypes.Structure):
                 ("corr", ctypes.c_float), ("J", ctypes.c_void_p), ("J_prev", ctypes.c_void_p)]
 
 
+class SfPlaneBC(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("axis", ctypes.c_int32), ("side", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("coeff", ctypes.c_double),
+                ("reflection", ctypes.c_double)]
+
+
 class SfSdfNode(ctypes.Structure):
     _fields_ = [("op", ctypes.c_int32), ("n", ctypes.c_int32), ("a", ctypes.c_double * 3),
                 ("b", ctypes.c_double * 3), ("s0", ctypes.c_double), ("s1", ctypes.c_double)]
@@ -120,6 +126,8 @@ SIGNATURES = {
     "sf_plan_step_ex": (_I, [_P, _I64, _P, _P, _P, _P]),
     "sf_plan_set_microphones": (_I, [_P, _I, _P, _P]),
     "sf_plan_set_microphones_ex": (_I, [_P, _I, _P, _P, _P]),
+    "sf_plan_set_nonuniform": (_I, [_P, _P, _P]),
+    "sf_plan_set_plane_boundaries": (_I, [_P, _I, _P]),
     "sf_energy_scratch_doubles": (_I64, [_P]),
     "sf_plan_energy": (_I, [_P, _D, _D, _D, _P, _P, _P]),
     "sf_plan_energy_noalloc": (_I, [_P, _D, _D, _D, _P, _P]),
@@ -138,6 +146,7 @@ SIGNATURES = {
     "sf_batch_autotune": (_I, [_P, _I, _P, _P, _P, _P]),
     "sf_batch_run": (_I, [_P, _I64, _I, _P]),
     "sf_voxelize": (_I, [_P, _I, _I, _I, _I, _D, _I, _P, _P]),
+    "sf_voxelize_coords": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P]),
     "sf_sdf_eval": (_I, [_P, _I, _P, _I64, _P, _P]),
 }
 

@@ -32,6 +32,11 @@ class BatchedSolver:
             raise ValueError("BatchedSolver needs at least one solver")
         if any(s._microphones for s in solvers):
             raise NotImplementedError("microphones are recorded by single-solver runs only")
+        if any(getattr(s, "_plane_bc_dirty", False) or
+               any(hasattr(b, "plane_ops") for b in s._boundaries) for s in solvers):
+            raise NotImplementedError("plane boundaries are stepped by single-solver runs only")
+        if any(not s.grid.is_uniform for s in solvers):
+            raise NotImplementedError("nonuniform grids are stepped by single-solver runs only")
         self.solvers = list(solvers)
         self._lib = _native.load()
         self._torch = self.solvers[0]._torch

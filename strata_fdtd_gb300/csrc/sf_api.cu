@@ -125,6 +125,8 @@ int sf_plan_destroy(sf_plan* P) {
     cudaFree(P->mic_idx);
     cudaFree(P->mic_w);
     cudaFree(P->mic_field);
+    cudaFree(P->nu);
+    cudaFree(P->plane_prev);
     delete P;
     return 0;
 }
@@ -182,6 +184,69 @@ int sf_plan_set_pml(sf_plan* P, const float* sx, const float* sy, const float* s
     return set_decays(P, host);
 }
 
+int sf_plan_set_nonuniform(sf_plan* P, const float* const* cv_face, const float* const* inv_cell) {
+    if (!P) return sf_fail("sf_plan_set_nonuniform: NULL plan");
+    DeviceGuard g(P->device);
+    cudaFree(P->nu);
+    P->nu = nullptr;
+    if (!cv_face && !inv_cell) return 0;  // back to a uniform grid
+    if (!cv_face || !inv_cell) return sf_fail("sf_plan_set_nonuniform: need both tables");
+    for (int a = 0; a < 3; ++a)
+        if (!cv_face[a] || !inv_cell[a]) return sf_fail("sf_plan_set_nonuniform: NULL axis table");
+    if (P->poles.n > 0) return sf_fail("sf_plan_set_nonuniform: ADE materials need a uniform grid");
+    const int n[3] = {P->d.nx, P->d.ny, P->d.nz};
+    const long long total = 2LL * (n[0] + n[1] + n[2]);
+    SF_CUDA_OK(cudaMalloc(&P->nu, sizeof(float) * total));
+    const float* const* tables[2] = {cv_face, inv_cell};
+    long long off = 0;
+    for (int t = 0; t < 2; ++t)
+        for (int a = 0; a < 3; ++a) {
+            SF_CUDA_OK(cudaMemcpy(P->nu + off, tables[t][a], sizeof(float) * n[a],
+                                  cudaMemcpyHostToDevice));
+            off += n[a];
+        }
+    P->tuned = 0;  // the autotuner's choice was made for the other arithmetic
+    P->tuned_ich = 0;
+    return 0;
+}
+
+int sf_plan_set_plane_boundaries(sf_plan* P, int n, const sf_plane_bc* ops) {
+    if (!P) return sf_fail("sf_plan_set_plane_boundaries: NULL plan");
+    if (n < 0 || n > SF_MAX_PLANE_OPS || (n > 0 && !ops))
+        return sf_fail("sf_plan_set_plane_boundaries: at most 8 operations");
+    const int dims[3] = {P->d.nx, P->d.ny, P->d.nz};
+    long long total = 0;
+    long long off[SF_MAX_PLANE_OPS][2];
+    for (int q = 0; q < n; ++q) {
+        const sf_plane_bc& o = ops[q];
+        if ((o.kind != 0 && o.kind != 1) || o.axis < 0 || o.axis > 2 ||
+            (o.kind == 1 && o.side != 0 && o.side != 1))
+            return sf_fail("sf_plan_set_plane_boundaries: bad operation");
+        if (dims[o.axis] < 2)
+            return sf_fail("sf_plan_set_plane_boundaries: the axis needs at least 2 cells");
+        const long long plane = (long long)(o.axis == 0 ? dims[1] : dims[0]) *
+                                (o.axis == 2 ? dims[1] : dims[2]);
+        off[q][0] = total;
+        total += plane;
+        off[q][1] = total;
+        if (o.kind == 0) total += plane;  // Mur keeps both ends
+    }
+    DeviceGuard g(P->device);
+    cudaFree(P->plane_prev);
+    P->plane_prev = nullptr;
+    P->n_plane = 0;
+    if (n == 0) return 0;
+    SF_CUDA_OK(cudaMalloc(&P->plane_prev, sizeof(float) * total));
+    SF_CUDA_OK(cudaMemset(P->plane_prev, 0, sizeof(float) * total));
+    for (int q = 0; q < n; ++q) {
+        P->plane_ops[q] = ops[q];
+        P->plane_off[q][0] = off[q][0];
+        P->plane_off[q][1] = off[q][1];
+    }
+    P->n_plane = n;
+    return 0;
+}
+
 int sf_plan_set_pml_decay(sf_plan* P, const float* dx, const float* dy, const float* dz) {
     if (!P) return sf_fail("sf_plan_set_pml_decay: NULL plan");
     DeviceGuard g(P->device);
@@ -230,6 +295,7 @@ int sf_plan_set_ade(sf_plan* P, const uint8_t* mat, int n, const sf_pole* poles,
     if (!P) return sf_fail("sf_plan_set_ade: NULL plan");
     if (n < 0 || n > SF_MAX_POLES) return sf_fail("sf_plan_set_ade: at most 16 poles");
     if (n > 0 && (!mat || !poles)) return sf_fail("sf_plan_set_ade: NULL material ids or poles");
+    if (n > 0 && P->nu) return sf_fail("sf_plan_set_ade: ADE materials need a uniform grid");
     SfPoles T{};
     T.inv_dx = inv_dx;
     for (int q = 0; q < n; ++q) {
@@ -315,6 +381,12 @@ void fill_args(const sf_plan* P, SfStepArgs& a, bool with_trace) {
         a.reg_lo[q] = 0;  // the per-cell kernel covers the grid
         a.reg_hi[q] = n3[q];
         a.skip_lo[q] = a.skip_hi[q] = 0;  // the warp-tile kernels skip nothing
+        a.nu_cv[q] = a.nu_inv[q] = nullptr;
+    }
+    if (P->nu) {
+        long long off = 0;
+        for (int q = 0; q < 3; off += n3[q], ++q) a.nu_cv[q] = P->nu + off;
+        for (int q = 0; q < 3; off += n3[q], ++q) a.nu_inv[q] = P->nu + off;
     }
 }
 
@@ -342,8 +414,11 @@ int effective_config(const sf_plan* P, const SfStepArgs& a) {
     else if (P->tuned > 0) cfg = P->tuned;
     else if (sf_tile_supported(a, 4)) cfg = SF_CFG_TILE_DEFAULT;
     else cfg = sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT;
-    if (P->poles.n > 0 &&
-        !(cfg >= SF_CFG_TILE_FIRST && sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec)))
+    const bool tile_ok =
+        cfg >= SF_CFG_TILE_FIRST && sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec);
+    if (P->nu && !tile_ok)  // nonuniform arithmetic lives in the warp-tile kernels only
+        cfg = sf_tile_supported(a, 4) ? SF_CFG_TILE_DEFAULT : SF_CFG_TILE1_DEFAULT;
+    else if (P->poles.n > 0 && !tile_ok)
         cfg = SF_CFG_CELL;
     return cfg;
 }
@@ -466,7 +541,22 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
         a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
         a.reverse = (int)(P->steps_done & 1);
-        if (int rc = launch_step_split(P, cfg, ich, a, P->src, st)) return rc;
+        if (P->n_plane == 0) {
+            if (int rc = launch_step_split(P, cfg, ich, a, P->src, st)) return rc;
+        } else {  // step, plane boundaries in order, then the sources
+            const SfSources none{};
+            if (int rc = launch_step_split(P, cfg, ich, a, none, st)) return rc;
+            float* po = P->f[1 - P->cur][0];
+            for (int q = 0; q < P->n_plane; ++q)
+                if (int rc = sf_launch_plane_bc(po, P->plane_prev + P->plane_off[q][0],
+                                                P->plane_prev + P->plane_off[q][1],
+                                                P->plane_ops[q], P->d.nx, P->d.ny, P->d.nz, st))
+                    return rc;
+            for (int q = 0; q < P->src.n; ++q)
+                if (int rc = sf_launch_inject(po, P->flags, P->src.s[q], a.src_val + q, P->d.nx,
+                                              P->d.ny, P->d.nz, st))
+                    return rc;
+        }
         P->cur = 1 - P->cur;
         ++P->steps_done;
         if (mics)
@@ -544,7 +634,7 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     float best_ms = 0.0f;
     int rc = 0;
     for (int cfg = SF_CFG_CELL; cfg < count && !rc; ++cfg) {
-        if (!config_native(P, cfg, a) || (ade && cfg < SF_CFG_TILE_FIRST)) continue;
+        if (!config_native(P, cfg, a) || ((ade || P->nu) && cfg < SF_CFG_TILE_FIRST)) continue;
         const int ich = chunk_for(P, cfg);
         SfStepArgs t = a;
         if (ade) ade_region(P, cfg, ich, t.skip_lo, t.skip_hi);
@@ -624,15 +714,24 @@ int sf_plan_energy(sf_plan* P, double rho, double c, double dx, double* scratch,
     return 0;
 }
 
-int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, double res,
-                int invert, uint8_t* out_dev, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// Upload the program (and the cell centres of a nonuniform grid), voxelise,
+// and report a malformed program.
+int voxelize_impl(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz,
+                  double res, const double* const* coords, int invert, uint8_t* out_dev,
+                  cudaStream_t st) {
     if (!nodes || n_nodes < 1 || !out_dev) return sf_fail("sf_voxelize: bad program or output");
     if (nx < 1 || ny < 1 || nz < 1 || nx > 65535) return sf_fail("sf_voxelize: bad grid");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    sf_sdf_node* prog = nullptr;
-    int* err = nullptr;
-    SF_CUDA_OK(cudaMalloc(&prog, sizeof(sf_sdf_node) * n_nodes + 16));
-    err = reinterpret_cast<int*>(reinterpret_cast<char*>(prog) + sizeof(sf_sdf_node) * n_nodes);
+    const size_t prog_bytes = (sizeof(sf_sdf_node) * n_nodes + 15) / 16 * 16;
+    const size_t coord_bytes = coords ? sizeof(double) * ((size_t)nx + ny + nz) : 0;
+    char* buf = nullptr;
+    SF_CUDA_OK(cudaMalloc(&buf, prog_bytes + 16 + coord_bytes));
+    sf_sdf_node* prog = reinterpret_cast<sf_sdf_node*>(buf);
+    int* err = reinterpret_cast<int*>(buf + prog_bytes);
+    double* cdev = coords ? reinterpret_cast<double*>(buf + prog_bytes + 16) : nullptr;
     int rc = 0;
     int herr = 0;
     if (cudaMemcpyAsync(prog, nodes, sizeof(sf_sdf_node) * n_nodes, cudaMemcpyHostToDevice, st) !=
@@ -640,13 +739,41 @@ int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, d
         cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) {
         rc = sf_fail("sf_voxelize: upload failed");
     }
-    if (!rc) rc = sf_launch_voxelize(prog, n_nodes, nx, ny, nz, res, invert, out_dev, err, st);
+    if (!rc && coords) {
+        const int n3[3] = {nx, ny, nz};
+        size_t off = 0;
+        for (int a = 0; a < 3 && !rc; ++a) {
+            if (cudaMemcpyAsync(cdev + off, coords[a], sizeof(double) * n3[a],
+                                cudaMemcpyHostToDevice, st) != cudaSuccess)
+                rc = sf_fail("sf_voxelize: coordinate upload failed");
+            off += n3[a];
+        }
+    }
+    if (!rc) rc = sf_launch_voxelize(prog, n_nodes, nx, ny, nz, res, cdev, invert, out_dev, err, st);
     if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess))
         rc = sf_fail("sf_voxelize: kernel failed");
-    cudaFree(prog);
+    cudaFree(buf);
     if (!rc && herr) rc = sf_fail("sf_voxelize: malformed SDF program (stack error)");
     return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, double res,
+                int invert, uint8_t* out_dev, void* stream) {
+    return voxelize_impl(nodes, n_nodes, nx, ny, nz, res, nullptr, invert, out_dev,
+                         static_cast<cudaStream_t>(stream));
+}
+
+int sf_voxelize_coords(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz,
+                       const double* const* coords, int invert, uint8_t* out_dev, void* stream) {
+    if (!coords || !coords[0] || !coords[1] || !coords[2])
+        return sf_fail("sf_voxelize_coords: NULL coordinate array");
+    return voxelize_impl(nodes, n_nodes, nx, ny, nz, 0.0, coords, invert, out_dev,
+                         static_cast<cudaStream_t>(stream));
 }
 
 int sf_sdf_eval(const sf_sdf_node* nodes, int n_nodes, const double* points_dev, int64_t n,

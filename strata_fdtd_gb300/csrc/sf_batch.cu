@@ -581,6 +581,8 @@ int sf_batch_add(sf_batch* B, sf_plan* P, int64_t n_steps, const double* src_val
     if (!B || !P) return sf_fail("sf_batch_add: NULL argument");
     if (!P->bound) return sf_fail("sf_batch_add: plan fields not bound");
     if (P->device != B->device) return sf_fail("sf_batch_add: plan on another device");
+    if (P->nu) return sf_fail("sf_batch_add: nonuniform grids are stepped alone");
+    if (P->n_plane) return sf_fail("sf_batch_add: plane boundaries are stepped alone");
     if (n_steps < 0) return sf_fail("sf_batch_add: negative step count");
     if (P->src.n > 0 && n_steps > 0 && !src_values_dev)
         return sf_fail("sf_batch_add: sources need src_values");

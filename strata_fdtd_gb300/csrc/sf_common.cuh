@@ -66,6 +66,8 @@ struct SfStepArgs {
     int ade_lo[3], ade_hi[3];         // box holding every material cell
     int reg_lo[3], reg_hi[3];         // per-cell kernel: the cells it updates
     int skip_lo[3], skip_hi[3];       // warp-tile kernels: tile-aligned cells they leave out
+    const float* nu_cv[3];            // nonuniform grid: face coefficients per axis, or null
+    const float* nu_inv[3];           // nonuniform grid: cell inverse spacings per axis
 };
 
 #define SF_CUDA_OK(expr)                                                   \

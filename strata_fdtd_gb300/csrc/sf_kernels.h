@@ -40,6 +40,10 @@ int sf_launch_step_col_cfg(const SfStepArgs& a, const SfSources& src, bool geom,
                            cudaStream_t st);
 int sf_launch_step_tile_cfg(const SfStepArgs& a, const SfSources& src, bool geom, int cfg, int ich,
                             cudaStream_t st);
+int sf_launch_plane_bc(float* p, float* prev_lo, float* prev_hi, const sf_plane_bc& op, int nx,
+                       int ny, int nz, cudaStream_t st);
+int sf_launch_inject(float* p, const uint8_t* flags, const sf_source& s, const double* val, int nx,
+                     int ny, int nz, cudaStream_t st);
 int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const float* vz,
                          const int* field, const long long* idx, const float* w, int n, float* out,
                          cudaStream_t st);
@@ -48,6 +52,7 @@ int sf_launch_energy(const float* p, const float* vx, const float* vy, const flo
                      const uint8_t* flags, long long n, double* scratch, double* out2,
                      cudaStream_t st);
 int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny, int nz,
-                       double res, int invert, uint8_t* out, int* err_dev, cudaStream_t st);
+                       double res, const double* coords_dev, int invert, uint8_t* out,
+                       int* err_dev, cudaStream_t st);
 int sf_launch_sdf_points(const sf_sdf_node* prog_dev, int n_nodes, const double* pts, long long n,
                          double* out, int* err_dev, cudaStream_t st);

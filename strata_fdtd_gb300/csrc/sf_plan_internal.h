@@ -30,6 +30,12 @@ struct sf_plan {
     int* mic_field = nullptr;      // owned: field per row (0 p, 1 vx, 2 vy, 3 vz)
     int ade_lo[3] = {0, 0, 0};     // box holding every material cell (density pre-pass)
     int ade_hi[3] = {0, 0, 0};
+    float* nu = nullptr;  // owned, nonuniform grid: face coefficients x, y, z, then
+                          // cell inverse spacings x, y, z (nx, ny, nz floats each)
+    int n_plane = 0;                    // pressure-plane boundary operations
+    sf_plane_bc plane_ops[SF_MAX_PLANE_OPS];
+    float* plane_prev = nullptr;        // owned: stored planes, low then high per op
+    long long plane_off[SF_MAX_PLANE_OPS][2];
 };
 
 // Planes per block: enough (j,k)-tile x i-chunk blocks for about four waves

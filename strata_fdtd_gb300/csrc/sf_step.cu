@@ -217,6 +217,67 @@ __global__ void k_mic_gather(const float* __restrict__ p, const float* __restric
     out[m] = s;
 }
 
+// One pressure-plane boundary operation over the plane perpendicular to
+// op.axis; thread t = (u, v), the plane's two in-plane indices in C order.
+// Mur (kind 0): low end then high end, each p_b = float(double(prev) +
+// coeff * double(p_i - p_b)) and prev = p_i -- NumPy's float64 coefficient
+// times the float32 difference, rounded once into p (_boundaries.py:479-513).
+// Radiation impedance (kind 1), one end: p_b = float(double(float(R) p_i) +
+// (1 - R) (double(prev) + coeff double(p_i - p_b))), prev = p_i
+// (_boundaries.py:707-770).
+__global__ void k_plane_bc(float* __restrict__ p, float* __restrict__ prev_lo,
+                           float* __restrict__ prev_hi, int kind, int axis, int side,
+                           double coeff, double R, int nx, int ny, int nz) {
+    const int n3[3] = {nx, ny, nz};
+    const int nu = axis == 0 ? ny : nx, nv = axis == 2 ? ny : nz;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nu * nv) return;
+    const int u = (int)(t / nv), v = (int)(t % nv);
+    const int n = n3[axis];
+    auto at = [&](int w) -> long long {  // cell at position w along the axis
+        if (axis == 0) return ((long long)w * ny + u) * nz + v;
+        if (axis == 1) return ((long long)u * ny + w) * nz + v;
+        return ((long long)u * ny + v) * nz + w;
+    };
+    if (kind == 0) {
+        const long long b0 = at(0), i0 = at(1);
+        p[b0] = __double2float_rn(d_add((double)prev_lo[t], d_mul(coeff, (double)f_sub(p[i0], p[b0]))));
+        prev_lo[t] = p[i0];
+        const long long b1 = at(n - 1), i1 = at(n - 2);
+        p[b1] = __double2float_rn(d_add((double)prev_hi[t], d_mul(coeff, (double)f_sub(p[i1], p[b1]))));
+        prev_hi[t] = p[i1];
+    } else {
+        const long long b = side == 0 ? at(0) : at(n - 1), in = side == 0 ? at(1) : at(n - 2);
+        const float pi = p[in], pb = p[b];
+        const double abc = d_add((double)prev_lo[t], d_mul(coeff, (double)f_sub(pi, pb)));
+        const float rig = f_mul(__double2float_rn(R), pi);
+        p[b] = __double2float_rn(d_add((double)rig, d_mul(d_sub(1.0, R), abc)));
+        prev_lo[t] = pi;
+    }
+}
+
+// One source after the plane boundaries (core/solver.py:2386-2433): air
+// cells of a point or a plane, p = float(double(p) + value).
+__global__ void k_inject(float* __restrict__ p, const uint8_t* __restrict__ flags, int kind,
+                         int a, int b, int c, const double* __restrict__ val, int nx, int ny,
+                         int nz) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long cell;
+    if (kind == 0) {
+        if (t > 0) return;
+        cell = ((long long)a * ny + b) * nz + c;
+    } else {
+        const int nu = a == 0 ? ny : nx, nv = a == 2 ? ny : nz;
+        if (t >= (long long)nu * nv) return;
+        const int u = (int)(t / nv), v = (int)(t % nv);
+        if (a == 0) cell = ((long long)b * ny + u) * nz + v;
+        else if (a == 1) cell = ((long long)u * ny + b) * nz + v;
+        else cell = ((long long)u * ny + v) * nz + b;
+    }
+    if (flags && !(flags[cell] & SF_AIR)) return;
+    p[cell] = __double2float_rn(d_add((double)p[cell], *val));
+}
+
 // Face flags from the geometry mask (boundaries.cpp:13-64 rule).
 __global__ void k_build_flags(const uint8_t* __restrict__ geom, uint8_t* __restrict__ flags,
                               int nx, int ny, int nz) {
@@ -334,6 +395,24 @@ int sf_launch_probe_gather(const float* p, const long long* cells, int n, float*
     if (n <= 0) return 0;
     k_probe_gather<<<(n + 127) / 128, 128, 0, st>>>(p, cells, n, out);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_probe_gather launch failed");
+}
+
+int sf_launch_plane_bc(float* p, float* prev_lo, float* prev_hi, const sf_plane_bc& op, int nx,
+                       int ny, int nz, cudaStream_t st) {
+    const long long n = (long long)(op.axis == 0 ? ny : nx) * (op.axis == 2 ? ny : nz);
+    k_plane_bc<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, prev_lo, prev_hi, op.kind, op.axis,
+                                                            op.side, op.coeff, op.reflection, nx,
+                                                            ny, nz);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_plane_bc launch failed");
+}
+
+int sf_launch_inject(float* p, const uint8_t* flags, const sf_source& s, const double* val, int nx,
+                     int ny, int nz, cudaStream_t st) {
+    long long n = 1;
+    if (s.kind != 0) n = (long long)(s.a == 0 ? ny : nx) * (s.a == 2 ? ny : nz);
+    k_inject<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, flags, s.kind, s.a, s.b, s.c, val, nx,
+                                                          ny, nz);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_inject launch failed");
 }
 
 int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const float* vz,

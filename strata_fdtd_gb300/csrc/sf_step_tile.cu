@@ -47,10 +47,14 @@ __device__ __forceinline__ SfTileIo tile_io(const SfStepArgs& a) {
     io.dy = a.dy;
     io.dz = a.dz;
     io.src_val = a.src_val;
+    for (int q = 0; q < 3; ++q) {
+        io.nu_cv[q] = a.nu_cv[q];
+        io.nu_inv[q] = a.nu_inv[q];
+    }
     return io;
 }
 
-template <bool GEOM, int R, int W, int MINB, bool PF>
+template <bool GEOM, int R, int W, int MINB, bool PF, bool NU>
 __global__ void __launch_bounds__(32 * W, MINB) k_step_tile(SfStepArgs a, SfSources src, int ich) {
     const int jw = (blockIdx.y * W + threadIdx.y) * (4 * R);  // the warp's first row
     const int chunk = a.reverse ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z;
@@ -62,11 +66,11 @@ __global__ void __launch_bounds__(32 * W, MINB) k_step_tile(SfStepArgs a, SfSour
     }
     if (jw >= a.ny) return;  // the whole warp is past the grid (no block barrier follows)
     if (in_skip(a, i0, blockIdx.y * W * 4 * R, blockIdx.x * 32)) return;  // the ADE kernel's cells
-    tile4_run<GEOM, R, PF>(tile_io(a), src, i0, i1, jw, blockIdx.x * 32);
+    tile4_run<GEOM, R, PF, NU>(tile_io(a), src, i0, i1, jw, blockIdx.x * 32);
 }
 
 // Scalar warp tiles: 32 lanes along k, R rows per lane, W warps along j.
-template <bool GEOM, int R, int W, int MINB, bool PF>
+template <bool GEOM, int R, int W, int MINB, bool PF, bool NU>
 __global__ void __launch_bounds__(32 * W, MINB) k_step_tile1(SfStepArgs a, SfSources src, int ich) {
     const int k = blockIdx.x * 32 + threadIdx.x;
     const int jb = (blockIdx.y * W + threadIdx.y) * R;
@@ -79,15 +83,20 @@ __global__ void __launch_bounds__(32 * W, MINB) k_step_tile1(SfStepArgs a, SfSou
     }
     if (jb >= a.ny) return;  // the whole warp is past the grid
     if (in_skip(a, i0, blockIdx.y * W * R, blockIdx.x * 32)) return;  // the ADE kernel's cells
-    tile1_run<GEOM, R, PF>(tile_io(a), src, i0, i1, jb, k);
+    tile1_run<GEOM, R, PF, NU>(tile_io(a), src, i0, i1, jb, k);
 }
 
 template <int R, int W, int MINB, bool PF>
 int launch1(const SfStepArgs& a, const SfSources& src, bool geom, int ich, cudaStream_t st) {
     dim3 blk(32, W, 1);
     dim3 grd((a.nz + 31) / 32, (a.ny + R * W - 1) / (R * W), (a.nx + ich - 1) / ich);
-    if (geom) k_step_tile1<true, R, W, MINB, PF><<<grd, blk, 0, st>>>(a, src, ich);
-    else k_step_tile1<false, R, W, MINB, PF><<<grd, blk, 0, st>>>(a, src, ich);
+    if (a.nu_cv[0] != nullptr) {
+        if (geom) k_step_tile1<true, R, W, MINB, PF, true><<<grd, blk, 0, st>>>(a, src, ich);
+        else k_step_tile1<false, R, W, MINB, PF, true><<<grd, blk, 0, st>>>(a, src, ich);
+    } else {
+        if (geom) k_step_tile1<true, R, W, MINB, PF, false><<<grd, blk, 0, st>>>(a, src, ich);
+        else k_step_tile1<false, R, W, MINB, PF, false><<<grd, blk, 0, st>>>(a, src, ich);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step_tile1 launch failed");
 }
 
@@ -96,8 +105,13 @@ int launch(const SfStepArgs& a, const SfSources& src, bool geom, int ich, cudaSt
     dim3 blk(32, W, 1);
     const int rows = 4 * R * W;
     dim3 grd((a.nz + 31) / 32, (a.ny + rows - 1) / rows, (a.nx + ich - 1) / ich);
-    if (geom) k_step_tile<true, R, W, MINB, PF><<<grd, blk, 0, st>>>(a, src, ich);
-    else k_step_tile<false, R, W, MINB, PF><<<grd, blk, 0, st>>>(a, src, ich);
+    if (a.nu_cv[0] != nullptr) {
+        if (geom) k_step_tile<true, R, W, MINB, PF, true><<<grd, blk, 0, st>>>(a, src, ich);
+        else k_step_tile<false, R, W, MINB, PF, true><<<grd, blk, 0, st>>>(a, src, ich);
+    } else {
+        if (geom) k_step_tile<true, R, W, MINB, PF, false><<<grd, blk, 0, st>>>(a, src, ich);
+        else k_step_tile<false, R, W, MINB, PF, false><<<grd, blk, 0, st>>>(a, src, ich);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step_tile launch failed");
 }
 

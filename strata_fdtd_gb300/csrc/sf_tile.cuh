@@ -48,6 +48,10 @@ struct SfTileIo {
     const float* __restrict__ dy;
     const float* __restrict__ dz;
     const double* __restrict__ src_val;
+    // nonuniform grids (NU kernels only): per-face velocity coefficients
+    // float(coeff_v_base * inv_face) and per-cell inverse spacings, per axis
+    const float* __restrict__ nu_cv[3];
+    const float* __restrict__ nu_inv[3];
 };
 
 namespace sf_tile {
@@ -78,7 +82,7 @@ __device__ __forceinline__ bool fbit(uint32_t f, uint32_t bit) {
 
 }  // namespace sf_tile
 
-template <bool GEOM, int R, bool PF>
+template <bool GEOM, int R, bool PF, bool NU = false>
 __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& src, int i0, int i1,
                                           int jw, int kw) {
     using namespace sf_tile;
@@ -102,6 +106,28 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
 #pragma unroll
     for (int e = 0; e < 4; ++e) dk[e] = kact ? io.dz[k0 + e] : 1.0f;
     const float cv = io.cv, cp = io.cp;
+    // face coefficients and cell scales (uniform: cv everywhere, scale 1)
+    float cvy[R], sy[R], cvz[4], sz[4], cvy_lo = cv, cvz_lo = cv;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        cvy[r] = cv;
+        sy[r] = 1.0f;
+        if (NU && ract[r]) {
+            cvy[r] = jb + r < ny - 1 ? io.nu_cv[1][jb + r] : 0.0f;
+            sy[r] = io.nu_inv[1][jb + r];
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        cvz[e] = cv;
+        sz[e] = 1.0f;
+        if (NU && kact) {
+            cvz[e] = k0 + e < nz - 1 ? io.nu_cv[2][k0 + e] : 0.0f;
+            sz[e] = io.nu_inv[2][k0 + e];
+        }
+    }
+    if (NU && kact && jb > 0) cvy_lo = io.nu_cv[1][jb - 1];
+    if (NU && kact && k0 > 0) cvz_lo = io.nu_cv[2][k0 - 1];
 
     // Sources that can reach this lane's cells, in source order.
     unsigned smask = 0;
@@ -144,10 +170,11 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
             ld4(io.p, c - plane, pm);
             ld4(io.vx, c - plane, vm);
             const uint32_t fm = GEOM ? ldflags(io.flags, c - plane) : 0x0f0f0f0fu;
-            vxm[r][0] = face_update(vm[0], cv, pc[r][0], pm[0]);
-            vxm[r][1] = face_update(vm[1], cv, pc[r][1], pm[1]);
-            vxm[r][2] = face_update(vm[2], cv, pc[r][2], pm[2]);
-            vxm[r][3] = face_update(vm[3], cv, pc[r][3], pm[3]);
+            const float cvm = NU ? io.nu_cv[0][i0 - 1] : cv;
+            vxm[r][0] = face_update(vm[0], cvm, pc[r][0], pm[0]);
+            vxm[r][1] = face_update(vm[1], cvm, pc[r][1], pm[1]);
+            vxm[r][2] = face_update(vm[2], cvm, pc[r][2], pm[2]);
+            vxm[r][3] = face_update(vm[3], cvm, pc[r][3], pm[3]);
             if (GEOM) {
                 if (!fbit<0>(fm, SF_OPX)) vxm[r][0] = 0.0f;
                 if (!fbit<1>(fm, SF_OPX)) vxm[r][1] = 0.0f;
@@ -159,6 +186,8 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
 
     for (int i = i0; i < i1; ++i) {
         const int ci = i * plane;
+        const float cvx = NU ? (i < nx - 1 ? io.nu_cv[0][i] : 0.0f) : cv;
+        const float sxi = NU ? io.nu_inv[0][i] : 1.0f;
         if (PF) {  // plane i+1's velocities and flags, p at i+2 (used next iteration)
 #pragma unroll
             for (int r = 0; r < R; ++r) {
@@ -228,11 +257,11 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 ux[r][e] = vx[r][e];
-                if (i < nx - 1) ux[r][e] = face_update(vx[r][e], cv, pn[r][e], pc[r][e]);
+                if (i < nx - 1) ux[r][e] = face_update(vx[r][e], cvx, pn[r][e], pc[r][e]);
                 const float ph = (r + 1 < R) ? pc[r + 1 < R ? r + 1 : r][e] : pup[e];
-                uy[r][e] = jhi ? face_update(vy[r][e], cv, ph, pc[r][e]) : vy[r][e];
+                uy[r][e] = jhi ? face_update(vy[r][e], cvy[r], ph, pc[r][e]) : vy[r][e];
                 const float pk = (e < 3) ? pc[r][e < 3 ? e + 1 : e] : pkp[r];
-                uz[r][e] = (k0 + e < nz - 1) ? face_update(vz[r][e], cv, pk, pc[r][e]) : vz[r][e];
+                uz[r][e] = (k0 + e < nz - 1) ? face_update(vz[r][e], cvz[e], pk, pc[r][e]) : vz[r][e];
             }
             if (GEOM) {
                 const uint32_t f = fc[r];
@@ -260,7 +289,7 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
         for (int e = 0; e < 4; ++e) {
             const float t = __shfl_up_sync(kFull, uy[R - 1][e], 8);
             uym0[e] = (ly != 0) ? t : 0.0f;
-            if (jlow) uym0[e] = face_update(vyjm[e], cv, pc[0][e], pjm[e]);
+            if (jlow) uym0[e] = face_update(vyjm[e], cvy_lo, pc[0][e], pjm[e]);
         }
         if (GEOM && jlow) {
             if (!fbit<0>(fjm, SF_OPY)) uym0[0] = 0.0f;
@@ -273,7 +302,7 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
             const float t = __shfl_up_sync(kFull, uz[r][3], 1);
             uzm0[r] = (lx != 0) ? t : 0.0f;
             if (lx == 0 && ract[r] && k0 > 0) {
-                uzm0[r] = face_update(vzkm[r], cv, pc[r][0], pkm[r]);
+                uzm0[r] = face_update(vzkm[r], cvz_lo, pc[r][0], pkm[r]);
                 if (GEOM && !(fkm[r] & SF_OPZ)) uzm0[r] = 0.0f;
             }
         }
@@ -287,10 +316,14 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
                 const bool air = !GEOM || ((fc[r] >> (8 * e)) & SF_AIR);
                 const float uym = (r > 0) ? uy[r > 0 ? r - 1 : 0][e] : uym0[e];
                 const float uzm = (e > 0) ? uz[r][e > 0 ? e - 1 : 0] : uzm0[r];
-                float pnew = air ? f_add(pc[r][e], f_mul(cp, f_add(f_add(f_sub(ux[r][e], vxm[r][e]),
-                                                                         f_sub(uy[r][e], uym)),
-                                                                   f_sub(uz[r][e], uzm))))
-                                 : 0.0f;
+                float dx_ = f_sub(ux[r][e], vxm[r][e]), dy_ = f_sub(uy[r][e], uym),
+                      dz_ = f_sub(uz[r][e], uzm);
+                if (NU) {  // update_pressure_nonuniform: each term scaled first
+                    dx_ = f_mul(sxi, dx_);
+                    dy_ = f_mul(sy[r], dy_);
+                    dz_ = f_mul(sz[e], dz_);
+                }
+                float pnew = air ? f_add(pc[r][e], f_mul(cp, f_add(f_add(dx_, dy_), dz_))) : 0.0f;
                 ox[e] = f_mul(ux[r][e], di);
                 oy[e] = f_mul(uy[r][e], dj[r]);
                 oz[e] = f_mul(uz[r][e], dk[e]);
@@ -340,7 +373,7 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
     }
 }
 
-template <bool GEOM, int R, bool PF = false>
+template <bool GEOM, int R, bool PF = false, bool NU = false>
 __device__ __forceinline__ void tile1_run(const SfTileIo& io, const SfSources& src, int i0, int i1,
                                           int jb, int k) {
     constexpr unsigned kFull1 = 0xffffffffu;
@@ -359,6 +392,21 @@ __device__ __forceinline__ void tile1_run(const SfTileIo& io, const SfSources& s
         dj[r] = ract[r] ? io.dy[jb + r] : 1.0f;
     }
     const float dk = kact ? io.dz[k] : 1.0f;
+    // face coefficients and cell scales (uniform: cv everywhere, scale 1)
+    float cvy[R], sy[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        cvy[r] = cv;
+        sy[r] = 1.0f;
+        if (NU && ract[r]) {
+            cvy[r] = jb + r < ny - 1 ? io.nu_cv[1][jb + r] : 0.0f;
+            sy[r] = io.nu_inv[1][jb + r];
+        }
+    }
+    const float cvz = NU ? (kact && k < nz - 1 ? io.nu_cv[2][k] : 0.0f) : cv;
+    const float sz = NU ? (kact ? io.nu_inv[2][k] : 1.0f) : 1.0f;
+    const float cvy_lo = NU && kact && jb > 0 ? io.nu_cv[1][jb - 1] : cv;
+    const float cvz_lo = NU && kact && k > 0 ? io.nu_cv[2][k - 1] : cv;
 
     unsigned smask = 0;
     if (kact) {
@@ -396,7 +444,7 @@ __device__ __forceinline__ void tile1_run(const SfTileIo& io, const SfSources& s
             if (i0 > 0) {  // chunk start: low x face from plane i0-1
                 const float pm = __ldg(P0 - plane + roff[r]);
                 const float vm = __ldg(io.vx + (long long)(i0 - 1) * plane + roff[r]);
-                vxm[r] = face_update(vm, cv, pc[r], pm);
+                vxm[r] = face_update(vm, NU ? io.nu_cv[0][i0 - 1] : cv, pc[r], pm);
                 if (GEOM && !(__ldg(io.flags + (long long)(i0 - 1) * plane + roff[r]) & SF_OPX))
                     vxm[r] = 0.0f;
             }
@@ -405,6 +453,8 @@ __device__ __forceinline__ void tile1_run(const SfTileIo& io, const SfSources& s
 
     for (int i = i0; i < i1; ++i) {
         const long long base = (long long)i * plane;
+        const float cvx = NU ? (i < nx - 1 ? io.nu_cv[0][i] : 0.0f) : cv;
+        const float sxi = NU ? io.nu_inv[0][i] : 1.0f;
         const float* __restrict__ P = io.p + base;
         const float* __restrict__ VX = io.vx + base;
         const float* __restrict__ VY = io.vy + base;
@@ -468,17 +518,18 @@ __device__ __forceinline__ void tile1_run(const SfTileIo& io, const SfSources& s
         for (int r = 0; r < R; ++r) {
             ux[r] = vx[r];
             if (i < nx - 1) {
-                ux[r] = face_update(vx[r], cv, pn[r], pc[r]);
+                ux[r] = face_update(vx[r], cvx, pn[r], pc[r]);
                 if (GEOM && !(fc[r] & SF_OPX)) ux[r] = 0.0f;
             }
             uy[r] = vy[r];
             if (jb + r < ny - 1) {
-                uy[r] = face_update(vy[r], cv, (r + 1 < R) ? pc[r + 1 < R ? r + 1 : r] : pup, pc[r]);
+                uy[r] = face_update(vy[r], cvy[r], (r + 1 < R) ? pc[r + 1 < R ? r + 1 : r] : pup,
+                                    pc[r]);
                 if (GEOM && !(fc[r] & SF_OPY)) uy[r] = 0.0f;
             }
             uz[r] = vz[r];
             if (k < nz - 1) {
-                uz[r] = face_update(vz[r], cv, pkp[r], pc[r]);
+                uz[r] = face_update(vz[r], cvz, pkp[r], pc[r]);
                 if (GEOM && !(fc[r] & SF_OPZ)) uz[r] = 0.0f;
             }
         }
@@ -488,13 +539,13 @@ __device__ __forceinline__ void tile1_run(const SfTileIo& io, const SfSources& s
             const float t = __shfl_up_sync(kFull1, uz[r], 1);
             uzm[r] = (lane != 0) ? t : 0.0f;
             if (lane == 0 && ract[r] && k > 0) {
-                uzm[r] = face_update(vzkm[r], cv, pc[r], pkm[r]);
+                uzm[r] = face_update(vzkm[r], cvz_lo, pc[r], pkm[r]);
                 if (GEOM && !(fkm[r] & SF_OPZ)) uzm[r] = 0.0f;
             }
         }
         float uym0 = 0.0f;
         if (jlow) {
-            uym0 = face_update(vyjm, cv, pc[0], pjm);
+            uym0 = face_update(vyjm, cvy_lo, pc[0], pjm);
             if (GEOM && !(fjm & SF_OPY)) uym0 = 0.0f;
         }
 
@@ -503,10 +554,13 @@ __device__ __forceinline__ void tile1_run(const SfTileIo& io, const SfSources& s
         for (int r = 0; r < R; ++r) {
             const bool air = !GEOM || (fc[r] & SF_AIR);
             const float uym = (r > 0) ? uy[r > 0 ? r - 1 : 0] : uym0;
-            float pnew = air ? f_add(pc[r], f_mul(cp, f_add(f_add(f_sub(ux[r], vxm[r]),
-                                                                  f_sub(uy[r], uym)),
-                                                            f_sub(uz[r], uzm[r]))))
-                             : 0.0f;
+            float dx_ = f_sub(ux[r], vxm[r]), dy_ = f_sub(uy[r], uym), dz_ = f_sub(uz[r], uzm[r]);
+            if (NU) {  // update_pressure_nonuniform: each term scaled first
+                dx_ = f_mul(sxi, dx_);
+                dy_ = f_mul(sy[r], dy_);
+                dz_ = f_mul(sz, dz_);
+            }
+            float pnew = air ? f_add(pc[r], f_mul(cp, f_add(f_add(dx_, dy_), dz_))) : 0.0f;
             const float ox = f_mul(ux[r], di), oy = f_mul(uy[r], dj[r]), oz = f_mul(uz[r], dk);
             pnew = f_mul(f_mul(f_mul(pnew, di), dj[r]), dk);
             if (smask != 0) {

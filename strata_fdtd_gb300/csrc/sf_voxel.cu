@@ -138,17 +138,26 @@ __device__ double eval_sdf(const sf_sdf_node* __restrict__ prog, int n, double x
     return ds[0];
 }
 
+// coords (nx + ny + nz doubles, may be null): the cell centres of a
+// nonuniform grid, else centres at (index + 1/2) * res.
 __global__ void k_voxelize(const sf_sdf_node* __restrict__ prog, int n_nodes, int nx, int ny,
-                           int nz, double res, int invert, uint8_t* __restrict__ out,
-                           int* __restrict__ err_flag) {
+                           int nz, double res, const double* __restrict__ coords, int invert,
+                           uint8_t* __restrict__ out, int* __restrict__ err_flag) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= nz || j >= ny) return;
-    const double half = d_mul(res, 0.5);
-    const double x = d_add(d_mul((double)i, res), half);
-    const double y = d_add(d_mul((double)j, res), half);
-    const double z = d_add(d_mul((double)k, res), half);
+    double x, y, z;
+    if (coords) {
+        x = coords[i];
+        y = coords[nx + j];
+        z = coords[nx + ny + k];
+    } else {
+        const double half = d_mul(res, 0.5);
+        x = d_add(d_mul((double)i, res), half);
+        y = d_add(d_mul((double)j, res), half);
+        z = d_add(d_mul((double)k, res), half);
+    }
     int err = 0;
     const double d = eval_sdf(prog, n_nodes, x, y, z, &err);
     if (err) atomicExch(err_flag, err);
@@ -179,8 +188,10 @@ int sf_launch_sdf_points(const sf_sdf_node* prog_dev, int n_nodes, const double*
 }
 
 int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny, int nz,
-                       double res, int invert, uint8_t* out, int* err_dev, cudaStream_t st) {
+                       double res, const double* coords_dev, int invert, uint8_t* out,
+                       int* err_dev, cudaStream_t st) {
     dim3 blk(32, 8, 1), grd((nz + 31) / 32, (ny + 7) / 8, nx);
-    k_voxelize<<<grd, blk, 0, st>>>(prog_dev, n_nodes, nx, ny, nz, res, invert, out, err_dev);
+    k_voxelize<<<grd, blk, 0, st>>>(prog_dev, n_nodes, nx, ny, nz, res, coords_dev, invert, out,
+                                    err_dev);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_voxelize launch failed");
 }

@@ -60,9 +60,18 @@ class SDFPrimitive:
             out = torch.empty((nx, ny, nz), dtype=torch.uint8, device="cuda")
         prog, n = self.program()
         st = (stream or torch.cuda.current_stream()).cuda_stream
-        _native.check(_native.load().sf_voxelize(ctypes.addressof(prog), n, nx, ny, nz,
-                                                 float(grid.min_spacing), int(invert),
-                                                 out.data_ptr(), st), "sf_voxelize")
+        if getattr(grid, "is_uniform", True):
+            _native.check(_native.load().sf_voxelize(ctypes.addressof(prog), n, nx, ny, nz,
+                                                     float(grid.min_spacing), int(invert),
+                                                     out.data_ptr(), st), "sf_voxelize")
+        else:  # the nonuniform grid's own cell centres
+            cs = [np.ascontiguousarray(c, dtype=np.float64)
+                  for c in (grid.x_coords, grid.y_coords, grid.z_coords)]
+            ptrs = (ctypes.c_void_p * 3)(*[c.ctypes.data for c in cs])
+            _native.check(_native.load().sf_voxelize_coords(ctypes.addressof(prog), n, nx, ny,
+                                                            nz, ptrs, int(invert),
+                                                            out.data_ptr(), st),
+                          "sf_voxelize_coords")
         return out
 
     def voxelize(self, grid) -> np.ndarray:

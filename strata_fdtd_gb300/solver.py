@@ -32,7 +32,7 @@ from typing import Literal
 import numpy as np
 
 from . import _native
-from .boundaries import PML, RigidBoundary
+from .boundaries import PML, ABCFirstOrder, RadiationImpedance, RigidBoundary
 from .grid import UniformGrid
 from .sdf import SDFPrimitive
 
@@ -91,10 +91,13 @@ class Probe:
 
 
 def step_coefficients(grid, c: float, rho: float, courant: float):
-    """dt, coeff_v, coeff_p with the FP64 expressions of core/solver.py:1576-1586."""
+    """dt, coeff_v, coeff_p with the FP64 expressions of core/solver.py:1576-1591;
+    on a nonuniform grid the base coefficients without the 1/dx factor."""
     dx = grid.min_spacing
     dt_max = grid.min_spacing / (c * np.sqrt(3))
     dt = courant * dt_max
+    if not getattr(grid, "is_uniform", True):
+        return dt, -dt / rho, -rho * c**2 * dt
     coeff_p = -rho * c**2 * dt / dx
     coeff_v = -dt / (rho * dx)
     return dt, coeff_v, coeff_p
@@ -151,8 +154,6 @@ class FDTDSolver:
             self.shape = tuple(self._grid.shape)
         else:
             raise ValueError("Must provide either 'grid' or both 'shape' and 'resolution'")
-        if not getattr(self._grid, "is_uniform", True):
-            raise NotImplementedError("nonuniform grids are not supported by the GB300 backend")
         if backend not in ("auto", "native"):
             raise ValueError(f"backend must be 'auto' or 'native' (GB300 kernels), got {backend!r}")
         if not torch.cuda.is_available():
@@ -187,6 +188,8 @@ class FDTDSolver:
         self._plan = plan
         ptrs = [t.data_ptr() for s in self._dev for t in s]
         _native.check(self._lib.sf_plan_bind_fields(self._plan, *ptrs), "sf_plan_bind_fields")
+        if not self._grid.is_uniform:
+            self._set_nonuniform()
 
         self._sources: list = []
         self._probes: dict[str, Probe] = {}
@@ -221,6 +224,24 @@ class FDTDSolver:
         self._ade_debye: list = []
         self._ade_lorentz: list = []
         self._mat_dev = None
+
+    def _set_nonuniform(self):
+        """Spacing tables of a nonuniform grid (core/solver.py:1587-1602):
+        face coefficients float(coeff_v_base) * inv_face in float, as
+        update_velocity_nonuniform forms them (fdtd_step.cpp:235-305), and
+        the cell inverse spacings of the divergence."""
+        sa = self._grid.get_spacing_arrays_for_stencil()
+        cvb = np.float32(self._coeff_v)
+        face, cell = [], []
+        for ax, n in zip("xyz", self.shape):
+            f = np.zeros(n, dtype=np.float32)
+            f[:n - 1] = cvb * sa[f"inv_d{ax}_face"]
+            face.append(f)
+            cell.append(np.ascontiguousarray(sa[f"inv_d{ax}_cell"], dtype=np.float32))
+        self._nu_tables = face + cell  # kept alive for the copy
+        fp = (ctypes.c_void_p * 3)(*[a.ctypes.data for a in face])
+        cp = (ctypes.c_void_p * 3)(*[a.ctypes.data for a in cell])
+        _native.check(self._lib.sf_plan_set_nonuniform(self._plan, fp, cp), "sf_plan_set_nonuniform")
 
     def __del__(self):
         plan = getattr(self, "_plan", None)
@@ -401,14 +422,25 @@ class FDTDSolver:
         return self._microphones
 
     def add_boundary(self, boundary) -> None:
+        """Boundaries act in the order added (core/solver.py:1983-1990,
+        2040-2047): the PML inside the fused step, then the pressure-plane
+        boundaries (Mur ABC, radiation impedance) in order."""
         if isinstance(boundary, RigidBoundary):
             boundary.initialize(self)
             self._boundaries.append(boundary)
+            return
+        if isinstance(boundary, (ABCFirstOrder, RadiationImpedance)):
+            boundary.initialize(self)
+            self._boundaries.append(boundary)
+            self._plane_bc_dirty = True
             return
         if not isinstance(boundary, PML):
             raise NotImplementedError(f"{type(boundary).__name__} is not supported by the GB300 backend")
         if any(isinstance(b, PML) for b in self._boundaries):
             raise NotImplementedError("one PML per solver is supported by the GB300 backend")
+        if any(isinstance(b, (ABCFirstOrder, RadiationImpedance)) for b in self._boundaries):
+            raise NotImplementedError("a PML must be added before plane boundaries "
+                                      "(the fused step applies it first)")
         boundary.initialize(self)
         self._boundaries.append(boundary)
         sx, sy, sz = boundary.sigmas
@@ -423,6 +455,9 @@ class FDTDSolver:
 
     # --------------------------------------------------------------- materials
     def register_material(self, material, material_id: int | None = None) -> int:
+        if not self._grid.is_uniform:
+            raise NotImplementedError("ADE materials on nonuniform grids are not implemented by "
+                                      "the GB300 backend")
         if material_id is None:
             material_id = next((i for i in range(1, 256) if i not in self._materials), None)
             if material_id is None:
@@ -526,6 +561,15 @@ class FDTDSolver:
 
     # ---------------------------------------------------------------- stepping
     def _sync_tables(self):
+        if getattr(self, "_plane_bc_dirty", False):
+            ops = [op for b in self._boundaries if hasattr(b, "plane_ops") for op in b.plane_ops()]
+            tab = (_native.SfPlaneBC * max(1, len(ops)))()
+            for q, (kind, axis, side, coeff, refl) in enumerate(ops):
+                tab[q].kind, tab[q].axis, tab[q].side = kind, axis, side
+                tab[q].coeff, tab[q].reflection = coeff, refl
+            _native.check(self._lib.sf_plan_set_plane_boundaries(self._plan, len(ops), tab),
+                          "sf_plan_set_plane_boundaries")
+            self._plane_bc_dirty = False
         if self._src_dirty:
             tab = (_native.SfSource * max(1, len(self._sources)))()
             for q, s in enumerate(self._sources):
@@ -812,8 +856,14 @@ class FDTDSolver:
         self._energy_history.clear()
         self._track_energy = False
         self._pending_traces.clear()
+        self._pending_mics = []
         for pr in self._probes.values():
             pr._samples.clear()
+        for m in self._microphones.values():
+            m._data.clear()
+            m._times.clear()
+        for b in self._boundaries:
+            b.reset()
         for e in self._ade_debye + self._ade_lorentz:
             e["J"].zero_()
             if "Jp" in e:

@@ -127,6 +127,57 @@ PLAIN_CASES = {
                                                         direction=(0, 0.6, 0.8)))],
         steps=120, store_fields=True,
     ),
+    "nu_stretch_blocks": dict(
+        # nonuniform grid, geometric growth from the centre (x, z) and from
+        # the low end (y, second case); nz % 4 != 0 (scalar warp tiles)
+        shape=(30, 26, 34), res=None, courant=0.5, pml=dict(depth=4),
+        grid=dict(kind="stretch", base=1e-3, stretch=(1.04, 1.0, 1.06)),
+        geometry=dict(kind="blocks", seed=41, n_boxes=1, n_spheres=1),
+        sources=[("point", (15, 13, 17), 20000.0, 1.0),
+                 ("plane", {"axis": 1, "index": 5}, 12000.0, 0.4)],
+        probes=[("a", (8, 13, 17)), ("b", (25, 20, 30))],
+        steps=120, store_fields=True,
+    ),
+    "nu_stretch_low_end": dict(
+        shape=(24, 28, 20), res=None, courant=0.6, pml=dict(depth=3, axis=("x", "z")),
+        grid=dict(kind="stretch", base=1e-3, stretch=(1.0, 1.05, 1.03), center_fine=False),
+        sources=[("point", (6, 9, 10), 25000.0, 1.0)],
+        probes=[("a", (18, 20, 10))],
+        steps=100, store_fields=True,
+    ),
+    "nu_regions_sdf": dict(
+        # piecewise resolution, SDF geometry voxelised at the grid's own cell
+        # centres; nz % 4 == 0 (float4 warp tiles)
+        shape=None, res=None, courant=0.5, pml=dict(depth=4),
+        grid=dict(kind="regions", x=[(0.0, 0.01, 1e-3), (0.01, 0.03, 5e-4), (0.03, 0.04, 1e-3)],
+                  y=[(0.0, 0.024, 1e-3)], z=[(0.0, 0.012, 1.5e-3), (0.012, 0.03, 7.5e-4)]),
+        geometry=dict(kind="sdf", which="nu_block"),
+        sources=[("point", (30, 12, 16), 20000.0, 1.0)],
+        probes=[("a", (12, 12, 16)), ("b", (50, 6, 28))],
+        steps=120, store_fields=True,
+    ),
+    "abc_all_sources": dict(
+        # Mur ABC on every axis instead of a PML; sources on boundary planes
+        # (injected after the boundary update, as the reference's step does)
+        shape=(26, 22, 30), res=1e-3, courant=0.5,
+        plane_bcs=[("abc", {})],
+        geometry=dict(kind="blocks", seed=52, n_boxes=1, n_spheres=1),
+        sources=[("point", (0, 11, 15), 20000.0, 1.0), ("point", (13, 11, 15), 15000.0, 0.5),
+                 ("plane", {"axis": 2, "index": 0}, 9000.0, 0.2)],
+        probes=[("edge", (0, 11, 15)), ("mid", (13, 5, 20)), ("corner", (25, 21, 29))],
+        steps=140, store_fields=True,
+    ),
+    "rad_pml_mix": dict(
+        # a PML on y, radiation impedance at both x ends (constant and
+        # pipe-radius reflection), Mur ABC on z, in that order
+        shape=(40, 20, 24), res=1e-3, courant=0.5, pml=dict(depth=3, axis="y"),
+        plane_bcs=[("rad", {"axis": "x", "side": "high", "reflection_coeff": 0.6}),
+                   ("rad", {"axis": "x", "side": "low", "pipe_radius": 0.01}),
+                   ("abc", {"axis": "z"})],
+        sources=[("point", (8, 10, 12), 18000.0, 1.0)],
+        probes=[("hi", (39, 10, 12)), ("lo", (0, 10, 12)), ("zl", (20, 10, 0))],
+        steps=160, store_fields=True,
+    ),
     "c1_full": dict(
         # the reference quick start, 100^3 x 1000 steps (hashes + traces only)
         shape=(100, 100, 100), res=1e-3, courant=0.5, pml=dict(depth=10),
@@ -216,6 +267,9 @@ def sdf_tree(api, which):
     Union, Intersection, Difference = api.Union, api.Intersection, api.Difference
     if which == "box":
         return Box(center=(0.016, 0.0205, 0.0117), size=(0.0101, 0.0203, 0.0071))
+    if which == "nu_block":  # a block and a sphere straddling the resolution changes
+        return Union(Box(center=(0.0095, 0.0121, 0.0147), size=(0.0043, 0.0102, 0.0061)),
+                     Sphere(center=(0.0318, 0.0127, 0.0219), radius=0.0041))
     if which == "sphere":
         return Sphere(center=(0.0151, 0.0149, 0.0153), radius=0.0097)
     if which == "cyl_axes":
@@ -288,8 +342,15 @@ def c2_probes(geometry, pml_depth=16, n=8, seed=0):
 
 def build_case(api, case, ade=False):
     """Construct a solver for ``case`` through the reference-shaped ``api``."""
-    kw = dict(grid=api.UniformGrid(shape=case["shape"], resolution=case["res"]),
-              c=AIR["c"], backend="native")
+    g = case.get("grid")
+    if g is None:
+        grid = api.UniformGrid(shape=case["shape"], resolution=case["res"])
+    elif g["kind"] == "stretch":
+        grid = api.NonuniformGrid.from_stretch(case["shape"], g["base"], *g["stretch"],
+                                               center_fine=g.get("center_fine", True))
+    else:
+        grid = api.NonuniformGrid.from_regions(g["x"], g["y"], g["z"])
+    kw = dict(grid=grid, c=AIR["c"], backend="native")
     rho = case.get("rho", AIR["rho"])
     if rho is not None:          # None: the reference default (1.2)
         kw["rho"] = rho
@@ -298,6 +359,9 @@ def build_case(api, case, ade=False):
     solver = api.FDTDSolver(**kw)
     if case.get("pml"):
         solver.add_boundary(api.PML(**case["pml"]))
+    for kind, opts in case.get("plane_bcs", []):
+        cls = api.ABCFirstOrder if kind == "abc" else api.RadiationImpedance
+        solver.add_boundary(cls(**opts))
     geo = case.get("geometry")
     if geo:
         if geo["kind"] == "blocks":

@@ -59,6 +59,9 @@ def load_reference():
     from strata_fdtd.materials import base
     api = types.SimpleNamespace(
         FDTDSolver=sf.FDTDSolver, UniformGrid=sf.UniformGrid, PML=sf.PML,
+        NonuniformGrid=sys.modules["strata_fdtd.core.grid"].NonuniformGrid,
+        ABCFirstOrder=sys.modules["strata_fdtd.boundaries"].ABCFirstOrder,
+        RadiationImpedance=sf.RadiationImpedance,
         GaussianPulse=sf.GaussianPulse, Box=sdf.Box, Sphere=sdf.Sphere,
         Cylinder=sdf.Cylinder, Union=sdf.Union, Intersection=sdf.Intersection,
         Difference=sdf.Difference, HelmholtzResonator=resonator.HelmholtzResonator,
@@ -140,8 +143,11 @@ def run_case(api, name, case, ade, manifest):
         out[f"trace__{pname}"] = tr
     for mic_name, mic in getattr(solver, "_microphones", {}).items():
         out[f"mic__{mic_name}"] = mic.get_waveform()
-    info = dict(steps=case["steps"], dt=float(solver.dt), coeff_v=float(solver._coeff_v),
-                coeff_p=float(solver._coeff_p), time=float(solver._time))
+    uniform = solver.grid.is_uniform
+    info = dict(steps=case["steps"], dt=float(solver.dt),
+                coeff_v=float(solver._coeff_v if uniform else solver._coeff_v_base),
+                coeff_p=float(solver._coeff_p if uniform else solver._coeff_p_base),
+                time=float(solver._time), uniform=bool(uniform))
     for f in ("p", "vx", "vy", "vz"):
         arr = getattr(solver, f)
         info[f"sha_{f}"] = sha(arr)

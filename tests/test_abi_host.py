@@ -130,3 +130,38 @@ def test_helmholtz_constants_match_oracle_construction():
         na, nb = a._combined.children[1], b._combined.children[1]
         assert np.array_equal(na.p1, nb.p1) and np.array_equal(na.p2, nb.p2)
         assert na.length == nb.length
+
+
+def test_nonuniform_grid_host_values(manifest):
+    """NonuniformGrid coordinates, spacings and float32 stencil arrays, the
+    base coefficients and the physical-distance PML profile, against the
+    oracle's restatement (which the nonuniform goldens pin to the reference)."""
+    from oracle import oracle as O
+
+    specs = [("stretch", ((30, 26, 34), 1e-3, 1.04, 1.0, 1.06), dict(center_fine=True)),
+             ("stretch", ((24, 28, 20), 1e-3, 1.0, 1.05, 1.03), dict(center_fine=False)),
+             ("regions", ([(0.0, 0.01, 1e-3), (0.01, 0.03, 5e-4), (0.03, 0.04, 1e-3)],
+                          [(0.0, 0.024, 1e-3)], [(0.0, 0.012, 1.5e-3), (0.012, 0.03, 7.5e-4)]),
+              {})]
+    for kind, args, kw in specs:
+        mk = "from_stretch" if kind == "stretch" else "from_regions"
+        g = getattr(S.NonuniformGrid, mk)(*args, **kw)
+        o = getattr(O.NonuniformGrid, mk)(*args, **kw)
+        for a in ("x_coords", "y_coords", "z_coords", "dx", "dy", "dz"):
+            np.testing.assert_array_equal(getattr(g, a), getattr(o, a))
+        assert g.min_spacing == o.min_spacing and g.shape == o.shape
+        ga, oa = g.get_spacing_arrays_for_stencil(), o.get_spacing_arrays_for_stencil()
+        for k in ga:
+            assert ga[k].dtype == np.float32
+            np.testing.assert_array_equal(ga[k], oa[k])
+        pml, opml = S.PML(depth=4), O.PML(depth=4)
+        pml._max_sigma = opml._max_sigma = 1234.5
+        pml.order = opml.order = 3
+        for c, sp in ((g.x_coords, g.dx), (g.z_coords, g.dz)):
+            np.testing.assert_array_equal(pml._create_profile_nonuniform(c, sp),
+                                          opml._profile_nu(c, sp, np.float32))
+    g = S.NonuniformGrid.from_stretch((30, 26, 34), 1e-3, 1.04, 1.0, 1.06)
+    dt, cvb, cpb = step_coefficients(g, 343.0, 1.204, 0.5)
+    info = manifest["plain_nu_stretch_blocks"]
+    assert (dt, cvb, cpb) == (info["dt"], info["coeff_v"], info["coeff_p"])
+    assert info["uniform"] is False

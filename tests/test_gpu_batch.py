@@ -20,7 +20,8 @@ API = types.SimpleNamespace(
     FDTDSolver=S.FDTDSolver, UniformGrid=S.UniformGrid, PML=S.PML, GaussianPulse=S.GaussianPulse,
     Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
-    PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial)
+    PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
+    ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance)
 
 MIX = [("plain", "c1_tiny"), ("plain", "blocks_odd"), ("plain", "plane_yz_geom"),
        ("plain", "impulse_default_coeffs"), ("ade", "debye_2pole"), ("ade", "lorentz_mixed_geom"),

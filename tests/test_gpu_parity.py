@@ -24,9 +24,11 @@ API = types.SimpleNamespace(
     FDTDSolver=S.FDTDSolver, UniformGrid=S.UniformGrid, PML=S.PML, GaussianPulse=S.GaussianPulse,
     Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
-    PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial)
+    PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
+    ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance)
 ORACLE = O.make_api()
 SMALL = [k for k, v in C.PLAIN_CASES.items() if not v.get("big") and k != "c1_full"]
+TILE_CONFIGS = [c for c in S.solver.kernel_configs() if c.startswith("tile")]
 
 
 def _compare(solver, key, manifest, fields=True):
@@ -115,6 +117,55 @@ def test_ade_autotune_then_steps(manifest):
     assert table["best"].startswith("tile")
     s.run_steps(case["steps"] - 10)
     _check_ade(s, "split_boxes_geom", manifest)
+
+
+@pytest.mark.parametrize("config", TILE_CONFIGS + ["auto", "col1", "cell"])
+@pytest.mark.parametrize("name", ["nu_stretch_blocks", "nu_regions_sdf"])
+def test_nonuniform_every_config(name, config, manifest):
+    """Nonuniform grids run the warp-tile kernels with per-face coefficients
+    and per-cell divergence scales; a configuration without them falls back
+    to the default warp tiles.  Fields and traces equal the reference's
+    update_velocity/pressure_nonuniform path."""
+    case = C.PLAIN_CASES[name]
+    s = C.build_case(API, case)
+    s.set_kernel(config, 3 if config.startswith("tile1") else 0)
+    s.run_steps(case["steps"] // 3)
+    s.run_steps(case["steps"] - case["steps"] // 3)
+    _compare(s, "plain_" + name, manifest)
+
+
+@pytest.mark.parametrize("config", ["tile_r1_w4", "tile1_r2_w8", "col4", "cell"])
+@pytest.mark.parametrize("name", ["abc_all_sources", "rad_pml_mix"])
+def test_plane_boundaries(name, config, manifest):
+    """Mur ABC and radiation-impedance planes after the fused step, sources
+    after them, stored planes carried across calls; reset() clears them."""
+    case = C.PLAIN_CASES[name]
+    s = C.build_case(API, case)
+    s.set_kernel(config)
+    s.run_steps(25)
+    s.reset()
+    for _ in range(5):
+        s.step()
+    s.run_steps(case["steps"] - 5)
+    _compare(s, "plain_" + name, manifest)
+    with pytest.raises(NotImplementedError):
+        s.add_boundary(S.PML(depth=2))  # a PML after plane boundaries
+    with pytest.raises(NotImplementedError):
+        S.BatchedSolver([s])
+
+
+def test_nonuniform_autotune_and_limits(manifest):
+    case = C.PLAIN_CASES["nu_stretch_low_end"]
+    s = C.build_case(API, case)
+    s.run_steps(7)
+    table = s.autotune(launches=2)
+    assert table["best"].startswith("tile")
+    s.run_steps(case["steps"] - 7)
+    _compare(s, "plain_nu_stretch_low_end", manifest)
+    with pytest.raises(NotImplementedError):
+        s.register_material(S.SimpleMaterial(name="m", _rho=1.2, _c=343.0, _poles=[]))
+    with pytest.raises(NotImplementedError):
+        S.BatchedSolver([s])
 
 
 def test_c1_quick_start_1000_steps(manifest):
@@ -266,9 +317,6 @@ def test_every_kernel_config_against_oracle(config):
         for f in ("p", "vx", "vy", "vz"):
             np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f"{config} {f}")
         np.testing.assert_array_equal(s.get_probe_data()["a"], ref.get_probe_data()["a"])
-
-
-TILE_CONFIGS = [c for c in S.solver.kernel_configs() if c.startswith("tile")]
 
 
 @pytest.mark.parametrize("config", TILE_CONFIGS)
