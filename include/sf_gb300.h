@@ -47,7 +47,9 @@ typedef struct {
 } sf_grid_desc;
 
 /* Source descriptor (core/solver.py:2413-2433): kind 0 = point at (a,b,c);
- * kind 1 = plane with axis a (0,1,2) at index b.  Sources inject into air
+ * kind 1 = plane with axis a (0,1,2) at index b; kind 2 = weighted cell
+ * list a (sf_plan_set_weighted_source) added to field b (0 p, 1 vx, 2 vy,
+ * 3 vz), a membrane source.  Sources inject into air
  * cells only, in the order given. */
 typedef struct {
     int32_t kind, a, b, c;
@@ -188,6 +190,15 @@ int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const 
  * scaled before the sum.  Steps run the warp-tile kernels; no ADE.  Both
  * NULL returns the plan to a uniform grid. */
 int sf_plan_set_nonuniform(sf_plan* plan, const float* const* cv_face, const float* const* inv_cell);
+
+/* Weighted cell list `slot` (0 .. SF_MAX_SOURCES-1) of a kind-2 source:
+ * after each step field[cells[q]] = float(double(field[cells[q]]) + value *
+ * weights[q]) for the air cells listed (the caller lists only air cells), as
+ * NumPy's p[mask] += value * weights[mask] (core/solver.py:2389-2412).  Host
+ * arrays of n; n = 0 clears the slot.  Kind-2 sources are injected after the
+ * step and its plane boundaries, with the other sources, in order. */
+int sf_plan_set_weighted_source(sf_plan* plan, int slot, int64_t n, const int64_t* cells,
+                                const double* weights);
 
 /* Plane boundary operations (at most SF_MAX_PLANE_OPS; n = 0 removes them)
  * and their stored planes, zeroed.  With any of them a step runs: the fused

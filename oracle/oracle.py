@@ -328,6 +328,78 @@ class PML:
         return sigma
 
 
+class _Membrane:
+    """Membrane sources (solver.py:210-755): mode-shape weights on the grid
+    plane nearest the centre, normalised to 1."""
+
+    source_type = "membrane"
+
+    def __init__(self, center, normal_axis, waveform, mode, injection_type="pressure"):
+        self.center, self.normal_axis, self.waveform = center, normal_axis, waveform
+        self.mode, self.injection_type, self._w = mode, injection_type, None
+
+    def _frame(self, grid):
+        X, Y, Z = np.meshgrid(grid.x_coords, grid.y_coords, grid.z_coords, indexing="ij")
+        ax = "xyz".index(self.normal_axis)
+        comps = [X - self.center[0], Y - self.center[1], Z - self.center[2]]
+        a, b = [c for q, c in enumerate(comps) if q != ax]
+        coords = (grid.x_coords, grid.y_coords, grid.z_coords)[ax]
+        k = int(np.argmin(np.abs(coords - self.center[ax])))
+        plane = np.zeros(grid.shape, dtype=bool)
+        idx = [slice(None)] * 3
+        idx[ax] = k
+        plane[tuple(idx)] = True
+        return a, b, plane
+
+    def weights(self, grid):
+        a, b, plane = self._frame(grid)
+        mask = plane & self._inside(a, b)
+        w = np.zeros(grid.shape, dtype=np.float64)
+        shape = np.abs(np.where(self._inside(a[mask], b[mask]), self._shape(a[mask], b[mask]),
+                                0.0))
+        mx = np.max(shape)
+        w[mask] = shape / mx if mx > 1e-10 else np.zeros_like(shape)
+        return w
+
+
+class CircularMembraneSource(_Membrane):
+    _Z = {(0, 1): 2.4048255576957727, (0, 2): 5.5200781102863115, (1, 1): 3.8317059702075125,
+          (1, 2): 7.0155866698156190, (2, 1): 5.1356223018406826, (2, 2): 8.4172441403998649}
+
+    def __init__(self, center, normal_axis, waveform, radius, mode=(0, 1),
+                 injection_type="pressure"):
+        super().__init__(center, normal_axis, waveform, mode, injection_type)
+        from scipy.special import jn_zeros
+        self.radius = radius
+        self.alpha = self._Z.get(tuple(mode)) or jn_zeros(mode[0], mode[1])[-1]
+
+    def _inside(self, a, b):
+        return np.sqrt(a**2 + b**2) <= self.radius
+
+    def _shape(self, a, b):
+        from scipy.special import j0, jv
+        rho = np.sqrt(a**2 + b**2) / self.radius
+        m = self.mode[0]
+        if m == 0:
+            return j0(self.alpha * rho)
+        return jv(m, self.alpha * rho) * np.cos(m * np.arctan2(b, a))
+
+
+class RectangularMembraneSource(_Membrane):
+    def __init__(self, center, normal_axis, waveform, size, mode=(1, 1),
+                 injection_type="pressure"):
+        super().__init__(center, normal_axis, waveform, mode, injection_type)
+        self.size = size
+
+    def _inside(self, a, b):
+        return (np.abs(a) <= self.size[0] / 2) & (np.abs(b) <= self.size[1] / 2)
+
+    def _shape(self, a, b):
+        m, n = self.mode
+        return (np.sin(m * np.pi * (a / self.size[0] + 0.5))
+                * np.sin(n * np.pi * (b / self.size[1] + 0.5)))
+
+
 class ABCFirstOrder:
     """_boundaries.py:420-527, the same NumPy operations (the Mur
     coefficient is a NumPy float64, so each plane update runs in FP64 and is
@@ -801,6 +873,17 @@ class FDTDSolver:
                 b.apply_pressure(self)
         g = _ptr(self.geometry.view(np.uint8))
         for s in self._sources:
+            if s.source_type == "membrane":  # solver.py:2389-2412
+                val = s.waveform.waveform(np.array([self._time]), self.dt)[0]
+                if s._w is None:
+                    s._w = s.weights(self.grid)
+                mask = (s._w > 0) & self.geometry
+                if s.injection_type == "pressure":
+                    f = p
+                else:
+                    f = {"x": vx, "y": vy, "z": vz}[s.normal_axis]
+                f[mask] += val * s._w[mask]
+                continue
             val = float(s.waveform(np.array([self._time]), self.dt)[0])
             kind, a, b_, c = self._src_desc(s)
             F("inject")(_ptr(p), g, nx, ny, nz, kind, a, b_, c, val)
@@ -820,7 +903,8 @@ class FDTDSolver:
         """n steps of the plain path through one C call (no ADE, one PML);
         with ADE materials or microphones, step by step."""
         if (self._materials or getattr(self, "_mics", None) or self._nu is not None
-                or any(not isinstance(b, PML) for b in self._boundaries)):
+                or any(not isinstance(b, PML) for b in self._boundaries)
+                or any(s.source_type == "membrane" for s in self._sources)):
             for _ in range(n):
                 self.step()
             return
@@ -878,6 +962,8 @@ def make_api():
     return types.SimpleNamespace(
         FDTDSolver=FDTDSolver, UniformGrid=UniformGrid, NonuniformGrid=NonuniformGrid, PML=PML,
         ABCFirstOrder=ABCFirstOrder, RadiationImpedance=RadiationImpedance,
+        CircularMembraneSource=CircularMembraneSource,
+        RectangularMembraneSource=RectangularMembraneSource,
         GaussianPulse=GaussianPulse,
         Box=Box, Sphere=Sphere, Cylinder=Cylinder, Union=Union, Intersection=Intersection,
         Difference=Difference, HelmholtzResonator=HelmholtzResonator, Pole=Pole,

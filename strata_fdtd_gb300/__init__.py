@@ -16,6 +16,7 @@ from .boundaries import PML, ABCFirstOrder, RadiationImpedance, RigidBoundary
 from .grid import NonuniformGrid, UniformGrid
 from .microphones import Microphone
 from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
+from .membranes import CircularMembraneSource, MembraneSource, RectangularMembraneSource
 from .resonator import HelmholtzResonator, helmholtz_array
 from .sdf import (Box, CSGNode, Cylinder, Difference, Intersection, Scale, SDFPrimitive, Sphere,
                   Translate, Union)
@@ -29,5 +30,6 @@ __all__ = [
     "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale",
     "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",
-    "NativeError", "BatchedSolver", "DifferentiableSolver",
+    "NativeError", "BatchedSolver", "DifferentiableSolver", "MembraneSource",
+    "CircularMembraneSource", "RectangularMembraneSource",
 ]

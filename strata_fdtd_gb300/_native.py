@@ -128,6 +128,7 @@ SIGNATURES = {
     "sf_plan_set_microphones_ex": (_I, [_P, _I, _P, _P, _P]),
     "sf_plan_set_nonuniform": (_I, [_P, _P, _P]),
     "sf_plan_set_plane_boundaries": (_I, [_P, _I, _P]),
+    "sf_plan_set_weighted_source": (_I, [_P, _I, _I64, _P, _P]),
     "sf_energy_scratch_doubles": (_I64, [_P]),
     "sf_plan_energy": (_I, [_P, _D, _D, _D, _P, _P, _P]),
     "sf_plan_energy_noalloc": (_I, [_P, _D, _D, _D, _P, _P]),

@@ -35,6 +35,8 @@ class BatchedSolver:
         if any(getattr(s, "_plane_bc_dirty", False) or
                any(hasattr(b, "plane_ops") for b in s._boundaries) for s in solvers):
             raise NotImplementedError("plane boundaries are stepped by single-solver runs only")
+        if any(src.source_type == "membrane" for s in solvers for src in s._sources):
+            raise NotImplementedError("membrane sources are stepped by single-solver runs only")
         if any(not s.grid.is_uniform for s in solvers):
             raise NotImplementedError("nonuniform grids are stepped by single-solver runs only")
         self.solvers = list(solvers)

@@ -127,6 +127,10 @@ int sf_plan_destroy(sf_plan* P) {
     cudaFree(P->mic_field);
     cudaFree(P->nu);
     cudaFree(P->plane_prev);
+    for (int q = 0; q < SF_MAX_SOURCES; ++q) {
+        cudaFree(P->wsrc_cells[q]);
+        cudaFree(P->wsrc_w[q]);
+    }
     delete P;
     return 0;
 }
@@ -210,6 +214,29 @@ int sf_plan_set_nonuniform(sf_plan* P, const float* const* cv_face, const float*
     return 0;
 }
 
+int sf_plan_set_weighted_source(sf_plan* P, int slot, int64_t n, const int64_t* cells,
+                                const double* weights) {
+    if (!P) return sf_fail("sf_plan_set_weighted_source: NULL plan");
+    if (slot < 0 || slot >= SF_MAX_SOURCES || n < 0 || (n > 0 && (!cells || !weights)))
+        return sf_fail("sf_plan_set_weighted_source: bad slot or table");
+    for (int64_t q = 0; q < n; ++q)
+        if (cells[q] < 0 || cells[q] >= P->n)
+            return sf_fail("sf_plan_set_weighted_source: cell outside the grid");
+    DeviceGuard g(P->device);
+    cudaFree(P->wsrc_cells[slot]);
+    cudaFree(P->wsrc_w[slot]);
+    P->wsrc_cells[slot] = nullptr;
+    P->wsrc_w[slot] = nullptr;
+    P->wsrc_n[slot] = 0;
+    if (n == 0) return 0;
+    SF_CUDA_OK(cudaMalloc(&P->wsrc_cells[slot], sizeof(long long) * n));
+    SF_CUDA_OK(cudaMalloc(&P->wsrc_w[slot], sizeof(double) * n));
+    SF_CUDA_OK(cudaMemcpy(P->wsrc_cells[slot], cells, sizeof(long long) * n, cudaMemcpyHostToDevice));
+    SF_CUDA_OK(cudaMemcpy(P->wsrc_w[slot], weights, sizeof(double) * n, cudaMemcpyHostToDevice));
+    P->wsrc_n[slot] = n;
+    return 0;
+}
+
 int sf_plan_set_plane_boundaries(sf_plan* P, int n, const sf_plane_bc* ops) {
     if (!P) return sf_fail("sf_plan_set_plane_boundaries: NULL plan");
     if (n < 0 || n > SF_MAX_PLANE_OPS || (n > 0 && !ops))
@@ -267,8 +294,11 @@ int sf_plan_set_sources(sf_plan* P, int n, const sf_source* s) {
         } else if (s[q].kind == 1) {
             if (s[q].a < 0 || s[q].a > 2 || s[q].b < 0 || s[q].b >= dims[s[q].a])
                 return sf_fail("sf_plan_set_sources: plane source outside the grid");
+        } else if (s[q].kind == 2) {
+            if (s[q].a < 0 || s[q].a >= SF_MAX_SOURCES || s[q].b < 0 || s[q].b > 3)
+                return sf_fail("sf_plan_set_sources: weighted source needs a slot and a field");
         } else {
-            return sf_fail("sf_plan_set_sources: kind must be 0 (point) or 1 (plane)");
+            return sf_fail("sf_plan_set_sources: kind must be 0 (point), 1 (plane) or 2 (weighted)");
         }
     }
     P->src.n = n;
@@ -536,26 +566,36 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
     const int cfg = effective_config(P, a);
     const int ich = chunk_for(P, cfg);
     const bool mics = mic_trace != nullptr && P->n_mic > 0;
+    // plane boundaries or weighted sources: sources move after the fused kernel
+    bool deferred = P->n_plane > 0;
+    for (int q = 0; q < P->src.n; ++q) deferred = deferred || P->src.s[q].kind == 2;
     for (int64_t s = 0; s < n_steps; ++s) {
         set_io(P, a, P->cur);
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
         a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
         a.reverse = (int)(P->steps_done & 1);
-        if (P->n_plane == 0) {
+        if (!deferred) {
             if (int rc = launch_step_split(P, cfg, ich, a, P->src, st)) return rc;
-        } else {  // step, plane boundaries in order, then the sources
+        } else {  // step, plane boundaries in order, then the sources in order
             const SfSources none{};
             if (int rc = launch_step_split(P, cfg, ich, a, none, st)) return rc;
-            float* po = P->f[1 - P->cur][0];
+            float* const* out = P->f[1 - P->cur];
             for (int q = 0; q < P->n_plane; ++q)
-                if (int rc = sf_launch_plane_bc(po, P->plane_prev + P->plane_off[q][0],
+                if (int rc = sf_launch_plane_bc(out[0], P->plane_prev + P->plane_off[q][0],
                                                 P->plane_prev + P->plane_off[q][1],
                                                 P->plane_ops[q], P->d.nx, P->d.ny, P->d.nz, st))
                     return rc;
-            for (int q = 0; q < P->src.n; ++q)
-                if (int rc = sf_launch_inject(po, P->flags, P->src.s[q], a.src_val + q, P->d.nx,
-                                              P->d.ny, P->d.nz, st))
-                    return rc;
+            for (int q = 0; q < P->src.n; ++q) {
+                const sf_source& S = P->src.s[q];
+                int rc;
+                if (S.kind == 2)
+                    rc = sf_launch_inject_weighted(out[S.b], P->wsrc_cells[S.a], P->wsrc_w[S.a],
+                                                   P->wsrc_n[S.a], a.src_val + q, st);
+                else
+                    rc = sf_launch_inject(out[0], P->flags, S, a.src_val + q, P->d.nx, P->d.ny,
+                                          P->d.nz, st);
+                if (rc) return rc;
+            }
         }
         P->cur = 1 - P->cur;
         ++P->steps_done;

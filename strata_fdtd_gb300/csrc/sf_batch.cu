@@ -583,6 +583,8 @@ int sf_batch_add(sf_batch* B, sf_plan* P, int64_t n_steps, const double* src_val
     if (P->device != B->device) return sf_fail("sf_batch_add: plan on another device");
     if (P->nu) return sf_fail("sf_batch_add: nonuniform grids are stepped alone");
     if (P->n_plane) return sf_fail("sf_batch_add: plane boundaries are stepped alone");
+    for (int q = 0; q < P->src.n; ++q)
+        if (P->src.s[q].kind == 2) return sf_fail("sf_batch_add: membrane sources are stepped alone");
     if (n_steps < 0) return sf_fail("sf_batch_add: negative step count");
     if (P->src.n > 0 && n_steps > 0 && !src_values_dev)
         return sf_fail("sf_batch_add: sources need src_values");

@@ -44,6 +44,8 @@ int sf_launch_plane_bc(float* p, float* prev_lo, float* prev_hi, const sf_plane_
                        int ny, int nz, cudaStream_t st);
 int sf_launch_inject(float* p, const uint8_t* flags, const sf_source& s, const double* val, int nx,
                      int ny, int nz, cudaStream_t st);
+int sf_launch_inject_weighted(float* f, const long long* cells, const double* w, long long n,
+                              const double* val, cudaStream_t st);
 int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const float* vz,
                          const int* field, const long long* idx, const float* w, int n, float* out,
                          cudaStream_t st);

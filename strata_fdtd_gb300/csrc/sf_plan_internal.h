@@ -36,6 +36,9 @@ struct sf_plan {
     sf_plane_bc plane_ops[SF_MAX_PLANE_OPS];
     float* plane_prev = nullptr;        // owned: stored planes, low then high per op
     long long plane_off[SF_MAX_PLANE_OPS][2];
+    long long* wsrc_cells[SF_MAX_SOURCES] = {nullptr};  // owned, weighted (membrane) sources
+    double* wsrc_w[SF_MAX_SOURCES] = {nullptr};
+    long long wsrc_n[SF_MAX_SOURCES] = {0};
 };
 
 // Planes per block: enough (j,k)-tile x i-chunk blocks for about four waves

@@ -278,6 +278,17 @@ __global__ void k_inject(float* __restrict__ p, const uint8_t* __restrict__ flag
     p[cell] = __double2float_rn(d_add((double)p[cell], *val));
 }
 
+// A weighted (membrane) source: f[cells[t]] = float(double(f) + value * w[t])
+// (core/solver.py:2389-2412, NumPy's float64 product and sum, one rounding).
+__global__ void k_inject_weighted(float* __restrict__ f, const long long* __restrict__ cells,
+                                  const double* __restrict__ w, long long n,
+                                  const double* __restrict__ val) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const long long c = cells[t];
+    f[c] = __double2float_rn(d_add((double)f[c], d_mul(*val, w[t])));
+}
+
 // Face flags from the geometry mask (boundaries.cpp:13-64 rule).
 __global__ void k_build_flags(const uint8_t* __restrict__ geom, uint8_t* __restrict__ flags,
                               int nx, int ny, int nz) {
@@ -413,6 +424,13 @@ int sf_launch_inject(float* p, const uint8_t* flags, const sf_source& s, const d
     k_inject<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, flags, s.kind, s.a, s.b, s.c, val, nx,
                                                           ny, nz);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_inject launch failed");
+}
+
+int sf_launch_inject_weighted(float* f, const long long* cells, const double* w, long long n,
+                              const double* val, cudaStream_t st) {
+    if (n <= 0) return 0;
+    k_inject_weighted<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(f, cells, w, n, val);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_inject_weighted launch failed");
 }
 
 int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const float* vz,

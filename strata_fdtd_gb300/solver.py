@@ -348,6 +348,7 @@ class FDTDSolver:
         self._geometry_set = True
         _native.check(self._lib.sf_plan_set_geometry(self._plan, dev.data_ptr(), self._stream()),
                       "sf_plan_set_geometry")
+        self._src_dirty = True  # membrane sources inject into air cells only
 
     def set_geometry_sdf(self, solid: SDFPrimitive) -> None:
         """Geometry from a solid's SDF: air is the complement of the solid
@@ -358,6 +359,7 @@ class FDTDSolver:
         self._geometry_set = True
         _native.check(self._lib.sf_plan_set_geometry(self._plan, dev.data_ptr(), self._stream()),
                       "sf_plan_set_geometry")
+        self._src_dirty = True  # membrane sources inject into air cells only
 
     # --------------------------------------------------------- sources/probes
     def _to_index(self, pos, what):
@@ -372,8 +374,15 @@ class FDTDSolver:
         return pos
 
     def add_source(self, source) -> None:
-        """core/solver.py:1782-1841 (point and plane GaussianPulse sources)."""
-        if source.source_type == "point":
+        """core/solver.py:1782-1841: point and plane GaussianPulse sources and
+        membrane sources (centre inside the physical extent)."""
+        if source.source_type == "membrane":
+            extent = self._grid.physical_extent()
+            for ax, (v, e) in enumerate(zip(source.center, extent)):
+                if not 0 <= v <= e:
+                    raise ValueError(f"Membrane center {'xyz'[ax]}={v:.4f}m is outside grid "
+                                     f"(0-{e:.4f}m)")
+        elif source.source_type == "point":
             source.position = self._to_index(source.position, "Source")
             if any(not 0 <= int(v) < n for v, n in zip(source.position, self.shape)):
                 raise ValueError(f"Source position {source.position} is outside the grid")
@@ -575,9 +584,21 @@ class FDTDSolver:
             for q, s in enumerate(self._sources):
                 if s.source_type == "point":
                     tab[q].kind, (tab[q].a, tab[q].b, tab[q].c) = 0, tuple(int(v) for v in s.position)
-                else:
+                elif s.source_type == "plane":
                     tab[q].kind, tab[q].a, tab[q].b, tab[q].c = 1, int(s.position["axis"]), int(
                         s.position["index"]), 0
+                else:  # membrane: weighted air cells of its plane (core/solver.py:2389-2412)
+                    if s._cached_weights is None:
+                        s._check_grid_alignment(self._grid)
+                        s._cached_weights = s.get_injection_weights(self._grid)
+                        s._cached_mask = s._cached_weights > 0
+                    cells = np.flatnonzero(s._cached_mask & self._geometry).astype(np.int64)
+                    w = np.ascontiguousarray(s._cached_weights.ravel()[cells], dtype=np.float64)
+                    _native.check(self._lib.sf_plan_set_weighted_source(
+                        self._plan, q, len(cells), cells.ctypes.data, w.ctypes.data),
+                        "sf_plan_set_weighted_source")
+                    field = 0 if s.injection_type == "pressure" else 1 + "xyz".index(s.normal_axis)
+                    tab[q].kind, tab[q].a, tab[q].b, tab[q].c = 2, q, field, 0
             _native.check(self._lib.sf_plan_set_sources(self._plan, len(self._sources),
                                                         ctypes.addressof(tab)), "sf_plan_set_sources")
             self._src_dirty = False
@@ -619,7 +640,8 @@ class FDTDSolver:
         t = self._time
         for q in range(n):
             for s, src in enumerate(self._sources):
-                vals[q, s] = src.waveform(np.array([t]), self.dt)[0]
+                wf = src.waveform if src.source_type == "membrane" else src
+                vals[q, s] = wf.waveform(np.array([t]), self.dt)[0]
             t += self.dt
         return vals
 

@@ -178,6 +178,23 @@ PLAIN_CASES = {
         probes=[("hi", (39, 10, 12)), ("lo", (0, 10, 12)), ("zl", (20, 10, 0))],
         steps=160, store_fields=True,
     ),
+    "membranes": dict(
+        # membrane sources: a circular (0,1) disc on a z plane, a circular
+        # (1,1) disc injecting normal velocity on an x plane, a rectangular
+        # (1,2) panel on a y plane, and a point source overlapping the disc
+        # (source order), with solids cutting into the membranes
+        shape=(36, 32, 40), res=1e-3, courant=0.5, pml=dict(depth=4),
+        geometry=dict(kind="blocks", seed=61, n_boxes=2, n_spheres=1),
+        sources=[("circle", dict(center=(0.018, 0.016, 0.0085), normal_axis="z",
+                                 radius=0.007, mode=(0, 1)), 8000.0, 1.0),
+                 ("point", (18, 16, 8), 11000.0, 0.5),
+                 ("circle", dict(center=(0.0253, 0.015, 0.021), normal_axis="x", radius=0.006,
+                                 mode=(1, 1), injection_type="velocity"), 9000.0, 0.002),
+                 ("rect", dict(center=(0.017, 0.0245, 0.02), normal_axis="y",
+                               size=(0.012, 0.009), mode=(1, 2)), 12000.0, 0.7)],
+        probes=[("a", (18, 16, 20)), ("b", (10, 8, 30))],
+        steps=120, store_fields=True,
+    ),
     "c1_full": dict(
         # the reference quick start, 100^3 x 1000 steps (hashes + traces only)
         shape=(100, 100, 100), res=1e-3, courant=0.5, pml=dict(depth=10),
@@ -384,9 +401,15 @@ def build_case(api, case, ade=False):
     for kind, pos, f, a in case.get("sources", []):
         if kind == "point":
             solver.add_source(api.GaussianPulse(position=pos, frequency=f, amplitude=a))
-        else:
+        elif kind == "plane":
             solver.add_source(api.GaussianPulse(position=dict(pos), frequency=f, amplitude=a,
                                                 source_type="plane"))
+        else:  # membrane: pos = constructor options, the waveform a GaussianPulse
+            opts = dict(pos)
+            cls = (api.CircularMembraneSource if kind == "circle"
+                   else api.RectangularMembraneSource)
+            wf = api.GaussianPulse(position=(0, 0, 0), frequency=f, amplitude=a)
+            solver.add_source(cls(waveform=wf, **opts))
     probes = case.get("probes", [])
     if probes == "c2":
         probes = c2_probes(solver.geometry)

@@ -62,6 +62,8 @@ def load_reference():
         NonuniformGrid=sys.modules["strata_fdtd.core.grid"].NonuniformGrid,
         ABCFirstOrder=sys.modules["strata_fdtd.boundaries"].ABCFirstOrder,
         RadiationImpedance=sf.RadiationImpedance,
+        CircularMembraneSource=sys.modules["strata_fdtd.core.solver"].CircularMembraneSource,
+        RectangularMembraneSource=sys.modules["strata_fdtd.core.solver"].RectangularMembraneSource,
         GaussianPulse=sf.GaussianPulse, Box=sdf.Box, Sphere=sdf.Sphere,
         Cylinder=sdf.Cylinder, Union=sdf.Union, Intersection=sdf.Intersection,
         Difference=sdf.Difference, HelmholtzResonator=resonator.HelmholtzResonator,

@@ -165,3 +165,28 @@ def test_nonuniform_grid_host_values(manifest):
     info = manifest["plain_nu_stretch_blocks"]
     assert (dt, cvb, cpb) == (info["dt"], info["coeff_v"], info["coeff_p"])
     assert info["uniform"] is False
+
+
+def test_membrane_weights_match_oracle():
+    """Mode-shape weights of the membrane sources (Bessel discs, sine
+    rectangles, every normal axis, a nonuniform grid), product vs oracle
+    restatement (the membrane golden pins the oracle to the reference)."""
+    from oracle import oracle as O
+
+    grids = [(S.UniformGrid((36, 32, 40), 1e-3), O.UniformGrid((36, 32, 40), 1e-3)),
+             (S.NonuniformGrid.from_stretch((30, 26, 34), 1e-3, 1.04, 1.0, 1.06),
+              O.NonuniformGrid.from_stretch((30, 26, 34), 1e-3, 1.04, 1.0, 1.06))]
+    wf = S.GaussianPulse(position=(0, 0, 0), frequency=1000.0)
+    for g, og in grids:
+        for ax in "xyz":
+            for mode in ((0, 1), (1, 1), (2, 2), (3, 1)):
+                a = S.CircularMembraneSource(center=(0.015, 0.013, 0.017), normal_axis=ax,
+                                             radius=0.0065, mode=mode, waveform=wf)
+                b = O.CircularMembraneSource((0.015, 0.013, 0.017), ax, wf, 0.0065, mode=mode)
+                np.testing.assert_array_equal(a.get_injection_weights(g), b.weights(og))
+            for mode in ((1, 1), (1, 2), (3, 2)):
+                a = S.RectangularMembraneSource(center=(0.014, 0.012, 0.016), normal_axis=ax,
+                                                size=(0.01, 0.007), mode=mode, waveform=wf)
+                b = O.RectangularMembraneSource((0.014, 0.012, 0.016), ax, wf, (0.01, 0.007),
+                                                mode=mode)
+                np.testing.assert_array_equal(a.get_injection_weights(g), b.weights(og))

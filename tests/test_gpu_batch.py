@@ -21,7 +21,9 @@ API = types.SimpleNamespace(
     Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
     PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
-    ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance)
+    ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance,
+    CircularMembraneSource=S.CircularMembraneSource,
+    RectangularMembraneSource=S.RectangularMembraneSource)
 
 MIX = [("plain", "c1_tiny"), ("plain", "blocks_odd"), ("plain", "plane_yz_geom"),
        ("plain", "impulse_default_coeffs"), ("ade", "debye_2pole"), ("ade", "lorentz_mixed_geom"),

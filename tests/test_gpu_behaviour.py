@@ -1,0 +1,179 @@
+"""Behaviour of the GPU solver as a drop-in for the reference API: physical
+properties of the scheme (CFL step, propagation speed, energy in a closed
+box, PML and Mur absorption, solids, cavity modes) and the solver controls
+(run durations, reset, snapshots, energy tracking and reports, frequency
+response).  The reference's own tests check the same behaviours
+(tests/test_fdtd.py); the set-ups and tolerances here are this project's."""
+import warnings
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import strata_fdtd_gb300 as S  # noqa: E402
+
+C_AIR, RHO = 343.0, 1.204
+
+
+def _solver(shape=(40, 40, 40), res=1e-3, courant=0.5, **kw):
+    return S.FDTDSolver(grid=S.UniformGrid(shape, res), c=C_AIR, rho=RHO, courant=courant, **kw)
+
+
+def test_time_step_is_the_cfl_limit_times_courant():
+    for res, courant in ((1e-3, 0.5), (2e-3, 0.9), (5e-4, 0.3)):
+        s = _solver((10, 10, 10), res, courant)
+        assert s.dt == pytest.approx(courant * res / (C_AIR * np.sqrt(3)), rel=1e-15)
+        assert s.dt * C_AIR * np.sqrt(3) / res <= 1.0
+
+
+def test_pulse_travels_at_the_speed_of_sound():
+    """The delay between two probes 40 cells apart on the source's axis
+    (cross-correlation peak) matches c within 3 %."""
+    s = _solver((150, 40, 40), courant=0.5)
+    s.add_boundary(S.PML(depth=8))
+    s.add_source(S.GaussianPulse(position=(20, 20, 20), frequency=15000.0))
+    s.add_probe("a", (50, 20, 20))
+    s.add_probe("b", (90, 20, 20))
+    s.run_steps(900)
+    a, b = (s.get_probe_data()[k].astype(np.float64) for k in ("a", "b"))
+    lag = np.argmax(np.correlate(b, a, mode="full")) - (len(a) - 1)
+    speed = 40e-3 / (lag * s.dt)
+    assert speed == pytest.approx(C_AIR, rel=0.03)
+
+
+def test_energy_stays_bounded_in_a_closed_box():
+    """Rigid walls all round, no absorber: the discrete energy neither grows
+    nor decays by more than a few percent once the source has stopped."""
+    s = _solver((30, 30, 30))
+    s.p[15, 15, 15] = 1.0
+    s.run_steps(20, track_energy=True)
+    s.run_steps(400, track_energy=True, energy_sample_interval=20)
+    e = np.array([v for _, _, v in s.get_energy_history()[1:]])
+    assert np.all(np.isfinite(e)) and e.min() > 0
+    assert e.max() / e.min() < 1.5
+    assert 0.67 < e[-1] / e[0] < 1.5
+
+
+def test_pml_drains_the_energy():
+    s = _solver((40, 40, 40))
+    s.add_boundary(S.PML(depth=8))
+    s.p[20, 20, 20] = 1.0
+    s.run_steps(600, track_energy=True, energy_sample_interval=50)
+    rep = s.energy_report()
+    assert rep["conservation_status"] == "decaying"
+    assert rep["final_energy"] < 0.05 * rep["max_energy"]
+
+
+def test_pml_and_mur_reduce_the_echo_from_the_far_wall():
+    def echo(boundary):
+        s = _solver((100, 24, 24))
+        if boundary is not None:
+            s.add_boundary(boundary)
+        s.add_source(S.GaussianPulse(position=(30, 12, 12), frequency=15000.0))
+        s.add_probe("p", (30, 12, 12))
+        s.run_steps(700)
+        tr = s.get_probe_data()["p"]
+        return np.abs(tr[350:]).max()  # after the direct pulse, while echoes return
+    rigid = echo(None)
+    assert echo(S.PML(depth=10)) < 0.5 * rigid
+    assert echo(S.ABCFirstOrder()) < rigid
+
+
+def test_solids_block_propagation_and_hold_zero_pressure():
+    s = _solver((60, 30, 30))
+    geom = np.ones(s.shape, dtype=bool)
+    geom[30:34, :, :] = False  # a full wall across x
+    s.set_geometry(geom)
+    s.add_source(S.GaussianPulse(position=(15, 15, 15), frequency=10000.0))
+    s.add_probe("behind", (45, 15, 15))
+    s.run_steps(300)
+    assert np.abs(s.get_probe_data()["behind"]).max() == 0.0
+    assert np.all(s.p[30:34] == 0.0)
+    assert np.all(s.vx[29:34] == 0.0)  # faces into and inside the wall
+
+
+def test_cavity_fundamental_mode():
+    """A rigid 60 x 20 x 20 mm box rings at c / (2 L) along its long axis."""
+    s = _solver((60, 20, 20), courant=0.5)
+    s.add_source(S.GaussianPulse(position=(3, 10, 10), frequency=6000.0))
+    s.add_probe("end", (57, 10, 10))
+    s.run_steps(16000)
+    f, mag = s.get_frequency_response("end")
+    band = (f > 1500) & (f < 4500)
+    peak = f[band][np.argmax(mag[band])]
+    assert peak == pytest.approx(C_AIR / (2 * 0.060), rel=0.05)
+
+
+def test_run_duration_sets_the_step_count_and_time():
+    s = _solver((16, 16, 16))
+    s.run(duration=50.5 * s.dt)
+    assert s.step_count == 51
+    assert s.time == pytest.approx(51 * s.dt, rel=1e-12)
+    assert s.get_sample_rate() == pytest.approx(1.0 / s.dt)
+
+
+def test_reset_clears_fields_traces_and_history():
+    s = _solver((16, 16, 16))
+    s.add_source(S.GaussianPulse(position=(8, 8, 8), frequency=20000.0))
+    s.add_probe("c", (8, 8, 8))
+    s.run_steps(40, track_energy=True)
+    assert np.abs(s.p).max() > 0
+    s.reset()
+    assert s.step_count == 0 and s.time == 0.0
+    assert np.all(s.p == 0) and np.all(s.vx == 0)
+    assert len(s.get_probe_data()["c"]) == 0
+    assert s.get_energy_history() == []
+    s.run_steps(40)
+    a = s.get_probe_data()["c"].copy()
+    s.reset()
+    s.run_steps(40)
+    np.testing.assert_array_equal(s.get_probe_data()["c"], a)  # deterministic
+
+
+def test_snapshots_at_the_interval_with_centred_velocity():
+    s = _solver((16, 16, 16))
+    s.add_source(S.GaussianPulse(position=(8, 8, 8), frequency=20000.0))
+    s.enable_snapshots(interval=10, capture_velocity=True)
+    s.run_steps(35)
+    snaps = s.get_snapshots()
+    assert len(snaps) == 4  # steps 0, 10, 20, 30
+    t, p = snaps[-1]
+    assert p.shape == s.shape and t == pytest.approx(30 * s.dt, rel=1e-12)
+    vs = s.get_velocity_snapshots()
+    assert len(vs) == 4 and vs[-1][1].shape == s.shape
+
+
+def test_energy_report_and_drift_warning():
+    s = _solver((20, 20, 20), warn_energy_drift=True, energy_drift_threshold=0.01)
+    s.add_source(S.GaussianPulse(position=(10, 10, 10), frequency=20000.0))
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        s.run_steps(60, track_energy=True)
+    assert any("Energy drift" in str(x.message) for x in w)  # the source adds energy
+    rep = s.energy_report()
+    assert rep["n_samples"] == 61 and rep["conservation_status"] == "growing"
+    with pytest.raises(ValueError):
+        _solver((8, 8, 8)).energy_report()
+
+
+def test_frequency_response_bins():
+    s = _solver((16, 16, 16))
+    s.add_source(S.GaussianPulse(position=(8, 8, 8), frequency=20000.0))
+    s.add_probe("c", (8, 8, 8))
+    s.run_steps(100)
+    f, mag = s.get_frequency_response("c")
+    assert len(f) == len(mag) == 128 // 2 + 1
+    assert f[-1] == pytest.approx(0.5 / s.dt)
+
+
+def test_duplicate_names_and_bad_positions_are_rejected():
+    s = _solver((16, 16, 16))
+    s.add_probe("a", (1, 1, 1))
+    with pytest.raises(ValueError):
+        s.add_probe("a", (2, 2, 2))
+    with pytest.raises(ValueError):
+        s.add_source(S.GaussianPulse(position=(16, 0, 0), frequency=1000.0))
+    with pytest.raises(ValueError):
+        s.set_geometry(np.ones((15, 16, 16), dtype=bool))

@@ -25,7 +25,9 @@ API = types.SimpleNamespace(
     Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
     PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
-    ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance)
+    ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance,
+    CircularMembraneSource=S.CircularMembraneSource,
+    RectangularMembraneSource=S.RectangularMembraneSource)
 ORACLE = O.make_api()
 SMALL = [k for k, v in C.PLAIN_CASES.items() if not v.get("big") and k != "c1_full"]
 TILE_CONFIGS = [c for c in S.solver.kernel_configs() if c.startswith("tile")]
@@ -152,6 +154,20 @@ def test_plane_boundaries(name, config, manifest):
         s.add_boundary(S.PML(depth=2))  # a PML after plane boundaries
     with pytest.raises(NotImplementedError):
         S.BatchedSolver([s])
+
+
+def test_membranes_step_by_step_and_limits(manifest):
+    """Membrane sources injected after the fused step (velocity injection
+    included), step by step with a host read in the middle."""
+    case = C.PLAIN_CASES["membranes"]
+    s = C.build_case(API, case)
+    for q in range(case["steps"]):
+        s.step()
+        if q == 37:
+            _ = s.vx[0, 0, 0]
+    _compare(s, "plain_membranes", manifest)
+    with pytest.raises(NotImplementedError):
+        S.BatchedSolver([C.build_case(API, case)])
 
 
 def test_nonuniform_autotune_and_limits(manifest):
