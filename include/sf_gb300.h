@@ -222,7 +222,9 @@ int sf_plan_set_ade_box(sf_plan* plan, const int32_t* lo, const int32_t* hi);
  * then thread columns along i ("col*": vector width, block rows, register
  * cap, streaming stores) and warp tiles with lane-shuffled neighbours
  * ("tile_*": float4 lanes, needs nz % 4 == 0 and 16-byte aligned fields;
- * "tile1_*": one cell per lane), as named by sf_kernel_config_name.  A
+ * "tile1_*": one cell per lane; "*_wb": ordinary write-back stores of the
+ * new state instead of evict-first ones), as named by
+ * sf_kernel_config_name.  A
  * configuration the grid cannot take falls back to scalar columns.  i_chunk
  * = planes per block (0 = automatic).  With ADE poles the warp-tile
  * configurations split each step with the per-cell kernel (see

@@ -54,7 +54,7 @@ __device__ __forceinline__ SfTileIo tile_io(const SfStepArgs& a) {
     return io;
 }
 
-template <bool GEOM, int R, int W, int MINB, bool PF, bool NU>
+template <bool GEOM, int R, int W, int MINB, bool PF, bool NU, bool WB>
 __global__ void __launch_bounds__(32 * W, MINB) k_step_tile(SfStepArgs a, SfSources src, int ich) {
     const int jw = (blockIdx.y * W + threadIdx.y) * (4 * R);  // the warp's first row
     const int chunk = a.reverse ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z;
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(32 * W, MINB) k_step_tile(SfStepArgs a, SfSour
     }
     if (jw >= a.ny) return;  // the whole warp is past the grid (no block barrier follows)
     if (in_skip(a, i0, blockIdx.y * W * 4 * R, blockIdx.x * 32)) return;  // the ADE kernel's cells
-    tile4_run<GEOM, R, PF, NU>(tile_io(a), src, i0, i1, jw, blockIdx.x * 32);
+    tile4_run<GEOM, R, PF, NU, WB>(tile_io(a), src, i0, i1, jw, blockIdx.x * 32);
 }
 
 // Scalar warp tiles: 32 lanes along k, R rows per lane, W warps along j.
@@ -100,17 +100,17 @@ int launch1(const SfStepArgs& a, const SfSources& src, bool geom, int ich, cudaS
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step_tile1 launch failed");
 }
 
-template <int R, int W, int MINB, bool PF>
+template <int R, int W, int MINB, bool PF, bool WB = false>
 int launch(const SfStepArgs& a, const SfSources& src, bool geom, int ich, cudaStream_t st) {
     dim3 blk(32, W, 1);
     const int rows = 4 * R * W;
     dim3 grd((a.nz + 31) / 32, (a.ny + rows - 1) / rows, (a.nx + ich - 1) / ich);
     if (a.nu_cv[0] != nullptr) {
-        if (geom) k_step_tile<true, R, W, MINB, PF, true><<<grd, blk, 0, st>>>(a, src, ich);
-        else k_step_tile<false, R, W, MINB, PF, true><<<grd, blk, 0, st>>>(a, src, ich);
+        if (geom) k_step_tile<true, R, W, MINB, PF, true, WB><<<grd, blk, 0, st>>>(a, src, ich);
+        else k_step_tile<false, R, W, MINB, PF, true, WB><<<grd, blk, 0, st>>>(a, src, ich);
     } else {
-        if (geom) k_step_tile<true, R, W, MINB, PF, false><<<grd, blk, 0, st>>>(a, src, ich);
-        else k_step_tile<false, R, W, MINB, PF, false><<<grd, blk, 0, st>>>(a, src, ich);
+        if (geom) k_step_tile<true, R, W, MINB, PF, false, WB><<<grd, blk, 0, st>>>(a, src, ich);
+        else k_step_tile<false, R, W, MINB, PF, false, WB><<<grd, blk, 0, st>>>(a, src, ich);
     }
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step_tile launch failed");
 }
@@ -136,6 +136,8 @@ const SfTileConfig kSfTileConfigs[] = {
     {1, 2, 8, 4, 0, "tile1_r2_w8"},
     {1, 1, 8, 4, 1, "tile1_r1_w8_pf"},
     {1, 2, 4, 6, 1, "tile1_r2_w4_pf"},
+    {4, 1, 4, 6, 0, "tile_r1_w4_m6_wb"},
+    {4, 1, 8, 4, 0, "tile_r1_w8_wb"},
 };
 const int kSfTileConfigCount = sizeof(kSfTileConfigs) / sizeof(kSfTileConfigs[0]);
 
@@ -169,6 +171,8 @@ int sf_launch_step_tile_cfg(const SfStepArgs& a, const SfSources& src, bool geom
         case 11: return launch1<2, 8, 4, false>(a, src, geom, ich, st);
         case 12: return launch1<1, 8, 4, true>(a, src, geom, ich, st);
         case 13: return launch1<2, 4, 6, true>(a, src, geom, ich, st);
+        case 14: return launch<1, 4, 6, false, true>(a, src, geom, ich, st);
+        case 15: return launch<1, 8, 4, false, true>(a, src, geom, ich, st);
     }
     return sf_fail("k_step_tile: bad configuration");
 }

@@ -70,8 +70,11 @@ __device__ __forceinline__ uint32_t ldflags(const uint8_t* __restrict__ base, in
     return __ldg(reinterpret_cast<const unsigned int*>(base + c));
 }
 
+// Streaming (evict-first) stores, or ordinary write-back ones with WB.
+template <bool WB = false>
 __device__ __forceinline__ void st4(float* __restrict__ base, int c, const float (&v)[4]) {
-    __stcs(reinterpret_cast<float4*>(base + c), make_float4(v[0], v[1], v[2], v[3]));
+    if (WB) *reinterpret_cast<float4*>(base + c) = make_float4(v[0], v[1], v[2], v[3]);
+    else __stcs(reinterpret_cast<float4*>(base + c), make_float4(v[0], v[1], v[2], v[3]));
 }
 
 // Flag bit `bit` of byte e of a packed 4-cell flag word.
@@ -82,7 +85,7 @@ __device__ __forceinline__ bool fbit(uint32_t f, uint32_t bit) {
 
 }  // namespace sf_tile
 
-template <bool GEOM, int R, bool PF, bool NU = false>
+template <bool GEOM, int R, bool PF, bool NU = false, bool WB = false>
 __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& src, int i0, int i1,
                                           int jw, int kw) {
     using namespace sf_tile;
@@ -348,10 +351,10 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
             }
             if (ract[r]) {
                 const int c = ci + roff[r];
-                st4(io.vxo, c, ox);
-                st4(io.vyo, c, oy);
-                st4(io.vzo, c, oz);
-                st4(io.po, c, po);
+                st4<WB>(io.vxo, c, ox);
+                st4<WB>(io.vyo, c, oy);
+                st4<WB>(io.vzo, c, oz);
+                st4<WB>(io.po, c, po);
             }
         }
 
