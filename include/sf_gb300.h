@@ -223,10 +223,16 @@ int sf_plan_set_ade_box(sf_plan* plan, const int32_t* lo, const int32_t* hi);
  * cap, streaming stores) and warp tiles with lane-shuffled neighbours
  * ("tile_*": float4 lanes, needs nz % 4 == 0 and 16-byte aligned fields;
  * "tile1_*": one cell per lane; "*_wb": ordinary write-back stores of the
- * new state instead of evict-first ones), as named by
+ * new state instead of evict-first ones), then multi-step pipelines
+ * ("tile_pipe*", "tile_stream*": 2 or 3 steps per launch, the intermediate
+ * states in rings of planes held in L2; used for whole groups of steps when
+ * the plan has float4 tiles, no ADE poles, no microphones, plane boundaries
+ * or weighted sources, and the streaming form's warps all fit on the device
+ * at once; other steps run the default warp tiles), as named by
  * sf_kernel_config_name.  A
  * configuration the grid cannot take falls back to scalar columns.  i_chunk
- * = planes per block (0 = automatic).  With ADE poles the warp-tile
+ * = planes per block (0 = automatic; pipelines: planes per chunk / between
+ * progress updates).  With ADE poles the warp-tile
  * configurations split each step with the per-cell kernel (see
  * sf_plan_set_ade_box); any other configuration runs the per-cell kernel.
  * Every configuration gives identical results.  No counterpart in the
@@ -239,10 +245,11 @@ const char* sf_kernel_config_name(int config);
  * step launches each (reading the current state and writing the other set
  * without swapping, no sources, no probes -- the state is unchanged) and
  * makes the fastest the plan's automatic choice, then times that one with
- * 8-48 planes per block (unless sf_plan_set_kernel fixed i_chunk) and keeps
- * the fastest chunk; with ADE poles only the warp-tile configurations, timed
- * outside their ADE region.  ms_out (host, may be NULL)
- * receives sf_kernel_config_count() per-launch times (-1 = not run);
+ * 8-48 planes per block (pipelines: 1-8 planes per chunk) unless
+ * sf_plan_set_kernel fixed i_chunk, and keeps the fastest; with ADE poles
+ * only the warp-tile configurations, timed outside their ADE region.  ms_out
+ * (host, may be NULL) receives sf_kernel_config_count() times per step (-1 =
+ * not run);
  * best_out (may be NULL) the chosen configuration.  Synchronises the stream.
  * No counterpart in the reference. */
 int sf_plan_autotune(sf_plan* plan, int launches, void* stream, float* ms_out, int* best_out);
@@ -250,7 +257,10 @@ int sf_plan_autotune(sf_plan* plan, int launches, void* stream, float* ms_out, i
 /* Advance n_steps.  src_values_dev: device doubles [n_steps][n_sources]
  * (the waveform at each step's time; may be NULL when there are no
  * sources).  trace_dev: device floats [n_steps][n_probes] receiving p at
- * each probe after each step (may be NULL when there are no probes).
+ * each probe after each step (may be NULL when there are no probes).  A
+ * call that ran a multi-step pipeline synchronises the stream at its end to
+ * read the pipeline's wait-expiry flag (outside stream capture), and fails
+ * if a bounded wait expired.
  * Replaces FDTDSolver.step's native dispatch (core/solver.py:2003-2102). */
 int sf_plan_step(sf_plan* plan, int64_t n_steps, const double* src_values_dev,
                  float* trace_dev, void* stream);

@@ -6,6 +6,8 @@
 // kernel per time step on the caller's stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -27,6 +29,7 @@
 #define SF_CFG_TILE_FIRST (SF_CFG_COL_FIRST + kSfColConfigCount)
 #define SF_CFG_TILE_DEFAULT (SF_CFG_TILE_FIRST + 2)
 #define SF_CFG_TILE1_DEFAULT (SF_CFG_TILE_FIRST + 11)
+#define SF_CFG_PIPE_FIRST (SF_CFG_TILE_FIRST + kSfTileConfigCount)
 #endif
 
 namespace {
@@ -131,6 +134,10 @@ int sf_plan_destroy(sf_plan* P) {
         cudaFree(P->wsrc_cells[q]);
         cudaFree(P->wsrc_w[q]);
     }
+    cudaFree(P->pipe_ring);
+    cudaFree(P->pipe_ctrl);
+    cudaFree(P->pipe_err);
+    cudaFree(P->pipe_order);
     delete P;
     return 0;
 }
@@ -315,7 +322,21 @@ int sf_plan_set_probes(sf_plan* P, int n, const int64_t* cells) {
     cudaFree(P->probe_cells);
     P->probe_cells = nullptr;
     P->n_probe = n;
+    P->probe_tile_max = 0;
     if (n == 0) return 0;
+    {  // probes per 32 k x 4 row tile column (the streaming pipeline holds at most 32)
+        const long long plane = (long long)P->d.ny * P->d.nz;
+        std::vector<long long> key(n);
+        for (int q = 0; q < n; ++q) {
+            const long long rem = cells[q] % plane;
+            key[q] = (rem / P->d.nz) / 4 * ((P->d.nz + 31) / 32) + (rem % P->d.nz) / 32;
+        }
+        std::sort(key.begin(), key.end());
+        for (int q = 0, run = 0; q < n; ++q) {
+            run = (q > 0 && key[q] == key[q - 1]) ? run + 1 : 1;
+            if (run > P->probe_tile_max) P->probe_tile_max = run;
+        }
+    }
     SF_CUDA_OK(cudaMalloc(&P->probe_cells, sizeof(long long) * n));
     SF_CUDA_OK(cudaMemcpy(P->probe_cells, cells, sizeof(long long) * n, cudaMemcpyHostToDevice));
     return 0;
@@ -371,7 +392,7 @@ int sf_plan_set_kernel(sf_plan* P, int config, int i_chunk) {
 }
 
 int sf_kernel_config_count(void) {
-    return SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount;
+    return SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount + kSfPipeConfigCount;
 }
 
 const char* sf_kernel_config_name(int config) {
@@ -380,8 +401,10 @@ const char* sf_kernel_config_name(int config) {
     if (config == SF_CFG_MARCH) return "march";
     if (config >= SF_CFG_COL_FIRST && config < SF_CFG_COL_FIRST + kSfColConfigCount)
         return kSfColConfigs[config - SF_CFG_COL_FIRST].name;
-    if (config >= SF_CFG_TILE_FIRST && config < sf_kernel_config_count())
+    if (config >= SF_CFG_TILE_FIRST && config < SF_CFG_PIPE_FIRST)
         return kSfTileConfigs[config - SF_CFG_TILE_FIRST].name;
+    if (config >= SF_CFG_PIPE_FIRST && config < sf_kernel_config_count())
+        return kSfPipeConfigs[config - SF_CFG_PIPE_FIRST].name;
     return nullptr;
 }
 
@@ -438,12 +461,21 @@ void set_io(const sf_plan* P, SfStepArgs& a, int in) {
 // column configuration.  With ADE poles only the warp-tile configurations
 // (which then leave the material box to the per-cell kernel, see
 // ade_region) and the per-cell kernel itself are used.
+bool is_pipe(int cfg) { return cfg >= SF_CFG_PIPE_FIRST; }
+bool pipe_fits(sf_plan* P, int cfg, const SfStepArgs& a);
+int chunk_for(const sf_plan* P, int cfg);
+
 int effective_config(const sf_plan* P, const SfStepArgs& a) {
     int cfg;
     if (P->variant != SF_CFG_AUTO) cfg = P->variant;
     else if (P->tuned > 0) cfg = P->tuned;
     else if (sf_tile_supported(a, 4)) cfg = SF_CFG_TILE_DEFAULT;
     else cfg = sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT;
+    if (is_pipe(cfg)) {  // when the pipeline fits the plan; else the default choice
+        if (pipe_fits(const_cast<sf_plan*>(P), cfg, a)) return cfg;
+        cfg = sf_tile_supported(a, 4) ? SF_CFG_TILE_DEFAULT
+                                      : (sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT);
+    }
     const bool tile_ok =
         cfg >= SF_CFG_TILE_FIRST && sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec);
     if (P->nu && !tile_ok)  // nonuniform arithmetic lives in the warp-tile kernels only
@@ -483,6 +515,8 @@ void ade_region(const sf_plan* P, int cfg, int ich, int lo[3], int hi[3]) {
 int chunk_for(const sf_plan* P, int cfg) {
     if (P->i_chunk > 0) return P->i_chunk;
     if (cfg == P->tuned && P->tuned_ich > 0) return P->tuned_ich;
+    if (is_pipe(cfg))  // planes per chunk / between progress updates
+        return kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST].stream ? 4 : 2;
     if (cfg >= SF_CFG_TILE_FIRST) {
         const SfTileConfig& t = kSfTileConfigs[cfg - SF_CFG_TILE_FIRST];
         if (t.vec == 1) return auto_chunk(P, 32, t.rows * t.warps);
@@ -500,6 +534,7 @@ int chunk_for(const sf_plan* P, int cfg) {
 // Whether configuration cfg runs as itself on this plan's grid (otherwise
 // its launcher substitutes the first column configuration).
 bool config_native(const sf_plan* P, int cfg, const SfStepArgs& a) {
+    if (is_pipe(cfg)) return pipe_fits(const_cast<sf_plan*>(P), cfg, a);
     if (cfg >= SF_CFG_TILE_FIRST)
         return sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec);
     if (cfg >= SF_CFG_COL_FIRST) return P->d.nz % kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec == 0;
@@ -542,6 +577,160 @@ int launch_step_split(const sf_plan* P, int cfg, int ich, SfStepArgs& a, const S
     return sf_launch_step(c, src, P->poles, P->flags != nullptr, st);
 }
 
+bool stream_capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+// Rings, counters and claim order of pipeline configuration cfg with S
+// planes per chunk; allocated (outside stream capture) when missing or too
+// small.  Fails when they would have to be made during a capture.
+int pipe_buffers(sf_plan* P, int cfg, int S, cudaStream_t st) {
+    const SfPipeConfig& pc = kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST];
+    const int T = pc.levels, L = pc.lag, M = pc.ring_chunks;
+    const int nchunks = (P->d.nx + S - 1) / S;
+    const long long ntiles = (long long)((P->d.nz + 31) / 32) * ((P->d.ny + 3) / 4);
+    // streaming: rings of M planes, a progress count per (level, tile)
+    const size_t ring = (size_t)(T - 1) * 4 * M * (pc.stream ? 1 : S) * (size_t)P->d.ny * P->d.nz;
+    const long long items = pc.stream ? T * ntiles : 1 + T * nchunks * ntiles;
+    if (items >= INT_MAX) return sf_fail("pipeline: too many work items");
+    const int ctrl_n = (int)items;
+    const bool order_ok = pc.stream || (P->pipe_order && P->pipe_key[0] == T && P->pipe_key[1] == S &&
+                                        P->pipe_key[2] == L && P->pipe_key[3] == M);
+    const bool ready = P->pipe_ring_floats >= ring && P->pipe_ctrl_n >= ctrl_n && P->pipe_err &&
+                       order_ok && P->pipe_grid[0] == cfg + 1;
+    if (ready) return 0;
+    if (stream_capturing(st)) return sf_fail("pipeline buffers must be made before a stream capture");
+    if (P->pipe_ring_floats < ring) {
+        cudaFree(P->pipe_ring);
+        P->pipe_ring = nullptr;
+        P->pipe_ring_floats = 0;
+        SF_CUDA_OK(cudaMalloc(&P->pipe_ring, ring * sizeof(float)));
+        P->pipe_ring_floats = ring;
+    }
+    if (P->pipe_ctrl_n < ctrl_n) {
+        cudaFree(P->pipe_ctrl);
+        P->pipe_ctrl = nullptr;
+        P->pipe_ctrl_n = 0;
+        SF_CUDA_OK(cudaMalloc(&P->pipe_ctrl, sizeof(int) * ctrl_n));
+        P->pipe_ctrl_n = ctrl_n;
+    }
+    if (!P->pipe_err) {
+        SF_CUDA_OK(cudaMalloc(&P->pipe_err, sizeof(int)));
+        SF_CUDA_OK(cudaMemset(P->pipe_err, 0, sizeof(int)));
+    }
+    if (!order_ok) {
+        // waves w: level s takes chunk w - (s-1)*lag, lower levels first
+        std::vector<int> order;
+        for (int w = 0; w < nchunks + (T - 1) * L; ++w)
+            for (int lv = 1; lv <= T; ++lv) {
+                const int c = w - (lv - 1) * L;
+                if (c >= 0 && c < nchunks) order.push_back((lv << 24) | c);
+            }
+        if ((int)order.size() > P->pipe_order_n) {
+            cudaFree(P->pipe_order);
+            P->pipe_order = nullptr;
+            P->pipe_order_n = 0;
+            SF_CUDA_OK(cudaMalloc(&P->pipe_order, sizeof(int) * order.size()));
+            P->pipe_order_n = (int)order.size();
+        }
+        SF_CUDA_OK(cudaMemcpy(P->pipe_order, order.data(), sizeof(int) * order.size(),
+                              cudaMemcpyHostToDevice));
+        P->pipe_key[0] = T;
+        P->pipe_key[1] = S;
+        P->pipe_key[2] = L;
+        P->pipe_key[3] = M;
+    }
+    if (P->pipe_grid[0] != cfg + 1) {
+        P->pipe_grid[1] = sf_pipe_grid(cfg - SF_CFG_PIPE_FIRST, P->flags != nullptr, P->nu != nullptr);
+        P->pipe_grid[0] = cfg + 1;
+    }
+    return 0;
+}
+
+// Whether pipeline configuration cfg can run this plan's steps: float4 warp
+// tiles, no ADE poles, and for a streaming configuration every warp resident
+// at once, at most 32 probes per tile column and a ring of at least S + 3
+// planes (S = planes between progress updates).
+bool pipe_fits(sf_plan* P, int cfg, const SfStepArgs& a) {
+    if (!sf_tile_supported(a, 4) || P->poles.n > 0) return false;
+    const SfPipeConfig& pc = kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST];
+    if (!pc.stream) return true;
+    if (P->probe_tile_max > 32) return false;
+    int S = chunk_for(P, cfg);
+    if (S + 3 > pc.ring_chunks) return false;
+    if (P->pipe_grid[0] != cfg + 1) {
+        P->pipe_grid[1] = sf_pipe_grid(cfg - SF_CFG_PIPE_FIRST, P->flags != nullptr, P->nu != nullptr);
+        P->pipe_grid[0] = cfg + 1;
+    }
+    const long long ntiles = (long long)((P->d.nz + 31) / 32) * ((P->d.ny + 3) / 4);
+    return (pc.levels * ntiles + 3) / 4 <= P->pipe_grid[1];
+}
+
+// One launch of pipeline configuration cfg: levels steps from set a.p.. to
+// set a.po.. (a.src_val: the first step's waveform row; trace_lvl[l]: probe
+// row of the state after level l+1, or null).
+int launch_pipe(sf_plan* P, int cfg, int S, const SfStepArgs& a, const SfSources& src,
+                float* const* trace_lvl, cudaStream_t st) {
+    const SfPipeConfig& pc = kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST];
+    if (S < 1) S = 1;
+    if (S > P->d.nx) S = P->d.nx;
+    if (int rc = pipe_buffers(P, cfg, S, st)) return rc;
+    if (pc.stream) {
+        SfPipeArgs A{};
+        A.a = a;
+        A.levels = pc.levels;
+        A.S = S;
+        A.M = pc.ring_chunks;
+        A.ntk = (P->d.nz + 31) / 32;
+        A.ntiles = A.ntk * ((P->d.ny + 3) / 4);
+        A.ring = P->pipe_ring;
+        A.ctrl = P->pipe_ctrl;
+        A.err = P->pipe_err;
+        for (int l = 0; l < SF_PIPE_MAX_LEVELS; ++l)
+            A.trace_lvl[l] = (trace_lvl && l < A.levels - 1) ? trace_lvl[l] : nullptr;
+        SF_CUDA_OK(cudaMemsetAsync(P->pipe_ctrl, 0, sizeof(int) * (size_t)A.levels * A.ntiles, st));
+        const int rc = sf_launch_step_stream(A, src, P->flags != nullptr, cfg - SF_CFG_PIPE_FIRST, st);
+        return rc == SF_PIPE_NOFIT ? sf_fail("k_step_stream: its warps do not fit on the device") : rc;
+    }
+    SfPipeArgs A{};
+    A.a = a;
+    A.levels = pc.levels;
+    A.S = S;
+    A.M = pc.ring_chunks;
+    A.nchunks = (P->d.nx + S - 1) / S;
+    A.ntk = (P->d.nz + 31) / 32;
+    A.ntiles = A.ntk * ((P->d.ny + 3) / 4);  // one warp: 32 k x 4 rows
+    A.ngroups = 0;
+    for (int w = 0; w < A.nchunks + (A.levels - 1) * pc.lag; ++w)
+        for (int lv = 1; lv <= A.levels; ++lv) {
+            const int c = w - (lv - 1) * pc.lag;
+            A.ngroups += (c >= 0 && c < A.nchunks) ? 1 : 0;
+        }
+    A.ring = P->pipe_ring;
+    A.order = P->pipe_order;
+    A.ctrl = P->pipe_ctrl;
+    A.err = P->pipe_err;
+    for (int l = 0; l < SF_PIPE_MAX_LEVELS; ++l)
+        A.trace_lvl[l] = (trace_lvl && l < A.levels - 1) ? trace_lvl[l] : nullptr;
+    SF_CUDA_OK(cudaMemsetAsync(P->pipe_ctrl, 0,
+                               sizeof(int) * (1 + (size_t)A.levels * A.nchunks * A.ntiles), st));
+    const long long items = (long long)A.ngroups * A.ntiles;
+    const int grid = (int)(items < P->pipe_grid[1] ? items : P->pipe_grid[1]);
+    return sf_launch_step_pipe(A, src, P->flags != nullptr, cfg - SF_CFG_PIPE_FIRST, grid, st);
+}
+
+// Reads and clears the pipeline's wait-expiry flag (synchronises the stream).
+int pipe_check(sf_plan* P, cudaStream_t st) {
+    if (!P->pipe_err || stream_capturing(st)) return 0;
+    int e = 0;
+    SF_CUDA_OK(cudaMemcpyAsync(&e, P->pipe_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SF_CUDA_OK(cudaStreamSynchronize(st));
+    if (e == 0) return 0;
+    cudaMemsetAsync(P->pipe_err, 0, sizeof(int), st);
+    return sf_fail("k_step_pipe: a dependency wait expired (results of this call are invalid)");
+}
+
 }  // namespace
 
 extern "C" {
@@ -563,13 +752,36 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
     SfStepArgs a;
     fill_args(P, a, trace != nullptr);
     set_io(P, a, P->cur);  // both sets: the alignment check covers every field
-    const int cfg = effective_config(P, a);
-    const int ich = chunk_for(P, cfg);
+    const int cfg0 = effective_config(P, a);
     const bool mics = mic_trace != nullptr && P->n_mic > 0;
     // plane boundaries or weighted sources: sources move after the fused kernel
     bool deferred = P->n_plane > 0;
     for (int q = 0; q < P->src.n; ++q) deferred = deferred || P->src.s[q].kind == 2;
-    for (int64_t s = 0; s < n_steps; ++s) {
+    // A pipeline configuration runs whole groups of its steps per launch when
+    // nothing has to happen between steps; remaining steps (and plans with
+    // microphones, plane boundaries or weighted sources) run single steps
+    // of the default warp-tile configuration.
+    const bool pipe = is_pipe(cfg0) && !deferred && !mics;
+    const int levels = pipe ? kSfPipeConfigs[cfg0 - SF_CFG_PIPE_FIRST].levels : 1;
+    const int pipe_S = pipe ? chunk_for(P, cfg0) : 0;
+    const int cfg = is_pipe(cfg0) ? SF_CFG_TILE_DEFAULT : cfg0;
+    const int ich = chunk_for(P, cfg);
+    bool piped = false;
+    for (int64_t s = 0; s < n_steps;) {
+        if (pipe && n_steps - s >= levels) {
+            set_io(P, a, P->cur);
+            a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
+            a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
+            float* tl[SF_PIPE_MAX_LEVELS] = {nullptr, nullptr, nullptr, nullptr};
+            if (a.n_probe > 0)
+                for (int l = 0; l + 1 < levels; ++l) tl[l] = trace + (s + l) * P->n_probe;
+            if (int rc = launch_pipe(P, cfg0, pipe_S, a, P->src, tl, st)) return rc;
+            piped = true;
+            P->cur = 1 - P->cur;
+            P->steps_done += levels;
+            s += levels;
+            continue;
+        }
         set_io(P, a, P->cur);
         a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
         a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
@@ -599,16 +811,19 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
         }
         P->cur = 1 - P->cur;
         ++P->steps_done;
+        ++s;
         if (mics)
             if (int rc = sf_launch_mic_gather(P->f[P->cur][0], P->f[P->cur][1], P->f[P->cur][2],
                                               P->f[P->cur][3], P->mic_field, P->mic_idx,
-                                              P->mic_w, P->n_mic, mic_trace + s * P->n_mic, st))
+                                              P->mic_w, P->n_mic, mic_trace + (s - 1) * P->n_mic,
+                                              st))
                 return rc;
     }
     if (trace && P->n_probe > 0)
-        return sf_launch_probe_gather(P->f[P->cur][0], P->probe_cells, P->n_probe,
-                                      trace + (n_steps - 1) * P->n_probe, st);
-    return 0;
+        if (int rc = sf_launch_probe_gather(P->f[P->cur][0], P->probe_cells, P->n_probe,
+                                            trace + (n_steps - 1) * P->n_probe, st))
+            return rc;
+    return piped ? pipe_check(P, st) : 0;
 }
 
 int sf_plan_set_microphones(sf_plan* P, int n, const int64_t* idx8, const float* w8) {
@@ -670,56 +885,63 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     cudaEvent_t e0, e1;
     SF_CUDA_OK(cudaEventCreate(&e0));
     SF_CUDA_OK(cudaEventCreate(&e1));
-    int best = 0;
-    float best_ms = 0.0f;
+    bool deferred = P->n_plane > 0;
+    for (int q = 0; q < P->src.n; ++q) deferred = deferred || P->src.s[q].kind == 2;
     int rc = 0;
-    for (int cfg = SF_CFG_CELL; cfg < count && !rc; ++cfg) {
-        if (!config_native(P, cfg, a) || ((ade || P->nu) && cfg < SF_CFG_TILE_FIRST)) continue;
-        const int ich = chunk_for(P, cfg);
+    // ms per step of configuration cfg with planes per block ich (a warm-up
+    // launch, then `launches` timed ones; a pipeline launch is `levels` steps)
+    auto trial = [&](int cfg, int ich, float* ms_step) -> int {
         SfStepArgs t = a;
-        if (ade) ade_region(P, cfg, ich, t.skip_lo, t.skip_hi);
-        if ((rc = launch_config(P, cfg, ich, t, none, st))) break;  // warm-up
-        if (cudaEventRecord(e0, st) != cudaSuccess) { rc = sf_fail("event record failed"); break; }
-        for (int q = 0; q < launches && !rc; ++q) rc = launch_config(P, cfg, ich, t, none, st);
-        if (rc) break;
-        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
-            rc = sf_fail("sf_plan_autotune: timing failed");
-            break;
-        }
+        if (ade && !is_pipe(cfg)) ade_region(P, cfg, ich, t.skip_lo, t.skip_hi);
+        auto one = [&]() -> int {
+            return is_pipe(cfg) ? launch_pipe(P, cfg, ich, t, none, nullptr, st)
+                                : launch_config(P, cfg, ich, t, none, st);
+        };
+        if (int r = one()) return r;
+        if (cudaEventRecord(e0, st) != cudaSuccess) return sf_fail("event record failed");
+        for (int q = 0; q < launches; ++q)
+            if (int r = one()) return r;
+        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+            return sf_fail("sf_plan_autotune: timing failed");
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
-        ms /= launches;
+        const int steps = is_pipe(cfg) ? kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST].levels : 1;
+        *ms_step = ms / (launches * steps);
+        return 0;
+    };
+    int best = 0;
+    float best_ms = 0.0f;
+    for (int cfg = SF_CFG_CELL; cfg < count && !rc; ++cfg) {
+        if (!config_native(P, cfg, a) || ((ade || P->nu) && cfg < SF_CFG_TILE_FIRST)) continue;
+        if (is_pipe(cfg) && deferred) continue;
+        float ms = 0.0f;
+        if ((rc = trial(cfg, chunk_for(P, cfg), &ms))) break;
         if (ms_out) ms_out[cfg] = ms;
         if (best == 0 || ms < best_ms) {
             best = cfg;
             best_ms = ms;
         }
     }
+    if (!rc) rc = pipe_check(P, st);
     // then the planes per block of the winner (unless the caller fixed them)
     if (!rc && best >= SF_CFG_COL_FIRST && P->i_chunk == 0) {
         const int auto_ich = chunk_for(P, best);
         int best_ich = auto_ich;
-        const int cand[] = {8, 12, 16, 20, 24, 32, 48};
-        for (int ich : cand) {
-            if (ich == auto_ich || ich > P->d.nx || rc) continue;
-            SfStepArgs t = a;
-            if (ade) ade_region(P, best, ich, t.skip_lo, t.skip_hi);
-            if ((rc = launch_config(P, best, ich, t, none, st))) break;
-            if (cudaEventRecord(e0, st) != cudaSuccess) { rc = sf_fail("event record failed"); break; }
-            for (int q = 0; q < launches && !rc; ++q) rc = launch_config(P, best, ich, t, none, st);
-            if (rc) break;
-            if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
-                rc = sf_fail("sf_plan_autotune: timing failed");
-                break;
-            }
+        static const int cand_step[] = {8, 12, 16, 20, 24, 32, 48};
+        static const int cand_pipe[] = {1, 2, 3, 4, 6, 8};
+        const int* cand = is_pipe(best) ? cand_pipe : cand_step;
+        const int ncand = is_pipe(best) ? 6 : 7;
+        for (int q = 0; q < ncand && !rc; ++q) {
+            const int ich = cand[q];
+            if (ich == auto_ich || ich > P->d.nx) continue;
             float ms = 0.0f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            ms /= launches;
+            if ((rc = trial(best, ich, &ms))) break;
             if (ms < best_ms) {
                 best_ms = ms;
                 best_ich = ich;
             }
         }
+        if (!rc && is_pipe(best)) rc = pipe_check(P, st);
         if (!rc && best_ich != auto_ich) P->tuned_ich = best_ich;
     }
     cudaEventDestroy(e0);

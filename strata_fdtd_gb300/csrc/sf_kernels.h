@@ -28,6 +28,52 @@ extern const int kSfTileConfigCount;
 // Whether a warp-tile kernel with `vec` cells per lane runs on this grid.
 bool sf_tile_supported(const SfStepArgs& a, int vec);
 
+// Multi-step pipeline configurations follow the warp-tile ones: index
+// SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount + t.  One launch
+// advances the state by `levels` steps (sf_step_pipe.cu).  Claimed-item
+// pipelines (stream = 0): level s runs `lag` chunks behind level s-1 and the
+// rings between levels hold `ring_chunks` chunks of planes each.  Streaming
+// pipelines (stream = 1): one co-resident warp per (level, tile) walks the
+// whole x extent; the rings hold `ring_chunks` planes (a power of two).
+#define SF_PIPE_MAX_LEVELS 4
+struct SfPipeConfig {
+    int levels, warps, minb, lag, ring_chunks, stream;
+    const char* name;
+};
+extern const SfPipeConfig kSfPipeConfigs[];
+extern const int kSfPipeConfigCount;
+
+// One launch of the pipeline: a.p.. is the input set, a.po.. the output
+// set, a.src_val the first step's waveform values (level s uses row s-1),
+// a.trace_prev the probe row of the input state.
+struct SfPipeArgs {
+    SfStepArgs a;
+    int levels;   // steps per launch
+    int S;        // planes per chunk
+    int M;        // chunks per ring
+    int nchunks;  // ceil(nx / S)
+    int ntk;      // tiles along k (32 cells each)
+    int ntiles;   // tiles per chunk
+    int ngroups;  // (level, chunk) groups in claim order
+    float* ring;        // (levels-1) rings x 4 fields x M*S planes
+    const int* order;   // per group: (level << 24) | chunk, level 1-based
+    int* ctrl;          // [0] next item; [1 + ((level-1)*nchunks + chunk)*ntiles + tile] done
+    int* err;           // nonzero: a bounded wait expired (2)
+    float* trace_lvl[SF_PIPE_MAX_LEVELS];  // probe row of level s+1's result, or null
+};
+int sf_launch_step_pipe(const SfPipeArgs& P, const SfSources& src, bool geom, int cfg, int grid,
+                        cudaStream_t st);
+// Resident blocks of pipeline configuration cfg on this device (grid size).
+int sf_pipe_grid(int cfg, bool geom, bool nu);
+// Streaming pipeline: P.ctrl holds the per-(level, tile) plane progress
+// (levels * ntiles ints, zeroed), P.S the publishing interval in planes,
+// P.M the ring planes; probe_tile[u] / probe_plane[u] place the probes.
+// Returns SF_PIPE_NOFIT (without launching) when its warps cannot all be
+// resident at once.
+#define SF_PIPE_NOFIT 77
+int sf_launch_step_stream(const SfPipeArgs& P, const SfSources& src, bool geom, int cfg,
+                          cudaStream_t st);
+
 int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, int nz,
                           cudaStream_t st);
 int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& poles, bool geom,

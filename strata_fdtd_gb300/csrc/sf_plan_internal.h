@@ -39,6 +39,17 @@ struct sf_plan {
     long long* wsrc_cells[SF_MAX_SOURCES] = {nullptr};  // owned, weighted (membrane) sources
     double* wsrc_w[SF_MAX_SOURCES] = {nullptr};
     long long wsrc_n[SF_MAX_SOURCES] = {0};
+    // multi-step pipeline (sf_step_pipe.cu)
+    float* pipe_ring = nullptr;  // owned: rings of planes between levels
+    size_t pipe_ring_floats = 0;
+    int* pipe_ctrl = nullptr;  // owned: claim counter, tiles done per (level, chunk)
+    int pipe_ctrl_n = 0;
+    int* pipe_err = nullptr;    // owned: wait-expiry flag
+    int* pipe_order = nullptr;  // owned: (level, chunk) claim order
+    int pipe_order_n = 0;
+    int pipe_key[4] = {0, 0, 0, 0};  // levels, planes per chunk, lag, ring chunks of the order
+    int pipe_grid[2] = {0, 0};       // configuration + 1, resident blocks
+    int probe_tile_max = 0;          // most probes in one 32 k x 4 row tile column
 };
 
 // Planes per block: enough (j,k)-tile x i-chunk blocks for about four waves

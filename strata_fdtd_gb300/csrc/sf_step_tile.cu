@@ -66,7 +66,8 @@ __global__ void __launch_bounds__(32 * W, MINB) k_step_tile(SfStepArgs a, SfSour
     }
     if (jw >= a.ny) return;  // the whole warp is past the grid (no block barrier follows)
     if (in_skip(a, i0, blockIdx.y * W * 4 * R, blockIdx.x * 32)) return;  // the ADE kernel's cells
-    tile4_run<GEOM, R, PF, NU, WB>(tile_io(a), src, i0, i1, jw, blockIdx.x * 32);
+    tile4_run<GEOM, R, PF, NU, WB>(tile_io(a), src, i0, i1, jw, blockIdx.x * 32,
+                                   SfPlainMem{a.ny * a.nz});
 }
 
 // Scalar warp tiles: 32 lanes along k, R rows per lane, W warps along j.

@@ -85,16 +85,42 @@ __device__ __forceinline__ bool fbit(uint32_t f, uint32_t bit) {
 
 }  // namespace sf_tile
 
-template <bool GEOM, int R, bool PF, bool NU = false, bool WB = false>
+// Plane addressing of the float4 warp tile: where plane i of the input and
+// output fields starts, and how they are read and written.  SfPlainMem is
+// the state sets themselves (plane i at i * plane, loads through the
+// read-only path, streaming or write-back stores); the multi-step pipeline
+// (sf_step_pipe.cu) substitutes ring buffers of planes.  The flag bytes are
+// always addressed by i * plane.  before(i) runs ahead of plane i's loads
+// (the planes up to i+2 may be read next) and after(i) once plane i is
+// stored: hooks for the streaming pipeline's synchronisation, empty here.
+struct SfPlainMem {
+    int plane;
+    __device__ __forceinline__ void before(int) const {}
+    __device__ __forceinline__ void after(int) const {}
+    __device__ __forceinline__ int in(int i) const { return i * plane; }
+    __device__ __forceinline__ int out(int i) const { return i * plane; }
+    __device__ __forceinline__ void ld4(const float* __restrict__ b, int c, float (&v)[4]) const {
+        sf_tile::ld4(b, c, v);
+    }
+    __device__ __forceinline__ float ld1(const float* __restrict__ b, int c) const {
+        return __ldg(b + c);
+    }
+    template <bool WB>
+    __device__ __forceinline__ void st4(float* __restrict__ b, int c, const float (&v)[4]) const {
+        sf_tile::st4<WB>(b, c, v);
+    }
+};
+
+template <bool GEOM, int R, bool PF, bool NU = false, bool WB = false, class Mem = SfPlainMem>
 __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& src, int i0, int i1,
-                                          int jw, int kw) {
+                                          int jw, int kw, const Mem& mem) {
     using namespace sf_tile;
     const int lane = threadIdx.x & 31;
     const int lx = lane & 7, ly = lane >> 3;
     const int nx = io.nx, ny = io.ny, nz = io.nz;
     const int k0 = kw + lx * 4;
     const int jb = jw + ly * R;  // this lane's first row
-    const int plane = ny * nz;
+    const int plane = mem.plane;  // ny * nz
     const bool kact = k0 < nz;
     bool ract[R];
     int roff[R];
@@ -151,6 +177,7 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
     float pnn[R][4], vxn[R][4], vyn[R][4], vzn[R][4];
     uint32_t fnn[R];
 #pragma unroll
+    mem.before(i0);
     for (int r = 0; r < R; ++r) {
         fc[r] = fnn[r] = 0x0f0f0f0fu;
 #pragma unroll
@@ -159,20 +186,22 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
             pnn[r][e] = vxn[r][e] = vyn[r][e] = vzn[r][e] = 0.0f;
         }
         if (!ract[r]) continue;
-        const int c = i0 * plane + roff[r];
-        ld4(io.p, c, pc[r]);
-        if (i0 + 1 < nx) ld4(io.p, c + plane, pn[r]);
+        const int c = mem.in(i0) + roff[r];
+        const int cf = i0 * plane + roff[r];
+        mem.ld4(io.p, c, pc[r]);
+        if (i0 + 1 < nx) mem.ld4(io.p, mem.in(i0 + 1) + roff[r], pn[r]);
         if (PF) {
-            ld4(io.vx, c, vx[r]);
-            ld4(io.vy, c, vy[r]);
-            ld4(io.vz, c, vz[r]);
-            if (GEOM) fc[r] = ldflags(io.flags, c);
+            mem.ld4(io.vx, c, vx[r]);
+            mem.ld4(io.vy, c, vy[r]);
+            mem.ld4(io.vz, c, vz[r]);
+            if (GEOM) fc[r] = ldflags(io.flags, cf);
         }
         if (i0 > 0) {  // chunk start: low x face from plane i0-1
             float pm[4], vm[4];
-            ld4(io.p, c - plane, pm);
-            ld4(io.vx, c - plane, vm);
-            const uint32_t fm = GEOM ? ldflags(io.flags, c - plane) : 0x0f0f0f0fu;
+            const int cm = mem.in(i0 - 1) + roff[r];
+            mem.ld4(io.p, cm, pm);
+            mem.ld4(io.vx, cm, vm);
+            const uint32_t fm = GEOM ? ldflags(io.flags, cf - plane) : 0x0f0f0f0fu;
             const float cvm = NU ? io.nu_cv[0][i0 - 1] : cv;
             vxm[r][0] = face_update(vm[0], cvm, pc[r][0], pm[0]);
             vxm[r][1] = face_update(vm[1], cvm, pc[r][1], pm[1]);
@@ -188,37 +217,41 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
     }
 
     for (int i = i0; i < i1; ++i) {
-        const int ci = i * plane;
+        mem.before(i);
+        const int ci = mem.in(i);      // input fields of plane i
+        const int cfi = i * plane;     // flag bytes of plane i
         const float cvx = NU ? (i < nx - 1 ? io.nu_cv[0][i] : 0.0f) : cv;
         const float sxi = NU ? io.nu_inv[0][i] : 1.0f;
         if (PF) {  // plane i+1's velocities and flags, p at i+2 (used next iteration)
+            const int cn = mem.in(i + 1), cnn = mem.in(i + 2);  // read only when in the grid
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 if (ract[r] && i + 1 < i1) {
-                    const int c = ci + plane + roff[r];
-                    ld4(io.vx, c, vxn[r]);
-                    ld4(io.vy, c, vyn[r]);
-                    ld4(io.vz, c, vzn[r]);
-                    if (GEOM) fnn[r] = ldflags(io.flags, c);
-                    if (i + 2 < nx) ld4(io.p, c + plane, pnn[r]);
+                    const int c = cn + roff[r];
+                    mem.ld4(io.vx, c, vxn[r]);
+                    mem.ld4(io.vy, c, vyn[r]);
+                    mem.ld4(io.vz, c, vzn[r]);
+                    if (GEOM) fnn[r] = ldflags(io.flags, cfi + plane + roff[r]);
+                    if (i + 2 < nx) mem.ld4(io.p, cnn + roff[r], pnn[r]);
                 }
             }
         } else {
+            const int cn = mem.in(i + 1);  // read only when in the grid
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 if (ract[r]) {
                     const int c = ci + roff[r];
-                    ld4(io.vx, c, vx[r]);
-                    ld4(io.vy, c, vy[r]);
-                    ld4(io.vz, c, vz[r]);
-                    if (GEOM) fc[r] = ldflags(io.flags, c);
-                    if (i > i0 && i + 1 < nx) ld4(io.p, c + plane, pn[r]);
+                    mem.ld4(io.vx, c, vx[r]);
+                    mem.ld4(io.vy, c, vy[r]);
+                    mem.ld4(io.vz, c, vz[r]);
+                    if (GEOM) fc[r] = ldflags(io.flags, cfi + roff[r]);
+                    if (i > i0 && i + 1 < nx) mem.ld4(io.p, cn + roff[r], pn[r]);
                 }
             }
         }
         // edge-lane neighbours from global memory, others from the lanes
         float pup[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // p at row jb+R (last row's +j)
-        if (ly == 3 && ract[R - 1] && jb + R < ny) ld4(io.p, ci + roff[R - 1] + nz, pup);
+        if (ly == 3 && ract[R - 1] && jb + R < ny) mem.ld4(io.p, ci + roff[R - 1] + nz, pup);
         float pkp[R];  // p at k0+4 (last cell's +k), per row
         float pkm[R], vzkm[R];
         uint32_t fkm[R];
@@ -226,20 +259,20 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
         for (int r = 0; r < R; ++r) {
             pkp[r] = pkm[r] = vzkm[r] = 0.0f;
             fkm[r] = SF_ALL;
-            if (lx == 7 && ract[r] && k0 + 4 < nz) pkp[r] = __ldg(io.p + ci + roff[r] + 4);
+            if (lx == 7 && ract[r] && k0 + 4 < nz) pkp[r] = mem.ld1(io.p, ci + roff[r] + 4);
             if (lx == 0 && ract[r] && k0 > 0) {
-                pkm[r] = __ldg(io.p + ci + roff[r] - 1);
-                vzkm[r] = __ldg(io.vz + ci + roff[r] - 1);
-                if (GEOM) fkm[r] = __ldg(io.flags + ci + roff[r] - 1);
+                pkm[r] = mem.ld1(io.p, ci + roff[r] - 1);
+                vzkm[r] = mem.ld1(io.vz, ci + roff[r] - 1);
+                if (GEOM) fkm[r] = __ldg(io.flags + cfi + roff[r] - 1);
             }
         }
         float pjm[4] = {0.0f, 0.0f, 0.0f, 0.0f}, vyjm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         uint32_t fjm = 0x0f0f0f0fu;
         const bool jlow = (ly == 0) && ract[0] && jb > 0;
         if (jlow) {
-            ld4(io.p, ci + roff[0] - nz, pjm);
-            ld4(io.vy, ci + roff[0] - nz, vyjm);
-            if (GEOM) fjm = ldflags(io.flags, ci + roff[0] - nz);
+            mem.ld4(io.p, ci + roff[0] - nz, pjm);
+            mem.ld4(io.vy, ci + roff[0] - nz, vyjm);
+            if (GEOM) fjm = ldflags(io.flags, cfi + roff[0] - nz);
         }
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -311,6 +344,7 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
         }
 
         const float di = io.dx[i];
+        const int co = mem.out(i);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             float po[4], ox[4], oy[4], oz[4];
@@ -350,13 +384,14 @@ __device__ __forceinline__ void tile4_run(const SfTileIo& io, const SfSources& s
                 po[e] = pnew;
             }
             if (ract[r]) {
-                const int c = ci + roff[r];
-                st4<WB>(io.vxo, c, ox);
-                st4<WB>(io.vyo, c, oy);
-                st4<WB>(io.vzo, c, oz);
-                st4<WB>(io.po, c, po);
+                const int c = co + roff[r];
+                mem.template st4<WB>(io.vxo, c, ox);
+                mem.template st4<WB>(io.vyo, c, oy);
+                mem.template st4<WB>(io.vzo, c, oz);
+                mem.template st4<WB>(io.po, c, po);
             }
         }
+        mem.after(i);
 
 #pragma unroll
         for (int r = 0; r < R; ++r) {
