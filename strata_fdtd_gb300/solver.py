@@ -103,6 +103,23 @@ def step_coefficients(grid, c: float, rho: float, courant: float):
     return dt, coeff_v, coeff_p
 
 
+def _fresh_host_array(shape) -> np.ndarray:
+    """A new float32 array for a snapshot: anonymous memory asking for
+    transparent huge pages when it is large (fewer page faults when it is
+    first written), else np.empty."""
+    n = int(np.prod(shape))
+    if n * 4 < (64 << 20):
+        return np.empty(shape, dtype=np.float32)
+    import mmap
+    mm = mmap.mmap(-1, n * 4)
+    if hasattr(mmap, "MADV_HUGEPAGE"):
+        try:
+            mm.madvise(mmap.MADV_HUGEPAGE)
+        except OSError:
+            pass
+    return np.frombuffer(mm, dtype=np.float32, count=n).reshape(shape)
+
+
 def kernel_configs() -> list[str]:
     """Names of the step-kernel configurations, by configuration index."""
     lib = _native.load()
@@ -208,6 +225,10 @@ class FDTDSolver:
         self._time = 0.0
         self._snapshots: list = []
         self._velocity_snapshots: list = []
+        self._snap_staged: list = []    # (t, device copies, event): waiting for the next steps
+        self._snap_inflight: list = []  # (t, futures of the host arrays): copies under way
+        self._snap_stream = None
+        self._snap_pool = None
         self._snapshot_interval = None
         self._snapshot_velocity = False
 
@@ -712,6 +733,7 @@ class FDTDSolver:
     def step(self) -> None:
         """Advance one time step (core/solver.py:2003-2077)."""
         self._advance(1)
+        self._snap_flush()
         self._after_steps(self._step_count - 1, self._step_count)
 
     def _after_steps(self, first: int, last: int):
@@ -719,26 +741,93 @@ class FDTDSolver:
         last of them can be due, run() splits chunks at these points)."""
         s = last - 1
         if self._snapshot_interval and s % self._snapshot_interval == 0:
-            t = self._time - self.dt
-            self._snapshots.append((t, self.p.copy()))
-            if self._snapshot_velocity:
-                self._velocity_snapshots.append((t, *self._centred_velocity()))
+            self._snap_capture(self._time - self.dt)
         if self._track_energy and last % self._energy_sample_interval == 0:
             self._energy_history.append((last, self._time, self.compute_energy()))
 
-    def _centred_velocity(self):
-        """Staggered velocities averaged to cell centres (core/solver.py:2647-2687)."""
-        vx, vy, vz = self.vx, self.vy, self.vz
-        cx = np.zeros(self.shape, dtype=np.float32)
-        cx[1:] = 0.5 * (vx[:-1] + vx[1:])
-        cx[0] = 0.5 * vx[0]
-        cy = np.zeros(self.shape, dtype=np.float32)
-        cy[:, 1:] = 0.5 * (vy[:, :-1] + vy[:, 1:])
-        cy[:, 0] = 0.5 * vy[:, 0]
-        cz = np.zeros(self.shape, dtype=np.float32)
-        cz[:, :, 1:] = 0.5 * (vz[:, :, :-1] + vz[:, :, 1:])
-        cz[:, :, 0] = 0.5 * vz[:, :, 0]
-        return cx, cy, cz
+    # ----------------------------------------------------------- snapshots
+    # A snapshot (core/solver.py:2050-2068) is staged as device copies on the
+    # compute stream.  Once the following steps are queued (_snap_flush) each
+    # copy goes to a pinned buffer on a separate stream (pinned blocks are
+    # reused through torch's host cache) and a worker thread moves it into
+    # the fresh NumPy array the caller receives, so neither the copy nor the
+    # host-memory provisioning holds up the steps; get_snapshots() waits.
+    _SNAP_MAX_INFLIGHT = 8
+    def _snap_capture(self, t: float) -> None:
+        torch = self._torch
+        f = self.device_fields()
+        staged = [f["p"].clone()]
+        if self._snapshot_velocity:
+            staged += self._centred_velocity_dev(f)
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self._device))
+        self._snap_staged.append((t, staged, ev))
+
+    def _snap_flush(self) -> None:
+        """Issue the device-to-host copies of the staged snapshots."""
+        if not self._snap_staged:
+            return
+        torch = self._torch
+        if self._snap_stream is None:
+            self._snap_stream = torch.cuda.Stream(self._device)
+        if self._snap_pool is None:
+            from concurrent.futures import ThreadPoolExecutor
+            self._snap_pool = ThreadPoolExecutor(max_workers=4, thread_name_prefix="sf-snapshot")
+        for t, staged, ev in self._snap_staged:
+            while len(self._snap_inflight) >= self._SNAP_MAX_INFLIGHT:
+                self._snap_retire_oldest()
+            arrays, futs = [], []
+            for x in staged:
+                pinned = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+                with torch.cuda.stream(self._snap_stream):
+                    self._snap_stream.wait_event(ev)
+                    pinned.copy_(x, non_blocking=True)
+                    x.record_stream(self._snap_stream)  # kept until the copy is done
+                    done = torch.cuda.Event()
+                    done.record(self._snap_stream)
+                out = _fresh_host_array(tuple(x.shape))
+                arrays.append(out)
+                n = out.shape[0]
+                for q in range(4):  # slabs along x, moved by the workers side by side
+                    lo, hi = n * q // 4, n * (q + 1) // 4
+                    if hi > lo:
+                        futs.append(self._snap_pool.submit(self._snap_slab, pinned, done, out, lo, hi))
+            self._snap_inflight.append((t, arrays, futs))
+        self._snap_staged.clear()
+
+    @staticmethod
+    def _snap_slab(pinned, done, out, lo, hi):
+        done.synchronize()
+        np.copyto(out[lo:hi], pinned.numpy()[lo:hi])
+
+    def _snap_retire_oldest(self) -> None:
+        t, arrays, futs = self._snap_inflight.pop(0)
+        for f in futs:
+            f.result()
+        self._snapshots.append((t, arrays[0]))
+        if len(arrays) > 1:
+            self._velocity_snapshots.append((t, *arrays[1:]))
+
+    def _snap_collect(self) -> None:
+        self._snap_flush()
+        while self._snap_inflight:
+            self._snap_retire_oldest()
+
+    def _centred_velocity_dev(self, f) -> list:
+        """Staggered velocities averaged to cell centres on the device, with
+        the reference's float32 operations: c[1:] = 0.5 * (v[:-1] + v[1:]),
+        c[0] = 0.5 * v[0] along each velocity's own axis
+        (core/solver.py:2647-2687)."""
+        out = []
+        for ax, name in enumerate(("vx", "vy", "vz")):
+            v = f[name]
+            n = v.shape[ax]
+            c = self._torch.empty_like(v)
+            if n > 1:
+                c.narrow(ax, 1, n - 1).copy_(0.5 * (v.narrow(ax, 0, n - 1) + v.narrow(ax, 1, n - 1)))
+            c.narrow(ax, 0, 1).copy_(0.5 * v.narrow(ax, 0, 1))
+            out.append(c)
+        return out
 
     def run(self, duration: float, progress: bool = False, track_energy: bool = False,
             energy_sample_interval: int = 1, output_file: str | None = None,
@@ -774,10 +863,12 @@ class FDTDSolver:
                 chunk = min(chunk, nxt - self._step_count)
             first = self._step_count
             self._advance(chunk)
+            self._snap_flush()  # copies of the previous snapshot run beside this chunk
             self._after_steps(first, self._step_count)
             if callback is not None:
                 callback(self._step_count - 1)
             done += chunk
+        self._snap_flush()
         if self._warn_energy_drift and len(self._energy_history) >= 2:
             rep = self.energy_report()
             if abs(rep["energy_change_percent"]) > self._energy_drift_threshold * 100:
@@ -828,9 +919,11 @@ class FDTDSolver:
         return {n: pr.get_data() for n, pr in self._probes.items()}
 
     def get_snapshots(self):
+        self._snap_collect()
         return self._snapshots
 
     def get_velocity_snapshots(self):
+        self._snap_collect()
         return self._velocity_snapshots
 
     def compute_energy(self) -> float:
@@ -874,6 +967,7 @@ class FDTDSolver:
         self._step_count = 0
         self._time = 0.0
         self._src_cache = None
+        self._snap_collect()
         self._snapshots.clear()
         self._energy_history.clear()
         self._track_energy = False

@@ -189,3 +189,46 @@ def test_duplicate_names_and_bad_positions_are_rejected():
         s.add_source(S.GaussianPulse(position=(16, 0, 0), frequency=1000.0))
     with pytest.raises(ValueError):
         s.set_geometry(np.ones((15, 16, 16), dtype=bool))
+
+
+def test_snapshots_equal_the_oracle_state_and_numpy_centring():
+    """Snapshot contents (staged on the device, copied to host beside the
+    following steps) are the oracle's p after the due steps, and the
+    centred velocities equal the reference's NumPy float32 averaging of the
+    oracle's staggered fields."""
+    import cases as C
+    from oracle import oracle as O
+    from test_gpu_parity import API
+
+    case = dict(shape=(18, 21, 24), res=1e-3, courant=0.6, pml=dict(depth=3),
+                geometry=dict(kind="blocks", seed=5, n_boxes=2, n_spheres=1),
+                sources=[("point", (9, 10, 11), 25000.0, 1.0)], probes=[("a", (4, 5, 6))],
+                steps=30)
+    ref = C.build_case(O.make_api(), case)
+    s = C.build_case(API, case)
+    s.enable_snapshots(interval=7, capture_velocity=True)
+    s.run_steps(12)
+    s.step()
+    s.run_steps(17)
+    want = []
+    for q in range(30):
+        ref.step()
+        if q % 7 == 0:
+            vx, vy, vz = ref.vx, ref.vy, ref.vz
+            cx = np.zeros(vx.shape, np.float32)
+            cx[1:] = 0.5 * (vx[:-1] + vx[1:])
+            cx[0] = 0.5 * vx[0]
+            cy = np.zeros(vy.shape, np.float32)
+            cy[:, 1:] = 0.5 * (vy[:, :-1] + vy[:, 1:])
+            cy[:, 0] = 0.5 * vy[:, 0]
+            cz = np.zeros(vz.shape, np.float32)
+            cz[:, :, 1:] = 0.5 * (vz[:, :, :-1] + vz[:, :, 1:])
+            cz[:, :, 0] = 0.5 * vz[:, :, 0]
+            want.append((q, ref.p.copy(), cx, cy, cz))
+    snaps, vsnaps = s.get_snapshots(), s.get_velocity_snapshots()
+    assert [round(t / s.dt) for t, _ in snaps] == [w[0] for w in want]
+    for (t, p), (tv, *cv), (q, wp, *wc) in zip(snaps, vsnaps, want):
+        assert t == tv
+        np.testing.assert_array_equal(p, wp, err_msg=f"p after step {q}")
+        for got, exp, name in zip(cv, wc, "xyz"):
+            np.testing.assert_array_equal(got, exp, err_msg=f"centred v{name} after step {q}")
