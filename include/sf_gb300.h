@@ -241,7 +241,9 @@ int sf_plan_set_kernel(sf_plan* plan, int config, int i_chunk);
 int sf_kernel_config_count(void);
 const char* sf_kernel_config_name(int config);
 
-/* Autotuner: times every configuration that fits the grid for `launches`
+/* Autotuner: times every single-step configuration (the multi-step
+ * pipelines only run when chosen with sf_plan_set_kernel) that fits the
+ * grid for `launches`
  * step launches each (reading the current state and writing the other set
  * without swapping, no sources, no probes -- the state is unchanged) and
  * makes the fastest the plan's automatic choice, then times that one with

@@ -885,8 +885,6 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     cudaEvent_t e0, e1;
     SF_CUDA_OK(cudaEventCreate(&e0));
     SF_CUDA_OK(cudaEventCreate(&e1));
-    bool deferred = P->n_plane > 0;
-    for (int q = 0; q < P->src.n; ++q) deferred = deferred || P->src.s[q].kind == 2;
     int rc = 0;
     // ms per step of configuration cfg with planes per block ich (a warm-up
     // launch, then `launches` timed ones; a pipeline launch is `levels` steps)
@@ -913,7 +911,10 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
     float best_ms = 0.0f;
     for (int cfg = SF_CFG_CELL; cfg < count && !rc; ++cfg) {
         if (!config_native(P, cfg, a) || ((ade || P->nu) && cfg < SF_CFG_TILE_FIRST)) continue;
-        if (is_pipe(cfg) && deferred) continue;
+        // multi-step pipelines only by explicit choice: on GB300 they are
+        // slower than single steps, and their fewer launches per step would
+        // win a trial timed under a profiler that serialises launches
+        if (is_pipe(cfg)) continue;
         float ms = 0.0f;
         if ((rc = trial(cfg, chunk_for(P, cfg), &ms))) break;
         if (ms_out) ms_out[cfg] = ms;
