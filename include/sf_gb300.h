@@ -175,7 +175,10 @@ int sf_plan_set_microphones_ex(sf_plan* plan, int n, const int32_t* field, const
  * order, as ADEMaterialData holds them).  inv_dx = float(1/dx).  Replaces
  * update_ade_* / apply_ade_*_correction / compute_divergence
  * (kernels.cpp:670-886, ade.cpp:25-580) in the order of
- * core/solver.py:2135-2193. n = 0 turns ADE off. */
+ * core/solver.py:2135-2193; on a nonuniform grid (sf_plan_set_nonuniform)
+ * compute_divergence_nonuniform (ade.cpp:582-694) in the order of
+ * core/solver.py:2195-2283, the corrections still with inv_dx (the
+ * reference passes 1/min spacing).  n = 0 turns ADE off. */
 int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const sf_pole* poles,
                     float inv_dx);
 
@@ -187,8 +190,9 @@ int sf_plan_set_ade(sf_plan* plan, const uint8_t* material_id_dev, int n, const 
  * then coeff_p_base = -rho c^2 dt and coeff_v is unused: the velocity update
  * is v += cv_face[i] * (p[i+1] - p[i]) and the pressure update p +=
  * coeff_p_base * ((inv_x (dvx) + inv_y (dvy)) + inv_z (dvz)), each term
- * scaled before the sum.  Steps run the warp-tile kernels; no ADE.  Both
- * NULL returns the plan to a uniform grid. */
+ * scaled before the sum.  Steps run the warp-tile kernels (and, with ADE
+ * materials, the per-cell kernel inside the material box).  Both NULL
+ * returns the plan to a uniform grid. */
 int sf_plan_set_nonuniform(sf_plan* plan, const float* const* cv_face, const float* const* inv_cell);
 
 /* Weighted cell list `slot` (0 .. SF_MAX_SOURCES-1) of a kind-2 source:

@@ -10,8 +10,12 @@ native kernels.  ``precision="f32"`` reproduces FDTDSolver(backend="native")
 bit for bit (pinned against the reference's own outputs in tests/golden/);
 ``precision="f64"`` runs the same arithmetic in double to state the error of
 an FP32 result.  ADE materials are stepped in the order of
-_step_python_uniform (core/solver.py:2135-2193) with the native ADE kernels'
-arithmetic (the reference's native step skips ADE altogether).
+_step_python_uniform / _step_python_nonuniform (core/solver.py:2135-2193,
+2195-2283) with the native kernels' arithmetic (the reference's native step
+skips ADE altogether); on a nonuniform grid that is the nonuniform velocity
+and pressure updates, the uniform-dx velocity and pressure corrections and
+compute_divergence_nonuniform, the calls its python path makes when the
+native module is loaded (solver.py:3150-3170, 3294-3305).
 
 Voxelisation restates geometry/sdf.py with the same NumPy calls, so on one
 machine it reproduces SDFPrimitive.voxelize exactly.
@@ -62,6 +66,7 @@ def _declare(L):
             "ade_velocity_correction": [P, P, P, P, P, I, R, I, I, I],
             "ade_pressure_correction": [P, P, P, I, R, L64],
             "divergence": [P, P, P, P, I, I, I, R],
+            "divergence_nu": [P, P, P, P, I, I, I, P, P, P],
             "run_plain": [P, P, P, P, P, L64, P, P],
             "omp_threads": [],
             "set_threads": [I],
@@ -838,8 +843,13 @@ class FDTDSolver:
             F("apply_rigid")(_ptr(vx), _ptr(vy), _ptr(vz), _ptr(self.geometry.view(np.uint8)),
                              nx, ny, nz)
         if ade and any(e["target"] == 1 for e in ade["debye"] + ade["lorentz"]):
-            F("divergence")(_ptr(ade["div"]), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz,
-                            ade["inv_dx"])
+            if nu is not None:  # compute_divergence_nonuniform (solver.py:3161)
+                F("divergence_nu")(_ptr(ade["div"]), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz,
+                                   _ptr(nu["inv_dx_cell"]), _ptr(nu["inv_dy_cell"]),
+                                   _ptr(nu["inv_dz_cell"]))
+            else:
+                F("divergence")(_ptr(ade["div"]), _ptr(vx), _ptr(vy), _ptr(vz), nx, ny, nz,
+                                ade["inv_dx"])
             for e in ade["debye"]:
                 if e["target"] == 1:
                     F("ade_debye")(_ptr(e["J"]), _ptr(ade["div"]), _ptr(mat), e["mid"], *e["co"],

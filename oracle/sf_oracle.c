@@ -308,6 +308,22 @@ void FN(divergence)(real* div, const real* vx, const real* vy, const real* vz, i
             }
 }
 
+/* _kernels/src/ade.cpp:582-694 (compute_divergence_nonuniform): the same
+ * three passes with each cell's inverse spacing per axis, inv_d*_cell. */
+void FN(divergence_nu)(real* div, const real* vx, const real* vy, const real* vz, int nx,
+                       int ny, int nz, const real* sx, const real* sy, const real* sz) {
+    OMP_FOR
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++)
+            for (int k = 0; k < nz; k++) {
+                const int64_t c = IDX(i, j, k);
+                real d = ((i > 0) ? (vx[c] - vx[IDX(i - 1, j, k)]) : vx[c]) * sx[i];
+                d += ((j > 0) ? (vy[c] - vy[IDX(i, j - 1, k)]) : vy[c]) * sy[j];
+                d += ((k > 0) ? (vz[c] - vz[c - 1]) : vz[c]) * sz[k];
+                div[c] = d;
+            }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Whole-step driver for the plain path (no ADE), so that tests and the CPU
  * baseline can run many steps without a Python call per kernel.  Order is

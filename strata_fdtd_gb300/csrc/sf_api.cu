@@ -204,7 +204,6 @@ int sf_plan_set_nonuniform(sf_plan* P, const float* const* cv_face, const float*
     if (!cv_face || !inv_cell) return sf_fail("sf_plan_set_nonuniform: need both tables");
     for (int a = 0; a < 3; ++a)
         if (!cv_face[a] || !inv_cell[a]) return sf_fail("sf_plan_set_nonuniform: NULL axis table");
-    if (P->poles.n > 0) return sf_fail("sf_plan_set_nonuniform: ADE materials need a uniform grid");
     const int n[3] = {P->d.nx, P->d.ny, P->d.nz};
     const long long total = 2LL * (n[0] + n[1] + n[2]);
     SF_CUDA_OK(cudaMalloc(&P->nu, sizeof(float) * total));
@@ -346,7 +345,6 @@ int sf_plan_set_ade(sf_plan* P, const uint8_t* mat, int n, const sf_pole* poles,
     if (!P) return sf_fail("sf_plan_set_ade: NULL plan");
     if (n < 0 || n > SF_MAX_POLES) return sf_fail("sf_plan_set_ade: at most 16 poles");
     if (n > 0 && (!mat || !poles)) return sf_fail("sf_plan_set_ade: NULL material ids or poles");
-    if (n > 0 && P->nu) return sf_fail("sf_plan_set_ade: ADE materials need a uniform grid");
     SfPoles T{};
     T.inv_dx = inv_dx;
     for (int q = 0; q < n; ++q) {
@@ -478,7 +476,7 @@ int effective_config(const sf_plan* P, const SfStepArgs& a) {
     }
     const bool tile_ok =
         cfg >= SF_CFG_TILE_FIRST && sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec);
-    if (P->nu && !tile_ok)  // nonuniform arithmetic lives in the warp-tile kernels only
+    if (P->nu && !tile_ok && cfg != SF_CFG_CELL)  // nonuniform: warp tiles or per-cell only
         cfg = sf_tile_supported(a, 4) ? SF_CFG_TILE_DEFAULT : SF_CFG_TILE1_DEFAULT;
     else if (P->poles.n > 0 && !tile_ok)
         cfg = SF_CFG_CELL;

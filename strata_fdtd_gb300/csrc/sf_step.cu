@@ -12,6 +12,11 @@
 //   probe sampling           core/solver.py:2435-2439
 // and, with ADE materials, the pole recursions and corrections of
 // _kernels/src/ade.cpp:25-580 in the order of core/solver.py:2135-2193.
+// NU: a nonuniform grid (update_velocity_nonuniform / update_pressure_
+// nonuniform, fdtd_step.cpp:235-456, and for ADE modulus poles
+// compute_divergence_nonuniform, ade.cpp:582-694, in the order of
+// core/solver.py:2195-2283; the density and pressure corrections keep the
+// minimum spacing, as the reference passes them).
 //
 // The reference updates the fields in place, pass after pass.  A single pass
 // cannot: the new pressure of a cell needs the new face velocities of its
@@ -48,7 +53,7 @@ __device__ __forceinline__ float ade_face(float v, const SfPoles& P, uint8_t m_l
     return v;
 }
 
-template <bool GEOM, bool ADE>
+template <bool GEOM, bool ADE, bool NU>
 __global__ void __launch_bounds__(BX* BY) k_step(SfStepArgs a, SfSources src, SfPoles poles) {
     const int k = a.reg_lo[2] + blockIdx.x * BX + threadIdx.x;
     const int j = a.reg_lo[1] + blockIdx.y * BY + threadIdx.y;
@@ -72,19 +77,22 @@ __global__ void __launch_bounds__(BX* BY) k_step(SfStepArgs a, SfSources src, Sf
 
     // Faces on the high side of this cell.  The last plane of each axis
     // carries no update (fdtd_step.cpp:34,54,77 loop bounds).
+    // face coefficients: cv, or per face float(coeff_v_base * inv_face)
+    const float cvx = NU ? a.nu_cv[0][i] : cv, cvy = NU ? a.nu_cv[1][j] : cv,
+                cvz = NU ? a.nu_cv[2][k] : cv;
     float vxn = a.vx[c], vyn = a.vy[c], vzn = a.vz[c];
     if (i < nx - 1) {
-        vxn = face_update(vxn, cv, a.p[c + plane], pc);
+        vxn = face_update(vxn, cvx, a.p[c + plane], pc);
         if (ADE) vxn = ade_face(vxn, poles, mc, a.mat[c + plane], c, c + plane);
         if (GEOM && !(fc & SF_OPX)) vxn = 0.0f;
     }
     if (j < ny - 1) {
-        vyn = face_update(vyn, cv, a.p[c + nz], pc);
+        vyn = face_update(vyn, cvy, a.p[c + nz], pc);
         if (ADE) vyn = ade_face(vyn, poles, mc, a.mat[c + nz], c, c + nz);
         if (GEOM && !(fc & SF_OPY)) vyn = 0.0f;
     }
     if (k < nz - 1) {
-        vzn = face_update(vzn, cv, a.p[c + 1], pc);
+        vzn = face_update(vzn, cvz, a.p[c + 1], pc);
         if (ADE) vzn = ade_face(vzn, poles, mc, a.mat[c + 1], c, c + 1);
         if (GEOM && !(fc & SF_OPZ)) vzn = 0.0f;
     }
@@ -94,21 +102,21 @@ __global__ void __launch_bounds__(BX* BY) k_step(SfStepArgs a, SfSources src, Sf
     float vxm = 0.0f, vym = 0.0f, vzm = 0.0f;
     if (i > 0) {
         const long long m = c - plane;
-        float t = face_update(a.vx[m], cv, pc, a.p[m]);
+        float t = face_update(a.vx[m], NU ? a.nu_cv[0][i - 1] : cv, pc, a.p[m]);
         if (ADE) t = ade_face(t, poles, a.mat[m], mc, m, c);
         if (GEOM && !(a.flags[m] & SF_OPX)) t = 0.0f;
         vxm = t;
     }
     if (j > 0) {
         const long long m = c - nz;
-        float t = face_update(a.vy[m], cv, pc, a.p[m]);
+        float t = face_update(a.vy[m], NU ? a.nu_cv[1][j - 1] : cv, pc, a.p[m]);
         if (ADE) t = ade_face(t, poles, a.mat[m], mc, m, c);
         if (GEOM && !(a.flags[m] & SF_OPY)) t = 0.0f;
         vym = t;
     }
     if (k > 0) {
         const long long m = c - 1;
-        float t = face_update(a.vz[m], cv, pc, a.p[m]);
+        float t = face_update(a.vz[m], NU ? a.nu_cv[2][k - 1] : cv, pc, a.p[m]);
         if (ADE) t = ade_face(t, poles, a.mat[m], mc, m, c);
         if (GEOM && !(a.flags[m] & SF_OPZ)) t = 0.0f;
         vzm = t;
@@ -116,12 +124,23 @@ __global__ void __launch_bounds__(BX* BY) k_step(SfStepArgs a, SfSources src, Sf
 
     const bool air = (fc & SF_AIR) != 0;
     const float ddx = f_sub(vxn, vxm), ddy = f_sub(vyn, vym), ddz = f_sub(vzn, vzm);
-    float pn = air ? f_add(pc, f_mul(a.cp, f_add(f_add(ddx, ddy), ddz))) : 0.0f;
+    // cell scales: 1, or the cell's inverse spacing per axis
+    const float sx = NU ? a.nu_inv[0][i] : 1.0f, sy = NU ? a.nu_inv[1][j] : 1.0f,
+                sz = NU ? a.nu_inv[2][k] : 1.0f;
+    float pn;
+    if (NU)  // update_pressure_nonuniform: each term scaled first
+        pn = air ? f_add(pc, f_mul(a.cp, f_add(f_add(f_mul(sx, ddx), f_mul(sy, ddy)),
+                                                f_mul(sz, ddz))))
+                 : 0.0f;
+    else
+        pn = air ? f_add(pc, f_mul(a.cp, f_add(f_add(ddx, ddy), ddz))) : 0.0f;
 
     if (ADE && mc != 0 && poles.n_modulus > 0) {
-        // compute_divergence (ade.cpp:479-580): each term scaled before the add
-        const float s = poles.inv_dx;
-        const float div = f_add(f_add(f_mul(ddx, s), f_mul(ddy, s)), f_mul(ddz, s));
+        // compute_divergence (ade.cpp:479-580; nonuniform :582-694): each
+        // difference scaled before the add
+        const float s0 = NU ? sx : poles.inv_dx, s1 = NU ? sy : poles.inv_dx,
+                    s2 = NU ? sz : poles.inv_dx;
+        const float div = f_add(f_add(f_mul(ddx, s0), f_mul(ddy, s1)), f_mul(ddz, s2));
 #pragma unroll 1
         for (int q = 0; q < poles.n; ++q) {
             const sf_pole& pl = poles.p[q];
@@ -387,16 +406,24 @@ int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& pol
         const int blocks = (int)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16);
         if (n > 0) k_ade_density<<<blocks, 256, 0, st>>>(a, poles, n);
     }
-    if (geom) {
-        if (ade)
-            k_step<true, true><<<grd, blk, 0, st>>>(a, src, poles);
+    const bool nu = a.nu_cv[0] != nullptr;
+    if (nu) {
+        if (geom)
+            ade ? k_step<true, true, true><<<grd, blk, 0, st>>>(a, src, poles)
+                : k_step<true, false, true><<<grd, blk, 0, st>>>(a, src, poles);
         else
-            k_step<true, false><<<grd, blk, 0, st>>>(a, src, poles);
+            ade ? k_step<false, true, true><<<grd, blk, 0, st>>>(a, src, poles)
+                : k_step<false, false, true><<<grd, blk, 0, st>>>(a, src, poles);
+    } else if (geom) {
+        if (ade)
+            k_step<true, true, false><<<grd, blk, 0, st>>>(a, src, poles);
+        else
+            k_step<true, false, false><<<grd, blk, 0, st>>>(a, src, poles);
     } else {
         if (ade)
-            k_step<false, true><<<grd, blk, 0, st>>>(a, src, poles);
+            k_step<false, true, false><<<grd, blk, 0, st>>>(a, src, poles);
         else
-            k_step<false, false><<<grd, blk, 0, st>>>(a, src, poles);
+            k_step<false, false, false><<<grd, blk, 0, st>>>(a, src, poles);
     }
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_step launch failed");
 }

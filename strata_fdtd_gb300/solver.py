@@ -485,9 +485,6 @@ class FDTDSolver:
 
     # --------------------------------------------------------------- materials
     def register_material(self, material, material_id: int | None = None) -> int:
-        if not self._grid.is_uniform:
-            raise NotImplementedError("ADE materials on nonuniform grids are not implemented by "
-                                      "the GB300 backend")
         if material_id is None:
             material_id = next((i for i in range(1, 256) if i not in self._materials), None)
             if material_id is None:

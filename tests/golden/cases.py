@@ -260,6 +260,27 @@ ADE_CASES = {
         probes=[("mid", (35, 20, 40)), ("far", (60, 35, 20))],
         steps=140, store_fields=False,
     ),
+    "nu_mixed_geom": dict(
+        # ADE on a stretched grid: nonuniform updates and divergence, the
+        # corrections with the minimum spacing (core/solver.py:2195-2283)
+        shape=(36, 30, 40), res=1e-3, courant=0.5, pml=dict(depth=4),
+        grid=dict(kind="stretch", base=1e-3, stretch=(1.03, 1.0, 1.04), center_fine=True),
+        geometry=dict(kind="blocks", seed=13, n_boxes=1, n_spheres=1),
+        materials=[
+            dict(id=1, rho=1.4, c=320.0,
+                 poles=[("debye", "density", 0.3, 2e-4),
+                        ("lorentz", "modulus", 0.25, 2 * np.pi * 9000.0, 4000.0)],
+                 box=((8, 20), (6, 18), (10, 24))),
+            dict(id=4, rho=1.1, c=360.0,
+                 poles=[("lorentz", "density", 0.2, 2 * np.pi * 11000.0, 5000.0),
+                        ("debye", "modulus", 0.35, 3e-4)],
+                 box=((19, 30), (14, 26), (20, 34))),
+        ],
+        sources=[("point", (18, 15, 3), 20000.0, 1.0),
+                 ("plane", {"axis": 1, "index": 4}, 12000.0, 0.2)],
+        probes=[("a", (14, 12, 16)), ("b", (24, 20, 28)), ("c", (30, 8, 36))],
+        steps=120, store_fields=True,
+    ),
 }
 
 # --------------------------------------------------------------------------

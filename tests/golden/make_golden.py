@@ -79,15 +79,28 @@ def sha(a):
 
 def ade_step_native(self):
     """Reference ADE kernels in _step_python_uniform's order
-    (core/solver.py:2135-2193), each through the reference's own helper."""
+    (core/solver.py:2135-2193), each through the reference's own helper; on a
+    nonuniform grid _step_python_nonuniform's order (2195-2283) with the
+    native nonuniform velocity and pressure updates of _step_native_nonuniform
+    (2104-2126).  The ADE helpers pick their own native calls (uniform-dx
+    corrections, compute_divergence_nonuniform on a nonuniform grid)."""
     K = sys.modules["strata_fdtd.core._kernels"]
+    uniform = self._grid.is_uniform
     self._update_ade_density_poles()
-    K.update_velocity(self.p, self.vx, self.vy, self.vz, self._coeff_v)
+    if uniform:
+        K.update_velocity(self.p, self.vx, self.vy, self.vz, self._coeff_v)
+    else:
+        K.update_velocity_nonuniform(self.p, self.vx, self.vy, self.vz, self._native_grid_data,
+                                     self._coeff_v_base)
     self._apply_ade_velocity_correction()
     if self._boundary_cells is not None:
         K.apply_rigid_boundaries(self.vx, self.vy, self.vz, self._boundary_cells)
     self._update_ade_modulus_poles()
-    K.update_pressure(self.p, self.vx, self.vy, self.vz, self.geometry, self._coeff_p)
+    if uniform:
+        K.update_pressure(self.p, self.vx, self.vy, self.vz, self.geometry, self._coeff_p)
+    else:
+        K.update_pressure_nonuniform(self.p, self.vx, self.vy, self.vz, self.geometry,
+                                     self._native_grid_data, self._coeff_p_base)
     self._apply_ade_pressure_correction()
     self.p[~self.geometry] = 0.0
 
@@ -136,6 +149,7 @@ def run_case(api, name, case, ade, manifest):
         solver._initialize_ade_fields()
         fill_ade_native(solver, api.kernels)
         solver._step_native = types.MethodType(ade_step_native, solver)
+        solver._step_native_nonuniform = types.MethodType(ade_step_native, solver)
     for _ in range(case["steps"]):
         solver.step()
     out = {}

@@ -98,7 +98,7 @@ def _check_ade(s, name, manifest):
 
 @pytest.mark.parametrize("config", ["cell"] + [c for c in S.solver.kernel_configs()
                                                if c.startswith("tile")])
-@pytest.mark.parametrize("name", ["split_boxes_geom", "lorentz_mixed_geom"])
+@pytest.mark.parametrize("name", ["split_boxes_geom", "lorentz_mixed_geom", "nu_mixed_geom"])
 def test_ade_split_step_every_tile_config(name, config, manifest):
     """ADE steps split between a warp-tile kernel (outside the material
     boxes, rounded out to its tiles) and the per-cell ADE kernel (inside):
@@ -178,8 +178,6 @@ def test_nonuniform_autotune_and_limits(manifest):
     assert table["best"].startswith("tile")
     s.run_steps(case["steps"] - 7)
     _compare(s, "plain_nu_stretch_low_end", manifest)
-    with pytest.raises(NotImplementedError):
-        s.register_material(S.SimpleMaterial(name="m", _rho=1.2, _c=343.0, _poles=[]))
     with pytest.raises(NotImplementedError):
         S.BatchedSolver([s])
 
