@@ -265,6 +265,9 @@ class FDTDSolver:
         _native.check(self._lib.sf_plan_set_nonuniform(self._plan, fp, cp), "sf_plan_set_nonuniform")
 
     def __del__(self):
+        pool = getattr(self, "_snap_pool", None)
+        if pool is not None:
+            pool.shutdown(wait=False)
         plan = getattr(self, "_plan", None)
         if plan is not None and plan.value:
             try:
