@@ -21,13 +21,135 @@ from . import _native
 PLAIN_KERNELS = ("column", "warp", "warp_prefetch", "warp_prefetch_m8")
 
 
+class _PaddedTwin:
+    """A member whose nz is not a multiple of 4, re-planned with z padded to
+    the next multiple of 4 so the batch runs float4 warp tiles on it (scalar
+    tiles cost about half again as much per cell).  The padding cells are
+    solid: flag byte 0, so they are never updated or injected into and hold
+    zero pressure and velocity, and the face between the last real plane
+    and the padding is held at zero like every face into a solid.  The
+    reference never updates that face (the last plane of vz), so it stays at
+    its value, which is zero unless set by hand: a member whose last vz plane
+    is nonzero is batched as it is.  The PML decays of the padding are 1,
+    probe cells are re-indexed, ADE material ids and auxiliary fields are
+    padded copies.  State goes into the twin before a run and back after it;
+    the cells are the member's cells, so results are bit-identical."""
+
+    def __init__(self, s):
+        from .boundaries import PML
+
+        torch, lib = s._torch, s._lib
+        nx, ny, nz = s.shape
+        self.nz, self.nzp = nz, (nz + 3) // 4 * 4
+        shp = (nx, ny, self.nzp)
+        dev = s._device
+        self.version = s._tables_version
+        self.f = [[torch.zeros(shp, dtype=torch.float32, device=dev) for _ in range(4)]
+                  for _ in range(2)]
+        desc = _native.SfGridDesc(nx, ny, self.nzp, float(s._coeff_v), float(s._coeff_p), 0)
+        plan = ctypes.c_void_p()
+        _native.check(lib.sf_plan_create(ctypes.byref(desc), ctypes.byref(plan)), "sf_plan_create")
+        self.plan, self._lib = plan, lib
+        _native.check(lib.sf_plan_bind_fields(plan, *[t.data_ptr() for st in self.f for t in st]),
+                      "sf_plan_bind_fields")
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        geom = torch.zeros(shp, dtype=torch.uint8, device=dev)
+        geom[..., :nz] = torch.from_numpy(np.ascontiguousarray(s._geometry).view(np.uint8)).to(dev)
+        self._geom = geom
+        _native.check(lib.sf_plan_set_geometry(plan, geom.data_ptr(), stream), "sf_plan_set_geometry")
+        pml = [b for b in s._boundaries if isinstance(b, PML)]
+        if pml:
+            sx, sy, sz = pml[0].sigmas
+            if sz is not None:
+                sz = np.ascontiguousarray(np.concatenate([sz, np.zeros(self.nzp - nz, sz.dtype)]),
+                                          dtype=np.float32)
+            self._pml = (sx, sy, sz)
+            ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+            _native.check(lib.sf_plan_set_pml(plan, ptr(sx), ptr(sy), ptr(sz), float(s.dt)),
+                          "sf_plan_set_pml")
+        tab = (_native.SfSource * max(1, len(s._sources)))()
+        for q, src in enumerate(s._sources):
+            if src.source_type == "point":
+                tab[q].kind, (tab[q].a, tab[q].b, tab[q].c) = 0, tuple(int(v) for v in src.position)
+            else:
+                tab[q].kind, tab[q].a, tab[q].b = 1, int(src.position["axis"]), int(src.position["index"])
+        _native.check(lib.sf_plan_set_sources(plan, len(s._sources), ctypes.addressof(tab)),
+                      "sf_plan_set_sources")
+        cells = np.array([np.ravel_multi_index(s._probes[n].position, shp) for n in s._probe_order]
+                         or [0], dtype=np.int64)
+        _native.check(lib.sf_plan_set_probes(plan, len(s._probe_order), cells.ctypes.data),
+                      "sf_plan_set_probes")
+        self.J = []
+        if s.has_materials:
+            entries = s._ade_debye + s._ade_lorentz
+            poles = (_native.SfPole * max(1, len(entries)))()
+            for q, e in enumerate(entries):
+                J = torch.zeros(shp, dtype=torch.float32, device=dev)
+                Jp = torch.zeros(shp, dtype=torch.float32, device=dev) if "Jp" in e else None
+                self.J.append((e, J, Jp))
+                pl = poles[q]
+                pl.material_id, pl.kind, pl.target = e["mid"], 0 if Jp is None else 1, e["target"]
+                c = list(e["co"]) + [0.0] * (3 - len(e["co"]))
+                pl.c0, pl.c1, pl.c2, pl.corr = float(c[0]), float(c[1]), float(c[2]), float(e["corr"])
+                pl.J = J.data_ptr()
+                pl.J_prev = None if Jp is None else Jp.data_ptr()
+            mat = torch.zeros(shp, dtype=torch.uint8, device=dev)
+            mat[..., :nz] = s._mat_dev.view(nx, ny, nz)
+            self._mat = mat
+            _native.check(lib.sf_plan_set_ade(plan, mat.data_ptr(), len(entries),
+                                              ctypes.addressof(poles), float(s._ade_inv_dx)),
+                          "sf_plan_set_ade")
+            lo, hi = s._ade_box
+            _native.check(lib.sf_plan_set_ade_box(plan, (ctypes.c_int32 * 3)(*lo),
+                                                  (ctypes.c_int32 * 3)(*hi)), "sf_plan_set_ade_box")
+
+    @staticmethod
+    def eligible(s) -> bool:
+        nz = s.shape[2]
+        if nz % 4 == 0 or s._grid.is_uniform is False:
+            return False
+        return float(s._dev[s._cur()][3][..., nz - 1].abs().max()) == 0.0
+
+    def copy_in(self, s):
+        cur, nz = s._cur(), self.nz
+        for q in range(4):
+            self.f[cur][q][..., :nz].copy_(s._dev[cur][q])
+        for e, J, Jp in self.J:
+            J[..., :nz].copy_(e["J"].view(J.shape[0], J.shape[1], nz))
+            if Jp is not None:
+                Jp[..., :nz].copy_(e["Jp"].view(J.shape[0], J.shape[1], nz))
+        _native.check(self._lib.sf_plan_set_current(self.plan, cur), "sf_plan_set_current")
+
+    def copy_out(self, s):
+        cur, nz = int(self._lib.sf_plan_current(self.plan)), self.nz
+        for q in range(4):
+            s._dev[cur][q].copy_(self.f[cur][q][..., :nz])
+        for e, J, Jp in self.J:
+            e["J"].view(J.shape[0], J.shape[1], nz).copy_(J[..., :nz])
+            if Jp is not None:
+                e["Jp"].view(J.shape[0], J.shape[1], nz).copy_(Jp[..., :nz])
+        _native.check(self._lib.sf_plan_set_current(s._plan, cur), "sf_plan_set_current")
+
+    def __del__(self):
+        plan = getattr(self, "plan", None)
+        if plan is not None and plan.value:
+            try:
+                self._lib.sf_plan_destroy(plan)
+            except Exception:
+                pass
+            self.plan = None
+
+
 class BatchedSolver:
     """Steps ``solvers`` together.  ``rows`` (4, 8, 16) and ``i_chunk``
     (planes per tile, 0 = 16) set the tile shape and ``kernel`` (one of
     PLAIN_KERNELS) the kernel of the tiles away from material boxes;
     :meth:`autotune` picks all three."""
 
-    def __init__(self, solvers, rows: int = 8, i_chunk: int = 0, kernel: str = "warp_prefetch"):
+    PAD_MIN_CELLS = 1 << 25  # total cells of a run from which members are padded
+
+    def __init__(self, solvers, rows: int = 8, i_chunk: int = 0, kernel: str = "warp_prefetch",
+                 pad: bool = True):
         if not solvers:
             raise ValueError("BatchedSolver needs at least one solver")
         if any(s._microphones for s in solvers):
@@ -46,6 +168,7 @@ class BatchedSolver:
         if kernel not in PLAIN_KERNELS:
             raise ValueError(f"kernel must be one of {PLAIN_KERNELS}")
         self.kernel = kernel
+        self.pad = pad  # members with nz % 4 != 0 run as padded twins (float4 tiles) in big runs
         h = ctypes.c_void_p()
         _native.check(self._lib.sf_batch_create(ctypes.byref(h)), "sf_batch_create")
         self._batch = h
@@ -75,14 +198,32 @@ class BatchedSolver:
         if len(counts) != len(self.solvers):
             raise ValueError("one step count per solver")
         keep = []
+        self._twins = []
+        # padded twins give float4 items twice the size of scalar ones: they
+        # pay when the run has work for every resident warp several times
+        # over, and make small runs slower (fewer, larger items)
+        busy = sum(int(np.prod(s.shape)) for s, n in zip(self.solvers, counts) if n)
+        pad = self.pad and self.kernel != "column" and busy >= self.PAD_MIN_CELLS
         for s, n in zip(self.solvers, counts):
+            vz_handed_out = s._host_exposed["vz"]  # the caller may have edited vz
             s._sync_tables()
             s._upload_exposed()
             src = s.source_table(n) if s._sources else None
             n_probe = len(s._probe_order)
             trace = (torch.empty((n, n_probe), dtype=torch.float32, device=s._device)
                      if n_probe and n else None)
-            _native.check(lib.sf_batch_add(self._batch, s._plan, n,
+            plan = s._plan
+            twin = getattr(s, "_batch_twin", None) if pad and n and s.shape[2] % 4 else None
+            if twin is not None and (twin.version != s._tables_version or vz_handed_out):
+                twin = None  # tables changed, or vz may have been edited: check again
+            if twin is None and pad and n and _PaddedTwin.eligible(s):
+                twin = _PaddedTwin(s)
+                s._batch_twin = twin  # kept with the solver for later runs
+            if twin is not None:
+                twin.copy_in(s)
+                self._twins.append((s, twin))
+                plan = twin.plan
+            _native.check(lib.sf_batch_add(self._batch, plan, n,
                                            None if src is None else src.data_ptr(),
                                            None if trace is None else trace.data_ptr()),
                           "sf_batch_add")
@@ -121,6 +262,8 @@ class BatchedSolver:
         longest = max(n for _, n, _, _ in keep)
         _native.check(self._lib.sf_batch_run(self._batch, longest, int(graph_steps),
                                              self._stream()), "sf_batch_run")
+        for s, twin in self._twins:
+            twin.copy_out(s)
         for s, n, src, trace in keep:
             if trace is not None:
                 s._pending_traces.append((trace, list(s._probe_order)))

@@ -214,6 +214,7 @@ class FDTDSolver:
         self._microphones: dict = {}
         self._src_dirty = True
         self._probe_dirty = True
+        self._tables_version = 0  # bumped by every change to geometry, sources, probes, PML, ADE
         self._probe_order: list[str] = []
         self._pending_traces: list = []
         self._mic_order: list = []  # (name, rows) per microphone
@@ -373,6 +374,7 @@ class FDTDSolver:
         _native.check(self._lib.sf_plan_set_geometry(self._plan, dev.data_ptr(), self._stream()),
                       "sf_plan_set_geometry")
         self._src_dirty = True  # membrane sources inject into air cells only
+        self._tables_version += 1
 
     def set_geometry_sdf(self, solid: SDFPrimitive) -> None:
         """Geometry from a solid's SDF: air is the complement of the solid
@@ -384,6 +386,7 @@ class FDTDSolver:
         _native.check(self._lib.sf_plan_set_geometry(self._plan, dev.data_ptr(), self._stream()),
                       "sf_plan_set_geometry")
         self._src_dirty = True  # membrane sources inject into air cells only
+        self._tables_version += 1
 
     # --------------------------------------------------------- sources/probes
     def _to_index(self, pos, what):
@@ -421,6 +424,7 @@ class FDTDSolver:
         self._sources.append(source)
         self._src_cache = None
         self._src_dirty = True
+        self._tables_version += 1
 
     def add_probe(self, name: str, position) -> None:
         """core/solver.py:1843-1885."""
@@ -433,6 +437,7 @@ class FDTDSolver:
         self._probes[name] = Probe(name=name, position=tuple(int(v) for v in position),
                                    _solver=self)
         self._probe_dirty = True
+        self._tables_version += 1
 
     def add_microphone(self, position, name=None, pattern="omni", direction=None, up=None):
         """Microphone at a physical position, omnidirectional or with a polar
@@ -481,6 +486,7 @@ class FDTDSolver:
         _native.check(self._lib.sf_plan_set_pml(self._plan, ptr(sx), ptr(sy), ptr(sz),
                                                 float(self.dt)), "sf_plan_set_pml")
         self._pml_keepalive = (sx, sy, sz)
+        self._tables_version += 1
 
     def enable_snapshots(self, interval: int, capture_velocity: bool = False) -> None:
         self._snapshot_interval = interval
@@ -572,7 +578,10 @@ class FDTDSolver:
         _native.check(self._lib.sf_plan_set_ade_box(self._plan, (ctypes.c_int32 * 3)(*lo),
                                                     (ctypes.c_int32 * 3)(*hi)),
                       "sf_plan_set_ade_box")
+        self._ade_box = (lo, hi)
+        self._ade_inv_dx = inv_dx
         self._ade_initialized = True
+        self._tables_version += 1
 
     @property
     def _ade_J_debye(self) -> np.ndarray:

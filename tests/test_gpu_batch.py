@@ -109,3 +109,40 @@ def test_generated_batch_workload_members_equal_alone():
         for f in ("p", "vx"):
             np.testing.assert_array_equal(getattr(x, f), getattr(y, f))
         assert np.abs(x.p).max() > 0
+
+
+def test_padded_twins_equal_unpadded_batch_and_follow_table_changes(manifest):
+    """Members with nz % 4 != 0 run as padded twins (float4 tiles): fields,
+    traces and ADE fields equal the unpadded batch's and the reference's,
+    over several runs, and a probe added between runs rebuilds the twin."""
+    mix = [("plain", "blocks_odd"), ("ade", "lorentz_mixed_geom"), ("plain", "plane_yz_geom")]
+    assert any(_case(k, n)["shape"][2] % 4 for k, n in mix)
+    a = [C.build_case(API, _case(k, n)) for k, n in mix]
+    b = [C.build_case(API, _case(k, n)) for k, n in mix]
+    pa = BatchedSolver(a, kernel="warp_prefetch", pad=True)
+    pa.PAD_MIN_CELLS = 0  # pad this small batch too
+    pb = BatchedSolver(b, kernel="warp_prefetch", pad=False)
+    steps = [_case(k, n)["steps"] for k, n in mix]
+    first = [n // 3 for n in steps]
+    pa.run_steps(first, graph_steps=8)
+    pb.run_steps(first, graph_steps=8)
+    assert any(getattr(s, "_batch_twin", None) is not None for s in a)
+    twins = [getattr(s, "_batch_twin", None) for s in a]
+    for s in a + b:
+        s.add_probe("late", tuple(n // 2 for n in s.shape))
+    rest = [n - f for n, f in zip(steps, first)]
+    pa.run_steps(rest, graph_steps=0)
+    pb.run_steps(rest, graph_steps=0)
+    for s, t in zip(a, twins):
+        if t is not None:
+            assert s._batch_twin is not t  # rebuilt after the table change
+    for sa, sb, (kind, name) in zip(a, b, mix):
+        key = ("ade_" if kind == "ade" else "plain_") + name
+        for f in ("p", "vx", "vy", "vz"):
+            np.testing.assert_array_equal(getattr(sa, f), getattr(sb, f), err_msg=f"{name} {f}")
+            assert sha256(getattr(sa, f)) == manifest[key][f"sha_{f}"], f"{key} {f}"
+        for pn, tr in sb.get_probe_data().items():
+            np.testing.assert_array_equal(sa.get_probe_data()[pn], tr, err_msg=f"{name} {pn}")
+        if kind == "ade":
+            np.testing.assert_array_equal(sa._ade_J_debye, sb._ade_J_debye)
+            np.testing.assert_array_equal(sa._ade_J_lorentz, sb._ade_J_lorentz)
