@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--ichunk", type=int, default=0, help="planes per block (march)")
     ap.add_argument("--workload", default="enclosure", choices=["enclosure", "batch", "serve"])
     ap.add_argument("--requests", type=int, default=200)
-    ap.add_argument("--step-group", type=int, default=100)
+    ap.add_argument("--step-group", type=int, default=250)
     ap.add_argument("--max-active-cells", type=int, default=1 << 26,
                     help="served stream: cap on the cells of the running solves (0 = none)")
     ap.add_argument("--solo-cells", type=int, default=1 << 24,

@@ -105,9 +105,8 @@ class _PaddedTwin:
 
     @staticmethod
     def eligible(s) -> bool:
+        """The member's last vz plane is zero (the face the padding holds at zero)."""
         nz = s.shape[2]
-        if nz % 4 == 0 or s._grid.is_uniform is False:
-            return False
         return float(s._dev[s._cur()][3][..., nz - 1].abs().max()) == 0.0
 
     def copy_in(self, s):
@@ -213,12 +212,7 @@ class BatchedSolver:
             trace = (torch.empty((n, n_probe), dtype=torch.float32, device=s._device)
                      if n_probe and n else None)
             plan = s._plan
-            twin = getattr(s, "_batch_twin", None) if pad and n and s.shape[2] % 4 else None
-            if twin is not None and (twin.version != s._tables_version or vz_handed_out):
-                twin = None  # tables changed, or vz may have been edited: check again
-            if twin is None and pad and n and _PaddedTwin.eligible(s):
-                twin = _PaddedTwin(s)
-                s._batch_twin = twin  # kept with the solver for later runs
+            twin = s._padded_twin(vz_handed_out) if pad and n else None
             if twin is not None:
                 twin.copy_in(s)
                 self._twins.append((s, twin))

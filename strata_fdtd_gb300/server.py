@@ -82,7 +82,7 @@ class SolveServer:
     instead of processor sharing); a solve larger than the cap still runs,
     alone."""
 
-    def __init__(self, executor, hbm_budget: float = 160e9, step_group: int = 100,
+    def __init__(self, executor, hbm_budget: float = 160e9, step_group: int = 250,
                  max_active: int = 512, max_active_cells: int | None = None,
                  clock=time.perf_counter):
         self.ex = executor

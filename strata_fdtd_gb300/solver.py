@@ -215,6 +215,7 @@ class FDTDSolver:
         self._src_dirty = True
         self._probe_dirty = True
         self._tables_version = 0  # bumped by every change to geometry, sources, probes, PML, ADE
+        self._kernel_auto = True  # no kernel chosen by set_kernel: odd nz may run padded
         self._probe_order: list[str] = []
         self._pending_traces: list = []
         self._mic_order: list = []  # (name, rows) per microphone
@@ -692,13 +693,45 @@ class FDTDSolver:
                 return tab[off:off + n]
         return self._torch.from_numpy(self._source_values(n)).to(self._device)
 
+    def _padded_twin(self, vz_handed_out: bool):
+        """This solve's padded twin (batch.py, _PaddedTwin: z padded to a
+        multiple of 4 with solid cells, so the float4 warp tiles run it), made
+        once and kept until the tables change, or None when the solve cannot
+        use one: nz already a multiple of 4, a nonuniform grid, microphones,
+        plane boundaries or membrane sources, offsets past 32 bits, or a
+        nonzero last vz plane (checked again when vz was handed out)."""
+        nx, ny, nz = self.shape
+        if nz % 4 == 0 or not self._grid.is_uniform or self._microphones:
+            return None
+        if any(hasattr(b, "plane_ops") for b in self._boundaries) or any(
+                src.source_type == "membrane" for src in self._sources):
+            return None
+        nzp = (nz + 3) // 4 * 4
+        if nx * ny * nzp + 2 * ny * nzp + 8 >= 2**31 - 1:
+            return None
+        twin = getattr(self, "_pad_twin", None)
+        if twin is not None and (twin.version != self._tables_version or vz_handed_out):
+            twin = None
+        if twin is None:
+            from .batch import _PaddedTwin
+
+            twin = _PaddedTwin(self) if _PaddedTwin.eligible(self) else None
+            self._pad_twin = twin
+        return twin
+
+    _TWIN_MIN_STEPS = 32  # runs this long go through the padded twin (two state copies)
+
     def _advance(self, n: int) -> None:
         """Run n time steps through one sf_plan_step call."""
         torch = self._torch
         if n <= 0:
             return
+        vz_handed_out = self._host_exposed["vz"]
         self._sync_tables()
         self._upload_exposed()
+        twin = None
+        if n >= self._TWIN_MIN_STEPS and self._kernel_auto:
+            twin = self._padded_twin(vz_handed_out)
         src_dev = self.source_table(n) if self._sources else None
         n_probe = len(self._probe_order)
         trace = (torch.empty((n, n_probe), dtype=torch.float32, device=self._device)
@@ -706,12 +739,16 @@ class FDTDSolver:
         n_mic = getattr(self, "_mic_rows", 0)
         mic_trace = (torch.empty((n, n_mic), dtype=torch.float32, device=self._device)
                      if n_mic else None)
-        rc = self._lib.sf_plan_step_ex(self._plan, n,
+        if twin is not None:
+            twin.copy_in(self)
+        rc = self._lib.sf_plan_step_ex(self._plan if twin is None else twin.plan, n,
                                        None if src_dev is None else src_dev.data_ptr(),
                                        None if trace is None else trace.data_ptr(),
                                        None if mic_trace is None else mic_trace.data_ptr(),
                                        self._stream())
         _native.check(rc, "sf_plan_step")
+        if twin is not None:
+            twin.copy_out(self)
         if trace is not None:
             self._pending_traces.append((trace, list(self._probe_order)))
         times = []
@@ -897,6 +934,7 @@ class FDTDSolver:
             raise ValueError(f"unknown kernel {variant!r}; choose from {names}")
         _native.check(self._lib.sf_plan_set_kernel(self._plan, names.index(name), int(i_chunk)),
                       "sf_plan_set_kernel")
+        self._kernel_auto = name == "auto" and int(i_chunk) == 0
 
     def autotune(self, launches: int = 20) -> dict:
         """Time every kernel configuration on this grid (the state is left

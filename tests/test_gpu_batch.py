@@ -126,8 +126,8 @@ def test_padded_twins_equal_unpadded_batch_and_follow_table_changes(manifest):
     first = [n // 3 for n in steps]
     pa.run_steps(first, graph_steps=8)
     pb.run_steps(first, graph_steps=8)
-    assert any(getattr(s, "_batch_twin", None) is not None for s in a)
-    twins = [getattr(s, "_batch_twin", None) for s in a]
+    assert any(getattr(s, "_pad_twin", None) is not None for s in a)
+    twins = [getattr(s, "_pad_twin", None) for s in a]
     for s in a + b:
         s.add_probe("late", tuple(n // 2 for n in s.shape))
     rest = [n - f for n, f in zip(steps, first)]
@@ -135,7 +135,7 @@ def test_padded_twins_equal_unpadded_batch_and_follow_table_changes(manifest):
     pb.run_steps(rest, graph_steps=0)
     for s, t in zip(a, twins):
         if t is not None:
-            assert s._batch_twin is not t  # rebuilt after the table change
+            assert s._pad_twin is not t  # rebuilt after the table change
     for sa, sb, (kind, name) in zip(a, b, mix):
         key = ("ade_" if kind == "ade" else "plain_") + name
         for f in ("p", "vx", "vy", "vz"):
