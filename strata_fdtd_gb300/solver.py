@@ -11,8 +11,9 @@ accumulation (:2071-2072), ``step``/``run`` semantics (:2003-2077,
 What changes: the fields live in HBM as two ping-pong sets of CUDA tensors;
 one fused kernel per time step does the velocity, rigid-wall, pressure, PML,
 ADE, source and probe work; ``run`` issues all steps of a call in one C-ABI
-call with the waveform values precomputed (same NumPy call per step as the
-reference) and the probe traces kept on the device until read.
+call with the waveform values precomputed (the reference's NumPy
+expression at the same FP64 times, elementwise-identical) and the probe
+traces kept on the device until read.
 
 Host/device coherence: reading ``solver.p`` (etc.) copies the current device
 state into one persistent NumPy array per field, and marks it as possibly
@@ -663,17 +664,28 @@ class FDTDSolver:
             self._initialize_ade_fields()
 
     def _source_values(self, n: int) -> np.ndarray:
-        """Waveform per step at the FP64-accumulated times, one NumPy call
-        per source and step exactly as _inject_sources (core/solver.py:2413)."""
+        """Waveform per step at the FP64-accumulated times (t += dt each
+        step, as _time), as _inject_sources evaluates it (core/solver.py:2413)
+        one step at a time.  A GaussianPulse is evaluated over all n times in
+        one NumPy call: its operations are elementwise, so every value equals
+        the one-element call's (the tests check both ways against each other
+        and against the reference's values); any other waveform object is
+        called one step at a time."""
         vals = np.zeros((n, len(self._sources)), dtype=np.float64)
         if not self._sources:
             return vals
+        times = np.empty(n, dtype=np.float64)
         t = self._time
         for q in range(n):
-            for s, src in enumerate(self._sources):
-                wf = src.waveform if src.source_type == "membrane" else src
-                vals[q, s] = wf.waveform(np.array([t]), self.dt)[0]
+            times[q] = t
             t += self.dt
+        for s, src in enumerate(self._sources):
+            wf = src.waveform if src.source_type == "membrane" else src
+            if type(wf) is GaussianPulse:
+                vals[:, s] = wf.waveform(times, self.dt)
+            else:
+                for q in range(n):
+                    vals[q, s] = wf.waveform(np.array([times[q]]), self.dt)[0]
         return vals
 
     def precompute_sources(self, n: int) -> None:

@@ -190,3 +190,25 @@ def test_membrane_weights_match_oracle():
                 b = O.RectangularMembraneSource((0.014, 0.012, 0.016), ax, wf, (0.01, 0.007),
                                                 mode=mode)
                 np.testing.assert_array_equal(a.get_injection_weights(g), b.weights(og))
+
+
+def waveform_table_matches_per_step_calls(n=4000):
+    """The source table evaluates a GaussianPulse over all times of a call in
+    one NumPy call; every value must equal the one-element call the
+    reference makes per step (elementwise ufuncs give the same bits)."""
+    rng = np.random.default_rng(5)
+    for f, bw, amp in ((1000.0, None, 1.0), (2500.0, 800.0, 0.7), (20000.0, 15000.0, 1.3),
+                       (31000.0, None, -0.4)):
+        g = S.GaussianPulse(position=(0, 0, 0), frequency=f, bandwidth=bw, amplitude=amp)
+        dt = float(rng.uniform(1e-7, 2e-6))
+        t, ts = float(rng.uniform(0.0, 5e-4)), []
+        for _ in range(n):
+            ts.append(t)
+            t += dt
+        ts = np.array(ts)
+        per = np.array([g.waveform(np.array([x]), dt)[0] for x in ts])
+        np.testing.assert_array_equal(g.waveform(ts, dt).view(np.int64), per.view(np.int64))
+
+
+def test_waveform_table_matches_per_step_calls():
+    waveform_table_matches_per_step_calls()

@@ -232,3 +232,9 @@ def test_snapshots_equal_the_oracle_state_and_numpy_centring():
         np.testing.assert_array_equal(p, wp, err_msg=f"p after step {q}")
         for got, exp, name in zip(cv, wc, "xyz"):
             np.testing.assert_array_equal(got, exp, err_msg=f"centred v{name} after step {q}")
+
+
+def test_waveform_table_matches_per_step_calls_on_this_host():
+    """The same check with the NumPy of the machine that runs the GPU."""
+    from test_abi_host import waveform_table_matches_per_step_calls
+    waveform_table_matches_per_step_calls(20000)
