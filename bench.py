@@ -56,7 +56,9 @@ def parse():
     ap.add_argument("--size", type=int, default=400, help="grid edge (400 = the workload)")
     ap.add_argument("--kernel", default="auto", help="auto (autotuned) or a kernel configuration name")
     ap.add_argument("--ichunk", type=int, default=0, help="planes per block (march)")
-    ap.add_argument("--workload", default="enclosure", choices=["enclosure", "batch", "serve"])
+    ap.add_argument("--workload", default="enclosure",
+                    choices=["enclosure", "batch", "serve", "adjoint"])
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--step-group", type=int, default=250)
     ap.add_argument("--max-active-cells", type=int, default=1 << 26,
@@ -493,6 +495,57 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def run_adjoint(args):
+    """The differentiable solve: 128^3, 10-cell PML, design field on the
+    central 64^3, 1.5 kHz source, two probes, 2000 steps, checkpoints every
+    100 steps.  Times one probe-loss gradient (forward with checkpoints,
+    segment recomputation, reverse-time adjoint, dL/dtheta) against the
+    forward alone, in FP32 and FP64 working precision."""
+    import torch
+
+    from strata_fdtd_gb300.adjoint import DifferentiableSolver
+    from strata_fdtd_gb300.workloads import design_field
+
+    shape, n = (128, 128, 128), args.adjoint_steps
+    cells = int(np.prod(shape))
+    probes = [(100, 64, 64), (64, 100, 40)]
+    out = {}
+    for name, dt in (("f32", torch.float32), ("f64", torch.float64)):
+        s = DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
+                                 probes=probes, dtype=dt, checkpoint_every=100)
+        theta = torch.tensor(design_field(shape, 64, seed=0), device="cuda", dtype=dt)
+        target = s.forward(torch.tensor(design_field(shape, 64, seed=1), device="cuda"), n)[0]
+        th = theta.clone().requires_grad_(True)
+        s.loss(th, target[:200], 200).backward()  # warm-up
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        s.forward(theta, n, keep_checkpoints=False)
+        e1.record()
+        th = theta.clone().requires_grad_(True)
+        s.loss(th, target, n).backward()
+        e2.record()
+        torch.cuda.synchronize()
+        t_fwd, t_grad = e0.elapsed_time(e1) / 1e3, e1.elapsed_time(e2) / 1e3
+        out[name] = {"gradient_seconds": t_grad, "forward_seconds": t_fwd,
+                     "gradient_over_forward": t_grad / t_fwd,
+                     "forward_gcell_updates_per_s": cells * n / t_fwd / 1e9,
+                     "gradient_gcell_updates_per_s": cells * n / t_grad / 1e9,
+                     "peak_device_bytes": int(torch.cuda.max_memory_allocated())}
+        del s, theta, target, th
+        torch.cuda.empty_cache()
+    line = {"metric": "Gcell-updates/s (probe-loss gradient, forward steps per second)",
+            "value": out["f32"]["gradient_gcell_updates_per_s"], "unit": "Gcell-updates/s",
+            "n_gpus": 1, "steps": n, "warmup": 1, "ms_per_step": out["f32"]["gradient_seconds"] / n * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"128^3, PML 10, design field on the central 64^3, 1.5 kHz "
+                                   f"source, 2 probes, {n} steps, checkpoints every 100 steps"},
+            "f32": out["f32"], "f64": out["f64"]}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -501,6 +554,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_gpu(args)
 
