@@ -385,6 +385,14 @@ def run_batch(args):
     n = args.batch_solves
     seq, steps, info = batch_workload(seed=0, n_solves=n)
     cell_updates = sum(int(np.prod(s.shape)) * q for s, q in zip(seq, steps))
+    # untimed warm-up of every path the arms use (CUDA modules, torch kernels,
+    # a padded twin, a batch with graphs), so no arm pays the first-use costs
+    warm, wsteps, _ = batch_workload(seed=1, n_solves=2)
+    for w in warm:
+        w.run_steps(40)
+    BatchedSolver(warm).run_steps(60, graph_steps=args.graph_steps)
+    del warm
+    torch.cuda.synchronize()
     t_seq = t_one = float("nan")
     traces_seq = None
     if not args.batch_only:
