@@ -11,8 +11,7 @@
 // Work item = (level s, chunk c of S planes, (j,k) tile of 32 k x 4 rows),
 // one warp's job.  Warps claim items from an atomic counter in a fixed
 // wavefront order (level s runs `lag` chunks behind level s-1) and run each
-// with
-// tile4_run, the routine of the single-step warp-tile kernels, so every
+// with tile4_run, the routine of the single-step warp-tile kernels, so every
 // cell gets the reference's arithmetic in the reference's order and the
 // result is bit-identical to T single steps.
 //
