@@ -217,6 +217,7 @@ class FDTDSolver:
         self._probe_dirty = True
         self._tables_version = 0  # bumped by every change to geometry, sources, probes, PML, ADE
         self._kernel_auto = True  # no kernel chosen by set_kernel: odd nz may run padded
+        self._graph_epoch = 0  # bumped when the plan's kernel choice changes
         self._probe_order: list[str] = []
         self._pending_traces: list = []
         self._mic_order: list = []  # (name, rows) per microphone
@@ -473,6 +474,7 @@ class FDTDSolver:
             boundary.initialize(self)
             self._boundaries.append(boundary)
             self._plane_bc_dirty = True
+            self._tables_version += 1
             return
         if not isinstance(boundary, PML):
             raise NotImplementedError(f"{type(boundary).__name__} is not supported by the GB300 backend")
@@ -732,6 +734,40 @@ class FDTDSolver:
         return twin
 
     _TWIN_MIN_STEPS = 32  # runs this long go through the padded twin (two state copies)
+    _GRAPH_STEPS = 50     # steps per captured CUDA graph (even: the current set comes back)
+
+    def _graph_for(self, owner, plan, n_src: int, n_probe: int):
+        """A CUDA graph of _GRAPH_STEPS steps of ``plan`` from its current
+        set, reading the source values of those steps from a device buffer
+        and writing their probe rows to another (filled and drained around
+        each replay), kept on ``owner`` (this solver or its padded twin) until
+        the tables or the kernel choice change.  It replays exactly the
+        launches one sf_plan_step call makes, without the host's per-launch
+        overhead."""
+        torch = self._torch
+        cur = int(self._lib.sf_plan_current(plan))
+        stamp = (self._tables_version, self._graph_epoch)
+        cache = owner.__dict__.setdefault("_graphs", {})
+        if cache.get("stamp") != stamp:
+            cache.clear()
+            cache["stamp"] = stamp
+        key = (cur, n_src, n_probe)
+        if key in cache:
+            return cache[key]
+        G = self._GRAPH_STEPS
+        src = torch.zeros((G, max(1, n_src)), dtype=torch.float64, device=self._device)
+        trace = torch.zeros((G, max(1, n_probe)), dtype=torch.float32, device=self._device)
+        stream = torch.cuda.Stream(self._device)
+        stream.wait_stream(torch.cuda.current_stream(self._device))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            rc = self._lib.sf_plan_step_ex(plan, G, src.data_ptr() if n_src else None,
+                                           trace.data_ptr() if n_probe else None, None,
+                                           stream.cuda_stream)
+        _native.check(rc, "sf_plan_step (graph capture)")
+        torch.cuda.current_stream(self._device).wait_stream(stream)
+        cache[key] = (g, src, trace)
+        return cache[key]
 
     def _advance(self, n: int) -> None:
         """Run n time steps through one sf_plan_step call."""
@@ -753,12 +789,24 @@ class FDTDSolver:
                      if n_mic else None)
         if twin is not None:
             twin.copy_in(self)
-        rc = self._lib.sf_plan_step_ex(self._plan if twin is None else twin.plan, n,
-                                       None if src_dev is None else src_dev.data_ptr(),
-                                       None if trace is None else trace.data_ptr(),
-                                       None if mic_trace is None else mic_trace.data_ptr(),
-                                       self._stream())
-        _native.check(rc, "sf_plan_step")
+        plan = self._plan if twin is None else twin.plan
+        G = self._GRAPH_STEPS
+        n_graph = n - n % G if (mic_trace is None and self._kernel_auto) else 0
+        if n_graph:
+            g, gsrc, gtrace = self._graph_for(twin if twin is not None else self, plan,
+                                              len(self._sources), n_probe)
+            for q in range(0, n_graph, G):
+                if src_dev is not None:
+                    gsrc.copy_(src_dev[q:q + G])
+                g.replay()
+                if trace is not None:
+                    trace[q:q + G].copy_(gtrace[:, :n_probe])
+        if n > n_graph:
+            rc = self._lib.sf_plan_step_ex(
+                plan, n - n_graph, None if src_dev is None else src_dev[n_graph:].data_ptr(),
+                None if trace is None else trace[n_graph:].data_ptr(),
+                None if mic_trace is None else mic_trace.data_ptr(), self._stream())
+            _native.check(rc, "sf_plan_step")
         if twin is not None:
             twin.copy_out(self)
         if trace is not None:
@@ -947,6 +995,7 @@ class FDTDSolver:
         _native.check(self._lib.sf_plan_set_kernel(self._plan, names.index(name), int(i_chunk)),
                       "sf_plan_set_kernel")
         self._kernel_auto = name == "auto" and int(i_chunk) == 0
+        self._graph_epoch += 1
 
     def autotune(self, launches: int = 20) -> dict:
         """Time every kernel configuration on this grid (the state is left
@@ -961,6 +1010,7 @@ class FDTDSolver:
         best = C.c_int()
         _native.check(self._lib.sf_plan_autotune(self._plan, int(launches), self._stream(),
                                                  ms, C.byref(best)), "sf_plan_autotune")
+        self._graph_epoch += 1
         out = {n: float(ms[q]) for q, n in enumerate(names) if ms[q] >= 0}
         out["best"] = names[best.value]
         return out
