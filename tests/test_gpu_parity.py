@@ -535,3 +535,40 @@ def test_padded_twin_and_its_fallback_against_oracle():
             np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f"{when} {f}")
         for name in ref.get_probe_data():
             np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name])
+
+
+def test_graph_replays_follow_table_changes_against_oracle():
+    """Runs of 50 steps or more replay captured CUDA graphs: a probe added
+    between runs, a host edit of p, runs that leave remainders, a kernel
+    chosen and then automatic again; fields and every probe trace equal the
+    oracle's, and the graph cache is rebuilt after each table change."""
+    case = dict(shape=(30, 33, 40), res=1e-3, courant=0.5, pml=dict(depth=4),
+                geometry=dict(kind="blocks", seed=9, n_boxes=2, n_spheres=1),
+                sources=[("point", (15, 16, 20), 20000.0, 1.0),
+                         ("plane", {"axis": 2, "index": 6}, 11000.0, 0.2)],
+                probes=[("a", (10, 11, 12))], steps=0)
+    ref = C.build_case(ORACLE, case)
+    s = C.build_case(API, case)
+    for x in (ref, s):
+        x.run_steps(120)
+    stamp = s._graphs["stamp"]
+    for x in (ref, s):
+        x.add_probe("b", (25, 20, 30))
+        x.run_steps(75)
+    assert s._graphs["stamp"] != stamp
+    ref.p[5, 6, 7] += np.float32(0.25)
+    p = s.p
+    p[5, 6, 7] += np.float32(0.25)
+    for x in (ref, s):
+        x.run_steps(100)
+    s.set_kernel("tile1_r2_w4")
+    ref.run_steps(60)
+    s.run_steps(60)
+    s.set_kernel("auto")
+    ref.run_steps(150)
+    s.run_steps(150)
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f)
+    for name in ref.get_probe_data():
+        np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name],
+                                      err_msg=name)
