@@ -791,7 +791,9 @@ class FDTDSolver:
             twin.copy_in(self)
         plan = self._plan if twin is None else twin.plan
         G = self._GRAPH_STEPS
-        n_graph = n - n % G if (mic_trace is None and self._kernel_auto) else 0
+        n_graph = 0
+        if mic_trace is None and self._kernel_auto and not torch.cuda.is_current_stream_capturing():
+            n_graph = n - n % G  # (inside a caller's capture the launches go into its graph)
         if n_graph:
             g, gsrc, gtrace = self._graph_for(twin if twin is not None else self, plan,
                                               len(self._sources), n_probe)
