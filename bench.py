@@ -307,7 +307,10 @@ def run_gpu(args):
     barrier()
     clk = clocks.stop()
     ms = max_over_ranks(start.elapsed_time(end), dist, "cuda")
-    launches = K * (inner + 1)
+    # per bench step: the step kernels, and one probe gather per sf_plan_step
+    # call or captured block of steps (run_steps replays 50-step graphs)
+    G = S.FDTDSolver._GRAPH_STEPS if s._kernel_auto else inner + 1
+    launches = K * (inner + inner // G + (1 if inner % G else 0))
     value = replica_rate(world, cells * inner * K, ms / 1e3)
     kernel_ms = ms / (K * inner)  # every timed launch attributed to the step kernel
     hbm, peak_kind = peaks()
