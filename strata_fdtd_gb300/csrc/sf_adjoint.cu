@@ -62,8 +62,8 @@ __global__ void k_dcoef(const T* __restrict__ theta, T* __restrict__ cvx, T* __r
     cvz[c] = (k < nz - 1) ? face(c + 1) : T(0);
 }
 
-// Forward step (per cell, ping-pong): out = step(in); records p at the probe
-// cells of the *input* into trace_prev (the previous step's samples).
+// Forward step (per cell, ping-pong): out = step(in); p_store, when given,
+// receives the step's input pressure (k_dprobe samples the output).
 template <typename T>
 __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restrict__ vx,
                        const T* __restrict__ vy, const T* __restrict__ vz, T* __restrict__ po,
