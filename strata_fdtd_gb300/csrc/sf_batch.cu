@@ -282,8 +282,8 @@ __global__ void __launch_bounds__(32 * W, MINB) k_batch_warp(
         const int i1 = min(i0 + g.ich, g.nx);
         if (g.vec4) {
             const SfPlainMem mem{io.ny * io.nz};
-            if (geom) tile4_run<true, 1, PF>(io, g.src, i0, i1, j0, T.w * 32, mem);
-            else tile4_run<false, 1, PF>(io, g.src, i0, i1, j0, T.w * 32, mem);
+            if (geom) tile4_run<true, 1, PF, false, true>(io, g.src, i0, i1, j0, T.w * 32, mem);
+            else tile4_run<false, 1, PF, false, true>(io, g.src, i0, i1, j0, T.w * 32, mem);
         } else {
             const int k = T.w * 32 + lane;
             if (geom) tile1_run<true, 2, PF>(io, g.src, i0, i1, j0, k);
