@@ -366,12 +366,15 @@ int sf_diff_forward(const sf_diff_desc* d, void* const* cv, void* const* set0, v
  * starting from set `cur` holding lambda after the last step; p_store as
  * written by the forward; the probe-loss gradient weight*2*(trace-target)
  * is injected before each step's adjoint; dL/dcv accumulates into
- * grad_cv[3], three arrays of N doubles whatever the dtype (the per-face sum
- * runs over every step and cancels, so it is kept in FP64). */
+ * grad_cv[3], three arrays of N 8-byte words, zero-filled by the caller (the
+ * per-face sum runs over every step and cancels, so it keeps more precision
+ * than the fields): doubles for dtype 1; for dtype 0 a pair of floats
+ * (hi, lo) per face whose exact sum is the value, updated in double-word
+ * arithmetic so that the FP32 adjoint needs no FP64 instruction. */
 int sf_diff_adjoint(const sf_diff_desc* d, void* const* cv, void* const* lam0, void* const* lam1,
                     int cur, int64_t n_steps, const void* p_store, const void* trace,
                     const void* target, double weight, void* const* grad_cv, void* stream);
-/* dL/dtheta (dtype) from dL/dcv (grad_cv: FP64, as sf_diff_adjoint). */
+/* dL/dtheta (dtype) from dL/dcv (grad_cv as sf_diff_adjoint left it). */
 int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* grad_cv, void* out,
                        void* stream);
 

@@ -96,10 +96,15 @@ class DifferentiableSolver:
         return d
 
     def source_values(self, n_steps):
-        t, vals = 0.0, []
-        for _ in range(n_steps):
-            vals.append(self.pulse.waveform(np.array([t]), self.dt)[0])
+        """Pulse value per step at the FP64-accumulated times t += dt, in one
+        NumPy call over all times (the pulse's operations are elementwise, so
+        each value equals the one-time call's)."""
+        times = np.empty(n_steps, dtype=np.float64)
+        t = 0.0
+        for q in range(n_steps):
+            times[q] = t
             t += self.dt
+        vals = self.pulse.waveform(times, self.dt)
         return self.torch.tensor(vals, dtype=self.dtype, device=self.dev)
 
     def _stream(self):
@@ -151,7 +156,8 @@ class DifferentiableSolver:
         tgt[:, :target.shape[1]] = target.to(self.dtype)
         lam = [self._zeros4(), self._zeros4()]
         lcur = 0
-        # per-face dL/dcv sums run over every step: FP64 accumulators
+        # per-face dL/dcv sums run over every step: 8 bytes per face (a double,
+        # or for an FP32 solve a double-word float pair), zero-filled
         grad_cv = [torch.zeros(self.shape, dtype=torch.float64, device=self.dev) for _ in range(3)]
         desc = self._desc()
         store = torch.empty((self.K,) + self.shape, dtype=self.dtype, device=self.dev)

@@ -41,6 +41,61 @@ struct DiffPtrs {
     const T* dz;
 };
 
+// Per-face dL/dcv accumulators, 8 bytes per face.  The FP64 solve keeps a
+// double.  The FP32 solve keeps a double-word pair of floats (hi, lo): each
+// term a*b is formed exactly as ph + pl (pl = fma(a, b, -ph)) and added with
+// the accurate double-word sum (AccurateDWPlusDW of Joldes, Muller and
+// Popescu, "Tight and rigorous error bounds for basic building blocks of
+// double-word arithmetic", ACM TOMS 44(2), 2017: relative error at most
+// 3u^2, u = 2^-24), so that the FP32 adjoint issues no FP64 instruction in
+// its per-step kernel (GB300's FP64 pipe bounded it).
+template <typename T>
+struct GradAcc;
+
+template <>
+struct GradAcc<double> {
+    static __device__ __forceinline__ void add(double* g, long long c, double a, double b) {
+        g[c] += a * b;
+    }
+    static __device__ __forceinline__ double load(const double* g, long long c) { return g[c]; }
+};
+
+template <>
+struct GradAcc<float> {
+    // s + e = a + b exactly (Knuth's 2Sum)
+    static __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+        s = __fadd_rn(a, b);
+        const float bv = __fsub_rn(s, a);
+        const float av = __fsub_rn(s, bv);
+        e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+    }
+    // s + e = a + b exactly when |a| >= |b| (Dekker's Fast2Sum)
+    static __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+        s = __fadd_rn(a, b);
+        e = __fsub_rn(b, __fsub_rn(s, a));
+    }
+    static __device__ __forceinline__ void add(double* g, long long c, float a, float b) {
+        float2* q = reinterpret_cast<float2*>(g) + c;
+        const float2 x = *q;
+        const float ph = __fmul_rn(a, b);
+        const float pl = __fmaf_rn(a, b, -ph);
+        float sh, sl, th, tl, vh, vl, zh, zl;
+        two_sum(x.x, ph, sh, sl);
+        two_sum(x.y, pl, th, tl);
+        fast_two_sum(sh, __fadd_rn(sl, th), vh, vl);
+        fast_two_sum(vh, __fadd_rn(tl, vl), zh, zl);
+        *q = make_float2(zh, zl);
+    }
+    static __device__ __forceinline__ double load(const double* g, long long c) {
+        const float2 v = reinterpret_cast<const float2*>(g)[c];
+        return double(v.x) + double(v.y);
+    }
+};
+
+// Forward launches record up to this many probes themselves (one warp-uniform
+// compare per probe and cell) instead of launching k_dprobe after each step.
+constexpr int kFusedProbes = 4;
+
 // Coefficients from theta: cv_a(c) for the face between c and c + e_a
 // (zero on the last plane of each axis, which carries no face update).
 template <typename T>
@@ -63,12 +118,15 @@ __global__ void k_dcoef(const T* __restrict__ theta, T* __restrict__ cvx, T* __r
 }
 
 // Forward step (per cell, ping-pong): out = step(in); p_store, when given,
-// receives the step's input pressure (k_dprobe samples the output).
+// receives the step's input pressure; with n_fused > 0 the cells listed in
+// probe_cells write their new pressure into trace_row (else k_dprobe samples
+// the output after the step).
 template <typename T>
 __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restrict__ vx,
                        const T* __restrict__ vy, const T* __restrict__ vz, T* __restrict__ po,
                        T* __restrict__ vxo, T* __restrict__ vyo, T* __restrict__ vzo,
-                       long long src_cell, const T* __restrict__ src_val, T* __restrict__ p_store) {
+                       long long src_cell, const T* __restrict__ src_val, T* __restrict__ p_store,
+                       const int64_t* __restrict__ probe_cells, int n_fused, T* __restrict__ trace_row) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -94,6 +152,8 @@ __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restri
     pn = ((pn * di) * dj) * dk;
     if (c == src_cell && src_val != nullptr) pn = pn + *src_val;
     po[c] = pn;
+    for (int q = 0; q < n_fused; ++q)
+        if (c == probe_cells[q]) trace_row[q] = pn;
 }
 
 template <typename T>
@@ -113,7 +173,8 @@ __global__ void k_dinject(T* __restrict__ lp, const int64_t* __restrict__ cells,
 
 // Adjoint of one step.  in: lambda after the step; out: lambda before it;
 // pst: p^n (the step's input pressure); g*: accumulated dL/dcv per face,
-// held in FP64 whatever T is (the sum runs over every step and cancels).
+// 8 bytes per face as GradAcc<T> keeps them (the sum runs over every step
+// and cancels, so it keeps about twice T's precision for T = float).
 template <typename T>
 __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restrict__ lx,
                        const T* __restrict__ ly, const T* __restrict__ lz, T* __restrict__ lpo,
@@ -157,9 +218,9 @@ __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restr
     lpo[c] = acc;
     // dL/dcv on the high faces: mu_v * (p^n[hi] - p^n[lo])
     const T p0 = pst[c];
-    if (i < nx - 1) gx[c] += double(vx_hi) * double(pst[c + plane] - p0);
-    if (j < ny - 1) gy[c] += double(vy_hi) * double(pst[c + nz] - p0);
-    if (k < nz - 1) gz[c] += double(vz_hi) * double(pst[c + 1] - p0);
+    if (i < nx - 1) GradAcc<T>::add(gx, c, vx_hi, pst[c + plane] - p0);
+    if (j < ny - 1) GradAcc<T>::add(gy, c, vy_hi, pst[c + nz] - p0);
+    if (k < nz - 1) GradAcc<T>::add(gz, c, vz_hi, pst[c + 1] - p0);
 }
 
 // dL/dtheta(c) = (dt/dx) rho0 / (2 rho(c)^2) * sum of dL/dcv over its faces.
@@ -173,10 +234,11 @@ __global__ void k_dgrad(const T* __restrict__ theta, const double* __restrict__ 
     if (k >= nz || j >= ny) return;
     const long long plane = (long long)ny * nz;
     const long long c = (long long)i * plane + (long long)j * nz + k;
-    double s = gx[c] + gy[c] + gz[c];  // high faces (zero on the last plane)
-    if (i > 0) s += gx[c - plane];
-    if (j > 0) s += gy[c - nz];
-    if (k > 0) s += gz[c - 1];
+    using A = GradAcc<T>;
+    double s = A::load(gx, c) + A::load(gy, c) + A::load(gz, c);  // high faces (zero on the last plane)
+    if (i > 0) s += A::load(gx, c - plane);
+    if (j > 0) s += A::load(gy, c - nz);
+    if (k > 0) s += A::load(gz, c - 1);
     const double rho = rho0 * (1.0 + double(theta[c]));
     out[c] = T(s * dt_dx * rho0 / (2.0 * rho * rho));
 }
@@ -208,14 +270,16 @@ int forward(const sf_diff_desc* d, const void* const* cv, void* const* set0, voi
     const T* sv = static_cast<const T*>(src_vals);
     T* tr = static_cast<T*>(trace);
     T* ps = static_cast<T*>(p_store);
+    const bool fuse = tr && d->n_probe > 0 && d->n_probe <= kFusedProbes;
     for (int64_t s = 0; s < n; ++s) {
         void* const* in = cur ? set1 : set0;
         void* const* out = cur ? set0 : set1;
         k_dfwd<T><<<grid_of(d), dim3(32, 8), 0, st>>>(
             g, (const T*)in[0], (const T*)in[1], (const T*)in[2], (const T*)in[3], (T*)out[0],
             (T*)out[1], (T*)out[2], (T*)out[3], d->src_cell, sv ? sv + s : nullptr,
-            ps ? ps + s * N : nullptr);
-        if (tr && d->n_probe > 0)
+            ps ? ps + s * N : nullptr, d->probe_cells, fuse ? d->n_probe : 0,
+            fuse ? tr + s * d->n_probe : nullptr);
+        if (tr && d->n_probe > 0 && !fuse)
             k_dprobe<T><<<(d->n_probe + 127) / 128, 128, 0, st>>>((const T*)out[0], d->probe_cells,
                                                                   d->n_probe, tr + s * d->n_probe);
         cur = 1 - cur;
