@@ -6,7 +6,9 @@ Tolerances: FP64 adjoint vs FP64 autograd, rel 1e-9 (same arithmetic up to
 summation order); FP64 adjoint vs central differences (h = 1e-3), rel 1e-5
 (O(h^2) truncation); at the 128^3 x 2000-step workload the FP64 adjoint
 vs central differences rel 1e-5 and the FP32 adjoint vs the FP64 adjoint
-rel 1e-3."""
+rel 1e-3; probe traces from the in-kernel and the separate gather bit-equal,
+and at small size with 6 probes the FP32 adjoint vs the FP64 adjoint within
+1e-4 of the largest gradient entry."""
 import numpy as np
 import pytest
 
@@ -62,7 +64,7 @@ def test_differentiable_workload_fp32_against_fd():
     1.5 kHz source, 2000 steps, checkpoints every 100 steps.  The FP64
     adjoint gradient must match FP64 central differences (h = 1e-3) on 16
     random cells to rel 1e-5 (O(h^2) truncation); the FP32 adjoint (FP32
-    fields, FP64 face-gradient sums) must match the FP64 adjoint to rel 1e-3
+    fields, double-word face-gradient sums) must match the FP64 adjoint to rel 1e-3
     per sampled cell and 1e-3 in L2 over the design region (FP32 rounding of
     2000 forward and 2000 adjoint steps)."""
     shape = (128, 128, 128)
@@ -97,3 +99,51 @@ def test_differentiable_workload_fp32_against_fd():
     assert worst64 < 1e-5, worst64
     assert worst32 < 1e-3, worst32
     assert l2 < 1e-3, l2
+
+
+def test_probe_gather_paths_and_many_probe_gradients():
+    """Up to 4 probes are sampled inside the forward kernel, more by a
+    separate gather after each step: the traces of the probes both solvers
+    share must be identical bit for bit, in FP32 and FP64.  With 6 probes
+    (the separate gather) the FP64 adjoint must match autograd through the
+    plain PyTorch stepping (rel 1e-9), and the FP32 adjoint, whose face sums
+    are double-word float pairs, the FP64 adjoint to 1e-4 of the largest
+    gradient entry (FP32 rounding of 60 forward and 60 adjoint steps)."""
+    pos = [(12, 7, 9), (8, 3, 14), (10, 10, 4), (4, 5, 6), (13, 11, 15), (6, 12, 3)]
+
+    def make(dtype, probes):
+        return DifferentiableSolver((16, 14, 18), pml_depth=3, frequency=20000.0,
+                                    source=(5, 7, 9), probes=probes, dtype=dtype,
+                                    checkpoint_every=25)
+
+    theta = torch.tensor(design_field((16, 14, 18), region=8, seed=4, sigma=1.5), device="cuda")
+    target64 = make(torch.float64, pos).forward(
+        torch.tensor(design_field((16, 14, 18), region=8, seed=5, sigma=1.5), device="cuda"),
+        60)[0]
+    grads = {}
+    for dtype in (torch.float32, torch.float64):
+        few, many = make(dtype, pos[:3]), make(dtype, pos)
+        trace_few = few.forward(theta, 60)[0]
+        trace_many = many.forward(theta, 60)[0]
+        assert trace_many.shape == (60, 6)
+        assert torch.equal(trace_few, trace_many[:, :3])
+        assert float(trace_many.abs().max()) > 0
+        target = target64.to(dtype)
+        th = theta.clone().to(dtype).requires_grad_(True)
+        loss = many.loss(th, target, 60)
+        loss.backward()
+        grads[dtype] = th.grad.double()
+        if dtype == torch.float64:
+            ref_th = theta.clone().requires_grad_(True)
+            ref = reference_loss_torch(many, ref_th, target, 60)
+            ref.backward()
+            assert float(loss) == pytest.approx(float(ref), rel=1e-12)
+            r = ref_th.grad.cpu().numpy()
+            np.testing.assert_allclose(th.grad.cpu().numpy(), r, rtol=1e-9,
+                                       atol=1e-12 * np.abs(r).max())
+    g32, g64 = grads[torch.float32], grads[torch.float64]
+    scale = float(g64.abs().max())
+    assert scale > 0
+    err = float((g32 - g64).abs().max()) / scale
+    print(f"fp32 vs fp64 adjoint, 6 probes: max abs err / max |g| = {err:.3e}")
+    assert err < 1e-4, err
