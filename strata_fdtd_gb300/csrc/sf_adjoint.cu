@@ -54,10 +54,12 @@ struct GradAcc;
 
 template <>
 struct GradAcc<double> {
-    static __device__ __forceinline__ void add(double* g, long long c, double a, double b) {
+    template <class I>
+    static __device__ __forceinline__ void add(double* g, I c, double a, double b) {
         g[c] += a * b;
     }
-    static __device__ __forceinline__ double load(const double* g, long long c) { return g[c]; }
+    template <class I>
+    static __device__ __forceinline__ double load(const double* g, I c) { return g[c]; }
 };
 
 template <>
@@ -74,7 +76,8 @@ struct GradAcc<float> {
         s = __fadd_rn(a, b);
         e = __fsub_rn(b, __fsub_rn(s, a));
     }
-    static __device__ __forceinline__ void add(double* g, long long c, float a, float b) {
+    template <class I>
+    static __device__ __forceinline__ void add(double* g, I c, float a, float b) {
         float2* q = reinterpret_cast<float2*>(g) + c;
         const float2 x = *q;
         const float ph = __fmul_rn(a, b);
@@ -86,7 +89,8 @@ struct GradAcc<float> {
         fast_two_sum(vh, __fadd_rn(tl, vl), zh, zl);
         *q = make_float2(zh, zl);
     }
-    static __device__ __forceinline__ double load(const double* g, long long c) {
+    template <class I>
+    static __device__ __forceinline__ double load(const double* g, I c) {
         const float2 v = reinterpret_cast<const float2*>(g)[c];
         return double(v.x) + double(v.y);
     }
@@ -120,8 +124,9 @@ __global__ void k_dcoef(const T* __restrict__ theta, T* __restrict__ cvx, T* __r
 // Forward step (per cell, ping-pong): out = step(in); p_store, when given,
 // receives the step's input pressure; with n_fused > 0 the cells listed in
 // probe_cells write their new pressure into trace_row (else k_dprobe samples
-// the output after the step).
-template <typename T>
+// the output after the step).  I: the cell index type (int when the grid
+// has fewer than 2^31 cells: cheaper address arithmetic, same results).
+template <typename T, typename I>
 __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restrict__ vx,
                        const T* __restrict__ vy, const T* __restrict__ vz, T* __restrict__ po,
                        T* __restrict__ vxo, T* __restrict__ vyo, T* __restrict__ vzo,
@@ -131,9 +136,9 @@ __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restri
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= g.nz || j >= g.ny) return;
-    const long long plane = g.plane;
-    const int nz = g.nz;
-    const long long c = (long long)i * plane + (long long)j * nz + k;
+    const I plane = (I)g.plane;
+    const I nz = g.nz;
+    const I c = (I)i * plane + (I)j * nz + k;
     const T pc = p[c];
     if (p_store) p_store[c] = pc;
     T ux = vx[c], uy = vy[c], uz = vz[c];
@@ -150,10 +155,10 @@ __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restri
     vyo[c] = uy * dj;
     vzo[c] = uz * dk;
     pn = ((pn * di) * dj) * dk;
-    if (c == src_cell && src_val != nullptr) pn = pn + *src_val;
+    if ((long long)c == src_cell && src_val != nullptr) pn = pn + *src_val;
     po[c] = pn;
     for (int q = 0; q < n_fused; ++q)
-        if (c == probe_cells[q]) trace_row[q] = pn;
+        if ((long long)c == probe_cells[q]) trace_row[q] = pn;
 }
 
 template <typename T>
@@ -175,7 +180,7 @@ __global__ void k_dinject(T* __restrict__ lp, const int64_t* __restrict__ cells,
 // pst: p^n (the step's input pressure); g*: accumulated dL/dcv per face,
 // 8 bytes per face as GradAcc<T> keeps them (the sum runs over every step
 // and cancels, so it keeps about twice T's precision for T = float).
-template <typename T>
+template <typename T, typename I>
 __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restrict__ lx,
                        const T* __restrict__ ly, const T* __restrict__ lz, T* __restrict__ lpo,
                        T* __restrict__ lxo, T* __restrict__ lyo, T* __restrict__ lzo,
@@ -186,11 +191,11 @@ __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restr
     const int i = blockIdx.z;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     if (k >= nz || j >= ny) return;
-    const long long plane = g.plane;
-    const long long c = (long long)i * plane + (long long)j * nz + k;
+    const I plane = (I)g.plane;
+    const I c = (I)i * plane + (I)j * nz + k;
     const T di = g.dx[i], dj = g.dy[j], dk = g.dz[k];
     // mu_p = Dp lambda_p at this cell and its six neighbours
-    auto mup = [&](int ii, int jj, int kk, long long q) -> T {
+    auto mup = [&](int ii, int jj, int kk, I q) -> T {
         return g.dx[ii] * g.dy[jj] * g.dz[kk] * lp[q];
     };
     const T m0 = di * dj * dk * lp[c];
@@ -271,10 +276,12 @@ int forward(const sf_diff_desc* d, const void* const* cv, void* const* set0, voi
     T* tr = static_cast<T*>(trace);
     T* ps = static_cast<T*>(p_store);
     const bool fuse = tr && d->n_probe > 0 && d->n_probe <= kFusedProbes;
+    const bool narrow = N < (1LL << 31);
     for (int64_t s = 0; s < n; ++s) {
         void* const* in = cur ? set1 : set0;
         void* const* out = cur ? set0 : set1;
-        k_dfwd<T><<<grid_of(d), dim3(32, 8), 0, st>>>(
+        auto kernel = narrow ? k_dfwd<T, int> : k_dfwd<T, long long>;
+        kernel<<<grid_of(d), dim3(32, 8), 0, st>>>(
             g, (const T*)in[0], (const T*)in[1], (const T*)in[2], (const T*)in[3], (T*)out[0],
             (T*)out[1], (T*)out[2], (T*)out[3], d->src_cell, sv ? sv + s : nullptr,
             ps ? ps + s * N : nullptr, d->probe_cells, fuse ? d->n_probe : 0,
@@ -296,6 +303,7 @@ int adjoint(const sf_diff_desc* d, const void* const* cv, void* const* lam0, voi
     const T* ps = static_cast<const T*>(p_store);
     const T* tr = static_cast<const T*>(trace);
     const T* tg = static_cast<const T*>(target);
+    const bool narrow = N < (1LL << 31);
     for (int64_t s = n - 1; s >= 0; --s) {
         void* const* in = cur ? lam1 : lam0;  // lambda after step s
         void* const* out = cur ? lam0 : lam1;
@@ -303,7 +311,8 @@ int adjoint(const sf_diff_desc* d, const void* const* cv, void* const* lam0, voi
             k_dinject<T><<<(d->n_probe + 127) / 128, 128, 0, st>>>(
                 (T*)in[0], d->probe_cells, d->n_probe, tr + s * d->n_probe, tg + s * d->n_probe,
                 (T)weight);
-        k_dadj<T><<<grid_of(d), dim3(32, 8), 0, st>>>(
+        auto kernel = narrow ? k_dadj<T, int> : k_dadj<T, long long>;
+        kernel<<<grid_of(d), dim3(32, 8), 0, st>>>(
             g, (const T*)in[0], (const T*)in[1], (const T*)in[2], (const T*)in[3], (T*)out[0],
             (T*)out[1], (T*)out[2], (T*)out[3], ps + s * N, (double*)grad_cv[0],
             (double*)grad_cv[1], (double*)grad_cv[2]);
