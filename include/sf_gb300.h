@@ -245,6 +245,16 @@ int sf_plan_set_kernel(sf_plan* plan, int config, int i_chunk);
 int sf_kernel_config_count(void);
 const char* sf_kernel_config_name(int config);
 
+/* Bound of every cross-warp wait inside the multi-step pipeline kernels:
+ * `spins` sleeps of 64-256 ns before a wait gives up (0 = the default 2^22,
+ * about 1 s).  On expiry the kernel sets an error flag, its other waits and
+ * claims return at once, and sf_plan_step returns nonzero with "a
+ * dependency wait expired" in sf_last_error(); the state of that call is
+ * void and the next call starts clean.  hold_first_item != 0 is a test hook:
+ * the first work item also waits on a device flag that nothing sets, so the
+ * expiry path runs without any fault.  No counterpart in the reference. */
+int sf_plan_set_wait_limit(sf_plan* plan, int64_t spins, int hold_first_item);
+
 /* Autotuner: times every single-step configuration (the multi-step
  * pipelines only run when chosen with sf_plan_set_kernel) that fits the
  * grid for `launches`
@@ -288,12 +298,14 @@ int sf_plan_energy(sf_plan* plan, double rho, double c, double dx, double* scrat
  * a real-time loop that must not call cudaMalloc / cudaFree).  No
  * counterpart in the reference.  It allocates nothing: its scratch is a
  * fixed 4096-double (32 KiB) array in the library's device image, present
- * on every GPU that loads the library until exit.  The first call on a
- * device looks the array's device address up (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture
- * begins.  Calls share the array: two calls whose work
- * overlaps on the GPU race.  Refuses (nonzero status) a reduction that would
- * need more than the 4096 doubles.  Synchronises the stream. */
+ * on every GPU that loads the library until exit.  The array's device
+ * address is looked up (cudaGetSymbolAddress) once per device, with that
+ * device current, by the first sf_plan_create on it, so this call neither
+ * loads the module nor looks anything up; plans and this entry point are not
+ * usable across a cudaDeviceReset.  Calls share the array: two calls whose
+ * work overlaps on the GPU race.  Refuses (nonzero status) a reduction that
+ * would need more than the 4096 doubles (a device with more than 255 SMs).
+ * Synchronises the stream. */
 int sf_plan_energy_noalloc(sf_plan* plan, double rho, double c, double dx, double* out_host,
                            void* stream);
 
@@ -389,6 +401,20 @@ int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, d
  * nx, ny, nz doubles (NonuniformGrid.x/y/z_coords, core/grid.py:148-532). */
 int sf_voxelize_coords(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz,
                        const double* const* coords, int invert, uint8_t* out_dev, void* stream);
+
+/* Geometry and material ids voxelised in one pass, replacing
+ * MaterializedGeometry.voxelize_with_materials
+ * (geometry/material_assignment.py:133-171): program 0 (nodes[prog_off[0]
+ * .. prog_off[1]-1]) is the geometry, whose inside is air (geom_dev = 1);
+ * programs 1..n_regions are the material regions in assignment order, with
+ * ids[0..n_regions-1].  mat_dev receives the id of the last region that
+ * contains the cell centre, in air cells only, else 0.  coords: NULL for a
+ * uniform grid of spacing res, else three host arrays of cell centres.
+ * Both outputs are nx*ny*nz device bytes.  Synchronous. */
+int sf_voxelize_materials(const sf_sdf_node* nodes, const int32_t* prog_off, int n_regions,
+                          const uint8_t* ids, int nx, int ny, int nz, double res,
+                          const double* const* coords, uint8_t* geom_dev, uint8_t* mat_dev,
+                          void* stream);
 
 /* Signed distance of the same program at n points (device doubles, n x 3,
  * row major) into out_dev[n]; replaces SDFPrimitive.sdf

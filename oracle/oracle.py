@@ -609,6 +609,37 @@ class HelmholtzResonator(SDFPrimitive):  # geometry/resonator.py:59-297
 
 # ---------------------------------------------------------------------------
 # Solver (core/solver.py:1441-2606, native step semantics)
+class MaterializedGeometry:
+    """geometry/material_assignment.py:48-198: an SDF whose inside is air,
+    material regions in assignment order (ids 1, 2, ...), later ones
+    overriding earlier ones, inside air only."""
+
+    def __init__(self, geometry, default_material=None):
+        self.geometry = geometry
+        self.default_material = default_material
+        self._regions = []
+
+    def set_material(self, region, material):
+        mid = len(self._regions) + 1
+        if mid > 255:
+            raise ValueError("Maximum of 255 material regions exceeded")
+        self._regions.append((region, material, mid))
+        return mid
+
+    def voxelize_with_materials(self, grid):
+        mask = self.geometry.voxelize(grid)
+        ids = np.zeros(grid.shape, dtype=np.uint8)
+        for region, _, mid in self._regions:
+            ids[mask & region.voxelize(grid)] = mid
+        return mask, ids
+
+    def get_material_table(self):
+        table = {0: self.default_material}
+        for _, material, mid in self._regions:
+            table[mid] = material
+        return table
+
+
 class Probe:
     def __init__(self, name, position):
         self.name, self.position, self.data = name, position, []
@@ -646,7 +677,17 @@ class FDTDSolver:
 
     # -- setup (solver.py:1682-1990)
     def set_geometry(self, mask):
-        if isinstance(mask, SDFPrimitive):
+        if isinstance(mask, MaterializedGeometry):  # core/solver.py:1715-1760
+            geo = mask
+            mask, ids = geo.voxelize_with_materials(self.grid)
+            for mid, material in geo.get_material_table().items():
+                if mid == 0:
+                    continue
+                if mid not in self._materials:
+                    self.register_material(material, material_id=mid)
+                if np.any(ids == mid):
+                    self.set_material_region(ids == mid, mid)
+        elif isinstance(mask, SDFPrimitive):
             mask = mask.voxelize(self.grid)
         self.geometry = np.ascontiguousarray(mask, dtype=bool)
         self._geometry_set = True
@@ -977,4 +1018,5 @@ def make_api():
         GaussianPulse=GaussianPulse,
         Box=Box, Sphere=Sphere, Cylinder=Cylinder, Union=Union, Intersection=Intersection,
         Difference=Difference, HelmholtzResonator=HelmholtzResonator, Pole=Pole,
-        PoleType=PoleType, SimpleMaterial=SimpleMaterial)
+        PoleType=PoleType, SimpleMaterial=SimpleMaterial,
+        MaterializedGeometry=MaterializedGeometry)

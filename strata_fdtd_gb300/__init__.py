@@ -14,6 +14,7 @@ from .adjoint import DifferentiableSolver
 from .batch import BatchedSolver
 from .boundaries import PML, ABCFirstOrder, RadiationImpedance, RigidBoundary
 from .grid import NonuniformGrid, UniformGrid
+from .material_assignment import MaterializedGeometry, MaterialVolume
 from .microphones import Microphone
 from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
 from .membranes import CircularMembraneSource, MembraneSource, RectangularMembraneSource
@@ -31,5 +32,6 @@ __all__ = [
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale",
     "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",
     "NativeError", "BatchedSolver", "DifferentiableSolver", "MembraneSource",
-    "CircularMembraneSource", "RectangularMembraneSource",
+    "CircularMembraneSource", "RectangularMembraneSource", "MaterializedGeometry",
+    "MaterialVolume",
 ]

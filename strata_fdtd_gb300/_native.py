@@ -118,6 +118,7 @@ SIGNATURES = {
     "sf_plan_set_probes": (_I, [_P, _I, _P]),
     "sf_plan_set_ade": (_I, [_P, _P, _I, _P, _F]),
     "sf_plan_set_kernel": (_I, [_P, _I, _I]),
+    "sf_plan_set_wait_limit": (_I, [_P, _I64, _I]),
     "sf_kernel_config_count": (_I, []),
     "sf_kernel_config_name": (ctypes.c_char_p, [_I]),
     "sf_plan_autotune": (_I, [_P, _I, _P, _P, _P]),
@@ -148,6 +149,7 @@ SIGNATURES = {
     "sf_voxelize": (_I, [_P, _I, _I, _I, _I, _D, _I, _P, _P]),
     "sf_voxelize_coords": (_I, [_P, _I, _I, _I, _I, _P, _I, _P, _P]),
     "sf_sdf_eval": (_I, [_P, _I, _P, _I64, _P, _P]),
+    "sf_voxelize_materials": (_I, [_P, _P, _I, _P, _I, _I, _I, _D, _P, _P, _P, _P]),
 }
 
 _LIB = None

@@ -20,13 +20,33 @@
 //     lambda_v = mu_v,  lambda_p = mu_p + G^T C mu_v,
 //     dL/dcv_face += mu_v(face) * (G p^n)(face)
 // which k_dadj evaluates per cell (one fused stencil pass, reverse time).
-// Both directions are templated on the working precision (float / double).
+// Both directions are templated on the working precision: float, double, or
+// dwf (double-word floats, sf_dw.cuh: FP64-class accuracy on the FP32 pipe).
+// Values crossing the boundary (design field, source values, traces,
+// targets, gradients) are in the "external" type: the working type itself,
+// or double for dwf.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "sf_common.cuh"
+#include "sf_dw.cuh"
 #include "sf_gb300.h"
 
 namespace {
+
+template <typename T>
+struct Ext {
+    using E = T;
+    static __device__ __forceinline__ T in(E v) { return v; }
+    static __device__ __forceinline__ E out(T v) { return v; }
+};
+template <>
+struct Ext<dwf> {
+    using E = double;
+    static __device__ __forceinline__ dwf in(double v) { return dwf(v); }
+    static __device__ __forceinline__ double out(dwf v) { return v.to_double(); }
+};
 
 template <typename T>
 struct DiffPtrs {
@@ -96,25 +116,45 @@ struct GradAcc<float> {
     }
 };
 
+// Double-word solve: double-word products of double-word factors, summed in
+// double-word (sf_dw.cuh), the same 8 bytes per face.
+template <>
+struct GradAcc<dwf> {
+    template <class I>
+    static __device__ __forceinline__ void add(double* g, I c, dwf a, dwf b) {
+        float2* q = reinterpret_cast<float2*>(g) + c;
+        const float2 x = *q;
+        const dwf z = dwf(x.x, x.y) + a * b;
+        *q = make_float2(z.hi, z.lo);
+    }
+    template <class I>
+    static __device__ __forceinline__ double load(const double* g, I c) {
+        const float2 v = reinterpret_cast<const float2*>(g)[c];
+        return double(v.x) + double(v.y);
+    }
+};
+
 // Forward launches record up to this many probes themselves (one warp-uniform
 // compare per probe and cell) instead of launching k_dprobe after each step.
 constexpr int kFusedProbes = 4;
 
 // Coefficients from theta: cv_a(c) for the face between c and c + e_a
 // (zero on the last plane of each axis, which carries no face update).
-template <typename T>
-__global__ void k_dcoef(const T* __restrict__ theta, T* __restrict__ cvx, T* __restrict__ cvy,
-                        T* __restrict__ cvz, int nx, int ny, int nz, T dt_dx, T rho0) {
+// (formed in the external type: in double for a double-word solve, then
+// rounded to the nearest double-word)
+template <typename T, typename E = typename Ext<T>::E>
+__global__ void k_dcoef(const E* __restrict__ theta, T* __restrict__ cvx, T* __restrict__ cvy,
+                        T* __restrict__ cvz, int nx, int ny, int nz, E dt_dx, E rho0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= nz || j >= ny) return;
     const long long plane = (long long)ny * nz;
     const long long c = (long long)i * plane + (long long)j * nz + k;
-    const T b0 = T(1) / (rho0 * (T(1) + theta[c]));
+    const E b0 = E(1) / (rho0 * (E(1) + theta[c]));
     auto face = [&](long long n) {
-        const T b1 = T(1) / (rho0 * (T(1) + theta[n]));
-        return -dt_dx * T(0.5) * (b0 + b1);
+        const E b1 = E(1) / (rho0 * (E(1) + theta[n]));
+        return Ext<T>::in(-dt_dx * E(0.5) * (b0 + b1));
     };
     cvx[c] = (i < nx - 1) ? face(c + plane) : T(0);
     cvy[c] = (j < ny - 1) ? face(c + nz) : T(0);
@@ -126,12 +166,12 @@ __global__ void k_dcoef(const T* __restrict__ theta, T* __restrict__ cvx, T* __r
 // probe_cells write their new pressure into trace_row (else k_dprobe samples
 // the output after the step).  I: the cell index type (int when the grid
 // has fewer than 2^31 cells: cheaper address arithmetic, same results).
-template <typename T, typename I>
+template <typename T, typename I, typename E = typename Ext<T>::E>
 __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restrict__ vx,
                        const T* __restrict__ vy, const T* __restrict__ vz, T* __restrict__ po,
                        T* __restrict__ vxo, T* __restrict__ vyo, T* __restrict__ vzo,
-                       long long src_cell, const T* __restrict__ src_val, T* __restrict__ p_store,
-                       const int64_t* __restrict__ probe_cells, int n_fused, T* __restrict__ trace_row) {
+                       long long src_cell, const E* __restrict__ src_val, T* __restrict__ p_store,
+                       const int64_t* __restrict__ probe_cells, int n_fused, E* __restrict__ trace_row) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -155,25 +195,33 @@ __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restri
     vyo[c] = uy * dj;
     vzo[c] = uz * dk;
     pn = ((pn * di) * dj) * dk;
-    if ((long long)c == src_cell && src_val != nullptr) pn = pn + *src_val;
+    if ((long long)c == src_cell && src_val != nullptr) pn = pn + Ext<T>::in(*src_val);
     po[c] = pn;
     for (int q = 0; q < n_fused; ++q)
-        if ((long long)c == probe_cells[q]) trace_row[q] = pn;
+        if ((long long)c == probe_cells[q]) trace_row[q] = Ext<T>::out(pn);
 }
 
-template <typename T>
+template <typename T, typename E = typename Ext<T>::E>
 __global__ void k_dprobe(const T* __restrict__ p, const int64_t* __restrict__ cells, int n,
-                         T* __restrict__ out) {
+                         E* __restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) out[t] = p[cells[t]];
+    if (t < n) out[t] = Ext<T>::out(p[cells[t]]);
 }
 
 // lambda_p(probe) += w * 2 (trace - target): the loss gradient at step n.
-template <typename T>
+// (A double-word solve has no atomic add: one thread adds the probes in
+// order, which also handles probes that share a cell.)
+template <typename T, typename E = typename Ext<T>::E>
 __global__ void k_dinject(T* __restrict__ lp, const int64_t* __restrict__ cells, int n,
-                          const T* __restrict__ trace, const T* __restrict__ target, T w) {
+                          const E* __restrict__ trace, const E* __restrict__ target, E w) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) atomicAdd(&lp[cells[t]], w * T(2) * (trace[t] - target[t]));
+    if constexpr (std::is_same<T, dwf>::value) {
+        if (t == 0)
+            for (int q = 0; q < n; ++q)
+                lp[cells[q]] = lp[cells[q]] + dwf(w * 2.0 * (trace[q] - target[q]));
+    } else {
+        if (t < n) atomicAdd(&lp[cells[t]], w * T(2) * (trace[t] - target[t]));
+    }
 }
 
 // Adjoint of one step.  in: lambda after the step; out: lambda before it;
@@ -229,10 +277,10 @@ __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restr
 }
 
 // dL/dtheta(c) = (dt/dx) rho0 / (2 rho(c)^2) * sum of dL/dcv over its faces.
-template <typename T>
-__global__ void k_dgrad(const T* __restrict__ theta, const double* __restrict__ gx,
+template <typename T, typename E = typename Ext<T>::E>
+__global__ void k_dgrad(const E* __restrict__ theta, const double* __restrict__ gx,
                         const double* __restrict__ gy, const double* __restrict__ gz,
-                        T* __restrict__ out, int nx, int ny, int nz, double dt_dx, double rho0) {
+                        E* __restrict__ out, int nx, int ny, int nz, double dt_dx, double rho0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -245,7 +293,7 @@ __global__ void k_dgrad(const T* __restrict__ theta, const double* __restrict__ 
     if (j > 0) s += A::load(gy, c - nz);
     if (k > 0) s += A::load(gz, c - 1);
     const double rho = rho0 * (1.0 + double(theta[c]));
-    out[c] = T(s * dt_dx * rho0 / (2.0 * rho * rho));
+    out[c] = E(s * dt_dx * rho0 / (2.0 * rho * rho));
 }
 
 template <typename T>
@@ -270,10 +318,11 @@ dim3 grid_of(const sf_diff_desc* d) { return dim3((d->nz + 31) / 32, (d->ny + 7)
 template <typename T>
 int forward(const sf_diff_desc* d, const void* const* cv, void* const* set0, void* const* set1,
             int cur, int64_t n, const void* src_vals, void* trace, void* p_store, cudaStream_t st) {
+    using E = typename Ext<T>::E;
     const DiffPtrs<T> g = ptrs<T>(d, cv);
     const long long N = (long long)d->nx * d->ny * d->nz;
-    const T* sv = static_cast<const T*>(src_vals);
-    T* tr = static_cast<T*>(trace);
+    const E* sv = static_cast<const E*>(src_vals);
+    E* tr = static_cast<E*>(trace);
     T* ps = static_cast<T*>(p_store);
     const bool fuse = tr && d->n_probe > 0 && d->n_probe <= kFusedProbes;
     const bool narrow = N < (1LL << 31);
@@ -298,11 +347,12 @@ template <typename T>
 int adjoint(const sf_diff_desc* d, const void* const* cv, void* const* lam0, void* const* lam1,
             int cur, int64_t n, const void* p_store, const void* trace, const void* target,
             double weight, void* const* grad_cv, cudaStream_t st) {
+    using E = typename Ext<T>::E;
     const DiffPtrs<T> g = ptrs<T>(d, cv);
     const long long N = (long long)d->nx * d->ny * d->nz;
     const T* ps = static_cast<const T*>(p_store);
-    const T* tr = static_cast<const T*>(trace);
-    const T* tg = static_cast<const T*>(target);
+    const E* tr = static_cast<const E*>(trace);
+    const E* tg = static_cast<const E*>(target);
     const bool narrow = N < (1LL << 31);
     for (int64_t s = n - 1; s >= 0; --s) {
         void* const* in = cur ? lam1 : lam0;  // lambda after step s
@@ -310,7 +360,7 @@ int adjoint(const sf_diff_desc* d, const void* const* cv, void* const* lam0, voi
         if (tr && tg && d->n_probe > 0)
             k_dinject<T><<<(d->n_probe + 127) / 128, 128, 0, st>>>(
                 (T*)in[0], d->probe_cells, d->n_probe, tr + s * d->n_probe, tg + s * d->n_probe,
-                (T)weight);
+                (E)weight);
         auto kernel = narrow ? k_dadj<T, int> : k_dadj<T, long long>;
         kernel<<<grid_of(d), dim3(32, 8), 0, st>>>(
             g, (const T*)in[0], (const T*)in[1], (const T*)in[2], (const T*)in[3], (T*)out[0],
@@ -325,7 +375,8 @@ int check_desc(const sf_diff_desc* d) {
     if (!d) return sf_fail("sf_diff: NULL descriptor");
     if (d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nx > 65535)
         return sf_fail("sf_diff: bad grid dimensions");
-    if (d->dtype != 0 && d->dtype != 1) return sf_fail("sf_diff: dtype must be 0 (f32) or 1 (f64)");
+    if (d->dtype < 0 || d->dtype > 2)
+        return sf_fail("sf_diff: dtype must be 0 (f32), 1 (f64) or 2 (double-word f32)");
     if (!d->decay[0] || !d->decay[1] || !d->decay[2]) return sf_fail("sf_diff: decay arrays required");
     if (d->src_cell >= (long long)d->nx * d->ny * d->nz) return sf_fail("sf_diff: source outside");
     if (d->n_probe < 0 || (d->n_probe > 0 && !d->probe_cells)) return sf_fail("sf_diff: bad probes");
@@ -345,6 +396,10 @@ int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, vo
         k_dcoef<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
             (const double*)theta, (double*)cvx, (double*)cvy, (double*)cvz, d->nx, d->ny, d->nz,
             d->dt_over_dx, d->rho0);
+    else if (d->dtype == 2)
+        k_dcoef<dwf><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            (const double*)theta, (dwf*)cvx, (dwf*)cvy, (dwf*)cvz, d->nx, d->ny, d->nz,
+            d->dt_over_dx, d->rho0);
     else
         k_dcoef<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
             (const float*)theta, (float*)cvx, (float*)cvy, (float*)cvz, d->nx, d->ny, d->nz,
@@ -359,6 +414,8 @@ int sf_diff_forward(const sf_diff_desc* d, void* const* cv, void* const* set0, v
     if (!cv || !set0 || !set1 || (cur != 0 && cur != 1) || n_steps < 0)
         return sf_fail("sf_diff_forward: bad arguments");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (d->dtype == 2)
+        return forward<dwf>(d, cv, set0, set1, cur, n_steps, src_vals, trace, p_store, st);
     return d->dtype == 1
                ? forward<double>(d, cv, set0, set1, cur, n_steps, src_vals, trace, p_store, st)
                : forward<float>(d, cv, set0, set1, cur, n_steps, src_vals, trace, p_store, st);
@@ -371,6 +428,9 @@ int sf_diff_adjoint(const sf_diff_desc* d, void* const* cv, void* const* lam0, v
     if (!cv || !lam0 || !lam1 || !p_store || !grad_cv || (cur != 0 && cur != 1) || n_steps < 0)
         return sf_fail("sf_diff_adjoint: bad arguments");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (d->dtype == 2)
+        return adjoint<dwf>(d, cv, lam0, lam1, cur, n_steps, p_store, trace, target, weight,
+                            grad_cv, st);
     return d->dtype == 1 ? adjoint<double>(d, cv, lam0, lam1, cur, n_steps, p_store, trace, target,
                                            weight, grad_cv, st)
                          : adjoint<float>(d, cv, lam0, lam1, cur, n_steps, p_store, trace, target,
@@ -384,6 +444,10 @@ int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* gr
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (d->dtype == 1)
         k_dgrad<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
+            (const double*)theta, (const double*)grad_cv[0], (const double*)grad_cv[1],
+            (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
+    else if (d->dtype == 2)
+        k_dgrad<dwf><<<grid_of(d), dim3(32, 8), 0, st>>>(
             (const double*)theta, (const double*)grad_cv[0], (const double*)grad_cv[1],
             (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     else

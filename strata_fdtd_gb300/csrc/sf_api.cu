@@ -51,6 +51,8 @@ int sf_fail_cuda(cudaError_t e, const char* what, const char* file, int line) {
 
 #include "sf_plan_internal.h"
 
+int sf_noalloc_setup(int dev);  // defined with the no-alloc energy array below
+
 namespace {
 
 int set_decays(sf_plan* P, const float* host[3]) {
@@ -103,6 +105,15 @@ int sf_plan_create(const sf_grid_desc* desc, sf_plan** out) {
     P->ade_hi[1] = desc->ny;
     P->ade_hi[2] = desc->nz;
     cudaGetDevice(&P->device);
+    if (cudaDeviceGetAttribute(&P->sms, cudaDevAttrMultiProcessorCount, P->device) != cudaSuccess ||
+        P->sms < 1) {
+        delete P;
+        return sf_fail("sf_plan_create: cannot query the device's SM count");
+    }
+    if (int rc = sf_noalloc_setup(P->device)) {
+        delete P;
+        return rc;
+    }
     const int n[3] = {desc->nx, desc->ny, desc->nz};
     for (int a = 0; a < 3; ++a) {
         if (cudaMalloc(&P->decay[a], sizeof(float) * n[a]) != cudaSuccess) {
@@ -389,6 +400,14 @@ int sf_plan_set_kernel(sf_plan* P, int config, int i_chunk) {
     return 0;
 }
 
+int sf_plan_set_wait_limit(sf_plan* P, int64_t spins, int hold_first_item) {
+    if (!P) return sf_fail("sf_plan_set_wait_limit: NULL plan");
+    if (spins < 0) return sf_fail("sf_plan_set_wait_limit: negative limit");
+    P->pipe_spin_limit = spins;
+    P->pipe_hold = hold_first_item != 0;
+    return 0;
+}
+
 int sf_kernel_config_count(void) {
     return SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount + kSfPipeConfigCount;
 }
@@ -614,8 +633,8 @@ int pipe_buffers(sf_plan* P, int cfg, int S, cudaStream_t st) {
         P->pipe_ctrl_n = ctrl_n;
     }
     if (!P->pipe_err) {
-        SF_CUDA_OK(cudaMalloc(&P->pipe_err, sizeof(int)));
-        SF_CUDA_OK(cudaMemset(P->pipe_err, 0, sizeof(int)));
+        SF_CUDA_OK(cudaMalloc(&P->pipe_err, 2 * sizeof(int)));
+        SF_CUDA_OK(cudaMemset(P->pipe_err, 0, 2 * sizeof(int)));
     }
     if (!order_ok) {
         // waves w: level s takes chunk w - (s-1)*lag, lower levels first
@@ -685,6 +704,8 @@ int launch_pipe(sf_plan* P, int cfg, int S, const SfStepArgs& a, const SfSources
         A.ring = P->pipe_ring;
         A.ctrl = P->pipe_ctrl;
         A.err = P->pipe_err;
+        A.spin_limit = P->pipe_spin_limit > 0 ? P->pipe_spin_limit : SF_PIPE_SPIN_DEFAULT;
+        A.hold = P->pipe_hold ? P->pipe_err + 1 : nullptr;
         for (int l = 0; l < SF_PIPE_MAX_LEVELS; ++l)
             A.trace_lvl[l] = (trace_lvl && l < A.levels - 1) ? trace_lvl[l] : nullptr;
         SF_CUDA_OK(cudaMemsetAsync(P->pipe_ctrl, 0, sizeof(int) * (size_t)A.levels * A.ntiles, st));
@@ -709,6 +730,8 @@ int launch_pipe(sf_plan* P, int cfg, int S, const SfStepArgs& a, const SfSources
     A.order = P->pipe_order;
     A.ctrl = P->pipe_ctrl;
     A.err = P->pipe_err;
+    A.spin_limit = P->pipe_spin_limit > 0 ? P->pipe_spin_limit : SF_PIPE_SPIN_DEFAULT;
+    A.hold = P->pipe_hold ? P->pipe_err + 1 : nullptr;
     for (int l = 0; l < SF_PIPE_MAX_LEVELS; ++l)
         A.trace_lvl[l] = (trace_lvl && l < A.levels - 1) ? trace_lvl[l] : nullptr;
     SF_CUDA_OK(cudaMemsetAsync(P->pipe_ctrl, 0,
@@ -953,7 +976,7 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
 }
 
 int64_t sf_energy_scratch_doubles(const sf_plan* P) {
-    return P ? 2 * sf_energy_blocks(P->n) + 2 : 0;
+    return P ? 2 * sf_energy_blocks(P->n, P->sms) + 2 : 0;
 }
 
 int sf_plan_energy(sf_plan* P, double rho, double c, double dx, double* scratch,
@@ -962,9 +985,9 @@ int sf_plan_energy(sf_plan* P, double rho, double c, double dx, double* scratch,
     if (!P->bound) return sf_fail("sf_plan_energy: fields not bound");
     DeviceGuard g(P->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const long long nb = sf_energy_blocks(P->n);
+    const long long nb = sf_energy_blocks(P->n, P->sms);
     float* const* f = P->f[P->cur];
-    if (int rc = sf_launch_energy(f[0], f[1], f[2], f[3], P->flags, P->n, scratch,
+    if (int rc = sf_launch_energy(f[0], f[1], f[2], f[3], P->flags, P->n, P->sms, scratch,
                                   scratch + 2 * nb, st))
         return rc;
     double sums[2];
@@ -1021,7 +1044,76 @@ int voxelize_impl(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz,
 
 }  // namespace
 
+namespace {
+
+// Geometry and material ids in one pass (k_voxelize_materials): program p
+// is nodes[prog_off[p] .. prog_off[p+1]-1], program 0 the geometry, 1..n the
+// regions with ids[0..n-1].
+int voxelize_materials_impl(const sf_sdf_node* nodes, const int32_t* prog_off, int n_regions,
+                            const uint8_t* ids, int nx, int ny, int nz, double res,
+                            const double* const* coords, uint8_t* geom_dev, uint8_t* mat_dev,
+                            cudaStream_t st) {
+    if (!nodes || !prog_off || n_regions < 0 || n_regions > 255 || (n_regions > 0 && !ids) ||
+        !geom_dev || !mat_dev)
+        return sf_fail("sf_voxelize_materials: bad programs, ids or outputs");
+    if (nx < 1 || ny < 1 || nz < 1 || nx > 65535) return sf_fail("sf_voxelize_materials: bad grid");
+    for (int p = 0; p <= n_regions; ++p)
+        if (prog_off[p] < 0 || prog_off[p + 1] <= prog_off[p])
+            return sf_fail("sf_voxelize_materials: every program needs at least one node");
+    const int n_nodes = prog_off[n_regions + 1];
+    const size_t prog_bytes = (sizeof(sf_sdf_node) * n_nodes + 15) / 16 * 16;
+    const size_t off_bytes = (sizeof(int) * (n_regions + 2) + 15) / 16 * 16;
+    const size_t ids_bytes = (size_t)(n_regions + 16) / 16 * 16;
+    const size_t coord_bytes = coords ? sizeof(double) * ((size_t)nx + ny + nz) : 0;
+    char* buf = nullptr;
+    SF_CUDA_OK(cudaMalloc(&buf, prog_bytes + off_bytes + ids_bytes + 16 + coord_bytes));
+    sf_sdf_node* prog = reinterpret_cast<sf_sdf_node*>(buf);
+    int* off = reinterpret_cast<int*>(buf + prog_bytes);
+    uint8_t* idd = reinterpret_cast<uint8_t*>(buf + prog_bytes + off_bytes);
+    int* err = reinterpret_cast<int*>(buf + prog_bytes + off_bytes + ids_bytes);
+    double* cdev = coords ? reinterpret_cast<double*>(buf + prog_bytes + off_bytes + ids_bytes + 16)
+                          : nullptr;
+    int rc = 0, herr = 0;
+    if (cudaMemcpyAsync(prog, nodes, sizeof(sf_sdf_node) * n_nodes, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(off, prog_off, sizeof(int) * (n_regions + 2), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        (n_regions > 0 &&
+         cudaMemcpyAsync(idd, ids, n_regions, cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+        cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess)
+        rc = sf_fail("sf_voxelize_materials: upload failed");
+    if (!rc && coords) {
+        const int n3[3] = {nx, ny, nz};
+        size_t o = 0;
+        for (int a = 0; a < 3 && !rc; ++a) {
+            if (!coords[a] || cudaMemcpyAsync(cdev + o, coords[a], sizeof(double) * n3[a],
+                                              cudaMemcpyHostToDevice, st) != cudaSuccess)
+                rc = sf_fail("sf_voxelize_materials: coordinate upload failed");
+            o += n3[a];
+        }
+    }
+    if (!rc)
+        rc = sf_launch_voxelize_materials(prog, off, idd, n_regions, nx, ny, nz, res, cdev,
+                                          geom_dev, mat_dev, err, st);
+    if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess))
+        rc = sf_fail("sf_voxelize_materials: kernel failed");
+    cudaFree(buf);
+    if (!rc && herr) rc = sf_fail("sf_voxelize_materials: malformed SDF program (stack error)");
+    return rc;
+}
+
+}  // namespace
+
 extern "C" {
+
+int sf_voxelize_materials(const sf_sdf_node* nodes, const int32_t* prog_off, int n_regions,
+                          const uint8_t* ids, int nx, int ny, int nz, double res,
+                          const double* const* coords, uint8_t* geom_dev, uint8_t* mat_dev,
+                          void* stream) {
+    return voxelize_materials_impl(nodes, prog_off, n_regions, ids, nx, ny, nz, res, coords,
+                                   geom_dev, mat_dev, static_cast<cudaStream_t>(stream));
+}
 
 int sf_voxelize(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz, double res,
                 int invert, uint8_t* out_dev, void* stream) {
@@ -1076,12 +1168,12 @@ int sf_sdf_eval(const sf_sdf_node* nodes, int n_nodes, const double* points_dev,
 // every GPU that loads the library until the process exits.
 //
 // The reduction needs 2 partial sums per block plus 2 totals; its block
-// count is capped at 8 per SM (1216 on a 152-SM GB300), so every grid size
-// fits; a device with so many SMs that it would not fit is refused with an
-// error.  Every partial-sum slot is written before it is read, so nothing
-// has to be cleared between calls.  All calls share the one array per
-// device: calls whose kernels overlap on the GPU (two streams at once) race
-// and must not be issued.
+// count is capped at 8 per SM of the plan's device (1216 on a 152-SM GB300,
+// 2434 doubles), so a device with more than 255 SMs is refused with an error.
+// Every partial-sum slot is written before it is read, so nothing has to be
+// cleared between calls.  All calls share the one array per device: calls
+// whose kernels overlap on the GPU (two streams at once) race and must not be
+// issued.
 #define SF_NOALLOC_ENERGY_DOUBLES 4096
 #define SF_NOALLOC_MAX_DEVICES 64
 
@@ -1090,15 +1182,18 @@ static __device__ __align__(256) double g_sf_noalloc_energy[SF_NOALLOC_ENERGY_DO
 namespace {
 std::mutex g_noalloc_mu;
 double* g_noalloc_addr[SF_NOALLOC_MAX_DEVICES] = {nullptr};
+}  // namespace
 
-// Device address of the array on device `dev`, looked up once per device with
-// that device current, by the first sf_plan_energy_noalloc call on that
-// device (make that call before any stream capture begins).  In host code the
-// array's name is only a host-side stand-in; the kernel must be given this
-// address.
-int noalloc_scratch(int dev, double** out) {
+// Looks the array's device address up on device `dev` (which must be
+// current), once per device.  Called by sf_plan_create, so the module load
+// and the lookup happen when a plan is made and no energy call does them.
+// In host code the array's name is only a host-side stand-in; kernels must be
+// given this address.  A cudaDeviceReset invalidates it together with every
+// plan made before the reset; the library does not support using plans or
+// this entry point across a reset.
+int sf_noalloc_setup(int dev) {
     if (dev < 0 || dev >= SF_NOALLOC_MAX_DEVICES)
-        return sf_fail("sf_plan_energy_noalloc: device ordinal out of range");
+        return sf_fail("sf_plan_create: device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (!g_noalloc_addr[dev]) {
         void* p = nullptr;
@@ -1106,25 +1201,29 @@ int noalloc_scratch(int dev, double** out) {
         if (e != cudaSuccess) return sf_fail_cuda(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
         g_noalloc_addr[dev] = static_cast<double*>(p);
     }
-    *out = g_noalloc_addr[dev];
     return 0;
 }
-}  // namespace
 
 extern "C" int sf_plan_energy_noalloc(sf_plan* P, double rho, double c, double dx,
                                       double* out_host, void* stream) {
     if (!P || !out_host) return sf_fail("sf_plan_energy_noalloc: NULL argument");
     if (!P->bound) return sf_fail("sf_plan_energy_noalloc: fields not bound");
+    if (P->device < 0 || P->device >= SF_NOALLOC_MAX_DEVICES)
+        return sf_fail("sf_plan_energy_noalloc: device ordinal out of range");
     DeviceGuard g(P->device);
-    const long long nb = sf_energy_blocks(P->n);
+    const long long nb = sf_energy_blocks(P->n, P->sms);
     if (2 * nb + 2 > SF_NOALLOC_ENERGY_DOUBLES)
         return sf_fail("sf_plan_energy_noalloc: reduction needs more than the 4096-double "
-                       "fixed scratch");
+                       "fixed scratch (device with more than 255 SMs)");
     double* scratch = nullptr;
-    if (int rc = noalloc_scratch(P->device, &scratch)) return rc;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        scratch = g_noalloc_addr[P->device];
+    }
+    if (!scratch) return sf_fail("sf_plan_energy_noalloc: scratch address not set up");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     float* const* f = P->f[P->cur];
-    if (int rc = sf_launch_energy(f[0], f[1], f[2], f[3], P->flags, P->n, scratch,
+    if (int rc = sf_launch_energy(f[0], f[1], f[2], f[3], P->flags, P->n, P->sms, scratch,
                                   scratch + 2 * nb, st))
         return rc;
     double sums[2];

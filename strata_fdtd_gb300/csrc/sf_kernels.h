@@ -60,7 +60,14 @@ struct SfPipeArgs {
     int* ctrl;          // [0] next item; [1 + ((level-1)*nchunks + chunk)*ntiles + tile] done
     int* err;           // nonzero: a bounded wait expired (2)
     float* trace_lvl[SF_PIPE_MAX_LEVELS];  // probe row of level s+1's result, or null
+    long long spin_limit;  // sleeps (64-256 ns each) before a wait gives up
+    // Expiry test hook, normally null: a flag that nothing ever sets.  The
+    // first claimed item (k_step_pipe) or the first warp (k_step_stream)
+    // also waits on it, so its wait runs out and the launch fails cleanly.
+    const int* hold;
 };
+// Default bound of every pipeline wait: 2^22 sleeps, about 1 s.
+#define SF_PIPE_SPIN_DEFAULT (1LL << 22)
 int sf_launch_step_pipe(const SfPipeArgs& P, const SfSources& src, bool geom, int cfg, int grid,
                         cudaStream_t st);
 // Resident blocks of pipeline configuration cfg on this device (grid size).
@@ -95,12 +102,18 @@ int sf_launch_inject_weighted(float* f, const long long* cells, const double* w,
 int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const float* vz,
                          const int* field, const long long* idx, const float* w, int n, float* out,
                          cudaStream_t st);
-long long sf_energy_blocks(long long n);
+// Blocks of the energy reduction over n cells on a device with `sms` SMs
+// (at most 8 per SM); its scratch holds 2 partial sums per block + 2 totals.
+long long sf_energy_blocks(long long n, int sms);
 int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,
-                     const uint8_t* flags, long long n, double* scratch, double* out2,
+                     const uint8_t* flags, long long n, int sms, double* scratch, double* out2,
                      cudaStream_t st);
 int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny, int nz,
                        double res, const double* coords_dev, int invert, uint8_t* out,
                        int* err_dev, cudaStream_t st);
+int sf_launch_voxelize_materials(const sf_sdf_node* prog_dev, const int* off_dev,
+                                 const uint8_t* ids_dev, int n_regions, int nx, int ny, int nz,
+                                 double res, const double* coords_dev, uint8_t* geom,
+                                 uint8_t* mat, int* err_dev, cudaStream_t st);
 int sf_launch_sdf_points(const sf_sdf_node* prog_dev, int n_nodes, const double* pts, long long n,
                          double* out, int* err_dev, cudaStream_t st);

@@ -9,6 +9,7 @@ struct sf_plan {
     sf_grid_desc d{};
     long long n = 0;
     int device = 0;
+    int sms = 0;  // SM count of the device (sizes the energy reduction)
     float* f[2][4] = {{nullptr}};
     int cur = 0;
     bool bound = false;
@@ -44,7 +45,9 @@ struct sf_plan {
     size_t pipe_ring_floats = 0;
     int* pipe_ctrl = nullptr;  // owned: claim counter, tiles done per (level, chunk)
     int pipe_ctrl_n = 0;
-    int* pipe_err = nullptr;    // owned: wait-expiry flag
+    int* pipe_err = nullptr;    // owned: [0] wait-expiry flag, [1] a flag nothing sets
+    long long pipe_spin_limit = 0;  // sleeps before a pipeline wait gives up (0 = default)
+    bool pipe_hold = false;         // expiry test hook: the first item waits on pipe_err[1]
     int* pipe_order = nullptr;  // owned: (level, chunk) claim order
     int pipe_order_n = 0;
     int pipe_key[4] = {0, 0, 0, 0};  // levels, planes per chunk, lag, ring chunks of the order

@@ -468,15 +468,16 @@ int sf_launch_mic_gather(const float* p, const float* vx, const float* vy, const
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_mic_gather launch failed");
 }
 
-long long sf_energy_blocks(long long n) {
+long long sf_energy_blocks(long long n, int sms) {
+    const long long cap = 8LL * (sms > 0 ? sms : 1);
     long long b = (n + EN_THREADS - 1) / EN_THREADS;
-    return b < 152 * 8 ? (b < 1 ? 1 : b) : 152 * 8;
+    return b < cap ? (b < 1 ? 1 : b) : cap;
 }
 
 int sf_launch_energy(const float* p, const float* vx, const float* vy, const float* vz,
-                     const uint8_t* flags, long long n, double* scratch, double* out2,
+                     const uint8_t* flags, long long n, int sms, double* scratch, double* out2,
                      cudaStream_t st) {
-    const int nb = (int)sf_energy_blocks(n);
+    const int nb = (int)sf_energy_blocks(n, sms);
     k_energy_partial<<<nb, EN_THREADS, 0, st>>>(p, vx, vy, vz, flags, n, scratch);
     k_energy_final<<<1, EN_THREADS, 0, st>>>(scratch, nb, out2);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("energy launch failed");

@@ -46,8 +46,6 @@ const int kSfPipeConfigCount = sizeof(kSfPipeConfigs) / sizeof(kSfPipeConfigs[0]
 
 namespace {
 
-constexpr long long kSpinLimit = 1LL << 22;  // ~1 s of 256 ns sleeps
-
 // Ring or state-set addressing for one level: input from the previous
 // level's ring (IN_RING) or the input set, output to this level's ring
 // (OUT_RING) or the output set.  Ring plane of grid plane i: i mod wrap.
@@ -95,17 +93,17 @@ __device__ __forceinline__ int ld_relaxed(const int* p) {
     return v;
 }
 
-// Waits until *p != 0 (bounded), then orders this thread's later accesses
-// after the writes the flag publishes.  False when the error flag is or
-// gets set.
-__device__ bool wait_flag(const int* p, int* err) {
+// Waits until *p != 0 (at most `limit` sleeps), then orders this thread's
+// later accesses after the writes the flag publishes.  False when the error
+// flag is or gets set.
+__device__ bool wait_flag(const int* p, int* err, long long limit) {
     for (long long it = 0;; ++it) {
         if (ld_relaxed(p) != 0) {
             asm volatile("fence.acq_rel.gpu;" ::: "memory");
             return true;
         }
         if (ld_relaxed(err) != 0) return false;
-        if (it >= kSpinLimit) {
+        if (it >= limit) {
             atomicExch(err, 2);
             return false;
         }
@@ -183,7 +181,9 @@ __global__ void __launch_bounds__(32 * W, MINB) k_step_pipe(SfPipeArgs P, SfSour
         bool ok = true;
         if (lane < 30) {
             const int* f = dep_flag(P, s, c, t, lane);
-            if (f != nullptr) ok = wait_flag(f, P.err);
+            if (f != nullptr) ok = wait_flag(f, P.err, P.spin_limit);
+        } else if (lane == 30 && q == 0 && P.hold != nullptr) {
+            ok = wait_flag(P.hold, P.err, P.spin_limit);  // expiry test hook
         }
         if (!__all_sync(kFull, ok)) break;
         const int i0 = c * P.S, i1 = min(i0 + P.S, a.nx);
@@ -325,7 +325,7 @@ struct SfStreamMem {
             lack = (IN_RING && seen_prev < need_p) || (OUT_RING && seen_next < need_n);
             if (!lack) break;
             bool give_up = ld_relaxed(P.err) != 0;
-            if (!give_up && it >= kSpinLimit) {
+            if (!give_up && it >= P.spin_limit) {
                 atomicExch(P.err, 2);
                 give_up = true;
             }
@@ -361,6 +361,11 @@ __global__ void __launch_bounds__(32 * W, MINB) k_step_stream(SfPipeArgs P, SfSo
             a.trace_prev[t] = a.p[a.probe_cells[t]];
     const int wid = blockIdx.x * W + threadIdx.y;
     if (wid >= P.levels * P.ntiles) return;  // whole warp; no block barrier follows
+    if (P.hold != nullptr && wid == 0) {  // expiry test hook: never satisfied
+        bool ok = true;
+        if (lane == 0) ok = wait_flag(P.hold, P.err, P.spin_limit);
+        if (!__all_sync(sf_tile::kFull, ok)) return;  // the error flag is set
+    }
     const int s = wid / P.ntiles + 1, t = wid - (s - 1) * P.ntiles;
     const int tk = t % P.ntk, tj = t / P.ntk, ntj = P.ntiles / P.ntk;
     const int plane = a.ny * a.nz, wrap = P.M;

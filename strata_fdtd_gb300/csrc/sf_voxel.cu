@@ -165,6 +165,52 @@ __global__ void k_voxelize(const sf_sdf_node* __restrict__ prog, int n_nodes, in
     out[((long long)i * ny + j) * nz + k] = (uint8_t)(inside != (invert != 0));
 }
 
+// MaterializedGeometry.voxelize_with_materials (geometry/
+// material_assignment.py:133-171) in one pass: program 0 (nodes
+// off[0]..off[1]-1) is the geometry, inside = air; programs 1..n_regions are
+// the material regions in assignment order, region r giving id ids[r-1].  A
+// cell's id is that of the last region containing it, within air only, else
+// 0 -- the reference's ordered overwrites.  Regions are tried from the last
+// down and the first hit wins, which gives the same id with fewer programs
+// evaluated.
+__global__ void k_voxelize_materials(const sf_sdf_node* __restrict__ prog,
+                                     const int* __restrict__ off, const uint8_t* __restrict__ ids,
+                                     int n_regions, int nx, int ny, int nz, double res,
+                                     const double* __restrict__ coords,
+                                     uint8_t* __restrict__ geom, uint8_t* __restrict__ mat,
+                                     int* __restrict__ err_flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    double x, y, z;
+    if (coords) {
+        x = coords[i];
+        y = coords[nx + j];
+        z = coords[nx + ny + k];
+    } else {
+        const double half = d_mul(res, 0.5);
+        x = d_add(d_mul((double)i, res), half);
+        y = d_add(d_mul((double)j, res), half);
+        z = d_add(d_mul((double)k, res), half);
+    }
+    int err = 0;
+    const bool air = eval_sdf(prog + off[0], off[1] - off[0], x, y, z, &err) <= 0.0;
+    uint8_t m = 0;
+    if (air) {
+        for (int r = n_regions; r >= 1; --r) {
+            if (eval_sdf(prog + off[r], off[r + 1] - off[r], x, y, z, &err) <= 0.0) {
+                m = ids[r - 1];
+                break;
+            }
+        }
+    }
+    if (err) atomicExch(err_flag, err);
+    const long long c = ((long long)i * ny + j) * nz + k;
+    geom[c] = (uint8_t)air;
+    mat[c] = m;
+}
+
 __global__ void k_sdf_points(const sf_sdf_node* __restrict__ prog, int n_nodes,
                              const double* __restrict__ pts, long long n, double* __restrict__ out,
                              int* __restrict__ err_flag) {
@@ -194,4 +240,14 @@ int sf_launch_voxelize(const sf_sdf_node* prog_dev, int n_nodes, int nx, int ny,
     k_voxelize<<<grd, blk, 0, st>>>(prog_dev, n_nodes, nx, ny, nz, res, coords_dev, invert, out,
                                     err_dev);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_voxelize launch failed");
+}
+
+int sf_launch_voxelize_materials(const sf_sdf_node* prog_dev, const int* off_dev,
+                                 const uint8_t* ids_dev, int n_regions, int nx, int ny, int nz,
+                                 double res, const double* coords_dev, uint8_t* geom,
+                                 uint8_t* mat, int* err_dev, cudaStream_t st) {
+    dim3 blk(32, 8, 1), grd((nz + 31) / 32, (ny + 7) / 8, nx);
+    k_voxelize_materials<<<grd, blk, 0, st>>>(prog_dev, off_dev, ids_dev, n_regions, nx, ny, nz,
+                                              res, coords_dev, geom, mat, err_dev);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("k_voxelize_materials launch failed");
 }

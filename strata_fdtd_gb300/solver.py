@@ -358,10 +358,30 @@ class FDTDSolver:
         return self._grid
 
     def set_geometry(self, geometry) -> None:
-        """Boolean mask (True = air) or an SDFPrimitive voxelised on the GPU
-        with inside = air (core/solver.py:1682-1780)."""
+        """Boolean mask (True = air), an SDFPrimitive voxelised on the GPU
+        with inside = air, or a MaterializedGeometry whose regions also set
+        the material ids (core/solver.py:1682-1780)."""
         torch = self._torch
-        if isinstance(geometry, SDFPrimitive):
+        from .material_assignment import MaterializedGeometry
+
+        if isinstance(geometry, MaterializedGeometry):
+            # core/solver.py:1715-1760: the mask, then every non-default
+            # material registered under its id (unless already registered)
+            # and written where the voxelised ids name it; ids already set
+            # elsewhere are left as they are
+            dev, mat_dev = geometry.voxelize_with_materials_device(self._grid)
+            ids = mat_dev.cpu().numpy()
+            self._geometry = dev.cpu().numpy().astype(bool)
+            for mid, material in geometry.get_material_table().items():
+                if mid == 0:
+                    continue
+                if mid not in self._materials:
+                    self.register_material(material, material_id=mid)
+                region = ids == mid
+                if region.any():
+                    self.set_material_region(region, material_id=mid)
+            self._ade_initialized = False
+        elif isinstance(geometry, SDFPrimitive):
             dev = geometry.voxelize_device(self._grid)
             self._geometry = dev.cpu().numpy().astype(bool)
             self._material_id.fill(0)

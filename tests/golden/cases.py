@@ -219,7 +219,7 @@ PLAIN_CASES = {
 ADE_CASES = {
     "debye_2pole": dict(
         shape=(24, 24, 24), res=1e-3, courant=0.5, pml=dict(depth=4),
-        materials=[dict(id=1, rho=1.204, c=343.0,
+        materials=[dict(id=1, name="m1", rho=1.204, c=343.0,
                         poles=[("debye", "density", 0.3, 2e-4), ("debye", "modulus", 0.5, 5e-4)],
                         box=((6, 18), (5, 17), (8, 20)))],
         sources=[("point", (12, 12, 3), 20000.0, 1.0)],
@@ -230,11 +230,11 @@ ADE_CASES = {
         shape=(22, 20, 26), res=1e-3, courant=0.5, pml=dict(depth=3),
         geometry=dict(kind="blocks", seed=5, n_boxes=1, n_spheres=1),
         materials=[
-            dict(id=1, rho=1.5, c=300.0,
+            dict(id=1, name="m1", rho=1.5, c=300.0,
                  poles=[("lorentz", "density", 0.2, 2 * np.pi * 8000.0, 3000.0),
                         ("debye", "modulus", 0.4, 1e-4)],
                  box=((3, 12), (2, 10), (4, 15))),
-            dict(id=3, rho=1.1, c=360.0,
+            dict(id=3, name="m3", rho=1.1, c=360.0,
                  poles=[("lorentz", "modulus", 0.3, 2 * np.pi * 12000.0, 5000.0),
                         ("debye", "density", 0.25, 3e-4)],
                  box=((12, 20), (8, 18), (12, 24))),
@@ -249,16 +249,38 @@ ADE_CASES = {
         shape=(70, 45, 76), res=1e-3, courant=0.5, pml=dict(depth=5),
         geometry=dict(kind="blocks", seed=8, n_boxes=2, n_spheres=1),
         materials=[
-            dict(id=2, rho=1.3, c=330.0,
+            dict(id=2, name="m2", rho=1.3, c=330.0,
                  poles=[("debye", "density", 0.35, 3e-4), ("debye", "modulus", 0.3, 4e-4)],
                  box=((29, 41), (13, 27), (33, 47))),
-            dict(id=5, rho=1.1, c=355.0,
+            dict(id=5, name="m5", rho=1.1, c=355.0,
                  poles=[("lorentz", "density", 0.15, 2 * np.pi * 9000.0, 4000.0)],
                  box=((40, 47), (20, 31), (45, 52))),
         ],
         sources=[("point", (20, 22, 38), 15000.0, 1.0), ("point", (50, 30, 60), 11000.0, 0.6)],
         probes=[("mid", (35, 20, 40)), ("far", (60, 35, 20))],
         steps=140, store_fields=False,
+    ),
+    "materialized_sdf": dict(
+        # MaterializedGeometry (geometry/material_assignment.py:48-171): air is
+        # the inside of an SDF (a box with a solid sphere taken out, rigid
+        # margins outside it), three SDF regions assigned in order -- a sphere,
+        # an x cylinder overlapping it (later wins), a box reaching into the
+        # rigid margin and the solid sphere (ids only in air)
+        shape=(40, 36, 44), res=1e-3, courant=0.5, pml=dict(depth=4),
+        materialized=dict(which="mat_air", regions=[
+            ("mat_sphere", dict(name="absorber", rho=1.3, c=330.0,
+                                poles=[("debye", "density", 0.3, 2e-4),
+                                       ("debye", "modulus", 0.4, 4e-4)])),
+            ("mat_cylinder", dict(name="resonant", rho=1.1, c=355.0,
+                                  poles=[("lorentz", "density", 0.2, 2 * np.pi * 9000.0, 4000.0),
+                                         ("debye", "modulus", 0.25, 3e-4)])),
+            ("mat_slab", dict(name="slab", rho=1.25, c=340.0,
+                              poles=[("debye", "density", 0.35, 5e-4)])),
+        ]),
+        sources=[("point", (20, 18, 8), 20000.0, 1.0)],
+        probes=[("sphere", (24, 18, 20)), ("cyl", (12, 22, 16)), ("slab", (6, 10, 36)),
+                ("air", (30, 28, 34))],
+        steps=110, store_fields=True,
     ),
     "nu_mixed_geom": dict(
         # ADE on a stretched grid: nonuniform updates and divergence, the
@@ -267,11 +289,11 @@ ADE_CASES = {
         grid=dict(kind="stretch", base=1e-3, stretch=(1.03, 1.0, 1.04), center_fine=True),
         geometry=dict(kind="blocks", seed=13, n_boxes=1, n_spheres=1),
         materials=[
-            dict(id=1, rho=1.4, c=320.0,
+            dict(id=1, name="m1", rho=1.4, c=320.0,
                  poles=[("debye", "density", 0.3, 2e-4),
                         ("lorentz", "modulus", 0.25, 2 * np.pi * 9000.0, 4000.0)],
                  box=((8, 20), (6, 18), (10, 24))),
-            dict(id=4, rho=1.1, c=360.0,
+            dict(id=4, name="m4", rho=1.1, c=360.0,
                  poles=[("lorentz", "density", 0.2, 2 * np.pi * 11000.0, 5000.0),
                         ("debye", "modulus", 0.35, 3e-4)],
                  box=((19, 30), (14, 26), (20, 34))),
@@ -346,6 +368,15 @@ def sdf_tree(api, which):
         return Difference(outer, inner, port)
     if which == "c2_enclosure":
         return c2_solid(api)
+    if which == "mat_air":  # air volume: a box 2 cells in from the faces, minus a sphere
+        return Difference(Box(center=(0.02, 0.018, 0.022), size=(0.036, 0.032, 0.040)),
+                          Sphere(center=(0.012, 0.02, 0.03), radius=0.004))
+    if which == "mat_sphere":
+        return Sphere(center=(0.0245, 0.0185, 0.0205), radius=0.009)
+    if which == "mat_cylinder":
+        return Cylinder(p1=(0.008, 0.0225, 0.0165), p2=(0.034, 0.0225, 0.0165), radius=0.006)
+    if which == "mat_slab":
+        return Box(min_corner=(0.0, 0.0, 0.03), max_corner=(0.013, 0.036, 0.044))
     raise KeyError(which)
 
 
@@ -378,6 +409,19 @@ def c2_probes(geometry, pml_depth=16, n=8, seed=0):
     return [(f"probe{q}", pos) for q, pos in enumerate(out)]
 
 
+def _material(api, m):
+    """SimpleMaterial from a case's material dict (rho, c, pole tuples)."""
+    poles = []
+    for pd in m["poles"]:
+        if pd[0] == "debye":
+            poles.append(api.Pole(pole_type=api.PoleType.DEBYE, delta_chi=pd[2],
+                                  target=pd[1], tau=pd[3]))
+        else:
+            poles.append(api.Pole(pole_type=api.PoleType.LORENTZ, delta_chi=pd[2],
+                                  target=pd[1], omega_0=pd[3], gamma=pd[4]))
+    return api.SimpleMaterial(name=m["name"], _rho=m["rho"], _c=m["c"], _poles=poles)
+
+
 def build_case(api, case, ade=False):
     """Construct a solver for ``case`` through the reference-shaped ``api``."""
     g = case.get("grid")
@@ -407,17 +451,14 @@ def build_case(api, case, ade=False):
                                              geo.get("n_boxes", 2), geo.get("n_spheres", 1)))
         else:
             solver.set_geometry(~sdf_tree(api, geo["which"]).voxelize(solver.grid))
+    mg = case.get("materialized")
+    if mg:  # MaterializedGeometry: SDF air volume + ordered SDF material regions
+        geo = api.MaterializedGeometry(sdf_tree(api, mg["which"]))
+        for which, m in mg["regions"]:
+            geo.set_material(sdf_tree(api, which), _material(api, m))
+        solver.set_geometry(geo)
     for m in case.get("materials", []):
-        poles = []
-        for pd in m["poles"]:
-            if pd[0] == "debye":
-                poles.append(api.Pole(pole_type=api.PoleType.DEBYE, delta_chi=pd[2],
-                                      target=pd[1], tau=pd[3]))
-            else:
-                poles.append(api.Pole(pole_type=api.PoleType.LORENTZ, delta_chi=pd[2],
-                                      target=pd[1], omega_0=pd[3], gamma=pd[4]))
-        mat = api.SimpleMaterial(name=f"m{m['id']}", _rho=m["rho"], _c=m["c"], _poles=poles)
-        mid = solver.register_material(mat, material_id=m["id"])
+        mid = solver.register_material(_material(api, m), material_id=m["id"])
         solver.set_material_box(mid, *m["box"])
     for kind, pos, f, a in case.get("sources", []):
         if kind == "point":

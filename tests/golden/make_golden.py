@@ -55,7 +55,7 @@ def load_reference():
                  "strata_fdtd.boundaries._kernels"):
         sys.modules[name] = mod
     import strata_fdtd as sf
-    from strata_fdtd.geometry import resonator, sdf
+    from strata_fdtd.geometry import material_assignment, resonator, sdf
     from strata_fdtd.materials import base
     api = types.SimpleNamespace(
         FDTDSolver=sf.FDTDSolver, UniformGrid=sf.UniformGrid, PML=sf.PML,
@@ -68,6 +68,7 @@ def load_reference():
         Cylinder=sdf.Cylinder, Union=sdf.Union, Intersection=sdf.Intersection,
         Difference=sdf.Difference, HelmholtzResonator=resonator.HelmholtzResonator,
         Pole=base.Pole, PoleType=base.PoleType, SimpleMaterial=base.SimpleMaterial,
+        MaterializedGeometry=material_assignment.MaterializedGeometry,
         kernels=mod, solver_module=sys.modules["strata_fdtd.core.solver"])
     assert api.solver_module.has_native_kernels()
     return api

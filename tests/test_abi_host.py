@@ -226,7 +226,7 @@ def test_differentiable_source_table_matches_per_step_calls():
     for f in (1500.0, 20000.0):
         stub = types.SimpleNamespace(pulse=S.GaussianPulse(position=(0, 0, 0), frequency=f),
                                      dt=1e-3 / (343.0 * np.sqrt(3)) * 0.5, torch=torch,
-                                     dtype=torch.float64, dev="cpu")
+                                     ext_dtype=torch.float64, dev="cpu")
         got = DifferentiableSolver.source_values(stub, 2000).numpy()
         t, per = 0.0, []
         for _ in range(2000):

@@ -2,13 +2,16 @@
 w.r.t. the density field, checked against torch.autograd through a plain
 PyTorch stepping of the same scheme and against central finite differences.
 
-Tolerances: FP64 adjoint vs FP64 autograd, rel 1e-9 (same arithmetic up to
-summation order); FP64 adjoint vs central differences (h = 1e-3), rel 1e-5
-(O(h^2) truncation); at the 128^3 x 2000-step workload the FP64 adjoint
-vs central differences rel 1e-5 and the FP32 adjoint vs the FP64 adjoint
-rel 1e-3; probe traces from the in-kernel and the separate gather bit-equal,
-and at small size with 6 probes the FP32 adjoint vs the FP64 adjoint within
-1e-4 of the largest gradient entry."""
+Tolerances: FP64 and double-word ("dw", the default) adjoints vs FP64
+autograd, rel 1e-9 and 1e-8 (same arithmetic up to summation order; dw
+carries about 48 bits); FP64 adjoint vs central differences (h = 1e-3), rel
+1e-5 (O(h^2) truncation); at the 128^3 x 2000-step workload, per sampled
+cell against FP64 central differences: the default dw adjoint rel 1e-4
+(the stated target), the FP64 adjoint rel 1e-5, the FP32 adjoint rel 2e-3
+(its documented accuracy); probe traces from the in-kernel and the separate
+gather bit-equal in every precision, and at small size with 6 probes the
+FP32 adjoint vs the FP64 adjoint within 1e-4 of the largest gradient
+entry."""
 import numpy as np
 import pytest
 
@@ -25,8 +28,9 @@ def _small(dtype, K=25):
                                 checkpoint_every=K)
 
 
-def test_adjoint_matches_autograd_fp64():
-    s = _small(torch.float64)
+@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-9), ("dw", 1e-8)])
+def test_adjoint_matches_autograd_fp64(dtype, rtol):
+    s = _small(dtype)
     theta = torch.tensor(design_field(s.shape, region=8, seed=1, sigma=1.5), device="cuda")
     target = s.forward(torch.tensor(design_field(s.shape, region=8, seed=2, sigma=1.5),
                                     device="cuda"), 60)[0]
@@ -34,12 +38,12 @@ def test_adjoint_matches_autograd_fp64():
     loss = s.loss(th, target, 60)
     loss.backward()
     ref_th = theta.clone().requires_grad_(True)
-    ref = reference_loss_torch(s, ref_th, target, 60)
+    ref = reference_loss_torch(_small(torch.float64), ref_th, target, 60)
     ref.backward()
-    assert float(loss) == pytest.approx(float(ref), rel=1e-12)
+    assert float(loss) == pytest.approx(float(ref), rel=rtol * 1e-3)
     g, r = th.grad.cpu().numpy(), ref_th.grad.cpu().numpy()
     assert np.abs(r).max() > 0
-    np.testing.assert_allclose(g, r, rtol=1e-9, atol=1e-12 * np.abs(r).max())
+    np.testing.assert_allclose(g, r, rtol=rtol, atol=rtol * 1e-3 * np.abs(r).max())
 
 
 def test_adjoint_matches_central_differences_fp64():
@@ -59,56 +63,62 @@ def test_adjoint_matches_central_differences_fp64():
         assert float(th.grad[c]) == pytest.approx(fd, rel=1e-5, abs=1e-14)
 
 
-def test_differentiable_workload_fp32_against_fd():
+def test_differentiable_workload_against_fd():
     """The 128^3 workload: 10-cell PML, design field on the central 64^3,
-    1.5 kHz source, 2000 steps, checkpoints every 100 steps.  The FP64
-    adjoint gradient must match FP64 central differences (h = 1e-3) on 16
-    random cells to rel 1e-5 (O(h^2) truncation); the FP32 adjoint (FP32
-    fields, double-word face-gradient sums) must match the FP64 adjoint to rel 1e-3
-    per sampled cell and 1e-3 in L2 over the design region (FP32 rounding of
-    2000 forward and 2000 adjoint steps)."""
+    1.5 kHz source, 2000 steps, checkpoints every 100 steps.  Against FP64
+    central differences (h = 1e-3) on 16 random cells of the design region,
+    per cell: the default double-word adjoint rel 1e-4 (the target), the
+    FP64 adjoint rel 1e-5 (O(h^2) truncation), the FP32 adjoint rel 2e-3
+    (FP32 rounding of 2000 forward and 2000 adjoint steps); the double-word
+    gradient also equals the FP64 one to 1e-6 in L2 over the region."""
     shape = (128, 128, 128)
     probes = [(100, 64, 64), (64, 100, 40)]
-    s32 = DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
-                               probes=probes, dtype=torch.float32, checkpoint_every=100)
-    s64 = DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
-                               probes=probes, dtype=torch.float64, checkpoint_every=100)
+
+    def make(dtype):
+        return DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
+                                    probes=probes, dtype=dtype, checkpoint_every=100)
+
+    s64 = make(torch.float64)
     theta = torch.tensor(design_field(shape, 64, seed=0), device="cuda")
     target = s64.forward(torch.tensor(design_field(shape, 64, seed=1), device="cuda"), 2000)[0]
-    th32 = theta.clone().to(torch.float32).requires_grad_(True)
-    s32.loss(th32, target.to(torch.float32), 2000).backward()
-    th64 = theta.clone().requires_grad_(True)
-    s64.loss(th64, target, 2000).backward()
-    g32 = th32.grad.double()
-    g64 = th64.grad
+    grads = {}
+    for name, dtype in (("dw", "dw"), ("f64", torch.float64), ("f32", torch.float32)):
+        s = s64 if dtype == torch.float64 else make(dtype)
+        th = theta.clone().to(s.ext_dtype).requires_grad_(True)
+        s.loss(th, target.to(s.ext_dtype), 2000).backward()
+        grads[name] = th.grad.double()
+        del s, th
     rng = np.random.default_rng(5)
     h = 1e-3
-    worst64 = worst32 = 0.0
+    worst = {k: 0.0 for k in grads}
     for _ in range(16):
         c = tuple(int(v) for v in rng.integers(32, 96, size=3))
         tp, tm = theta.clone(), theta.clone()
         tp[c] += h
         tm[c] -= h
         fd = (float(s64.loss(tp, target, 2000)) - float(s64.loss(tm, target, 2000))) / (2 * h)
-        worst64 = max(worst64, abs(float(g64[c]) - fd) / abs(fd))
-        worst32 = max(worst32, abs(float(g32[c]) - float(g64[c])) / abs(float(g64[c])))
+        for k, g in grads.items():
+            worst[k] = max(worst[k], abs(float(g[c]) - fd) / abs(fd))
     region = (slice(32, 96),) * 3
-    l2 = float(torch.linalg.norm(g32[region] - g64[region]) / torch.linalg.norm(g64[region]))
-    print(f"fp64 adjoint vs FD worst rel {worst64:.3e}; fp32 vs fp64 adjoint worst rel "
-          f"{worst32:.3e}, L2 rel {l2:.3e}")
-    assert worst64 < 1e-5, worst64
-    assert worst32 < 1e-3, worst32
-    assert l2 < 1e-3, l2
+    l2 = float(torch.linalg.norm(grads["dw"][region] - grads["f64"][region])
+               / torch.linalg.norm(grads["f64"][region]))
+    print("adjoint vs FD, worst rel per sampled cell: "
+          + ", ".join(f"{k} {v:.3e}" for k, v in worst.items()) + f"; dw vs f64 L2 {l2:.3e}")
+    assert worst["dw"] < 1e-4, worst
+    assert worst["f64"] < 1e-5, worst
+    assert worst["f32"] < 2e-3, worst
+    assert l2 < 1e-6, l2
 
 
 def test_probe_gather_paths_and_many_probe_gradients():
     """Up to 4 probes are sampled inside the forward kernel, more by a
     separate gather after each step: the traces of the probes both solvers
-    share must be identical bit for bit, in FP32 and FP64.  With 6 probes
+    share must be identical bit for bit, in every precision.  With 6 probes
     (the separate gather) the FP64 adjoint must match autograd through the
-    plain PyTorch stepping (rel 1e-9), and the FP32 adjoint, whose face sums
-    are double-word float pairs, the FP64 adjoint to 1e-4 of the largest
-    gradient entry (FP32 rounding of 60 forward and 60 adjoint steps)."""
+    plain PyTorch stepping (rel 1e-9); the FP32 adjoint, whose face sums are
+    double-word float pairs, the FP64 adjoint to 1e-4 of the largest
+    gradient entry (FP32 rounding of 60 forward and 60 adjoint steps), and
+    the double-word adjoint to 1e-9."""
     pos = [(12, 7, 9), (8, 3, 14), (10, 10, 4), (4, 5, 6), (13, 11, 15), (6, 12, 3)]
 
     def make(dtype, probes):
@@ -121,15 +131,15 @@ def test_probe_gather_paths_and_many_probe_gradients():
         torch.tensor(design_field((16, 14, 18), region=8, seed=5, sigma=1.5), device="cuda"),
         60)[0]
     grads = {}
-    for dtype in (torch.float32, torch.float64):
+    for dtype in (torch.float32, torch.float64, "dw"):
         few, many = make(dtype, pos[:3]), make(dtype, pos)
         trace_few = few.forward(theta, 60)[0]
         trace_many = many.forward(theta, 60)[0]
         assert trace_many.shape == (60, 6)
         assert torch.equal(trace_few, trace_many[:, :3])
         assert float(trace_many.abs().max()) > 0
-        target = target64.to(dtype)
-        th = theta.clone().to(dtype).requires_grad_(True)
+        target = target64.to(many.ext_dtype)
+        th = theta.clone().to(many.ext_dtype).requires_grad_(True)
         loss = many.loss(th, target, 60)
         loss.backward()
         grads[dtype] = th.grad.double()
@@ -141,9 +151,12 @@ def test_probe_gather_paths_and_many_probe_gradients():
             r = ref_th.grad.cpu().numpy()
             np.testing.assert_allclose(th.grad.cpu().numpy(), r, rtol=1e-9,
                                        atol=1e-12 * np.abs(r).max())
-    g32, g64 = grads[torch.float32], grads[torch.float64]
+    g32, g64, gdw = grads[torch.float32], grads[torch.float64], grads["dw"]
     scale = float(g64.abs().max())
     assert scale > 0
     err = float((g32 - g64).abs().max()) / scale
-    print(f"fp32 vs fp64 adjoint, 6 probes: max abs err / max |g| = {err:.3e}")
+    err_dw = float((gdw - g64).abs().max()) / scale
+    print(f"6 probes, max abs err / max |g| against the fp64 adjoint: fp32 {err:.3e}, "
+          f"dw {err_dw:.3e}")
     assert err < 1e-4, err
+    assert err_dw < 1e-9, err_dw

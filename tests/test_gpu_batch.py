@@ -21,6 +21,7 @@ API = types.SimpleNamespace(
     Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
     PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
+    MaterializedGeometry=S.MaterializedGeometry,
     ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance,
     CircularMembraneSource=S.CircularMembraneSource,
     RectangularMembraneSource=S.RectangularMembraneSource)

@@ -25,6 +25,7 @@ API = types.SimpleNamespace(
     Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
     PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
+    MaterializedGeometry=S.MaterializedGeometry,
     ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance,
     CircularMembraneSource=S.CircularMembraneSource,
     RectangularMembraneSource=S.RectangularMembraneSource)
@@ -79,6 +80,7 @@ def test_ade_cases(name, manifest):
     s.run_steps(case["steps"])
     _compare(s, "ade_" + name, manifest)
     g = golden("ade_" + name)
+    np.testing.assert_array_equal(s._material_id, g["material_id"])
     if s._ade_debye:
         np.testing.assert_array_equal(s._ade_J_debye, g["ade_ade_J_debye"])
     if s._ade_lorentz:
@@ -98,7 +100,8 @@ def _check_ade(s, name, manifest):
 
 @pytest.mark.parametrize("config", ["cell"] + [c for c in S.solver.kernel_configs()
                                                if c.startswith("tile")])
-@pytest.mark.parametrize("name", ["split_boxes_geom", "lorentz_mixed_geom", "nu_mixed_geom"])
+@pytest.mark.parametrize("name", ["split_boxes_geom", "lorentz_mixed_geom", "nu_mixed_geom",
+                                  "materialized_sdf"])
 def test_ade_split_step_every_tile_config(name, config, manifest):
     """ADE steps split between a warp-tile kernel (outside the material
     boxes, rounded out to its tiles) and the per-cell ADE kernel (inside):
@@ -109,6 +112,38 @@ def test_ade_split_step_every_tile_config(name, config, manifest):
     s.run_steps(case["steps"] // 2)
     s.run_steps(case["steps"] - case["steps"] // 2)
     _check_ade(s, name, manifest)
+
+
+def test_materialized_geometry_voxelised_in_one_pass():
+    """voxelize_with_materials on the GPU (one kernel for the geometry and
+    every region) equals the reference's mask and ids, on the uniform grid of
+    the golden case and on a stretched grid against the oracle's NumPy
+    restatement; MaterialVolume regions behave as Box regions."""
+    case = C.ADE_CASES["materialized_sdf"]
+    g = golden("ade_materialized_sdf")
+    geo = S.MaterializedGeometry(C.sdf_tree(API, "mat_air"))
+    ref = O.MaterializedGeometry(C.sdf_tree(ORACLE, "mat_air"))
+    for which, m in case["materialized"]["regions"]:
+        geo.set_material(C.sdf_tree(API, which), C._material(API, m))
+        ref.set_material(C.sdf_tree(ORACLE, which), None)
+    grid = S.UniformGrid(case["shape"], case["res"])
+    mask, ids = geo.voxelize_with_materials(grid)
+    np.testing.assert_array_equal(mask, np.unpackbits(g["geometry"])[: mask.size].reshape(
+        mask.shape).astype(bool))
+    np.testing.assert_array_equal(ids, g["material_id"])
+    assert geo.material_count() == 4 and set(geo.get_material_table()) == {0, 1, 2, 3}
+    nu = S.NonuniformGrid.from_stretch((40, 36, 44), 1e-3, 1.02, 1.0, 1.03, center_fine=True)
+    onu = O.NonuniformGrid.from_stretch((40, 36, 44), 1e-3, 1.02, 1.0, 1.03, center_fine=True)
+    mask2, ids2 = geo.voxelize_with_materials(nu)
+    rmask, rids = ref.voxelize_with_materials(onu)
+    np.testing.assert_array_equal(mask2, rmask)
+    np.testing.assert_array_equal(ids2, rids)
+    vol = S.MaterialVolume.from_corners((0.0, 0.0, 0.03), (0.013, 0.036, 0.044), None)
+    geo2 = S.MaterializedGeometry(C.sdf_tree(API, "mat_air"))
+    geo2.set_material(vol.region, C._material(API, case["materialized"]["regions"][2][1]))
+    _, ids3 = geo2.voxelize_with_materials(grid)
+    slab = C.sdf_tree(API, "mat_slab").voxelize(grid) & mask
+    np.testing.assert_array_equal(ids3, slab.astype(np.uint8))
 
 
 def test_ade_autotune_then_steps(manifest):

@@ -130,3 +130,36 @@ def test_pipeline_full_size_matches_single_steps(config):
         assert sha256(getattr(a, f)) == sha256(getattr(b, f)), f
     for name in a.get_probe_data():
         np.testing.assert_array_equal(a.get_probe_data()[name], b.get_probe_data()[name])
+
+
+@pytest.mark.parametrize("config", PIPES)
+def test_expired_wait_fails_cleanly_and_next_call_is_exact(config):
+    """The pipelines' cross-warp waits are bounded.  With a short bound and
+    the test hook that makes the first work item also wait on a device flag
+    nothing sets, the wait runs out: the kernel raises its error flag, every
+    other wait and claim returns, and sf_plan_step reports the expiry (no
+    fault, no hang).  The next call, with the hook off, steps the restored
+    state exactly like the oracle."""
+    from strata_fdtd_gb300 import _native
+
+    lib = _native.load()
+    case = _case((23, 37, 64), 6)
+    s = C.build_case(API, case)
+    ref = C.build_case(ORACLE, case)
+    s.set_kernel(config)
+    s.run_steps(4)
+    ref.run_steps(4)
+    saved = {f: getattr(s, f).copy() for f in ("p", "vx", "vy", "vz")}
+    _native.check(lib.sf_plan_set_wait_limit(s._plan, 2000, 1), "sf_plan_set_wait_limit")
+    with pytest.raises(_native.NativeError, match="dependency wait expired"):
+        s.run_steps(6)
+    torch.cuda.synchronize()  # the context is intact
+    _native.check(lib.sf_plan_set_wait_limit(s._plan, 0, 0), "sf_plan_set_wait_limit")
+    for f, v in saved.items():
+        setattr(s, f, v)
+    s.run_steps(6)
+    ref.run_steps(6)
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(s, f), getattr(ref, f), err_msg=f)
+    for name, tr in ref.get_probe_data().items():
+        np.testing.assert_array_equal(s.get_probe_data()[name], tr, err_msg=name)

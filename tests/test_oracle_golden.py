@@ -78,6 +78,18 @@ def test_ade_matches_reference_kernels(name, manifest):
         np.testing.assert_array_equal(np.concatenate(jl), g["ade_ade_J_lorentz"])
 
 
+def test_materialized_geometry_ids_match_reference():
+    """MaterializedGeometry (geometry/material_assignment.py:133-171) through
+    the oracle's set_geometry: mask and material ids equal the reference's."""
+    case = C.ADE_CASES["materialized_sdf"]
+    s = C.build_case(API, case)
+    g = golden("ade_materialized_sdf")
+    geom = np.unpackbits(g["geometry"])[: s.geometry.size].reshape(s.geometry.shape)
+    np.testing.assert_array_equal(s.geometry, geom.astype(bool))
+    np.testing.assert_array_equal(s._material_id, g["material_id"])
+    assert sorted(s._materials) == [1, 2, 3]
+
+
 def test_fp64_run_is_close_to_fp32():
     case = C.PLAIN_CASES["blocks_odd"]
     a = _run(case, False)
