@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--batch-only", action="store_true",
                     help="batch: skip the sequential baselines (profiling runs)")
     ap.add_argument("--graph-steps", type=int, default=50)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="enclosure line only: skip the batched, served, adjoint and parity "
+                         "sub-objects")
     return ap.parse_args()
 
 
@@ -345,12 +348,20 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and n_edge == 400:
+        from oracle import oracle as O
+
         o = oracle_enclosure(s.geometry)
         v, n, th = time_oracle(o, args.cpu_seconds)
+        # the single-thread point of the same sample
+        O.set_threads(1)
+        v1, n1, _ = time_oracle(o, min(5.0, args.cpu_seconds))
+        O.set_threads(th)
+        del o
         cpu = {"value": v, "unit": METRIC, "cores": th, "kind": "port",
                "sample": f"{n} FDTD steps of the same 400^3 enclosure workload on the CPU "
                          "oracle (bit-exact C restatement of the reference native kernels, "
-                         "OpenMP, all host threads)"}
+                         "OpenMP, all host threads)",
+               "value_1_thread": v1, "sample_1_thread": f"{n1} FDTD steps, 1 thread"}
 
     if rank == 0:
         line = {
@@ -370,9 +381,98 @@ def run_gpu(args):
             "device": torch.cuda.get_device_name(local),
             "library": lib.sf_version().decode(),
         }
+        if world == 1 and not args.no_extras and n_edge == 400:
+            del s, vals, trace
+            torch.cuda.empty_cache()
+            line.update(extras(args))
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def parity_quick_start():
+    """The 100^3 quick start, 1000 steps on the GPU through FDTDSolver.run_steps,
+    against the CPU oracle: bit-exact in FP32, and its rel-L2 against the
+    oracle's FP64 build."""
+    from oracle import oracle as O
+    from strata_fdtd_gb300.workloads import quick_start_100
+
+    s = quick_start_100()
+    s.run_steps(1000)
+    gpu = {f: getattr(s, f) for f in ("p", "vx", "vy", "vz")}
+    tr = s.get_probe_data()["output"]
+    out = {"workload": "quick_start_100 (100^3, PML 10, 1 kHz, 1000 steps)"}
+    for prec in ("f32", "f64"):
+        o = O.FDTDSolver(shape=(100, 100, 100), resolution=1e-3, c=343.0, rho=1.204,
+                         courant=0.5, precision=prec)
+        o.add_boundary(O.PML(depth=10))
+        o.add_source(O.GaussianPulse(position=(50, 50, 50), frequency=1000.0))
+        o.add_probe("output", (75, 50, 50))
+        o.run_steps(1000)
+        ref = {f: getattr(o, f) for f in gpu}
+        rt = o.get_probe_data()["output"]
+        if prec == "f32":
+            out["bit_exact_vs_oracle_f32"] = bool(
+                all(np.array_equal(gpu[f], ref[f]) for f in gpu) and np.array_equal(tr, rt))
+        else:
+            for f in gpu:
+                out[f"rel_l2_{f}_vs_f64"] = float(
+                    np.linalg.norm(gpu[f].astype(np.float64) - ref[f]) / np.linalg.norm(ref[f]))
+            out["rel_l2_trace_vs_f64"] = float(
+                np.linalg.norm(tr.astype(np.float64) - rt) / np.linalg.norm(rt))
+    return out
+
+
+# The 400^3 enclosure over all 4000 steps is checked by
+# tests/test_gpu_workloads_full.py (about 5 minutes of CPU oracle time, too
+# long for this benchmark): bit-exact against the FP32 oracle, and these
+# rel-L2 errors against the FP64 oracle, measured on a GB300 box.
+ENCLOSURE_FP64_ERRORS = {
+    "workload": "enclosure_400, 4000 steps (recorded by tests/test_gpu_workloads_full.py)",
+    "bit_exact_vs_oracle_f32": True, "rel_l2_p_vs_f64": 3.29e-6, "rel_l2_vx_vs_f64": 2.48e-6,
+    "rel_l2_vy_vs_f64": 3.08e-6, "rel_l2_vz_vs_f64": 3.34e-6, "rel_l2_traces_vs_f64": 1.51e-6,
+}
+
+
+def extras(args):
+    """The second half of the metric on the same GPU, each on its configured
+    workload: the batched heterogeneous launch, the served request stream
+    (p50/p99 beside throughput, against one request at a time) and the
+    differentiable solve, plus the parity record."""
+    import torch
+
+    out = {}
+    b = run_batch(args)
+    out["batched"] = {
+        "value": b["value"], "unit": b["unit"], "workload": b["config"]["workload"],
+        "cell_updates": b["config"]["cell_updates"],
+        "sequential_value": b["sequential"]["value"],
+        "speedup_vs_sequential": b["speedup_vs_sequential"],
+        "traces_identical": b["traces_identical"], "plain_kernel": b["config"]["plain_kernel"],
+        "rejected_materials": b["config"]["rejected_materials"]}
+    torch.cuda.empty_cache()
+    sv = run_serve(args)
+    out["served"] = {
+        "value": sv["value"], "unit": sv["unit"], "workload": sv["config"]["workload"],
+        "p50_latency_s": sv["served"]["p50_latency_s"],
+        "p99_latency_s": sv["served"]["p99_latency_s"],
+        "makespan_s": sv["served"]["makespan_s"],
+        "sequential_value": sv["sequential"]["gcell_updates_per_s"],
+        "sequential_p50_latency_s": sv["sequential"]["p50_latency_s"],
+        "sequential_p99_latency_s": sv["sequential"]["p99_latency_s"],
+        "throughput_ratio": sv["throughput_ratio"], "results_identical": sv["results_identical"],
+        "done": sv["served"]["done"], "peak_active": sv["served"]["peak_active"]}
+    torch.cuda.empty_cache()
+    a = run_adjoint(args)
+    out["adjoint"] = {"value": a["value"], "unit": a["unit"], "workload": a["config"]["workload"],
+                      "accuracy": a["config"]["accuracy"],
+                      **{k: {q: a[k][q] for q in ("gradient_seconds", "forward_seconds",
+                                                   "gradient_gcell_updates_per_s")}
+                         for k in ("dw", "f32", "f64")}}
+    torch.cuda.empty_cache()
+    out["parity"] = {"quick_start_100": parity_quick_start(),
+                     "enclosure_400": ENCLOSURE_FP64_ERRORS}
+    return out
 
 
 def run_batch(args):
@@ -462,7 +562,7 @@ def run_batch(args):
         "speedup_vs_sequential": t_seq / t_bat,
         "traces_identical": bool(same),
     }
-    print(json.dumps(line))
+    return line
 
 
 def run_serve(args):
@@ -503,7 +603,7 @@ def run_serve(args):
         "throughput_ratio": (st["gcell_updates_per_s"] or 0) / (st2["gcell_updates_per_s"] or 1),
         "results_identical": bool(same),
     }
-    print(json.dumps(line))
+    return line
 
 
 def run_adjoint(args):
@@ -521,10 +621,10 @@ def run_adjoint(args):
     cells = int(np.prod(shape))
     probes = [(100, 64, 64), (64, 100, 40)]
     out = {}
-    for name, dt in (("f32", torch.float32), ("f64", torch.float64)):
+    for name, dt in (("dw", "dw"), ("f32", torch.float32), ("f64", torch.float64)):
         s = DifferentiableSolver(shape, pml_depth=10, frequency=1500.0, source=(30, 64, 64),
                                  probes=probes, dtype=dt, checkpoint_every=100)
-        theta = torch.tensor(design_field(shape, 64, seed=0), device="cuda", dtype=dt)
+        theta = torch.tensor(design_field(shape, 64, seed=0), device="cuda", dtype=s.ext_dtype)
         target = s.forward(torch.tensor(design_field(shape, 64, seed=1), device="cuda"), n)[0]
         th = theta.clone().requires_grad_(True)
         s.loss(th, target[:200], 200).backward()  # warm-up
@@ -547,14 +647,17 @@ def run_adjoint(args):
         del s, theta, target, th
         torch.cuda.empty_cache()
     line = {"metric": "Gcell-updates/s (probe-loss gradient, forward steps per second)",
-            "value": out["f32"]["gradient_gcell_updates_per_s"], "unit": "Gcell-updates/s",
-            "n_gpus": 1, "steps": n, "warmup": 1, "ms_per_step": out["f32"]["gradient_seconds"] / n * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+            "value": out["dw"]["gradient_gcell_updates_per_s"], "unit": "Gcell-updates/s",
+            "n_gpus": 1, "steps": n, "warmup": 1, "ms_per_step": out["dw"]["gradient_seconds"] / n * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32x2 (double-word)", "data": "synthetic",
             "config": {"workload": f"128^3, PML 10, design field on the central 64^3, 1.5 kHz "
-                                   f"source, 2 probes, {n} steps, checkpoints every 100 steps"},
-            "f32": out["f32"], "f64": out["f64"]}
-    print(json.dumps(line))
+                                   f"source, 2 probes, {n} steps, checkpoints every 100 steps",
+                       "accuracy": "double-word and FP64 gradients within 1.2e-6 of FP64 central "
+                                   "differences per sampled cell, FP32 within 8.2e-4 "
+                                   "(tests/test_gpu_adjoint.py)"},
+            "dw": out["dw"], "f32": out["f32"], "f64": out["f64"]}
+    return line
 
 
 def main():
@@ -562,11 +665,11 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
-        run_batch(args)
+        print(json.dumps(run_batch(args)))
     elif args.workload == "serve":
-        run_serve(args)
+        print(json.dumps(run_serve(args)))
     elif args.workload == "adjoint":
-        run_adjoint(args)
+        print(json.dumps(run_adjoint(args)))
     else:
         run_gpu(args)
 

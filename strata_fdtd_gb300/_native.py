@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB_PATH = os.path.join(BUILD, "libsf_gb300.so")
 SOURCES = ("sf_step.cu", "sf_step_march.cu", "sf_step_col.cu", "sf_step_tile.cu", "sf_step_pipe.cu",
-           "sf_voxel.cu", "sf_batch.cu", "sf_adjoint.cu", "sf_api.cu")
+           "sf_step_tb.cu", "sf_voxel.cu", "sf_batch.cu", "sf_adjoint.cu", "sf_api.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr"]

@@ -30,6 +30,7 @@
 #define SF_CFG_TILE_DEFAULT (SF_CFG_TILE_FIRST + 2)
 #define SF_CFG_TILE1_DEFAULT (SF_CFG_TILE_FIRST + 11)
 #define SF_CFG_PIPE_FIRST (SF_CFG_TILE_FIRST + kSfTileConfigCount)
+#define SF_CFG_TB_FIRST (SF_CFG_PIPE_FIRST + kSfPipeConfigCount)
 #endif
 
 namespace {
@@ -409,7 +410,8 @@ int sf_plan_set_wait_limit(sf_plan* P, int64_t spins, int hold_first_item) {
 }
 
 int sf_kernel_config_count(void) {
-    return SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount + kSfPipeConfigCount;
+    return SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount + kSfPipeConfigCount +
+           kSfTbConfigCount;
 }
 
 const char* sf_kernel_config_name(int config) {
@@ -420,8 +422,10 @@ const char* sf_kernel_config_name(int config) {
         return kSfColConfigs[config - SF_CFG_COL_FIRST].name;
     if (config >= SF_CFG_TILE_FIRST && config < SF_CFG_PIPE_FIRST)
         return kSfTileConfigs[config - SF_CFG_TILE_FIRST].name;
-    if (config >= SF_CFG_PIPE_FIRST && config < sf_kernel_config_count())
+    if (config >= SF_CFG_PIPE_FIRST && config < SF_CFG_TB_FIRST)
         return kSfPipeConfigs[config - SF_CFG_PIPE_FIRST].name;
+    if (config >= SF_CFG_TB_FIRST && config < sf_kernel_config_count())
+        return kSfTbConfigs[config - SF_CFG_TB_FIRST].name;
     return nullptr;
 }
 
@@ -478,7 +482,16 @@ void set_io(const sf_plan* P, SfStepArgs& a, int in) {
 // column configuration.  With ADE poles only the warp-tile configurations
 // (which then leave the material box to the per-cell kernel, see
 // ade_region) and the per-cell kernel itself are used.
-bool is_pipe(int cfg) { return cfg >= SF_CFG_PIPE_FIRST; }
+bool is_pipe(int cfg) { return cfg >= SF_CFG_PIPE_FIRST && cfg < SF_CFG_TB_FIRST; }
+bool is_tb(int cfg) { return cfg >= SF_CFG_TB_FIRST; }
+// The two-step kernels take uniform grids without ADE poles.
+bool tb_fits(const sf_plan* P, const SfStepArgs& a) {
+    return P->poles.n == 0 && P->nu == nullptr && sf_tb_supported(a);
+}
+int default_single(const SfStepArgs& a) {
+    return sf_tile_supported(a, 4) ? SF_CFG_TILE_DEFAULT
+                                   : (sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT);
+}
 bool pipe_fits(sf_plan* P, int cfg, const SfStepArgs& a);
 int chunk_for(const sf_plan* P, int cfg);
 
@@ -490,8 +503,11 @@ int effective_config(const sf_plan* P, const SfStepArgs& a) {
     else cfg = sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT;
     if (is_pipe(cfg)) {  // when the pipeline fits the plan; else the default choice
         if (pipe_fits(const_cast<sf_plan*>(P), cfg, a)) return cfg;
-        cfg = sf_tile_supported(a, 4) ? SF_CFG_TILE_DEFAULT
-                                      : (sf_tile_supported(a, 1) ? SF_CFG_TILE1_DEFAULT : SF_CFG_DEFAULT);
+        cfg = default_single(a);
+    }
+    if (is_tb(cfg)) {  // likewise for the two-step kernels
+        if (tb_fits(P, a)) return cfg;
+        cfg = default_single(a);
     }
     const bool tile_ok =
         cfg >= SF_CFG_TILE_FIRST && sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec);
@@ -534,6 +550,21 @@ int chunk_for(const sf_plan* P, int cfg) {
     if (cfg == P->tuned && P->tuned_ich > 0) return P->tuned_ich;
     if (is_pipe(cfg))  // planes per chunk / between progress updates
         return kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST].stream ? 4 : 2;
+    if (is_tb(cfg)) {  // about four waves of blocks, chunks of at least 4 planes
+        const SfTbConfig& c = kSfTbConfigs[cfg - SF_CFG_TB_FIRST];
+        int sms = 152;
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess)
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long tiles =
+            (long long)((P->d.nz + c.tk - 1) / c.tk) * ((P->d.ny + c.tj - 1) / c.tj);
+        long long chunks = (4LL * c.minb * sms + tiles - 1) / tiles;
+        if (chunks < 1) chunks = 1;
+        long long ich = (P->d.nx + chunks - 1) / chunks;
+        if (ich < 4) ich = 4;
+        if (ich > P->d.nx) ich = P->d.nx;
+        return (int)ich;
+    }
     if (cfg >= SF_CFG_TILE_FIRST) {
         const SfTileConfig& t = kSfTileConfigs[cfg - SF_CFG_TILE_FIRST];
         if (t.vec == 1) return auto_chunk(P, 32, t.rows * t.warps);
@@ -552,6 +583,7 @@ int chunk_for(const sf_plan* P, int cfg) {
 // its launcher substitutes the first column configuration).
 bool config_native(const sf_plan* P, int cfg, const SfStepArgs& a) {
     if (is_pipe(cfg)) return pipe_fits(const_cast<sf_plan*>(P), cfg, a);
+    if (is_tb(cfg)) return tb_fits(P, a);
     if (cfg >= SF_CFG_TILE_FIRST)
         return sf_tile_supported(a, kSfTileConfigs[cfg - SF_CFG_TILE_FIRST].vec);
     if (cfg >= SF_CFG_COL_FIRST) return P->d.nz % kSfColConfigs[cfg - SF_CFG_COL_FIRST].vec == 0;
@@ -785,7 +817,10 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
     const bool pipe = is_pipe(cfg0) && !deferred && !mics;
     const int levels = pipe ? kSfPipeConfigs[cfg0 - SF_CFG_PIPE_FIRST].levels : 1;
     const int pipe_S = pipe ? chunk_for(P, cfg0) : 0;
-    const int cfg = is_pipe(cfg0) ? SF_CFG_TILE_DEFAULT : cfg0;
+    // a two-step configuration runs pairs of steps under the same conditions
+    const bool tb = is_tb(cfg0) && !deferred && !mics;
+    const int tb_ich = tb ? chunk_for(P, cfg0) : 0;
+    const int cfg = (is_pipe(cfg0) || is_tb(cfg0)) ? SF_CFG_TILE_DEFAULT : cfg0;
     const int ich = chunk_for(P, cfg);
     bool piped = false;
     for (int64_t s = 0; s < n_steps;) {
@@ -801,6 +836,20 @@ int sf_plan_step_ex(sf_plan* P, int64_t n_steps, const double* src_values, float
             P->cur = 1 - P->cur;
             P->steps_done += levels;
             s += levels;
+            continue;
+        }
+        if (tb && n_steps - s >= 2) {
+            set_io(P, a, P->cur);
+            a.src_val = P->src.n > 0 ? src_values + s * P->src.n : nullptr;
+            a.trace_prev = (a.n_probe > 0 && s > 0) ? trace + (s - 1) * P->n_probe : nullptr;
+            a.reverse = (int)((P->steps_done >> 1) & 1);
+            float* t1 = a.n_probe > 0 ? trace + s * P->n_probe : nullptr;
+            if (int rc = sf_launch_step_tb(a, P->src, P->flags != nullptr, cfg0 - SF_CFG_TB_FIRST,
+                                           tb_ich, t1, st))
+                return rc;
+            P->cur = 1 - P->cur;
+            P->steps_done += 2;
+            s += 2;
             continue;
         }
         set_io(P, a, P->cur);
@@ -913,6 +962,9 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
         SfStepArgs t = a;
         if (ade && !is_pipe(cfg)) ade_region(P, cfg, ich, t.skip_lo, t.skip_hi);
         auto one = [&]() -> int {
+            if (is_tb(cfg))
+                return sf_launch_step_tb(t, none, P->flags != nullptr, cfg - SF_CFG_TB_FIRST, ich,
+                                         nullptr, st);
             return is_pipe(cfg) ? launch_pipe(P, cfg, ich, t, none, nullptr, st)
                                 : launch_config(P, cfg, ich, t, none, st);
         };
@@ -924,7 +976,8 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
             return sf_fail("sf_plan_autotune: timing failed");
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
-        const int steps = is_pipe(cfg) ? kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST].levels : 1;
+        const int steps = is_pipe(cfg) ? kSfPipeConfigs[cfg - SF_CFG_PIPE_FIRST].levels
+                                        : (is_tb(cfg) ? 2 : 1);
         *ms_step = ms / (launches * steps);
         return 0;
     };
@@ -951,8 +1004,9 @@ int sf_plan_autotune(sf_plan* P, int launches, void* stream, float* ms_out, int*
         int best_ich = auto_ich;
         static const int cand_step[] = {8, 12, 16, 20, 24, 32, 48};
         static const int cand_pipe[] = {1, 2, 3, 4, 6, 8};
-        const int* cand = is_pipe(best) ? cand_pipe : cand_step;
-        const int ncand = is_pipe(best) ? 6 : 7;
+        static const int cand_tb[] = {4, 8, 12, 16, 25, 32, 50, 64};
+        const int* cand = is_pipe(best) ? cand_pipe : (is_tb(best) ? cand_tb : cand_step);
+        const int ncand = is_pipe(best) ? 6 : (is_tb(best) ? 8 : 7);
         for (int q = 0; q < ncand && !rc; ++q) {
             const int ich = cand[q];
             if (ich == auto_ich || ich > P->d.nx) continue;

@@ -81,6 +81,21 @@ int sf_pipe_grid(int cfg, bool geom, bool nu);
 int sf_launch_step_stream(const SfPipeArgs& P, const SfSources& src, bool geom, int cfg,
                           cudaStream_t st);
 
+// Two-step configurations (sf_step_tb.cu) follow the pipeline ones: index
+// SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount +
+// kSfPipeConfigCount + t.  One launch advances the state by two steps over
+// output tiles of tj x tk cells (threads per block, min blocks per SM);
+// trace1 receives the probe row of the state after the first step.
+struct SfTbConfig {
+    int tj, tk, threads, minb;
+    const char* name;
+};
+extern const SfTbConfig kSfTbConfigs[];
+extern const int kSfTbConfigCount;
+bool sf_tb_supported(const SfStepArgs& a);
+int sf_launch_step_tb(const SfStepArgs& a, const SfSources& src, bool geom, int cfg, int ich,
+                      float* trace1, cudaStream_t st);
+
 int sf_launch_build_flags(const uint8_t* geom, uint8_t* flags, int nx, int ny, int nz,
                           cudaStream_t st);
 int sf_launch_step(const SfStepArgs& a, const SfSources& src, const SfPoles& poles, bool geom,

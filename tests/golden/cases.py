@@ -202,6 +202,17 @@ PLAIN_CASES = {
         probes=[("output", (75, 50, 50))],
         steps=1000, store_fields=False,
     ),
+    "served_helmholtz": dict(
+        # one request of the served stream's Helmholtz kind: a solid block on
+        # the low-x side carved with 9 box-cavity resonators (cavity 10
+        # cells, neck radius 3 cells, necks opening to +x), PML 6, the source
+        # in front of the necks
+        shape=(60, 52, 56), res=1e-3, courant=0.5, pml=dict(depth=6),
+        geometry=dict(kind="sdf", which="served_helmholtz"),
+        sources=[("point", (28, 26, 28), 2500.0, 1.0)],
+        probes=[("near", (28, 26, 28)), ("far", (51, 43, 47))],
+        steps=300, store_fields=False,
+    ),
     "c2_enclosure_20": dict(
         # the 400^3 enclosure workload, first 20 steps (hashes + traces only)
         shape=(400, 400, 400), res=1e-3, courant=0.5, pml=dict(depth=16),
@@ -259,6 +270,19 @@ ADE_CASES = {
         sources=[("point", (20, 22, 38), 15000.0, 1.0), ("point", (50, 30, 60), 11000.0, 0.6)],
         probes=[("mid", (35, 20, 40)), ("far", (60, 35, 20))],
         steps=140, store_fields=False,
+    ),
+    "served_box_debye": dict(
+        # one request of the served stream's sealed-box kind with its Debye
+        # region: 3-cell walls around a cavity holding the source, a 2-pole
+        # Debye block inside the cavity, PML 5
+        shape=(50, 44, 48), res=1e-3, courant=0.5, pml=dict(depth=5),
+        geometry=dict(kind="sdf", which="served_box"),
+        materials=[dict(id=1, name="debye2", rho=1.204, c=343.0,
+                        poles=[("debye", "density", 0.4, 3e-4), ("debye", "modulus", 0.6, 5e-4)],
+                        box=((26, 34), (15, 25), (20, 30)))],
+        sources=[("point", (25, 22, 24), 2000.0, 1.0)],
+        probes=[("near", (25, 22, 24)), ("cavity", (30, 28, 30))],
+        steps=300, store_fields=False,
     ),
     "materialized_sdf": dict(
         # MaterializedGeometry (geometry/material_assignment.py:48-171): air is
@@ -368,6 +392,27 @@ def sdf_tree(api, which):
         return Difference(outer, inner, port)
     if which == "c2_enclosure":
         return c2_solid(api)
+    if which == "served_helmholtz":  # as workloads.served_stream builds its Helmholtz kind
+        res, lo, hi, cav, neck_r, per = 1e-3, 8, (52, 44, 48), 10, 3, 3
+        span = [h - lo for h in hi]
+        bx = lo + cav + 6
+        rs = []
+        for q in range(9):
+            a, b = q % per, q // per
+            cy = lo + (a + 0.5) * span[1] / per
+            cz = lo + (b + 0.5) * span[2] / per
+            rs.append(api.HelmholtzResonator(
+                position=(lo * res + cav * res / 2 + 2 * res, cy * res, cz * res),
+                cavity_shape="box", cavity_size=(cav * res,) * 3, neck_length=4 * res,
+                neck_radius=neck_r * res, neck_direction=(1, 0, 0)))
+        block = Box(min_corner=(lo * res, lo * res, lo * res),
+                    max_corner=(bx * res, hi[1] * res, hi[2] * res))
+        return Difference(block, Union(*rs))
+    if which == "served_box":  # the served stream's sealed box: 3-cell walls
+        res, src, half = 1e-3, (25, 22, 24), (12, 10, 11)
+        ctr = [(c + 0.5) * res for c in src]
+        return Difference(Box(center=ctr, size=[2 * (h + 3) * res for h in half]),
+                          Box(center=ctr, size=[2 * h * res for h in half]))
     if which == "mat_air":  # air volume: a box 2 cells in from the faces, minus a sphere
         return Difference(Box(center=(0.02, 0.018, 0.022), size=(0.036, 0.032, 0.040)),
                           Sphere(center=(0.012, 0.02, 0.03), radius=0.004))
