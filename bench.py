@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--workload", default="enclosure",
                     choices=["enclosure", "batch", "serve", "adjoint"])
     ap.add_argument("--adjoint-steps", type=int, default=2000)
-    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--requests", type=int, default=1000)
     ap.add_argument("--step-group", type=int, default=250)
     ap.add_argument("--max-active-cells", type=int, default=1 << 27,
                     help="served stream: cap on the cells of the running solves (0 = none)")

@@ -556,8 +556,8 @@ int chunk_for(const sf_plan* P, int cfg) {
         int dev = 0;
         if (cudaGetDevice(&dev) == cudaSuccess)
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const long long tiles =
-            (long long)((P->d.nz + c.tk - 1) / c.tk) * ((P->d.ny + c.tj - 1) / c.tj);
+        const long long tiles = (long long)((P->d.nz + 27) / 28) *
+                                ((P->d.ny + c.rows * c.warps - 1) / (c.rows * c.warps));
         long long chunks = (4LL * c.minb * sms + tiles - 1) / tiles;
         if (chunks < 1) chunks = 1;
         long long ich = (P->d.nx + chunks - 1) / chunks;

@@ -83,11 +83,11 @@ int sf_launch_step_stream(const SfPipeArgs& P, const SfSources& src, bool geom, 
 
 // Two-step configurations (sf_step_tb.cu) follow the pipeline ones: index
 // SF_CFG_COL_FIRST + kSfColConfigCount + kSfTileConfigCount +
-// kSfPipeConfigCount + t.  One launch advances the state by two steps over
-// output tiles of tj x tk cells (threads per block, min blocks per SM);
+// kSfPipeConfigCount + t.  One launch advances the state by two steps;
+// warps of 28 output k x `rows` output j, `warps` per block along j;
 // trace1 receives the probe row of the state after the first step.
 struct SfTbConfig {
-    int tj, tk, threads, minb;
+    int rows, warps, minb;
     const char* name;
 };
 extern const SfTbConfig kSfTbConfigs[];
