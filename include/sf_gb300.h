@@ -325,6 +325,13 @@ int sf_batch_destroy(sf_batch* batch);
  * [n_steps][n_probes] floats or NULL.  Pointers advance with each run. */
 int sf_batch_add(sf_batch* batch, sf_plan* plan, int64_t n_steps, const double* src_values_dev,
                  float* trace_dev);
+/* Same, with mic_trace_dev [n_steps][microphone rows] floats receiving the
+ * plan's microphone rows after each step (required when it has any).
+ * Nonuniform grids join the batch (warp-tile items) unless they also carry
+ * ADE materials; plans with plane boundaries or weighted (membrane) sources
+ * are refused: they step alone.  No counterpart in the reference. */
+int sf_batch_add_ex(sf_batch* batch, sf_plan* plan, int64_t n_steps,
+                    const double* src_values_dev, float* trace_dev, float* mic_trace_dev);
 int sf_batch_clear(sf_batch* batch);
 /* Work-item shape: rows of 32 columns (4, 8 or 16; the thread-column path
  * only -- warp tiles take 4 rows with float4 lanes, else 2) and i planes per

@@ -140,6 +140,7 @@ SIGNATURES = {
     "sf_batch_create": (_I, [ctypes.POINTER(_P)]),
     "sf_batch_destroy": (_I, [_P]),
     "sf_batch_add": (_I, [_P, _P, _I64, _P, _P]),
+    "sf_batch_add_ex": (_I, [_P, _P, _I64, _P, _P, _P]),
     "sf_batch_clear": (_I, [_P]),
     "sf_batch_set_tiles": (_I, [_P, _I, _I]),
     "sf_batch_tiles": (_I, [_P]),

@@ -1,13 +1,18 @@
 """Batched solves: many FDTDSolver instances stepped together on one GPU.
 
 Each member is an ordinary, fully configured :class:`FDTDSolver` (grid size,
-geometry, PML, sources, probes and ADE materials may all differ).  A run
-issues, per time step, one persistent launch whose blocks pull
-(grid, i-chunk, rows, columns) tiles from a device work queue
-(``sf_batch_*`` in include/sf_gb300.h); members with fewer steps drop out
-when they are done.  Every member's fields, traces and auxiliary ADE fields
-are bit-identical to running it alone.  No counterpart in the reference,
-which steps one solver at a time.
+geometry, PML, sources, probes, microphones, nonuniform spacing and ADE
+materials may all differ).  A run issues, per time step, one persistent
+launch whose blocks pull (grid, i-chunk, rows, columns) tiles from a device
+work queue (``sf_batch_*`` in include/sf_gb300.h), then one launch that
+samples every member's probes and microphone rows; members with fewer steps
+drop out when they are done.  Members with plane boundaries (Mur ABC,
+radiation impedance) or membrane sources need ordered per-plane passes
+after each step, and a nonuniform grid with ADE materials needs the
+per-cell nonuniform ADE kernel: those step through their own single-grid
+plan within the same run.  Every member's fields, traces, microphone
+waveforms and auxiliary ADE fields are bit-identical to running it alone.
+No counterpart in the reference, which steps one solver at a time.
 """
 from __future__ import annotations
 
@@ -151,15 +156,6 @@ class BatchedSolver:
                  pad: bool = True):
         if not solvers:
             raise ValueError("BatchedSolver needs at least one solver")
-        if any(s._microphones for s in solvers):
-            raise NotImplementedError("microphones are recorded by single-solver runs only")
-        if any(getattr(s, "_plane_bc_dirty", False) or
-               any(hasattr(b, "plane_ops") for b in s._boundaries) for s in solvers):
-            raise NotImplementedError("plane boundaries are stepped by single-solver runs only")
-        if any(src.source_type == "membrane" for s in solvers for src in s._sources):
-            raise NotImplementedError("membrane sources are stepped by single-solver runs only")
-        if any(not s.grid.is_uniform for s in solvers):
-            raise NotImplementedError("nonuniform grids are stepped by single-solver runs only")
         self.solvers = list(solvers)
         self._lib = _native.load()
         self._torch = self.solvers[0]._torch
@@ -184,6 +180,17 @@ class BatchedSolver:
     def _stream(self):
         return self._torch.cuda.current_stream().cuda_stream
 
+    @staticmethod
+    def steps_alone(s) -> bool:
+        """Whether member ``s`` steps through its own plan within a run:
+        plane boundaries or membrane sources (ordered passes after each step),
+        or a nonuniform grid with ADE materials."""
+        if any(hasattr(b, "plane_ops") for b in s._boundaries):
+            return True
+        if any(src.source_type == "membrane" for src in s._sources):
+            return True
+        return not s.grid.is_uniform and s.has_materials
+
     def _load(self, steps):
         """(Re)build the member list for a run of ``steps`` (int or per solver)."""
         torch = self._torch
@@ -198,12 +205,16 @@ class BatchedSolver:
             raise ValueError("one step count per solver")
         keep = []
         self._twins = []
+        self._alone = []
         # padded twins give float4 items twice the size of scalar ones: they
         # pay when the run has work for every resident warp several times
         # over, and make small runs slower (fewer, larger items)
         busy = sum(int(np.prod(s.shape)) for s, n in zip(self.solvers, counts) if n)
         pad = self.pad and self.kernel != "column" and busy >= self.PAD_MIN_CELLS
         for s, n in zip(self.solvers, counts):
+            if self.steps_alone(s):
+                self._alone.append((s, n))
+                continue
             vz_handed_out = s._host_exposed["vz"]  # the caller may have edited vz
             s._sync_tables()
             s._upload_exposed()
@@ -211,17 +222,21 @@ class BatchedSolver:
             n_probe = len(s._probe_order)
             trace = (torch.empty((n, n_probe), dtype=torch.float32, device=s._device)
                      if n_probe and n else None)
+            n_mic = getattr(s, "_mic_rows", 0)
+            mics = (torch.empty((n, n_mic), dtype=torch.float32, device=s._device)
+                    if n_mic and n else None)
             plan = s._plan
             twin = s._padded_twin(vz_handed_out) if pad and n else None
             if twin is not None:
                 twin.copy_in(s)
                 self._twins.append((s, twin))
                 plan = twin.plan
-            _native.check(lib.sf_batch_add(self._batch, plan, n,
-                                           None if src is None else src.data_ptr(),
-                                           None if trace is None else trace.data_ptr()),
+            _native.check(lib.sf_batch_add_ex(self._batch, plan, n,
+                                              None if src is None else src.data_ptr(),
+                                              None if trace is None else trace.data_ptr(),
+                                              None if mics is None else mics.data_ptr()),
                           "sf_batch_add")
-            keep.append((s, n, src, trace))
+            keep.append((s, n, src, trace, mics))
         return keep
 
     def autotune(self, launches: int = 3) -> dict:
@@ -253,19 +268,27 @@ class BatchedSolver:
         solver) in one batched run; ``graph_steps`` > 0 replays CUDA graphs
         of that many steps."""
         keep = self._load(steps)
-        longest = max(n for _, n, _, _ in keep)
-        _native.check(self._lib.sf_batch_run(self._batch, longest, int(graph_steps),
-                                             self._stream()), "sf_batch_run")
+        if keep:
+            longest = max(n for _, n, _, _, _ in keep)
+            _native.check(self._lib.sf_batch_run(self._batch, longest, int(graph_steps),
+                                                 self._stream()), "sf_batch_run")
         for s, twin in self._twins:
             twin.copy_out(s)
-        for s, n, src, trace in keep:
+        for s, n, src, trace, mics in keep:
             if trace is not None:
                 s._pending_traces.append((trace, list(s._probe_order)))
+            times = []
+            for _ in range(n):
+                times.append(s._time)
+                s._time += s.dt
+            if mics is not None:
+                s._pending_mics.append((mics, list(s._mic_order), times))
             if n:
                 s._mark_device_newer()
                 s._step_count += n
-                for _ in range(n):
-                    s._time += s.dt
+        for s, n in self._alone:  # their own plans, queued after the batch on the same stream
+            if n:
+                s.run_steps(n)
         self._keepalive = keep  # tables stay alive until the stream has used them
 
     @property

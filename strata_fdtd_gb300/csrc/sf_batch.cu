@@ -47,6 +47,16 @@ struct SfGridDev {
     int ade_lo[3], ade_hi[3];
     SfSources src;
     SfPoles poles;
+    // nonuniform grid (warp-tile items only): per-face velocity coefficients
+    // and per-cell inverse spacings per axis, or null
+    const float* nu_cv[3];
+    const float* nu_inv[3];
+    // microphone rows sampled after each step (k_mic_gather's arithmetic)
+    int n_mic;
+    const int* mic_field;
+    const long long* mic_idx;
+    const float* mic_w;
+    float* mic_trace;
 };
 
 namespace {
@@ -292,6 +302,65 @@ __global__ void __launch_bounds__(32 * W, MINB) k_batch_warp(
     }
 }
 
+// The items of nonuniform members (no ADE), in a persistent kernel of their
+// own: the warp tiles with per-face coefficients and per-cell divergence
+// scales (NU variants of sf_tile.cuh), from the queue's second counter.
+// Keeping them out of k_batch_warp keeps its register allocation as it is.
+template <int W, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) k_batch_warp_nu(
+    const SfGridDev* __restrict__ grids, const int4* __restrict__ items, int n_items,
+    int* __restrict__ queue, const long long* __restrict__ step_ptr) {
+    const int lane = threadIdx.x;
+    const long long s = *step_ptr;
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(queue, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= n_items) return;  // warp-uniform
+        const int4 T = items[it];
+        const SfGridDev& g = grids[T.x];
+        if (s >= g.n_steps) continue;
+        const bool geom = g.flags != nullptr;
+        const int j0 = T.z * g.jspan;
+        const int in = (int)((g.cur0 + s) & 1);
+        SfTileIo io;
+        io.nx = g.nx;
+        io.ny = g.ny;
+        io.nz = g.nz;
+        io.plane = g.plane;
+        io.cv = g.cv;
+        io.cp = g.cp;
+        io.p = g.f[in][0];
+        io.vx = g.f[in][1];
+        io.vy = g.f[in][2];
+        io.vz = g.f[in][3];
+        io.po = g.f[1 - in][0];
+        io.vxo = g.f[1 - in][1];
+        io.vyo = g.f[1 - in][2];
+        io.vzo = g.f[1 - in][3];
+        io.flags = g.flags;
+        io.dx = g.dx;
+        io.dy = g.dy;
+        io.dz = g.dz;
+        io.src_val = g.src_val + s * g.src.n;
+        for (int q = 0; q < 3; ++q) {
+            io.nu_cv[q] = g.nu_cv[q];
+            io.nu_inv[q] = g.nu_inv[q];
+        }
+        const int i0 = T.y * g.ich;
+        const int i1 = min(i0 + g.ich, g.nx);
+        if (g.vec4) {
+            const SfPlainMem mem{io.ny * io.nz};
+            if (geom) tile4_run<true, 1, false, true, true>(io, g.src, i0, i1, j0, T.w * 32, mem);
+            else tile4_run<false, 1, false, true, true>(io, g.src, i0, i1, j0, T.w * 32, mem);
+        } else {
+            const int k = T.w * 32 + lane;
+            if (geom) tile1_run<true, 2, false, true>(io, g.src, i0, i1, j0, k);
+            else tile1_run<false, 2, false, true>(io, g.src, i0, i1, j0, k);
+        }
+    }
+}
+
 constexpr int kBatchWarps = 4;  // warps per block of the persistent kernel
 
 // ADE density poles of every grid that has them, over its material box
@@ -329,14 +398,28 @@ __global__ void k_batch_ade_density(const SfGridDev* __restrict__ grids, const i
     }
 }
 
-// Probe samples of every grid after the step (core/solver.py:2435-2439).
+// Probe samples of every grid after the step (core/solver.py:2435-2439), and
+// its microphone rows: 8 weighted corner values of p or a velocity
+// component, summed from 0 in corner order (the arithmetic of k_mic_gather).
 __global__ void k_batch_post(const SfGridDev* __restrict__ grids, const long long* __restrict__ step_ptr) {
     const long long s = *step_ptr;
     const SfGridDev& g = grids[blockIdx.x];
-    if (s >= g.n_steps || g.n_probe == 0 || g.trace == nullptr) return;
-    const float* __restrict__ P = g.f[(g.cur0 + s + 1) & 1][0];
-    for (int t = threadIdx.x; t < g.n_probe; t += blockDim.x)
-        g.trace[s * g.n_probe + t] = P[g.probe_cells[t]];
+    if (s >= g.n_steps) return;
+    float* const* f = g.f[(g.cur0 + s + 1) & 1];
+    if (g.n_probe > 0 && g.trace != nullptr)
+        for (int t = threadIdx.x; t < g.n_probe; t += blockDim.x)
+            g.trace[s * g.n_probe + t] = f[0][g.probe_cells[t]];
+    if (g.n_mic > 0 && g.mic_trace != nullptr) {
+        for (int m = threadIdx.x; m < g.n_mic; m += blockDim.x) {
+            const int fi = g.mic_field ? g.mic_field[m] : 0;
+            const float* __restrict__ src = f[fi >= 0 && fi <= 3 ? fi : 0];
+            float acc = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                acc = f_add(acc, f_mul(g.mic_w[8 * m + q], src[g.mic_idx[8 * m + q]]));
+            g.mic_trace[s * g.n_mic + m] = acc;
+        }
+    }
 }
 
 __global__ void k_batch_advance(long long* step_ptr, int* queue) {
@@ -355,6 +438,7 @@ struct sf_batch {
         long long steps;
         const double* src;
         float* trace;
+        float* mic_trace;
     };
     std::vector<Member> members;
     int rows = 8;
@@ -366,6 +450,8 @@ struct sf_batch {
     int4* d_tiles = nullptr;  // work items: those meeting a material box first
     int n_tiles = 0;          // all work items
     int n_tiles_ade = 0;      // items that meet a material box
+    int n_tiles_nu = 0;       // items of nonuniform members, after the others in d_tiles
+    int blocks_nu = 0;        // persistent grid size of k_batch_warp_nu
     int* d_ade_ids = nullptr;
     int n_ade = 0;
     int ade_blocks = 1;
@@ -434,7 +520,7 @@ int build(sf_batch* B) {
     free_device(B);
     if (B->members.empty()) return sf_fail("sf_batch: no members");
     std::vector<SfGridDev> grids;
-    std::vector<int4> tiles, tiles_ade;
+    std::vector<int4> tiles, tiles_ade, tiles_nu;
     std::vector<int> ade_ids;
     // largest grids first, so the queue hands out the long work early
     std::vector<int> order(B->members.size());
@@ -458,10 +544,11 @@ int build(sf_batch* B) {
         for (int a = 0; a < 2; ++a)
             for (int f = 0; f < 4; ++f)
                 aligned = aligned && (reinterpret_cast<uintptr_t>(P->f[a][f]) & 15u) == 0;
-        g.vec4 = B->plain_kernel != 0 && P->d.nz % 4 == 0 && aligned &&
+        g.vec4 = (B->plain_kernel != 0 || P->nu != nullptr) && P->d.nz % 4 == 0 && aligned &&
                  (P->flags == nullptr || (reinterpret_cast<uintptr_t>(P->flags) & 3u) == 0) &&
                  n_cells + 2LL * P->d.ny * P->d.nz + 8 < 0x7fffffffLL;
-        g.jspan = B->plain_kernel == 0 ? B->rows : (g.vec4 ? 4 : 2);  // rows per item
+        // rows per item; a nonuniform member always takes the warp tiles
+        g.jspan = (B->plain_kernel == 0 && !P->nu) ? B->rows : (g.vec4 ? 4 : 2);
         g.plane = (long long)P->d.ny * P->d.nz;
         g.n_steps = m.steps;
         g.cv = P->d.coeff_v;
@@ -484,6 +571,17 @@ int build(sf_batch* B) {
         }
         g.src = P->src;
         g.poles = P->poles;
+        if (P->nu) {  // face coefficients x, y, z, then cell inverse spacings x, y, z
+            const int n3[3] = {P->d.nx, P->d.ny, P->d.nz};
+            long long off = 0;
+            for (int a = 0; a < 3; off += n3[a], ++a) g.nu_cv[a] = P->nu + off;
+            for (int a = 0; a < 3; off += n3[a], ++a) g.nu_inv[a] = P->nu + off;
+        }
+        g.n_mic = m.mic_trace ? P->n_mic : 0;
+        g.mic_field = P->mic_field;
+        g.mic_idx = P->mic_idx;
+        g.mic_w = P->mic_w;
+        g.mic_trace = m.mic_trace;
         const int gi = (int)grids.size();
         grids.push_back(g);
         if (g.poles.n > 0 && g.poles.n_density > 0) {
@@ -498,16 +596,20 @@ int build(sf_batch* B) {
             for (int jb = 0; jb < njb; ++jb)
                 for (int kb = 0; kb < nkb; ++kb) {
                     const bool ade = g.poles.n > 0 && tile_meets_box(g, ch, jb, kb);
-                    (ade ? tiles_ade : tiles).push_back(make_int4(gi, ch, jb, kb));
+                    if (g.nu_cv[0] != nullptr) tiles_nu.push_back(make_int4(gi, ch, jb, kb));
+                    else (ade ? tiles_ade : tiles).push_back(make_int4(gi, ch, jb, kb));
                 }
     }
-    if (tiles.size() + tiles_ade.size() > 0x7fffffff) return sf_fail("sf_batch: too many tiles");
+    if (tiles.size() + tiles_ade.size() + tiles_nu.size() > 0x7fffffff)
+        return sf_fail("sf_batch: too many tiles");
     // items meeting a material box first: they are the slowest, so they
     // start early and the step ends on short plain items
     B->n_tiles_ade = (int)tiles_ade.size();
     tiles_ade.insert(tiles_ade.end(), tiles.begin(), tiles.end());
     tiles.swap(tiles_ade);
     B->n_tiles = (int)tiles.size();
+    B->n_tiles_nu = (int)tiles_nu.size();
+    tiles.insert(tiles.end(), tiles_nu.begin(), tiles_nu.end());
     B->n_ade = (int)ade_ids.size();
     B->ade_blocks = (int)std::min<long long>(std::max<long long>(1, (ade_cells + 255) / 256), 512);
     SF_CUDA_OK(cudaMalloc(&B->d_grids, sizeof(SfGridDev) * grids.size()));
@@ -523,12 +625,22 @@ int build(sf_batch* B) {
     SF_CUDA_OK(cudaMalloc(&B->d_queue, 2 * sizeof(int)));
     SF_CUDA_OK(cudaMalloc(&B->d_step, sizeof(long long)));
     if (int rc = occupancy_warp(B)) return rc;
+    if (B->n_tiles_nu > 0)
+        if (int rc = occupancy_blocks(k_batch_warp_nu<kBatchWarps, kMinBlocksTile>, 32 * kBatchWarps,
+                                      &B->blocks_nu))
+            return rc;
     B->built = true;
     return 0;
 }
 
 int launch_step_kernel(sf_batch* B, cudaStream_t st, int trial) {
     constexpr int W = kBatchWarps;
+    if (B->n_tiles_nu > 0 && !trial) {  // nonuniform members: their own persistent kernel
+        const int blocks = std::min(B->blocks_nu, (B->n_tiles_nu + W - 1) / W);
+        k_batch_warp_nu<W, kMinBlocksTile><<<blocks, dim3(32, W), 0, st>>>(
+            B->d_grids, B->d_tiles + B->n_tiles, B->n_tiles_nu, B->d_queue + 1, B->d_step);
+        if (cudaGetLastError() != cudaSuccess) return sf_fail("k_batch_warp_nu launch failed");
+    }
     if (B->n_tiles == 0) return 0;
     const dim3 blk(32, W);
     if (B->plain_kernel == 1)
@@ -579,17 +691,25 @@ int sf_batch_destroy(sf_batch* B) {
 
 int sf_batch_add(sf_batch* B, sf_plan* P, int64_t n_steps, const double* src_values_dev,
                  float* trace_dev) {
+    return sf_batch_add_ex(B, P, n_steps, src_values_dev, trace_dev, nullptr);
+}
+
+int sf_batch_add_ex(sf_batch* B, sf_plan* P, int64_t n_steps, const double* src_values_dev,
+                    float* trace_dev, float* mic_trace_dev) {
     if (!B || !P) return sf_fail("sf_batch_add: NULL argument");
     if (!P->bound) return sf_fail("sf_batch_add: plan fields not bound");
     if (P->device != B->device) return sf_fail("sf_batch_add: plan on another device");
-    if (P->nu) return sf_fail("sf_batch_add: nonuniform grids are stepped alone");
+    if (P->nu && P->poles.n > 0)
+        return sf_fail("sf_batch_add: nonuniform grids with ADE materials are stepped alone");
+    if (P->n_mic > 0 && n_steps > 0 && !mic_trace_dev)
+        return sf_fail("sf_batch_add: microphone rows need a microphone trace");
     if (P->n_plane) return sf_fail("sf_batch_add: plane boundaries are stepped alone");
     for (int q = 0; q < P->src.n; ++q)
         if (P->src.s[q].kind == 2) return sf_fail("sf_batch_add: membrane sources are stepped alone");
     if (n_steps < 0) return sf_fail("sf_batch_add: negative step count");
     if (P->src.n > 0 && n_steps > 0 && !src_values_dev)
         return sf_fail("sf_batch_add: sources need src_values");
-    B->members.push_back({P, n_steps, src_values_dev, trace_dev});
+    B->members.push_back({P, n_steps, src_values_dev, trace_dev, mic_trace_dev});
     B->built = false;
     return 0;
 }

@@ -39,6 +39,41 @@ def _fields(s):
     return {f: getattr(s, f).copy() for f in ("p", "vx", "vy", "vz")}
 
 
+WIDE_MIX = [("plain", "nu_stretch_blocks"), ("plain", "nu_regions_sdf"),
+            ("plain", "nu_stretch_low_end"), ("plain", "mics_geom"),
+            ("plain", "mics_directional"), ("plain", "abc_all_sources"),
+            ("plain", "rad_pml_mix"), ("plain", "membranes"), ("ade", "nu_mixed_geom"),
+            ("plain", "blocks_odd"), ("ade", "debye_2pole")]
+
+
+@pytest.mark.parametrize("graph_steps", [0, 16])
+def test_batch_of_the_wider_feature_set_matches_goldens(graph_steps, manifest):
+    """Nonuniform grids (their own persistent kernel), microphones (omni and
+    directional rows sampled after each batch step), and members that step
+    through their own plans inside the run (Mur ABC and radiation-impedance
+    planes, membrane sources, a nonuniform grid with ADE materials), mixed
+    with plain and ADE members: every member equals its reference fixture --
+    fields, probe traces and microphone waveforms."""
+    solvers = [C.build_case(API, _case(k, n)) for k, n in WIDE_MIX]
+    steps = [_case(k, n)["steps"] for k, n in WIDE_MIX]
+    alone = [BatchedSolver.steps_alone(s) for s in solvers]
+    assert alone == [False, False, False, False, False, True, True, True, True, False, False]
+    b = BatchedSolver(solvers, rows=8, i_chunk=5)
+    b.run_steps(steps, graph_steps=graph_steps)
+    for s, (kind, name) in zip(solvers, WIDE_MIX):
+        key = ("ade_" if kind == "ade" else "plain_") + name
+        info, g = manifest[key], golden(key)
+        for f in ("p", "vx", "vy", "vz"):
+            assert sha256(getattr(s, f)) == info[f"sha_{f}"], f"{key} {f}"
+        for pn in g["probe_names"]:
+            np.testing.assert_array_equal(s.get_probe_data()[str(pn)], g[f"trace__{pn}"],
+                                          err_msg=f"{key} probe {pn}")
+        for k in g.files:
+            if k.startswith("mic__"):
+                np.testing.assert_array_equal(s.microphones[k[5:]].get_waveform(), g[k],
+                                              err_msg=f"{key} microphone {k[5:]}")
+
+
 @pytest.mark.parametrize("graph_steps", [0, 16])
 def test_batch_matches_reference_goldens(graph_steps, manifest):
     """The mix (plain, solids, plane sources, Debye and Lorentz ADE, different

@@ -187,8 +187,7 @@ def test_plane_boundaries(name, config, manifest):
     _compare(s, "plain_" + name, manifest)
     with pytest.raises(NotImplementedError):
         s.add_boundary(S.PML(depth=2))  # a PML after plane boundaries
-    with pytest.raises(NotImplementedError):
-        S.BatchedSolver([s])
+    assert S.BatchedSolver.steps_alone(s)  # a batch steps it through its own plan
 
 
 def test_membranes_step_by_step_and_limits(manifest):
@@ -201,8 +200,7 @@ def test_membranes_step_by_step_and_limits(manifest):
         if q == 37:
             _ = s.vx[0, 0, 0]
     _compare(s, "plain_membranes", manifest)
-    with pytest.raises(NotImplementedError):
-        S.BatchedSolver([C.build_case(API, case)])
+    assert S.BatchedSolver.steps_alone(C.build_case(API, case))
 
 
 def test_nonuniform_autotune_and_limits(manifest):
@@ -213,8 +211,7 @@ def test_nonuniform_autotune_and_limits(manifest):
     assert table["best"].startswith("tile")
     s.run_steps(case["steps"] - 7)
     _compare(s, "plain_nu_stretch_low_end", manifest)
-    with pytest.raises(NotImplementedError):
-        S.BatchedSolver([s])
+    assert not S.BatchedSolver.steps_alone(s)  # batched: its own persistent kernel
 
 
 def test_c1_quick_start_1000_steps(manifest):

@@ -112,3 +112,27 @@ def test_budget_holds_on_the_gpu():
     assert stats["peak_hbm_bytes"] <= budget
     # smaller solves may fit three at a time, never all six
     assert 1 <= stats["peak_active"] < 6
+
+
+def test_served_requests_with_the_wider_feature_set_match_goldens():
+    """Requests using a nonuniform grid, microphones, Mur/radiation plane
+    boundaries and membrane sources, served together (the batch steps the
+    last two kinds through their own plans): each result equals the
+    reference's probe traces."""
+    keys = ["nu_regions_sdf", "mics_geom", "abc_all_sources", "membranes", "c1_tiny"]
+    reqs = []
+    for q, key in enumerate(keys):
+        case = C.PLAIN_CASES[key]
+        shape = case.get("shape") or (40, 40, 40)
+        reqs.append(Request(rid=q, build=lambda case=case: C.build_case(API, case),
+                            steps=case["steps"], arrival=0.0, nbytes=solve_bytes(shape),
+                            cells=int(np.prod(shape))))
+    srv = SolveServer(GPUExecutor(graph_steps=0), hbm_budget=160e9, step_group=48)
+    stats = srv.run(reqs, realtime=False)
+    assert stats["done"] == len(keys), stats["errors"]
+    results = {r.rid: r.result for r in srv.finished}
+    for q, key in enumerate(keys):
+        g = golden("plain_" + key)
+        for name in g["probe_names"]:
+            np.testing.assert_array_equal(results[q][str(name)], g[f"trace__{name}"],
+                                          err_msg=f"{key} probe {name}")
