@@ -80,7 +80,9 @@ typedef struct {
  *   op 21 PUSH_SCALE a     push point / a
  *   op 22 POP_POINT
  *   op 23 SCALE_DIST s0    top distance *= s0
- *   op 24 NEGATE           top distance = -top                         */
+ *   op 24 NEGATE           top distance = -top
+ *   op 25 PUSH_ROTATE a, b push the point times rows a, b (and the next
+ *                          node's a, op 26 ROTATE_ROW2) of a 3x3 matrix  */
 typedef struct {
     int32_t op, n;
     double a[3], b[3];

@@ -475,6 +475,18 @@ class SDFPrimitive:
     def scale(self, factor):
         return Scale(self, factor)
 
+    def rotate(self, axis, angle):
+        return Rotate(self, axis=axis, angle=angle)
+
+    def rotate_x(self, angle):
+        return self.rotate((1, 0, 0), angle)
+
+    def rotate_y(self, angle):
+        return self.rotate((0, 1, 0), angle)
+
+    def rotate_z(self, angle):
+        return self.rotate((0, 0, 1), angle)
+
 
 class Box(SDFPrimitive):  # sdf.py:232-299
     def __init__(self, center=None, size=None, min_corner=None, max_corner=None):
@@ -577,6 +589,24 @@ class Scale(SDFPrimitive):  # sdf.py:1239-1300
     def sdf(self, points):
         d = self.child.sdf(points / self.scale)
         return d * self.scale[0] if self.uniform else d * np.min(self.scale)
+
+
+def rotation_matrix(axis, angle):  # geometry/sdf.py:1151-1185
+    axis = np.asarray(axis, dtype=np.float64)
+    axis = axis / np.linalg.norm(axis)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    return np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * (K @ K)
+
+
+class Rotate(SDFPrimitive):  # geometry/sdf.py:1303-1355
+    def __init__(self, child, axis=None, angle=None, matrix=None):
+        self.child = child
+        self.matrix = (np.asarray(matrix, dtype=np.float64) if matrix is not None
+                       else rotation_matrix(np.asarray(axis), angle))
+        self.inv_matrix = self.matrix.T
+
+    def sdf(self, points):
+        return self.child.sdf(np.asarray(points, dtype=np.float64) @ self.inv_matrix.T)
 
 
 class HelmholtzResonator(SDFPrimitive):  # geometry/resonator.py:59-297

@@ -19,8 +19,8 @@ from .microphones import Microphone
 from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
 from .membranes import CircularMembraneSource, MembraneSource, RectangularMembraneSource
 from .resonator import HelmholtzResonator, helmholtz_array
-from .sdf import (Box, CSGNode, Cylinder, Difference, Intersection, Scale, SDFPrimitive, Sphere,
-                  Translate, Union)
+from .sdf import (Box, CSGNode, Cylinder, Difference, Intersection, Rotate, Scale, SDFPrimitive,
+                  Sphere, Translate, Union, rotation_matrix)
 from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_native_kernels
 
 __version__ = "0.1.0"
@@ -29,7 +29,8 @@ __all__ = [
     "FDTDSolver", "GaussianPulse", "Probe", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
     "RigidBoundary", "ABCFirstOrder", "RadiationImpedance", "Pole",
     "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
-    "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale",
+    "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale", "Rotate",
+    "rotation_matrix",
     "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",
     "NativeError", "BatchedSolver", "DifferentiableSolver", "MembraneSource",
     "CircularMembraneSource", "RectangularMembraneSource", "MaterializedGeometry",

@@ -10,6 +10,8 @@
 //   Cylinder sdf.py:382-424  projection, clamp, radial/axial distance
 //   Union / Intersection / Difference  sdf.py:566-584, 629-647, 704-721
 //   Translate / Scale        sdf.py:1225-1236, 1285-1294
+//   Rotate                   sdf.py:1351-1355: point @ R (rows of R^T
+//                            dotted in the order ((p0 m0 + p1 m1) + p2 m2))
 // np.linalg.norm over three components sums ((x0^2 + x1^2) + x2^2).  The
 // cylinder's axis projection uses np.dot (BLAS), whose rounding depends on
 // the BLAS build; here it is ((v0*a0 + v1*a1) + v2*a2), which equals any
@@ -115,6 +117,16 @@ __device__ double eval_sdf(const sf_sdf_node* __restrict__ prog, int n, double x
                     py[ptop] = __ddiv_rn(Y, N.a[1]);
                     pz[ptop] = __ddiv_rn(Z, N.a[2]);
                 }
+                break;
+            }
+            case 25: {  // PUSH_ROTATE: rows 0, 1 here (a, b), row 2 in the next node's a
+                if (ptop + 1 >= VX_PSTACK || q + 1 >= n || prog[q + 1].op != 26) { *err = 3; return 1.0; }
+                const sf_sdf_node& N2 = prog[q + 1];
+                ++ptop;
+                px[ptop] = d_add(d_add(d_mul(X, N.a[0]), d_mul(Y, N.a[1])), d_mul(Z, N.a[2]));
+                py[ptop] = d_add(d_add(d_mul(X, N.b[0]), d_mul(Y, N.b[1])), d_mul(Z, N.b[2]));
+                pz[ptop] = d_add(d_add(d_mul(X, N2.a[0]), d_mul(Y, N2.a[1])), d_mul(Z, N2.a[2]));
+                ++q;  // the row-2 node is consumed
                 break;
             }
             case 22:

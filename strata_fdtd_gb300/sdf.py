@@ -10,8 +10,9 @@ reference's own NumPy arithmetic, so the constants the kernel sees are the
 reference's constants.
 
 Supported: Box, Sphere, Cylinder, Union, Intersection, Difference, Translate,
-Scale, HelmholtzResonator (geometry/resonator.py).  Rotation, smooth CSG,
-cones and horns are outside the time-step path and raise on use.
+Scale, Rotate (axis-angle or matrix, rotate_x/y/z), HelmholtzResonator
+(geometry/resonator.py).  Smooth CSG, cones and horns are outside the
+time-step path and raise on use.
 """
 from __future__ import annotations
 
@@ -25,6 +26,7 @@ from . import _native
 OP_BOX, OP_SPHERE, OP_CYLINDER = 1, 2, 3
 OP_UNION, OP_INTERSECTION, OP_DIFFERENCE = 10, 11, 12
 OP_PUSH_TRANSLATE, OP_PUSH_SCALE, OP_POP_POINT, OP_SCALE_DIST, OP_NEGATE = 20, 21, 22, 23, 24
+OP_PUSH_ROTATE, OP_ROTATE_ROW2 = 25, 26
 
 
 def _node(op, n=0, a=(0.0, 0.0, 0.0), b=(0.0, 0.0, 0.0), s0=0.0, s1=0.0):
@@ -103,6 +105,18 @@ class SDFPrimitive:
 
     def scale(self, factor):
         return Scale(self, factor)
+
+    def rotate(self, axis, angle):
+        return Rotate(self, axis=axis, angle=angle)
+
+    def rotate_x(self, angle):
+        return self.rotate((1, 0, 0), angle)
+
+    def rotate_y(self, angle):
+        return self.rotate((0, 1, 0), angle)
+
+    def rotate_z(self, angle):
+        return self.rotate((0, 0, 1), angle)
 
 
 class Box(SDFPrimitive):
@@ -297,3 +311,49 @@ class Scale(Transform):
     def bounding_box(self):
         lo, hi = self.child.bounding_box
         return lo * self.scale, hi * self.scale
+
+
+def rotation_matrix(axis, angle):
+    """Rodrigues' rotation matrix I + sin(a) K + (1 - cos(a)) K K for the
+    normalised axis (geometry/sdf.py:1151-1185): the reference's NumPy
+    expression, so the matrix entries are the reference's."""
+    axis = np.asarray(axis, dtype=np.float64)
+    axis = axis / np.linalg.norm(axis)
+    K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]], [-axis[1], axis[0], 0]])
+    return np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * (K @ K)
+
+
+class Rotate(Transform):
+    """Evaluate the child at the inversely rotated point, point @ R
+    (geometry/sdf.py:1303-1390): each coordinate the sum
+    ((p0 m0 + p1 m1) + p2 m2) of a row of R^T.  NumPy's matrix product
+    goes through BLAS, whose summation order is its own: for a rotation that
+    is not a multiple of 90 degrees about a coordinate axis, cells within
+    rounding (about 1e-16 m) of a surface may fall on the other side."""
+
+    def __init__(self, child, axis=None, angle=None, matrix=None):
+        super().__init__(child)
+        if matrix is not None:
+            self.matrix = np.asarray(matrix, dtype=np.float64)
+            if self.matrix.shape != (3, 3):
+                raise ValueError(f"matrix must be 3x3, got shape {self.matrix.shape}")
+        elif axis is not None and angle is not None:
+            self.matrix = rotation_matrix(np.asarray(axis), angle)
+        else:
+            raise ValueError("Must provide either (axis, angle) or matrix")
+        self.inv_matrix = self.matrix.T
+
+    def _emit(self, prog):
+        m = self.inv_matrix  # point' = point @ inv.T: coordinate i = sum_j p_j inv[i, j]
+        prog.append(_node(OP_PUSH_ROTATE, a=m[0], b=m[1]))
+        prog.append(_node(OP_ROTATE_ROW2, a=m[2]))
+        self.child._emit(prog)
+        prog.append(_node(OP_POP_POINT))
+
+    @property
+    def bounding_box(self):
+        lo, hi = self.child.bounding_box
+        corners = np.array([[x, y, z] for x in (lo[0], hi[0]) for y in (lo[1], hi[1])
+                            for z in (lo[2], hi[2])])
+        rc = corners @ self.matrix.T
+        return rc.min(axis=0), rc.max(axis=0)

@@ -339,6 +339,7 @@ VOXEL_CASES = {
     "cyl_oblique": ((32, 32, 32), 1e-3, "cyl_oblique"),
     "csg_mix": ((48, 40, 44), 1e-3, "csg_mix"),
     "translate_scale": ((40, 40, 40), 1e-3, "translate_scale"),
+    "rotated": ((44, 40, 48), 1e-3, "rotated"),
     "helmholtz": ((60, 48, 56), 1e-3, "helmholtz"),
     "small_enclosure": ((36, 30, 40), 1e-3, "small_enclosure"),
     "c2_enclosure_4mm": ((100, 100, 100), 4e-3, "c2_enclosure"),
@@ -370,6 +371,14 @@ def sdf_tree(api, which):
         c = Cylinder(p1=(0.024, 0.02, 0.0), p2=(0.024, 0.02, 0.044), radius=0.005)
         d = Box(min_corner=(0.002, 0.002, 0.002), max_corner=(0.01, 0.012, 0.042))
         return Union(Difference(Intersection(a, b), c), d)
+    if which == "rotated":  # Rotate (geometry/sdf.py:1303-1390): z, x and oblique axes
+        b = Box(center=(0.0, 0.0, 0.0), size=(0.018, 0.008, 0.012)).rotate_z(0.5).translate(
+            (0.02, 0.021, 0.019))
+        c = Cylinder(p1=(-0.008, 0.0, 0.0), p2=(0.008, 0.0, 0.0), radius=0.004).rotate(
+            (1.0, 1.0, 1.0), 0.9).translate((0.024, 0.018, 0.03))
+        e = Box(center=(0.0, 0.0, 0.0), size=(0.03, 0.004, 0.006)).rotate_x(-0.35).translate(
+            (0.022, 0.03, 0.012))
+        return Difference(Union(b, c, e), Sphere(center=(0.02, 0.021, 0.019), radius=0.003))
     if which == "translate_scale":
         s = Sphere(center=(0.0, 0.0, 0.0), radius=0.006).translate((0.02, 0.021, 0.019))
         b = Box(center=(0.0, 0.0, 0.0), size=(0.01, 0.006, 0.008)).scale(1.5).translate(
