@@ -119,7 +119,16 @@ int sf_device_info(int device, sf_device_info_t* out);
 /* Replaces the per-call shape checks of kernels.cpp:21-65 and the
  * coefficient hand-off of core/solver.py:1584-1586. */
 int sf_plan_create(const sf_grid_desc* desc, sf_plan** out);
+/* The plan's own device tables (face flags, decays, probe cells ...) are
+ * queued for release rather than freed at once: cudaFree waits for every
+ * kernel on the device, which would stall a host that retires one solve
+ * while others run.  The queue is released when 1 GiB or 4096 buffers have
+ * accumulated, or by sf_release_deferred(); batches (sf_batch_destroy) do
+ * the same with their tables and graphs. */
 int sf_plan_destroy(sf_plan* plan);
+/* Free every queued buffer and graph now (waits for the device).  No
+ * counterpart in the reference. */
+int sf_release_deferred(void);
 
 /* Bind the two ping-pong copies of p, vx, vy, vz (8 device buffers of
  * nx*ny*nz floats).  Set 0 holds the current state.  The plan never frees

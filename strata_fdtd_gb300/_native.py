@@ -108,6 +108,7 @@ SIGNATURES = {
     "sf_device_info": (_I, [_I, ctypes.POINTER(SfDeviceInfo)]),
     "sf_plan_create": (_I, [ctypes.POINTER(SfGridDesc), ctypes.POINTER(_P)]),
     "sf_plan_destroy": (_I, [_P]),
+    "sf_release_deferred": (_I, []),
     "sf_plan_bind_fields": (_I, [_P] + [_P] * 8),
     "sf_plan_current": (_I, [_P]),
     "sf_plan_set_current": (_I, [_P, _I]),

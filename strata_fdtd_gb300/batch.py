@@ -267,11 +267,16 @@ class BatchedSolver:
         """Advance every member by ``steps`` (an int, or one count per
         solver) in one batched run; ``graph_steps`` > 0 replays CUDA graphs
         of that many steps."""
+        import time as _time
+
+        t0 = _time.perf_counter()
         keep = self._load(steps)
+        t1 = _time.perf_counter()
         if keep:
             longest = max(n for _, n, _, _, _ in keep)
             _native.check(self._lib.sf_batch_run(self._batch, longest, int(graph_steps),
                                                  self._stream()), "sf_batch_run")
+        self.host_s = {"load": t1 - t0, "run": _time.perf_counter() - t1}
         for s, twin in self._twins:
             twin.copy_out(s)
         for s, n, src, trace, mics in keep:

@@ -54,6 +54,63 @@ int sf_fail_cuda(cudaError_t e, const char* what, const char* file, int line) {
 
 int sf_noalloc_setup(int dev);  // defined with the no-alloc energy array below
 
+// Deferred device frees.  cudaFree waits for all work on the device, so a
+// plan or a batch released while other solves' kernels run would stall the
+// host until they finish (a served stream retires and builds solves while
+// the next group runs).  The buffers of destroyed plans and batches and the
+// batches' graphs are queued here instead and released together once 1 GiB
+// or 4096 entries have accumulated, or by sf_release_deferred().
+namespace {
+struct SfDeferred {
+    int device;
+    void* ptr;
+    cudaGraphExec_t exec;
+    cudaGraph_t graph;
+};
+std::mutex g_def_mu;
+std::vector<SfDeferred> g_def;
+size_t g_def_bytes = 0;
+constexpr size_t kDeferredBytes = size_t(1) << 30, kDeferredCount = 4096;
+
+void release_deferred_locked() {
+    for (const SfDeferred& d : g_def) {
+        DeviceGuard g(d.device);
+        if (d.exec) cudaGraphExecDestroy(d.exec);
+        if (d.graph) cudaGraphDestroy(d.graph);
+        if (d.ptr) cudaFree(d.ptr);
+    }
+    g_def.clear();
+    g_def_bytes = 0;
+}
+
+void defer_push(const SfDeferred& d, size_t bytes) {
+    std::lock_guard<std::mutex> lock(g_def_mu);
+    g_def.push_back(d);
+    g_def_bytes += bytes;
+    if (g_def_bytes >= kDeferredBytes || g_def.size() >= kDeferredCount) release_deferred_locked();
+}
+}  // namespace
+
+void sf_defer_free(void* p, size_t bytes) {
+    if (!p) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    defer_push({dev, p, nullptr, nullptr}, bytes);
+}
+
+void sf_defer_graph(cudaGraphExec_t exec, cudaGraph_t graph) {
+    if (!exec && !graph) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    defer_push({dev, nullptr, exec, graph}, 0);
+}
+
+extern "C" int sf_release_deferred(void) {
+    std::lock_guard<std::mutex> lock(g_def_mu);
+    release_deferred_locked();
+    return 0;
+}
+
 namespace {
 
 int set_decays(sf_plan* P, const float* host[3]) {
@@ -134,22 +191,22 @@ int sf_plan_create(const sf_grid_desc* desc, sf_plan** out) {
 int sf_plan_destroy(sf_plan* P) {
     if (!P) return 0;
     DeviceGuard g(P->device);
-    for (auto& d : P->decay) cudaFree(d);
-    cudaFree(P->flags);
-    cudaFree(P->probe_cells);
-    cudaFree(P->mic_idx);
-    cudaFree(P->mic_w);
-    cudaFree(P->mic_field);
-    cudaFree(P->nu);
-    cudaFree(P->plane_prev);
+    for (auto& d : P->decay) sf_defer_free(d, 0);
+    sf_defer_free(P->flags, (size_t)P->n);
+    sf_defer_free(P->probe_cells, 0);
+    sf_defer_free(P->mic_idx, 0);
+    sf_defer_free(P->mic_w, 0);
+    sf_defer_free(P->mic_field, 0);
+    sf_defer_free(P->nu, 0);
+    sf_defer_free(P->plane_prev, 0);
     for (int q = 0; q < SF_MAX_SOURCES; ++q) {
-        cudaFree(P->wsrc_cells[q]);
-        cudaFree(P->wsrc_w[q]);
+        sf_defer_free(P->wsrc_cells[q], 0);
+        sf_defer_free(P->wsrc_w[q], 0);
     }
-    cudaFree(P->pipe_ring);
-    cudaFree(P->pipe_ctrl);
-    cudaFree(P->pipe_err);
-    cudaFree(P->pipe_order);
+    sf_defer_free(P->pipe_ring, P->pipe_ring_floats * sizeof(float));
+    sf_defer_free(P->pipe_ctrl, 0);
+    sf_defer_free(P->pipe_err, 0);
+    sf_defer_free(P->pipe_order, 0);
     delete P;
     return 0;
 }
@@ -1065,8 +1122,8 @@ int voxelize_impl(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz,
     if (nx < 1 || ny < 1 || nz < 1 || nx > 65535) return sf_fail("sf_voxelize: bad grid");
     const size_t prog_bytes = (sizeof(sf_sdf_node) * n_nodes + 15) / 16 * 16;
     const size_t coord_bytes = coords ? sizeof(double) * ((size_t)nx + ny + nz) : 0;
-    char* buf = nullptr;
-    SF_CUDA_OK(cudaMalloc(&buf, prog_bytes + 16 + coord_bytes));
+    char* buf = nullptr;  // stream-ordered: no device-wide wait on release
+    SF_CUDA_OK(cudaMallocAsync(reinterpret_cast<void**>(&buf), prog_bytes + 16 + coord_bytes, st));
     sf_sdf_node* prog = reinterpret_cast<sf_sdf_node*>(buf);
     int* err = reinterpret_cast<int*>(buf + prog_bytes);
     double* cdev = coords ? reinterpret_cast<double*>(buf + prog_bytes + 16) : nullptr;
@@ -1091,7 +1148,7 @@ int voxelize_impl(const sf_sdf_node* nodes, int n_nodes, int nx, int ny, int nz,
     if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess))
         rc = sf_fail("sf_voxelize: kernel failed");
-    cudaFree(buf);
+    cudaFreeAsync(buf, st);
     if (!rc && herr) rc = sf_fail("sf_voxelize: malformed SDF program (stack error)");
     return rc;
 }
@@ -1119,8 +1176,9 @@ int voxelize_materials_impl(const sf_sdf_node* nodes, const int32_t* prog_off, i
     const size_t off_bytes = (sizeof(int) * (n_regions + 2) + 15) / 16 * 16;
     const size_t ids_bytes = (size_t)(n_regions + 16) / 16 * 16;
     const size_t coord_bytes = coords ? sizeof(double) * ((size_t)nx + ny + nz) : 0;
-    char* buf = nullptr;
-    SF_CUDA_OK(cudaMalloc(&buf, prog_bytes + off_bytes + ids_bytes + 16 + coord_bytes));
+    char* buf = nullptr;  // stream-ordered: no device-wide wait on release
+    SF_CUDA_OK(cudaMallocAsync(reinterpret_cast<void**>(&buf),
+                               prog_bytes + off_bytes + ids_bytes + 16 + coord_bytes, st));
     sf_sdf_node* prog = reinterpret_cast<sf_sdf_node*>(buf);
     int* off = reinterpret_cast<int*>(buf + prog_bytes);
     uint8_t* idd = reinterpret_cast<uint8_t*>(buf + prog_bytes + off_bytes);
@@ -1152,7 +1210,7 @@ int voxelize_materials_impl(const sf_sdf_node* nodes, const int32_t* prog_off, i
     if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess))
         rc = sf_fail("sf_voxelize_materials: kernel failed");
-    cudaFree(buf);
+    cudaFreeAsync(buf, st);
     if (!rc && herr) rc = sf_fail("sf_voxelize_materials: malformed SDF program (stack error)");
     return rc;
 }
@@ -1190,7 +1248,7 @@ int sf_sdf_eval(const sf_sdf_node* nodes, int n_nodes, const double* points_dev,
     if (n == 0) return 0;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     sf_sdf_node* prog = nullptr;
-    SF_CUDA_OK(cudaMalloc(&prog, sizeof(sf_sdf_node) * n_nodes + 16));
+    SF_CUDA_OK(cudaMallocAsync(reinterpret_cast<void**>(&prog), sizeof(sf_sdf_node) * n_nodes + 16, st));
     int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(prog) + sizeof(sf_sdf_node) * n_nodes);
     int rc = 0, herr = 0;
     if (cudaMemcpyAsync(prog, nodes, sizeof(sf_sdf_node) * n_nodes, cudaMemcpyHostToDevice, st) !=
@@ -1201,7 +1259,7 @@ int sf_sdf_eval(const sf_sdf_node* nodes, int n_nodes, const double* points_dev,
     if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess))
         rc = sf_fail("sf_sdf_eval: kernel failed");
-    cudaFree(prog);
+    cudaFreeAsync(prog, st);
     if (!rc && herr) rc = sf_fail("sf_sdf_eval: malformed SDF program (stack error)");
     return rc;
 }

@@ -467,16 +467,15 @@ struct sf_batch {
 namespace {
 
 void free_device(sf_batch* B) {
-    if (B->graph_exec) cudaGraphExecDestroy(B->graph_exec);
-    if (B->graph) cudaGraphDestroy(B->graph);
+    sf_defer_graph(B->graph_exec, B->graph);  // released later, without a device-wide wait
     B->graph_exec = nullptr;
     B->graph = nullptr;
     B->graph_steps = 0;
-    cudaFree(B->d_grids);
-    cudaFree(B->d_tiles);
-    cudaFree(B->d_ade_ids);
-    cudaFree(B->d_queue);
-    cudaFree(B->d_step);
+    sf_defer_free(B->d_grids, 0);
+    sf_defer_free(B->d_tiles, 0);
+    sf_defer_free(B->d_ade_ids, 0);
+    sf_defer_free(B->d_queue, 0);
+    sf_defer_free(B->d_step, 0);
     B->d_grids = nullptr;
     B->d_tiles = nullptr;
     B->d_ade_ids = nullptr;

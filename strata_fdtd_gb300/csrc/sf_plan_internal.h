@@ -72,6 +72,11 @@ inline int auto_chunk(const sf_plan* P, int kspan, int jspan = 8) {
 }
 
 
+// Queue a device buffer (bytes: its size, for the release threshold) or a
+// graph for release without a device-wide wait (sf_api.cu).
+void sf_defer_free(void* p, size_t bytes);
+void sf_defer_graph(cudaGraphExec_t exec, cudaGraph_t graph);
+
 // Makes the plan's device current for the scope of a call.
 struct DeviceGuard {
     int prev = -1;

@@ -49,6 +49,8 @@ class Request:
     cancel_requested: bool = False
     cell_updates: int = 0
     cells: int = 0
+    last_group: int = -1      # index of the group that enqueued its last steps
+    collect: Any = None       # pipelined executors: waits for and returns the result
 
     @property
     def latency(self) -> float | None:
@@ -182,6 +184,8 @@ class SolveServer:
         def now():
             return self.clock() - t0
 
+        if getattr(self.ex, "pipelined", False):
+            return self._run_pipelined(now, realtime)
         while self.queue or self.active:
             self._admit(now() if realtime else float("inf"))
             if not self.active:
@@ -205,6 +209,90 @@ class SolveServer:
             self.groups += 1
             self._retire(now())
         return self.stats()
+
+    def _run_pipelined(self, now, realtime: bool) -> dict:
+        """The same loop with one group in flight: group g+1 is built and
+        queued while the device runs group g, and group g's solves are
+        retired once it has completed (its finished solves' results were
+        queued for copy-out right behind it).  Solves whose steps are all
+        queued stop counting against the cell cap at once and free their
+        memory budget when they retire; a non-finite pressure is caught one
+        group later."""
+        pending = None  # (token, members, group index) of the group in flight
+        self._release_later = []
+        while self.queue or self.active or pending is not None:
+            self._admit(now() if realtime else float("inf"))
+            group = None
+            if self.active:
+                members = list(self.active)
+                counts = [min(self.step_group, r.remaining) for r in members]
+                self.ex.advance([r.handle for r in members], counts)
+                gi = self.groups
+                self.groups += 1
+                still = []
+                for r, n in zip(members, counts):
+                    r.remaining -= n
+                    r.cell_updates += n * self.ex.cells(r.handle)
+                    r.last_group = gi
+                    if r.remaining > 0 and not r.cancel_requested:
+                        still.append(r)
+                        continue
+                    self.active_cells -= r.cells
+                    if r.remaining <= 0:  # its result follows the group on the stream
+                        r.collect = self.ex.collect(r.handle)
+                self.active = still
+                group = (self.ex.mark(), members, gi)
+                if realtime:  # arrivals are set up while the device works
+                    self._admit(now())
+            elif pending is None:
+                if not self.queue:
+                    break
+                wait = min(r.arrival for r in self.queue) - now()
+                if realtime and wait > 0:
+                    time.sleep(min(wait, 0.01))
+                continue
+            if pending is not None:
+                self.ex.wait_for(pending[0])
+                done_gi = pending[2]
+                keep = []
+                for last, h in self._release_later:
+                    if last <= done_gi:
+                        self.ex.release(h)
+                    else:
+                        keep.append((last, h))
+                self._release_later = keep
+                self._retire_group(pending[1], pending[2], now())
+            pending = group
+        return self.stats()
+
+    def _retire_group(self, members, gi: int, now: float) -> None:
+        """Retire the members of completed group gi that are finished (their
+        last steps were in it), failed or cancelled."""
+        for r in members:
+            if r.status != "running":
+                continue
+            bad = self.ex.failed(r.handle)
+            if not bad and not r.cancel_requested and not (r.remaining <= 0 and r.last_group == gi):
+                continue
+            if bad:
+                r.status, r.error = "failed", bad
+            elif r.cancel_requested and r.remaining > 0:
+                r.status = "cancelled"
+            else:
+                r.status = "done"
+                r.result = r.collect() if r.collect is not None else self.ex.finish(r.handle)
+            if r in self.active:  # stopped early (failed or cancelled while still stepping)
+                self.active.remove(r)
+                self.active_cells -= r.cells
+            r.collect = None
+            if r.last_group > gi:  # a group still in flight uses it: release after that
+                self._release_later.append((r.last_group, r.handle))
+            else:
+                self.ex.release(r.handle)
+            r.handle = None
+            r.t_done = now
+            self.in_use -= r.nbytes
+            self.finished.append(r)
 
     def stats(self) -> dict:
         done = [r for r in self.finished if r.status == "done"]
@@ -235,7 +323,8 @@ class GPUExecutor:
     through the single-grid column kernels instead (same results, a faster
     kernel for one large grid); None batches everything."""
 
-    def __init__(self, graph_steps: int = 0, solo_cells: int | None = 1 << 24):
+    def __init__(self, graph_steps: int = 50, solo_cells: int | None = 1 << 24,
+                 batch_min_cells: int = 0):
         import torch
 
         from .batch import BatchedSolver
@@ -244,20 +333,44 @@ class GPUExecutor:
         self.Batched = BatchedSolver
         self.graph_steps = graph_steps
         self.solo_cells = solo_cells
+        # a group whose batchable solves hold fewer cells than this steps them
+        # one by one through the single-grid path instead (the tail of a
+        # stream, when a few small solves are left)
+        self.batch_min_cells = int(batch_min_cells)
         self.host_advance_s = 0.0  # host time spent enqueueing groups
         self.host_wait_s = 0.0     # host time blocked on the device
+        # groups run on a stream of their own: the library's synchronous
+        # set-up copies (legacy default stream) then never wait for them
         self.side = torch.cuda.Stream()
-        self.main = torch.cuda.current_stream()
+        self.main = torch.cuda.Stream()
         self._pending = None
         self._new: list = []
+        self._groups: list = []  # groups queued and not yet waited for
+        self.host_s: dict = {}   # host time by part of a group's set-up
+
+    host_build_s = 0.0  # host time constructing admitted solves
 
     def start(self, req):
+        t0 = time.perf_counter()
         with self.torch.cuda.stream(self.side):
             s = req.build()
+            # the rest of the set-up a run would do first (device tables, ADE
+            # fields, the padded twin for odd nz) happens here, on the side
+            # stream: its blocking host-to-device copies then wait for this
+            # stream only, not for the group running on the main one
+            s._sync_tables()
+            s._upload_exposed()
+            if self.solo_cells is None or int(np.prod(s.shape)) < self.solo_cells:
+                s._padded_twin(False)
+        self.host_build_s += time.perf_counter() - t0
         self._new.append(s)
         return {"solver": s, "bad": None}
 
     def advance(self, handles, counts):
+        with self.torch.cuda.stream(self.main):
+            self._advance(handles, counts)
+
+    def _advance(self, handles, counts):
         t0 = time.perf_counter()
         if self._new:
             self.main.wait_stream(self.side)
@@ -270,16 +383,75 @@ class GPUExecutor:
             else:
                 batch.append(s)
                 steps.append(n)
+        self._tick("solo", t0)
+        t1 = time.perf_counter()
         b = None
+        if batch and sum(int(np.prod(s.shape)) for s in batch) < self.batch_min_cells:
+            for s, n in zip(batch, steps):
+                s.run_steps(n)
+            batch = []
         if batch:
             b = self.Batched(batch)
             b.run_steps(steps, graph_steps=self.graph_steps)
+            for k, v in b.host_s.items():
+                self.host_s["batch_" + k] = self.host_s.get("batch_" + k, 0.0) + v
+        self._tick("batch", t1)
         self._pending = (b, handles)
+        t2 = time.perf_counter()
+        self._queue_checks(handles)
+        self._tick("checks", t2)
         self.host_advance_s += time.perf_counter() - t0
+
+    def _tick(self, part, t0):
+        self.host_s[part] = self.host_s.get(part, 0.0) + time.perf_counter() - t0
+
+    # -- one group in flight (SolveServer's pipelined loop) ------------------
+    pipelined = True
+
+    def _queue_checks(self, handles):
+        """Copy the last probe row of each solve's new trace to pinned host
+        memory behind the group, for the non-finite check."""
+        torch = self.torch
+        checks = []
+        for h in handles:
+            s = h["solver"]
+            if s is not None and s._pending_traces:
+                tr = s._pending_traces[-1][0]
+                row = torch.empty((1, tr.shape[1]), dtype=tr.dtype, pin_memory=True)
+                row.copy_(tr[-1:], non_blocking=True)
+                checks.append((h, row))
+        self._groups.append({"batch": self._pending[0], "checks": checks, "event": None})
+
+    def mark(self):
+        """A token for the group just queued: a CUDA event behind it."""
+        ev = self.torch.cuda.Event()
+        ev.record(self.main)
+        rec = self._groups[-1]
+        rec["event"] = ev
+        self._pending = None
+        return rec
+
+    def collect(self, h):
+        """Queue the copy-out of a finished solve's traces; returns the
+        function that waits for it and gives the result."""
+        t0 = time.perf_counter()
+        with self.torch.cuda.stream(self.main):
+            out = h["solver"].probe_data_async()
+        self._tick("collect", t0)
+        return out
+
+    def wait_for(self, rec):
+        t0 = time.perf_counter()
+        rec["event"].synchronize()
+        self.host_wait_s += time.perf_counter() - t0
+        for h, row in rec["checks"]:
+            if not np.all(np.isfinite(row.numpy())):
+                h["bad"] = "pressure became non-finite at a probe"
+        self._groups.remove(rec)
 
     def wait(self):
         t0 = time.perf_counter()
-        self.torch.cuda.current_stream().synchronize()
+        self.main.synchronize()
         self.host_wait_s += time.perf_counter() - t0
         if self._pending is not None:
             _, handles = self._pending
@@ -305,7 +477,7 @@ class GPUExecutor:
 class SequentialExecutor(GPUExecutor):
     """The baseline: one solve at a time through the single-grid path."""
 
-    def advance(self, handles, counts):
+    def _advance(self, handles, counts):
         t0 = time.perf_counter()
         if self._new:
             self.main.wait_stream(self.side)
@@ -313,4 +485,5 @@ class SequentialExecutor(GPUExecutor):
         for h, n in zip(handles, counts):
             h["solver"].run_steps(n)
         self._pending = (None, handles)
+        self._queue_checks(handles)
         self.host_advance_s += time.perf_counter() - t0

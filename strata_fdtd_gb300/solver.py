@@ -195,6 +195,9 @@ class FDTDSolver:
         self._host = {f: np.zeros(self.shape, dtype=np.float32) for f in _FIELDS}
         self._host_fresh = {f: True for f in _FIELDS}
         self._host_exposed = {f: False for f in _FIELDS}
+        # whether vz was ever handed out or set: until then its last plane
+        # (a face no step updates) is known to be zero without a device read
+        self._vz_seen = False
         self._geometry = np.ones(self.shape, dtype=bool)
         self._geometry_dev = None
         self._geometry_set = False
@@ -293,6 +296,7 @@ class FDTDSolver:
             self._torch.from_numpy(self._host[name]).copy_(src)
             self._host_fresh[name] = True
         self._host_exposed[name] = True
+        self._vz_seen = self._vz_seen or name == "vz"
         return self._host[name]
 
     def _set_field(self, name, value):
@@ -304,6 +308,7 @@ class FDTDSolver:
         self._host[name] = arr
         self._host_fresh[name] = True
         self._host_exposed[name] = True
+        self._vz_seen = self._vz_seen or name == "vz"
 
     p = property(lambda s: s._field("p"), lambda s, v: s._set_field("p", v))
     vx = property(lambda s: s._field("vx"), lambda s, v: s._set_field("vx", v))
@@ -312,6 +317,7 @@ class FDTDSolver:
 
     def device_fields(self) -> dict:
         """The current state as CUDA tensors (no copy); valid until the next step."""
+        self._vz_seen = True  # the caller may write vz through the tensor
         self._upload_exposed()
         cur = self._cur()
         return {f: self._dev[cur][q] for q, f in enumerate(_FIELDS)}
@@ -749,7 +755,8 @@ class FDTDSolver:
         if twin is None:
             from .batch import _PaddedTwin
 
-            twin = _PaddedTwin(self) if _PaddedTwin.eligible(self) else None
+            ok = not self._vz_seen or _PaddedTwin.eligible(self)
+            twin = _PaddedTwin(self) if ok else None
             self._pad_twin = twin
         return twin
 
@@ -1041,6 +1048,33 @@ class FDTDSolver:
         self._torch.cuda.synchronize(self._device)
 
     # ----------------------------------------------------------------- outputs
+    def probe_data_async(self):
+        """Start copying every probe trace still on the device to pinned host
+        memory, queued on the current stream after the steps so far, and
+        return a function that waits for those copies only (not for work
+        queued later on the stream) and returns get_probe_data()'s dict."""
+        torch = self._torch
+        copies = []
+        for trace, names in self._pending_traces:
+            host = torch.empty(trace.shape, dtype=trace.dtype, pin_memory=True)
+            host.copy_(trace, non_blocking=True)
+            copies.append((host, names))
+        self._pending_traces = []
+        done = torch.cuda.Event()
+        done.record()
+
+        def result() -> dict:
+            done.synchronize()
+            for host, names in copies:
+                arr = host.numpy()
+                for q, name in enumerate(names):
+                    if name in self._probes:
+                        self._probes[name]._samples.extend(arr[:, q].tolist())
+            copies.clear()
+            return {n: np.array(pr._samples, dtype=np.float32) for n, pr in self._probes.items()}
+
+        return result
+
     def get_probe_data(self, name: str | None = None) -> dict:
         self._flush_traces()
         if name is not None:

@@ -161,7 +161,13 @@ def served_stream(seed=0, n_requests=1000, rate=200.0, edges=(48, 320), steps=(5
     uniform in ``pml``, geometry drawn from free field / a sealed box / a
     block of 4-32 Helmholtz resonators (neck radius 3-8 cells, cavity 10-20
     cells), an optional 1-2 pole Debye region.  Returns a list of
-    server.Request whose ``build`` constructs the solver on admission."""
+    server.Request whose ``build`` constructs the solver on admission.
+
+    Every random parameter of a request is drawn here, including its Debye
+    material, which is redrawn until it passes the stability screen
+    (material_is_stable, on the GPU): the screen is the workload's rejection
+    rule, not part of serving, so it runs before the stream starts and
+    ``build`` only constructs."""
     from .resonator import HelmholtzResonator
     from .sdf import Union
     from .server import Request, solve_bytes
@@ -183,9 +189,28 @@ def served_stream(seed=0, n_requests=1000, rate=200.0, edges=(48, 320), steps=(5
             n_poles = int(rng.integers(1, 3))
         spec["n_poles"] = n_poles
         nbytes = solve_bytes(shape, geometry=kind != "free", debye_poles=n_poles)
+        # the request's own draws, in the order they are used
+        r = np.random.default_rng(spec["seed"])
+        inner_lo = [depth + 2 for _ in shape]
+        inner_hi = [n - depth - 2 for n in shape]
+        if kind == "helmholtz":
+            spec["nres"] = int(r.integers(4, 33))
+            spec["cav"] = int(r.integers(10, 21))
+            spec["neck_r"] = int(r.integers(3, 9))
+        if n_poles:
+            while True:
+                mat = random_debye_material(r)
+                mat._poles = mat._poles[:n_poles]
+                if not screen or material_is_stable(mat)[0]:
+                    break
+            spec["material"] = mat
+            half = [int(r.integers(3, 9)) for _ in shape]
+            spec["box"] = [(c - h, c + h) for c, h in zip(
+                [int(r.integers(lo + h, max(lo + h + 1, hi - h)))
+                 for lo, hi, h in zip(inner_lo, inner_hi, half)], half)]
+        spec["frequency"] = float(r.uniform(1000, 4000))
 
         def build(spec=spec, res=res):
-            r = np.random.default_rng(spec["seed"])
             shp, d = spec["shape"], spec["depth"]
             s = FDTDSolver(grid=UniformGrid(shp, res), c=C_AIR, rho=RHO_AIR, courant=0.5)
             s.add_boundary(PML(depth=d))
@@ -202,9 +227,7 @@ def served_stream(seed=0, n_requests=1000, rate=200.0, edges=(48, 320), steps=(5
             elif spec["kind"] == "helmholtz":
                 # a block of resonators on the low-x side, necks opening to +x
                 span = [hi - lo for lo, hi in zip(inner_lo, inner_hi)]
-                nres = int(r.integers(4, 33))
-                cav = int(r.integers(10, 21))
-                neck_r = int(r.integers(3, 9))
+                nres, cav, neck_r = spec["nres"], spec["cav"], spec["neck_r"]
                 per = max(1, int(np.ceil(np.sqrt(nres))))
                 bx = inner_lo[0] + cav + 6
                 res_list = []
@@ -221,23 +244,15 @@ def served_stream(seed=0, n_requests=1000, rate=200.0, edges=(48, 320), steps=(5
                 s.set_geometry_sdf(Difference(block, Union(*res_list)))
                 src = (min(inner_hi[0] - 1, bx + 4), src[1], src[2])
             if spec["n_poles"]:
-                while True:
-                    mat = random_debye_material(r)
-                    mat._poles = mat._poles[: spec["n_poles"]]
-                    if not screen or material_is_stable(mat)[0]:
-                        break
-                mid = s.register_material(mat)
-                half = [int(r.integers(3, 9)) for _ in shp]
-                cen = [int(r.integers(lo + h, max(lo + h + 1, hi - h)))
-                       for lo, hi, h in zip(inner_lo, inner_hi, half)]
-                s.set_material_box(mid, *[(c - h, c + h) for c, h in zip(cen, half)])
+                mid = s.register_material(spec["material"])
+                s.set_material_box(mid, *spec["box"])
             geom = s.geometry
             if not geom[src]:
                 air = np.argwhere(geom[inner_lo[0]:inner_hi[0], inner_lo[1]:inner_hi[1],
                                        inner_lo[2]:inner_hi[2]])
                 if len(air):
                     src = tuple(int(v) + lo for v, lo in zip(air[len(air) // 2], inner_lo))
-            s.add_source(GaussianPulse(position=src, frequency=float(r.uniform(1000, 4000))))
+            s.add_source(GaussianPulse(position=src, frequency=spec["frequency"]))
             s.add_probe("near", src)
             s.add_probe("far", tuple(hi - 1 for hi in inner_hi))
             s.precompute_sources(spec["steps"])

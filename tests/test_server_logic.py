@@ -127,3 +127,61 @@ def test_cell_cap_admits_in_order_and_lets_an_oversized_solve_run_alone():
     assert not any(3 in g and len(g) > 1 for g in ex.groups)
     assert ex.groups[-1] == [4, 5]            # admitted together after it
     assert srv.active_cells == 0
+
+
+class FakePipelinedExecutor(FakeExecutor):
+    """The pipelined interface: groups are queued (advance + mark), their
+    effects become visible only when waited for (wait_for), and a finished
+    solve's result is collected from a copy queued behind its last group."""
+
+    pipelined = True
+
+    def __init__(self, clock, **kw):
+        super().__init__(clock, **kw)
+        self.queued = []      # group records not yet waited for
+        self.completed = set()
+        self.max_in_flight = 0
+
+    def advance(self, handles, counts):
+        super().advance(handles, counts)
+        self.queued.append(len(self.groups) - 1)
+        self.max_in_flight = max(self.max_in_flight, len(self.queued))
+
+    def mark(self):
+        return self.queued[-1]
+
+    def wait_for(self, token):
+        assert token == self.queued[0], "groups complete in queue order"
+        self.queued.pop(0)
+        self.completed.add(token)
+
+    def collect(self, h):
+        rid, steps, group = h["rid"], self.done_steps[h["rid"]], len(self.groups) - 1
+
+        def result():
+            assert group in self.completed, "result read before its group completed"
+            return {"steps": steps}
+
+        return result
+
+
+def test_pipelined_loop_keeps_one_group_in_flight_and_retires_after_completion():
+    clock = FakeClock()
+    ex = FakePipelinedExecutor(clock, nan_after={4: 30})
+    srv = SolveServer(ex, hbm_budget=30, step_group=10, clock=clock)
+    for q in range(6):
+        srv.submit(_req(q, 25 + 5 * q, nbytes=10))
+    assert srv.cancel(5)
+    stats = srv.run(realtime=False)
+    assert ex.max_in_flight == 2 and not ex.queued
+    assert stats["peak_hbm_bytes"] <= 30
+    by = {r.rid: r for r in srv.finished}
+    for q in (0, 1, 2, 3):
+        assert by[q].status == "done" and by[q].result == {"steps": 25 + 5 * q}, by[q]
+    assert by[4].status == "failed" and "non-finite" in by[4].error
+    assert by[5].status == "cancelled"
+    assert srv.in_use == 0 and srv.active_cells == 0 and not srv.active
+    # FIFO admission: request 3 joins only after one of the first three left
+    first_with_3 = next(i for i, g in enumerate(ex.groups) if 3 in g)
+    assert all(3 not in g for g in ex.groups[:first_with_3])
+    assert all(len(g) <= 3 for g in ex.groups)
