@@ -369,9 +369,17 @@ int sf_batch_run(sf_batch* batch, int64_t n_steps, int graph_steps, void* stream
  * density is a scalar, core/solver.py:1584-1586): per-cell density
  * rho = rho0 (1 + theta) with face coefficients
  * cv = -(dt/dx) (1/rho_lo + 1/rho_hi) / 2, K = rho0 c^2 fixed, PML decays and
- * a point source as the reference, no solids.  dtype 0 = float32, 1 =
- * float64 for every array below.  decay[3]: device arrays of nx, ny, nz
- * (1 where an axis has no PML).  src_cell < 0: no source. */
+ * a point source as the reference.  Rigid walls come from an optional air
+ * mask (geometry: device, nx*ny*nz bytes, nonzero = air, as the reference's
+ * set_geometry, core/solver.py:1682): a face that touches a solid cell has
+ * cv = 0, so its velocity stays zero and a solid cell's pressure stays zero,
+ * which is the reference's rigid pass (boundaries.cpp:66-89, p = 0 in
+ * solids, fdtd_step.cpp:84-212) for a solve started from rest; such faces
+ * carry no gradient.  The caller passes src_cell < 0 when the source cell is
+ * solid (the reference injects into air cells only).  dtype 0 = float32,
+ * 1 = float64, 2 = double-word float32 for every array below.  decay[3]:
+ * device arrays of nx, ny, nz (1 where an axis has no PML).  src_cell < 0:
+ * no source. */
 typedef struct {
     int32_t nx, ny, nz, dtype;
     double cp;         /* -K dt / dx */
@@ -381,6 +389,7 @@ typedef struct {
     int64_t src_cell;
     int32_t n_probe, reserved;
     const int64_t* probe_cells; /* device */
+    const uint8_t* geometry;    /* device air mask, or NULL: no solids */
 } sf_diff_desc;
 /* cv arrays (3 x N) from theta (N). */
 int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, void* cvy, void* cvz,

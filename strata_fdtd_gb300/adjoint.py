@@ -31,7 +31,8 @@ class _Desc(ctypes.Structure):
                 ("dtype", ctypes.c_int32), ("cp", ctypes.c_double), ("dt_over_dx", ctypes.c_double),
                 ("rho0", ctypes.c_double), ("decay", ctypes.c_void_p * 3),
                 ("src_cell", ctypes.c_int64), ("n_probe", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("probe_cells", ctypes.c_void_p)]
+                ("reserved", ctypes.c_int32), ("probe_cells", ctypes.c_void_p),
+                ("geometry", ctypes.c_void_p)]
 
 
 def _ptrs(ts):
@@ -49,10 +50,19 @@ class DifferentiableSolver:
     at a small fraction of its FP32 rate) --, torch.float64, or
     torch.float32 (fastest, about 1e-3 worst-cell relative gradient error
     after 2000 steps).  Design fields, traces and gradients are float64 for
-    "dw" and the working dtype otherwise."""
+    "dw" and the working dtype otherwise.
+
+    ``geometry`` (optional, grid shape, True = air, as the reference's
+    ``set_geometry``) adds rigid walls: every face that touches a solid cell
+    keeps zero velocity and solid cells zero pressure, the reference's rigid
+    boundary for a solve started from rest.  The gradient is then taken with
+    respect to theta in the air cells (zero in solid ones, whose density
+    never enters the solve); a source in a solid cell injects nothing, as in
+    the reference."""
 
     def __init__(self, shape, resolution=1e-3, c=343.0, rho0=1.204, courant=0.5, pml_depth=10,
-                 source=None, frequency=1500.0, probes=(), dtype="dw", checkpoint_every=100):
+                 source=None, frequency=1500.0, probes=(), dtype="dw", checkpoint_every=100,
+                 geometry=None):
         import torch
 
         self.torch = torch
@@ -75,7 +85,8 @@ class DifferentiableSolver:
         self.K = int(checkpoint_every)
         dev = torch.device("cuda")
         self.dev = dev
-        # PML decays exp(-sigma dt) in the working precision
+        # PML decays exp(-sigma dt) in the working precision, from the
+        # reference's sigma profile evaluated in double
         pml = PML(depth=pml_depth)
 
         class _S:
@@ -85,14 +96,22 @@ class DifferentiableSolver:
         stub.shape, stub.c, stub.grid = self.shape, c, self.grid
         pml.initialize(stub)
         self.decay = []
-        for sig in pml.sigmas:
-            d = np.exp(-sig.astype(np.float64) * self.dt)
+        for n in self.shape:
+            d = np.exp(-pml._create_profile(n, np.float64) * self.dt)
             self.decay.append(self._working(d))
         self.source = tuple(source) if source is not None else tuple(n // 2 for n in self.shape)
         self.pulse = GaussianPulse(position=self.source, frequency=frequency)
         self.probe_pos = [tuple(p) for p in probes]
         cells = [int(np.ravel_multi_index(p, self.shape)) for p in self.probe_pos]
         self.probe_cells = torch.tensor(cells or [0], dtype=torch.int64, device=dev)
+        self.geometry = None
+        self._air = None
+        if geometry is not None:
+            g = np.asarray(geometry, dtype=bool)
+            if g.shape != self.shape:
+                raise ValueError(f"geometry shape {g.shape} does not match the grid {self.shape}")
+            self.geometry = g
+            self._air = torch.from_numpy(g.astype(np.uint8)).to(dev)
         self.lib = _native.load()
 
     def _working(self, values):
@@ -117,8 +136,11 @@ class DifferentiableSolver:
         for a in range(3):
             d.decay[a] = self.decay[a].data_ptr()
         d.src_cell = int(np.ravel_multi_index(self.source, self.shape))
+        if self.geometry is not None and not self.geometry[self.source]:
+            d.src_cell = -1  # the reference injects into air cells only
         d.n_probe = len(self.probe_pos)
         d.probe_cells = self.probe_cells.data_ptr()
+        d.geometry = self._air.data_ptr() if self._air is not None else None
         return d
 
     def source_values(self, n_steps):
@@ -263,6 +285,13 @@ def reference_loss_torch(solver: DifferentiableSolver, theta, target, n_steps):
     cvx = -dt_dx * 0.5 * (b[:-1] + b[1:])
     cvy = -dt_dx * 0.5 * (b[:, :-1] + b[:, 1:])
     cvz = -dt_dx * 0.5 * (b[:, :, :-1] + b[:, :, 1:])
+    inject = True
+    if solver.geometry is not None:
+        air = torch.as_tensor(solver.geometry, device=theta.device).to(theta.dtype)
+        cvx = cvx * (air[:-1] * air[1:])
+        cvy = cvy * (air[:, :-1] * air[:, 1:])
+        cvz = cvz * (air[:, :, :-1] * air[:, :, 1:])
+        inject = bool(solver.geometry[solver.source])
     dx, dy, dz = solver.decay
     p = torch.zeros_like(theta)
     vx, vy, vz = torch.zeros_like(theta), torch.zeros_like(theta), torch.zeros_like(theta)
@@ -282,7 +311,7 @@ def reference_loss_torch(solver: DifferentiableSolver, theta, target, n_steps):
         vz = vz * dz[None, None, :]
         p = p * dx[:, None, None] * dy[None, :, None] * dz[None, None, :]
         onehot = torch.zeros_like(p)
-        onehot[si, sj, sk] = 1.0
+        onehot[si, sj, sk] = 1.0 if inject else 0.0
         p = p + src[n] * onehot
         traces.append(torch.stack([p[q] for q in solver.probe_pos]))
     trace = torch.stack(traces)

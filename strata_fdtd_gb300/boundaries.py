@@ -93,9 +93,10 @@ class PML:
             sigma[i] = self._max_sigma * (nd ** self.order)
         return sigma
 
-    def _create_profile(self, n: int) -> np.ndarray:
-        """_boundaries.py:228-255: sigma_max * dist**order, float32."""
-        sigma = np.zeros(n, dtype=np.float32)
+    def _create_profile(self, n: int, dtype=np.float32) -> np.ndarray:
+        """_boundaries.py:228-255: sigma_max * dist**order, float32 (float64
+        for the differentiable solve's double and double-word forms)."""
+        sigma = np.zeros(n, dtype=dtype)
         d = self.depth
         for i in range(d):
             dist = (d - i) / d

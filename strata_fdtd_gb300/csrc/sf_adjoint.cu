@@ -5,9 +5,14 @@
 // per-cell density rho = rho0 * (1 + theta) in place of the scalar rho of
 // core/solver.py:1584-1586: every face velocity uses its own coefficient
 //     cv_face = -(dt/dx) * (1/rho_lo + 1/rho_hi) / 2
-// while the pressure coefficient cp = -K dt/dx keeps K = rho0 c^2.  No solids;
-// PML decays and the point source as the reference (pml.cpp:47-149,
-// core/solver.py:2413-2421); probe samples after each step.  The per-cell
+// while the pressure coefficient cp = -K dt/dx keeps K = rho0 c^2.  Rigid
+// walls (an optional air mask) set cv = 0 on every face that touches a solid
+// cell: from rest such a face's velocity and a solid cell's pressure stay
+// zero, as the reference's rigid pass and its p = 0 in solids
+// (boundaries.cpp:66-89, fdtd_step.cpp:84-212) keep them, and the forward and
+// adjoint kernels need no mask of their own.  PML decays and the point source
+// as the reference (pml.cpp:47-149, core/solver.py:2413-2421); probe samples
+// after each step.  The per-cell
 // density is a builder-defined design field: the reference has only a scalar
 // rho.
 //
@@ -139,12 +144,14 @@ struct GradAcc<dwf> {
 constexpr int kFusedProbes = 4;
 
 // Coefficients from theta: cv_a(c) for the face between c and c + e_a
-// (zero on the last plane of each axis, which carries no face update).
+// (zero on the last plane of each axis, which carries no face update, and on
+// faces that touch a solid cell of the air mask `air`, when given).
 // (formed in the external type: in double for a double-word solve, then
 // rounded to the nearest double-word)
 template <typename T, typename E = typename Ext<T>::E>
-__global__ void k_dcoef(const E* __restrict__ theta, T* __restrict__ cvx, T* __restrict__ cvy,
-                        T* __restrict__ cvz, int nx, int ny, int nz, E dt_dx, E rho0) {
+__global__ void k_dcoef(const E* __restrict__ theta, const uint8_t* __restrict__ air,
+                        T* __restrict__ cvx, T* __restrict__ cvy, T* __restrict__ cvz, int nx,
+                        int ny, int nz, E dt_dx, E rho0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -152,7 +159,9 @@ __global__ void k_dcoef(const E* __restrict__ theta, T* __restrict__ cvx, T* __r
     const long long plane = (long long)ny * nz;
     const long long c = (long long)i * plane + (long long)j * nz + k;
     const E b0 = E(1) / (rho0 * (E(1) + theta[c]));
+    const bool solid = air && !air[c];
     auto face = [&](long long n) {
+        if (solid || (air && !air[n])) return T(0);
         const E b1 = E(1) / (rho0 * (E(1) + theta[n]));
         return Ext<T>::in(-dt_dx * E(0.5) * (b0 + b1));
     };
@@ -276,11 +285,14 @@ __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restr
     if (k < nz - 1) GradAcc<T>::add(gz, c, vz_hi, pst[c + 1] - p0);
 }
 
-// dL/dtheta(c) = (dt/dx) rho0 / (2 rho(c)^2) * sum of dL/dcv over its faces.
+// dL/dtheta(c) = (dt/dx) rho0 / (2 rho(c)^2) * sum of dL/dcv over its faces;
+// a wall face's cv is zero whatever theta is, so it contributes nothing, and a
+// solid cell's gradient is zero.
 template <typename T, typename E = typename Ext<T>::E>
-__global__ void k_dgrad(const E* __restrict__ theta, const double* __restrict__ gx,
-                        const double* __restrict__ gy, const double* __restrict__ gz,
-                        E* __restrict__ out, int nx, int ny, int nz, double dt_dx, double rho0) {
+__global__ void k_dgrad(const E* __restrict__ theta, const uint8_t* __restrict__ air,
+                        const double* __restrict__ gx, const double* __restrict__ gy,
+                        const double* __restrict__ gz, E* __restrict__ out, int nx, int ny,
+                        int nz, double dt_dx, double rho0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -288,10 +300,19 @@ __global__ void k_dgrad(const E* __restrict__ theta, const double* __restrict__ 
     const long long plane = (long long)ny * nz;
     const long long c = (long long)i * plane + (long long)j * nz + k;
     using A = GradAcc<T>;
-    double s = A::load(gx, c) + A::load(gy, c) + A::load(gz, c);  // high faces (zero on the last plane)
-    if (i > 0) s += A::load(gx, c - plane);
-    if (j > 0) s += A::load(gy, c - nz);
-    if (k > 0) s += A::load(gz, c - 1);
+    if (air && !air[c]) {
+        out[c] = E(0);
+        return;
+    }
+    auto open = [&](long long n) { return !air || air[n]; };
+    // high faces (zero on the last plane), then the low ones
+    double s = 0.0;
+    if (i < nx - 1 && open(c + plane)) s += A::load(gx, c);
+    if (j < ny - 1 && open(c + nz)) s += A::load(gy, c);
+    if (k < nz - 1 && open(c + 1)) s += A::load(gz, c);
+    if (i > 0 && open(c - plane)) s += A::load(gx, c - plane);
+    if (j > 0 && open(c - nz)) s += A::load(gy, c - nz);
+    if (k > 0 && open(c - 1)) s += A::load(gz, c - 1);
     const double rho = rho0 * (1.0 + double(theta[c]));
     out[c] = E(s * dt_dx * rho0 / (2.0 * rho * rho));
 }
@@ -394,16 +415,16 @@ int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, vo
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (d->dtype == 1)
         k_dcoef<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, (double*)cvx, (double*)cvy, (double*)cvz, d->nx, d->ny, d->nz,
-            d->dt_over_dx, d->rho0);
+            (const double*)theta, d->geometry, (double*)cvx, (double*)cvy, (double*)cvz, d->nx,
+            d->ny, d->nz, d->dt_over_dx, d->rho0);
     else if (d->dtype == 2)
         k_dcoef<dwf><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, (dwf*)cvx, (dwf*)cvy, (dwf*)cvz, d->nx, d->ny, d->nz,
-            d->dt_over_dx, d->rho0);
+            (const double*)theta, d->geometry, (dwf*)cvx, (dwf*)cvy, (dwf*)cvz, d->nx, d->ny,
+            d->nz, d->dt_over_dx, d->rho0);
     else
         k_dcoef<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const float*)theta, (float*)cvx, (float*)cvy, (float*)cvz, d->nx, d->ny, d->nz,
-            (float)d->dt_over_dx, (float)d->rho0);
+            (const float*)theta, d->geometry, (float*)cvx, (float*)cvy, (float*)cvz, d->nx,
+            d->ny, d->nz, (float)d->dt_over_dx, (float)d->rho0);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_coefficients: launch failed");
 }
 
@@ -444,15 +465,15 @@ int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* gr
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (d->dtype == 1)
         k_dgrad<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, (const double*)grad_cv[0], (const double*)grad_cv[1],
+            (const double*)theta, d->geometry, (const double*)grad_cv[0], (const double*)grad_cv[1],
             (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     else if (d->dtype == 2)
         k_dgrad<dwf><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, (const double*)grad_cv[0], (const double*)grad_cv[1],
+            (const double*)theta, d->geometry, (const double*)grad_cv[0], (const double*)grad_cv[1],
             (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     else
         k_dgrad<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const float*)theta, (const double*)grad_cv[0], (const double*)grad_cv[1],
+            (const float*)theta, d->geometry, (const double*)grad_cv[0], (const double*)grad_cv[1],
             (const double*)grad_cv[2], (float*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_grad_theta: launch failed");
 }

@@ -160,3 +160,110 @@ def test_probe_gather_paths_and_many_probe_gradients():
           f"dw {err_dw:.3e}")
     assert err < 1e-4, err
     assert err_dw < 1e-9, err_dw
+
+
+def _walled_geometry(shape=(20, 18, 22)):
+    """A rigid slab across x = 10-11 with a 4x4 aperture, and a solid block
+    beside the source: faces on every axis touch a solid cell."""
+    g = np.ones(shape, dtype=bool)
+    g[10:12] = False
+    g[10:12, 7:11, 9:13] = True
+    g[4:7, 12:15, 5:9] = False
+    return g
+
+
+def _walled(dtype, geometry, K=25, source=(5, 9, 11)):
+    return DifferentiableSolver(geometry.shape, pml_depth=3, frequency=20000.0, source=source,
+                                probes=[(15, 9, 11), (14, 4, 16)], dtype=dtype,
+                                checkpoint_every=K, geometry=geometry)
+
+
+@pytest.mark.parametrize("walls", [False, True])
+def test_forward_matches_oracle_fp64(walls):
+    """The differentiable forward at theta = 0 is the reference scheme with a
+    scalar density: its FP64 probe traces against the oracle's FP64 build of
+    the same solve (the oracle's samples as doubles, before get_probe_data
+    rounds them to float32 as the reference stores them) (same PML, pulse, probes and, with
+    walls, the same air mask through the reference's rigid pass and p = 0 in
+    solids), rel-L2 1e-12 (the face coefficient is formed as
+    (dt/dx)(1/rho + 1/rho)/2 instead of dt/(rho dx): rounding-level
+    differences in FP64)."""
+    from oracle import oracle as O
+
+    g = _walled_geometry()
+    s = DifferentiableSolver(g.shape, pml_depth=3, frequency=20000.0, source=(5, 9, 11),
+                             probes=[(15, 9, 11), (14, 4, 16)], dtype=torch.float64,
+                             checkpoint_every=25, geometry=g if walls else None)
+    n = 150
+    trace = s.forward(torch.zeros(g.shape, dtype=torch.float64, device="cuda"), n,
+                      keep_checkpoints=False)[0].cpu().numpy()
+    o = O.FDTDSolver(shape=g.shape, resolution=1e-3, c=343.0, rho=1.204, courant=0.5,
+                     precision="f64")
+    o.add_boundary(O.PML(depth=3))
+    if walls:
+        o.set_geometry(g)
+    o.add_source(O.GaussianPulse(position=(5, 9, 11), frequency=20000.0))
+    o.add_probe("a", (15, 9, 11))
+    o.add_probe("b", (14, 4, 16))
+    o.run_steps(n)
+    for q, name in enumerate("ab"):
+        r = np.asarray(o._probes[name].data, dtype=np.float64)
+        assert np.abs(r).max() > 0
+        err = np.linalg.norm(trace[:, q] - r) / np.linalg.norm(r)
+        assert err < 1e-12, (name, err)
+
+
+@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-9), ("dw", 1e-8)])
+def test_walled_adjoint_matches_autograd(dtype, rtol):
+    """With rigid walls the adjoint matches autograd through the plain
+    PyTorch stepping (wall faces' coefficients held at zero), and the
+    gradient is zero in every solid cell."""
+    g = _walled_geometry()
+    s = _walled(dtype, g)
+    theta = torch.tensor(design_field(g.shape, region=10, seed=6, sigma=1.5), device="cuda")
+    target = s.forward(torch.tensor(design_field(g.shape, region=10, seed=7, sigma=1.5),
+                                    device="cuda"), 80)[0]
+    th = theta.clone().requires_grad_(True)
+    loss = s.loss(th, target, 80)
+    loss.backward()
+    ref_th = theta.clone().requires_grad_(True)
+    ref = reference_loss_torch(_walled(torch.float64, g), ref_th, target, 80)
+    ref.backward()
+    assert float(loss) == pytest.approx(float(ref), rel=rtol * 1e-3)
+    gr, r = th.grad.cpu().numpy(), ref_th.grad.cpu().numpy()
+    assert np.abs(r).max() > 0
+    np.testing.assert_allclose(gr, r, rtol=rtol, atol=rtol * 1e-3 * np.abs(r).max())
+    assert not np.any(gr[~g]), "gradient in a solid cell"
+    # cells next to a wall carry gradient through their open faces
+    assert np.abs(gr[9, 7:11, 9:13]).max() > 0
+
+
+def test_walled_adjoint_matches_central_differences():
+    """FP64 and double-word adjoints with walls against FP64 central
+    differences (h = 1e-3) on cells beside the walls, rel 1e-5."""
+    g = _walled_geometry()
+    cells = [(9, 8, 10), (12, 9, 11), (7, 13, 7), (4, 11, 6), (9, 3, 4), (13, 10, 12)]
+    theta = torch.tensor(design_field(g.shape, region=10, seed=8, sigma=1.5), device="cuda")
+    base = _walled(torch.float64, g, K=16)
+    target = base.forward(torch.zeros_like(theta), 70)[0] * 0.5
+    h = 1e-3
+    fd = {}
+    for c in cells:
+        assert g[c]
+        tp, tm = theta.clone(), theta.clone()
+        tp[c] += h
+        tm[c] -= h
+        fd[c] = (float(base.loss(tp, target, 70)) - float(base.loss(tm, target, 70))) / (2 * h)
+    for dtype in (torch.float64, "dw"):
+        s = _walled(dtype, g, K=16)
+        th = theta.clone().requires_grad_(True)
+        s.loss(th, target, 70).backward()
+        for c in cells:
+            assert float(th.grad[c]) == pytest.approx(fd[c], rel=1e-5, abs=1e-14), (dtype, c)
+
+
+def test_source_in_a_solid_cell_injects_nothing():
+    g = _walled_geometry()
+    s = _walled(torch.float64, g, source=(10, 2, 2))
+    tr = s.forward(torch.zeros(g.shape, dtype=torch.float64, device="cuda"), 40)[0]
+    assert float(tr.abs().max()) == 0.0
