@@ -224,6 +224,13 @@ def time_oracle(o, seconds):
     return CELLS * n / dt / 1e9, n, O.threads()
 
 
+def workload_config(world):
+    """The ``config`` object of both arms' lines: the workload and how it is
+    spread over the ranks (one full replica per rank)."""
+    return {"workload": WORKLOAD, "global_batch": world, "parallelism": f"replicas x{world}",
+            "l2": "state 1.1 GB per replica > 129 MB L2, no flush"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -245,7 +252,8 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "bench_step": f"{inner} FDTD steps on the CPU"},
+        "config": workload_config(args.gpus),
+        "bench_step": f"{inner} FDTD steps on the CPU (rank 0)",
         "cpu_baseline": {"value": v, "unit": METRIC, "cores": O.threads(), "kind": "port",
                          "sample": f"{inner * args.steps} FDTD steps of the 400^3 enclosure "
                                    "workload (oracle/sf_oracle.c, bit-exact restatement of the "
@@ -374,11 +382,11 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD if n_edge == 400 else f"enclosure at {n_edge}^3",
-                       "bench_step": f"{inner} FDTD time steps", "kernel": chosen,
-                       "i_chunk": args.ichunk, "autotune_ms_per_step": tune,
-                       "global_batch": world, "parallelism": f"replicas x{world}",
-                       "l2": "state 1.1 GB per replica > 129 MB L2, no flush"},
+            "config": (workload_config(world) if n_edge == 400 else
+                       {"workload": f"enclosure at {n_edge}^3", "global_batch": world,
+                        "parallelism": f"replicas x{world}"}),
+            "bench_step": f"{inner} FDTD time steps",
+            "kernel": {"name": chosen, "i_chunk": args.ichunk, "autotune_ms_per_step": tune},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "bytes_per_cell": BYTES_PER_CELL,
