@@ -463,7 +463,8 @@ def extras(args):
         "sequential_value": b["sequential"]["value"],
         "speedup_vs_sequential": b["speedup_vs_sequential"],
         "traces_identical": b["traces_identical"], "plain_kernel": b["config"]["plain_kernel"],
-        "rejected_materials": b["config"]["rejected_materials"]}
+        "rejected_materials": b["config"]["rejected_materials"],
+        "cpu_baseline": b.get("cpu_baseline")}
     torch.cuda.empty_cache()
     sv = run_serve(args)
     out["served"] = {
@@ -475,7 +476,8 @@ def extras(args):
         "sequential_p50_latency_s": sv["sequential"]["p50_latency_s"],
         "sequential_p99_latency_s": sv["sequential"]["p99_latency_s"],
         "throughput_ratio": sv["throughput_ratio"], "results_identical": sv["results_identical"],
-        "done": sv["served"]["done"], "peak_active": sv["served"]["peak_active"]}
+        "done": sv["served"]["done"], "peak_active": sv["served"]["peak_active"],
+        "cpu_baseline": sv.get("cpu_baseline")}
     torch.cuda.empty_cache()
     a = run_adjoint(args)
     out["adjoint"] = {"value": a["value"], "unit": a["unit"], "workload": a["config"]["workload"],
@@ -487,6 +489,55 @@ def extras(args):
     out["parity"] = {"quick_start_100": parity_quick_start(),
                      "enclosure_400": ENCLOSURE_FP64_ERRORS}
     return out
+
+
+def oracle_twin(s):
+    """The same solve on the CPU oracle, built from a GPU solver's set-up:
+    mask, PML depth, ADE materials and their ids, point sources, probes."""
+    from oracle import oracle as O
+
+    o = O.FDTDSolver(shape=s.shape, resolution=s.dx, c=s.c, rho=s.rho, courant=0.5)
+    assert o.dt == s.dt
+    for b in s._boundaries:
+        o.add_boundary(O.PML(depth=b.depth))
+    if s._geometry_set:
+        o.set_geometry(s.geometry.copy())
+    for mid, mat in s._materials.items():
+        o.register_material(mat, material_id=mid)
+    if s._materials:
+        o._material_id[...] = s._material_id
+    for src in s._sources:
+        o.add_source(O.GaussianPulse(position=tuple(src.position), frequency=src.frequency,
+                                     amplitude=src.amplitude))
+    for name, pr in s._probes.items():
+        o.add_probe(name, tuple(pr.position))
+    return o
+
+
+def cpu_subsample(solvers, steps_each, full_cell_updates, what):
+    """The CPU baseline of a many-solve workload: the oracle (all host
+    threads) runs ``steps_each`` steps of each solve of a seeded subsample,
+    after one untimed step; the rate is cell-updates over the summed time,
+    and the whole workload's CPU time is extrapolated from it by
+    cell-updates."""
+    from oracle import oracle as O
+
+    el, cu = 0.0, 0
+    for s in solvers:
+        o = oracle_twin(s)
+        o.run_steps(1)
+        t0 = time.perf_counter()
+        o.run_steps(steps_each)
+        el += time.perf_counter() - t0
+        cu += int(np.prod(s.shape)) * steps_each
+        del o
+    v = cu / el / 1e9
+    return {"value": v, "unit": METRIC, "cores": O.threads(), "kind": "port",
+            "sample": f"{steps_each} steps of each of {what} on the CPU oracle (bit-exact C "
+                      "restatement of the reference native kernels and its ADE kernels, OpenMP), "
+                      f"{cu / 1e9:.3f} G cell-updates in {el:.2f} s; the whole workload "
+                      "extrapolated by cell-updates",
+            "full_workload_seconds_estimate": full_cell_updates / (v * 1e9)}
 
 
 def run_batch(args):
@@ -576,6 +627,9 @@ def run_batch(args):
         "speedup_vs_sequential": t_seq / t_bat,
         "traces_identical": bool(same),
     }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_subsample(bat[:16], 60, cell_updates,
+                                             "the first 16 solves of the batch")
     return line
 
 
@@ -625,6 +679,12 @@ def run_serve(args):
                              if st2["gcell_updates_per_s"] else None),
         "results_identical": same,
     }
+    if not args.no_cpu_baseline:
+        sub = [r.build() for r in served_stream(seed=0, n_requests=20)]
+        line["cpu_baseline"] = cpu_subsample(sub, 50, st.get("cell_updates") or 0,
+                                             "the first 20 requests of the stream")
+        del sub
+        torch.cuda.empty_cache()
     return line
 
 
