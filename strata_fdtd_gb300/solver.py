@@ -322,6 +322,62 @@ class FDTDSolver:
         cur = self._cur()
         return {f: self._dev[cur][q] for q, f in enumerate(_FIELDS)}
 
+    def load_fields_async(self, **fields) -> None:
+        """Copy host arrays into the device state on the current stream
+        without waiting for the copies: any of p, vx, vy, vz, each a
+        C-contiguous float32 array of the grid's shape (from pinned memory
+        the copies run asynchronously).  The arrays must stay unchanged until
+        the copies have run (an event recorded on the stream after this call
+        marks that); the fields not given keep their values."""
+        torch = self._torch
+        for name, value in fields.items():
+            if name not in _FIELDS:
+                raise ValueError(f"unknown field {name!r}; the fields are {_FIELDS}")
+            a = np.asarray(value)
+            if a.shape != self.shape or a.dtype != np.float32 or not a.flags.c_contiguous:
+                raise ValueError(f"{name} must be a C-contiguous float32 array of shape "
+                                 f"{self.shape}")
+        self._upload_exposed()
+        cur = self._cur()
+        for name, value in fields.items():
+            self._dev[cur][_FIELDS.index(name)].copy_(torch.from_numpy(np.asarray(value)),
+                                                       non_blocking=True)
+            self._host_fresh[name] = False
+            self._host_exposed[name] = False
+            self._vz_seen = self._vz_seen or name == "vz"
+
+    def fields_async(self, names=_FIELDS, out: dict | None = None):
+        """Start copying the named fields of the current state to pinned host
+        memory, queued on the current stream after the steps so far, and
+        return a function that waits for those copies only and returns
+        {name: array}.  ``out`` may give a pinned float32 array of the grid's
+        shape per name to copy into (no allocation); the arrays must not be
+        read before the function returns."""
+        torch = self._torch
+        self._upload_exposed()
+        cur = self._cur()
+        dst = {}
+        for name in names:
+            src = self._dev[cur][_FIELDS.index(name)]
+            if out is not None and name in out:
+                a = out[name]
+                if a.shape != self.shape or a.dtype != np.float32 or not a.flags.c_contiguous:
+                    raise ValueError(f"out[{name!r}] must be a C-contiguous float32 array of "
+                                     f"shape {self.shape}")
+                host = torch.from_numpy(a)
+            else:
+                host = torch.empty(self.shape, dtype=torch.float32, pin_memory=True)
+            host.copy_(src, non_blocking=True)
+            dst[name] = host
+        done = torch.cuda.Event()
+        done.record()
+
+        def result() -> dict:
+            done.synchronize()
+            return {n: t.numpy() for n, t in dst.items()}
+
+        return result
+
     def _upload_exposed(self):
         cur = None
         for q, f in enumerate(_FIELDS):
@@ -1055,9 +1111,13 @@ class FDTDSolver:
         queued later on the stream) and returns get_probe_data()'s dict."""
         torch = self._torch
         copies = []
+        stream = torch.cuda.current_stream(self._device)
         for trace, names in self._pending_traces:
             host = torch.empty(trace.shape, dtype=trace.dtype, pin_memory=True)
             host.copy_(trace, non_blocking=True)
+            # the trace may have been allocated on another stream: keep its
+            # block from reuse until this stream's copy has run
+            trace.record_stream(stream)
             copies.append((host, names))
         self._pending_traces = []
         done = torch.cuda.Event()

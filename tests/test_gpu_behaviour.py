@@ -238,3 +238,63 @@ def test_waveform_table_matches_per_step_calls_on_this_host():
     """The same check with the NumPy of the machine that runs the GPU."""
     from test_abi_host import waveform_table_matches_per_step_calls
     waveform_table_matches_per_step_calls(20000)
+
+
+def test_async_field_load_and_readback_on_a_copy_stream():
+    """load_fields_async / fields_async / probe_data_async on a copy stream
+    around steps on the compute stream (the pattern of the end-to-end bench:
+    two replicas alternating) give the same bits as assigning the fields,
+    stepping and reading p, vz and the traces synchronously."""
+    shape = (40, 36, 44)
+    rng = np.random.default_rng(11)
+    host = {f: torch.from_numpy(rng.standard_normal(shape).astype(np.float32) * 1e-3)
+            .pin_memory().numpy() for f in ("p", "vx", "vy", "vz")}
+    geom = np.ones(shape, dtype=bool)
+    geom[18:22, 10:30, 6:40] = False
+    for f in host:
+        host[f][~geom] = 0.0
+
+    def make():
+        s = _solver(shape)
+        s.add_boundary(S.PML(depth=6))
+        s.set_geometry(geom)
+        s.add_source(S.GaussianPulse(position=(10, 18, 22), frequency=8000.0))
+        s.add_probe("a", (30, 18, 22))
+        s.add_probe("b", (12, 30, 8))
+        return s
+
+    ref = make()
+    for f in host:
+        setattr(ref, f, host[f].copy())  # an assigned array becomes the solver's field
+    ref.run_steps(64)
+    want = {"p": ref.p.copy(), "vz": ref.vz.copy()}
+    want_tr = ref.get_probe_data()
+
+    reps = (make(), make())
+    comp, cp = torch.cuda.current_stream(), torch.cuda.Stream()
+    outs = [{f: torch.empty(shape, dtype=torch.float32).pin_memory().numpy() for f in ("p", "vz")}
+            for _ in reps]
+    got = []
+    for k, a in enumerate(reps):
+        with torch.cuda.stream(cp):
+            a.load_fields_async(**host)
+            up = torch.cuda.Event()
+            up.record(cp)
+        comp.wait_event(up)
+        a.run_steps(64)
+        ran = torch.cuda.Event()
+        ran.record(comp)
+        with torch.cuda.stream(cp):
+            cp.wait_event(ran)
+            got.append((a.fields_async(("p", "vz"), out=outs[k]), a.probe_data_async()))
+    for fp, ft in got:
+        fields, traces = fp(), ft()
+        for f in ("p", "vz"):
+            np.testing.assert_array_equal(fields[f], want[f])
+        for n in want_tr:
+            np.testing.assert_array_equal(traces[n], want_tr[n])
+    assert np.abs(want_tr["a"]).max() > 0
+    with pytest.raises(ValueError):
+        reps[0].load_fields_async(p=np.zeros((3, 3, 3), dtype=np.float32))
+    with pytest.raises(ValueError):
+        reps[0].load_fields_async(q=host["p"])
