@@ -390,6 +390,12 @@ typedef struct {
     int32_t n_probe, reserved;
     const int64_t* probe_cells; /* device */
     const uint8_t* geometry;    /* device air mask, or NULL: no solids */
+    /* device occupancy field phi (N values of the external type: float for
+     * dtype 0, double otherwise), or NULL.  Each face coefficient is scaled
+     * by the open fractions of its two cells, (1 - phi_lo)(1 - phi_hi): phi
+     * = 1 closes every face of a cell (a rigid wall), phi in (0, 1) a
+     * partly open one, so the solve is differentiable in the geometry. */
+    const void* occupancy;
 } sf_diff_desc;
 /* cv arrays (3 x N) from theta (N). */
 int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, void* cvy, void* cvz,
@@ -416,6 +422,10 @@ int sf_diff_adjoint(const sf_diff_desc* d, void* const* cv, void* const* lam0, v
 /* dL/dtheta (dtype) from dL/dcv (grad_cv as sf_diff_adjoint left it). */
 int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* grad_cv, void* out,
                        void* stream);
+/* dL/dtheta and, when out_occupancy is not NULL (it needs d->occupancy),
+ * dL/dphi, both in the external type, from the same grad_cv. */
+int sf_diff_grad_fields(const sf_diff_desc* d, const void* theta, void* const* grad_cv,
+                        void* out_theta, void* out_occupancy, void* stream);
 
 /* --- voxelisation -------------------------------------------------------- */
 /* mask[i,j,k] = sdf(cell centre) <= 0, cell centre = (i + 0.5)*res, as

@@ -138,6 +138,7 @@ SIGNATURES = {
     "sf_diff_forward": (_I, [_P, _P, _P, _P, _I, _I64, _P, _P, _P, _P]),
     "sf_diff_adjoint": (_I, [_P, _P, _P, _P, _I, _I64, _P, _P, _P, _D, _P, _P]),
     "sf_diff_grad_theta": (_I, [_P, _P, _P, _P, _P]),
+    "sf_diff_grad_fields": (_I, [_P, _P, _P, _P, _P, _P]),
     "sf_batch_create": (_I, [ctypes.POINTER(_P)]),
     "sf_batch_destroy": (_I, [_P]),
     "sf_batch_add": (_I, [_P, _P, _I64, _P, _P]),

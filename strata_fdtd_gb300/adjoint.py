@@ -32,7 +32,7 @@ class _Desc(ctypes.Structure):
                 ("rho0", ctypes.c_double), ("decay", ctypes.c_void_p * 3),
                 ("src_cell", ctypes.c_int64), ("n_probe", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("probe_cells", ctypes.c_void_p),
-                ("geometry", ctypes.c_void_p)]
+                ("geometry", ctypes.c_void_p), ("occupancy", ctypes.c_void_p)]
 
 
 def _ptrs(ts):
@@ -58,7 +58,14 @@ class DifferentiableSolver:
     boundary for a solve started from rest.  The gradient is then taken with
     respect to theta in the air cells (zero in solid ones, whose density
     never enters the solve); a source in a solid cell injects nothing, as in
-    the reference."""
+    the reference.
+
+    An occupancy field ``phi`` (grid shape, values in [0, 1], the solid
+    fraction of each cell) can be passed with theta to ``forward`` and
+    ``loss``: every face coefficient is scaled by the open fractions of its
+    two cells, (1 - phi_lo)(1 - phi_hi), so phi = 1 is a rigid wall and the
+    loss is differentiable in the geometry as well as in the density; with a
+    phi that requires grad, ``loss(...).backward()`` fills both gradients."""
 
     def __init__(self, shape, resolution=1e-3, c=343.0, rho0=1.204, courant=0.5, pml_depth=10,
                  source=None, frequency=1500.0, probes=(), dtype="dw", checkpoint_every=100,
@@ -126,7 +133,7 @@ class DifferentiableSolver:
         pair[..., 1] = (v - pair[..., 0].astype(np.float64)).astype(np.float32)
         return torch.from_numpy(pair.view(np.float64).reshape(v.shape).copy()).to(self.dev)
 
-    def _desc(self):
+    def _desc(self, occupancy=None):
         d = _Desc()
         d.nx, d.ny, d.nz = self.shape
         d.dtype = {"f32": 0, "f64": 1, "dw": 2}[self.precision]
@@ -141,7 +148,17 @@ class DifferentiableSolver:
         d.n_probe = len(self.probe_pos)
         d.probe_cells = self.probe_cells.data_ptr()
         d.geometry = self._air.data_ptr() if self._air is not None else None
+        d.occupancy = occupancy.data_ptr() if occupancy is not None else None
         return d
+
+    def _occupancy(self, occupancy):
+        if occupancy is None:
+            return None
+        occ = occupancy.detach().to(device=self.dev, dtype=self.ext_dtype).contiguous()
+        if tuple(occ.shape) != self.shape:
+            raise ValueError(f"occupancy shape {tuple(occ.shape)} does not match the grid "
+                             f"{self.shape}")
+        return occ
 
     def source_values(self, n_steps):
         """Pulse value per step at the FP64-accumulated times t += dt, in one
@@ -158,10 +175,11 @@ class DifferentiableSolver:
     def _stream(self):
         return self.torch.cuda.current_stream().cuda_stream
 
-    def coefficients(self, theta):
+    def coefficients(self, theta, occupancy=None):
         torch = self.torch
+        occ = self._occupancy(occupancy)
         cv = [torch.empty(self.shape, dtype=self.dtype, device=self.dev) for _ in range(3)]
-        _native.check(self.lib.sf_diff_coefficients(ctypes.byref(self._desc()), theta.data_ptr(),
+        _native.check(self.lib.sf_diff_coefficients(ctypes.byref(self._desc(occ)), theta.data_ptr(),
                                                     *[c.data_ptr() for c in cv], self._stream()),
                       "sf_diff_coefficients")
         return cv
@@ -169,11 +187,12 @@ class DifferentiableSolver:
     def _zeros4(self):
         return [self.torch.zeros(self.shape, dtype=self.dtype, device=self.dev) for _ in range(4)]
 
-    def forward(self, theta, n_steps, keep_checkpoints=True):
-        """Run n_steps from rest.  Returns (trace [n, n_probe], checkpoints)."""
+    def forward(self, theta, n_steps, keep_checkpoints=True, occupancy=None):
+        """Run n_steps from rest.  Returns (trace [n, n_probe], checkpoints,
+        face coefficients, source values)."""
         torch = self.torch
         theta = theta.to(self.ext_dtype).contiguous()
-        cv = self.coefficients(theta)
+        cv = self.coefficients(theta, occupancy)
         sets = [self._zeros4(), self._zeros4()]
         cur = 0
         src = self.source_values(n_steps)
@@ -192,9 +211,10 @@ class DifferentiableSolver:
             cur = (cur + n) & 1
         return trace[:, :len(self.probe_pos)], ckpts, cv, src
 
-    def gradient(self, theta, trace, target, ckpts, cv, src, weight=1.0):
+    def gradient(self, theta, trace, target, ckpts, cv, src, weight=1.0, occupancy=None):
         """dL/dtheta of L = weight * sum((trace - target)^2) by checkpointed
-        recomputation and the reverse-time adjoint."""
+        recomputation and the reverse-time adjoint; with an occupancy field,
+        (dL/dtheta, dL/dphi)."""
         torch = self.torch
         n_steps = trace.shape[0]
         theta = theta.to(self.ext_dtype).contiguous()
@@ -223,16 +243,19 @@ class DifferentiableSolver:
                 store.data_ptr(), full[s0:].data_ptr(), tgt[s0:].data_ptr(), float(weight),
                 _ptrs(grad_cv), self._stream()), "sf_diff_adjoint")
             lcur = (lcur + n) & 1
+        occ = self._occupancy(occupancy)
         out = torch.empty(self.shape, dtype=self.ext_dtype, device=self.dev)
-        _native.check(self.lib.sf_diff_grad_theta(ctypes.byref(desc), theta.data_ptr(),
-                                                  _ptrs(grad_cv), out.data_ptr(), self._stream()),
-                      "sf_diff_grad_theta")
-        return out
+        out_occ = None if occ is None else torch.empty_like(out)
+        _native.check(self.lib.sf_diff_grad_fields(
+            ctypes.byref(self._desc(occ)), theta.data_ptr(), _ptrs(grad_cv), out.data_ptr(),
+            None if out_occ is None else out_occ.data_ptr(), self._stream()), "sf_diff_grad_fields")
+        return out if occ is None else (out, out_occ)
 
-    def loss(self, theta, target, n_steps):
+    def loss(self, theta, target, n_steps, occupancy=None):
         """L2 loss of the probe traces against ``target`` [n_steps, n_probe],
-        differentiable w.r.t. ``theta`` through the adjoint kernels."""
-        return ProbeLoss.apply(theta, target, self, n_steps)
+        differentiable w.r.t. ``theta`` (and ``occupancy``, when given)
+        through the adjoint kernels."""
+        return ProbeLoss.apply(theta, target, self, n_steps, occupancy)
 
 
 def _make_function():
@@ -242,21 +265,25 @@ def _make_function():
         """loss = sum((trace(theta) - target)^2); backward via the adjoint."""
 
         @staticmethod
-        def forward(ctx, theta, target, solver, n_steps):
-            trace, ckpts, cv, src = solver.forward(theta.detach(), n_steps)
+        def forward(ctx, theta, target, solver, n_steps, occupancy=None):
+            occ = None if occupancy is None else occupancy.detach()
+            trace, ckpts, cv, src = solver.forward(theta.detach(), n_steps, occupancy=occ)
             loss = ((trace - target.to(trace.dtype)) ** 2).sum()
             ctx.solver = solver
             ctx.saved = (trace, ckpts, cv, src)
-            ctx.save_for_backward(theta, target)
+            ctx.save_for_backward(theta, target, occupancy)
             return loss.to(theta.dtype)
 
         @staticmethod
         def backward(ctx, grad_out):
-            theta, target = ctx.saved_tensors
+            theta, target, occupancy = ctx.saved_tensors
             trace, ckpts, cv, src = ctx.saved
             g = ctx.solver.gradient(theta.detach(), trace, target, ckpts, cv, src,
-                                    weight=float(grad_out))
-            return g.to(theta.dtype), None, None, None
+                                    weight=float(grad_out),
+                                    occupancy=None if occupancy is None else occupancy.detach())
+            if occupancy is None:
+                return g.to(theta.dtype), None, None, None, None
+            return g[0].to(theta.dtype), None, None, None, g[1].to(occupancy.dtype)
 
     return ProbeLossFn
 
@@ -274,7 +301,7 @@ class _Lazy:
 ProbeLoss = _Lazy
 
 
-def reference_loss_torch(solver: DifferentiableSolver, theta, target, n_steps):
+def reference_loss_torch(solver: DifferentiableSolver, theta, target, n_steps, occupancy=None):
     """The same scheme stepped with plain PyTorch tensor ops (for checking the
     adjoint kernels with torch.autograd at small sizes).  Not used by the
     GPU path."""
@@ -285,6 +312,11 @@ def reference_loss_torch(solver: DifferentiableSolver, theta, target, n_steps):
     cvx = -dt_dx * 0.5 * (b[:-1] + b[1:])
     cvy = -dt_dx * 0.5 * (b[:, :-1] + b[:, 1:])
     cvz = -dt_dx * 0.5 * (b[:, :, :-1] + b[:, :, 1:])
+    if occupancy is not None:
+        w = 1.0 - occupancy
+        cvx = cvx * (w[:-1] * w[1:])
+        cvy = cvy * (w[:, :-1] * w[:, 1:])
+        cvz = cvz * (w[:, :, :-1] * w[:, :, 1:])
     inject = True
     if solver.geometry is not None:
         air = torch.as_tensor(solver.geometry, device=theta.device).to(theta.dtype)

@@ -145,13 +145,16 @@ constexpr int kFusedProbes = 4;
 
 // Coefficients from theta: cv_a(c) for the face between c and c + e_a
 // (zero on the last plane of each axis, which carries no face update, and on
-// faces that touch a solid cell of the air mask `air`, when given).
+// faces that touch a solid cell of the air mask `air`, when given).  With an
+// occupancy field phi (solid fraction per cell) the face coefficient is
+// scaled by the open fractions of its two cells, (1 - phi_c)(1 - phi_n):
+// phi = 1 closes every face of the cell, a rigid wall.
 // (formed in the external type: in double for a double-word solve, then
 // rounded to the nearest double-word)
 template <typename T, typename E = typename Ext<T>::E>
 __global__ void k_dcoef(const E* __restrict__ theta, const uint8_t* __restrict__ air,
-                        T* __restrict__ cvx, T* __restrict__ cvy, T* __restrict__ cvz, int nx,
-                        int ny, int nz, E dt_dx, E rho0) {
+                        const E* __restrict__ occ, T* __restrict__ cvx, T* __restrict__ cvy,
+                        T* __restrict__ cvz, int nx, int ny, int nz, E dt_dx, E rho0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -160,10 +163,12 @@ __global__ void k_dcoef(const E* __restrict__ theta, const uint8_t* __restrict__
     const long long c = (long long)i * plane + (long long)j * nz + k;
     const E b0 = E(1) / (rho0 * (E(1) + theta[c]));
     const bool solid = air && !air[c];
+    const E w0 = occ ? E(1) - occ[c] : E(1);
     auto face = [&](long long n) {
         if (solid || (air && !air[n])) return T(0);
         const E b1 = E(1) / (rho0 * (E(1) + theta[n]));
-        return Ext<T>::in(-dt_dx * E(0.5) * (b0 + b1));
+        const E base = -dt_dx * E(0.5) * (b0 + b1);
+        return Ext<T>::in(occ ? base * (w0 * (E(1) - occ[n])) : base);
     };
     cvx[c] = (i < nx - 1) ? face(c + plane) : T(0);
     cvy[c] = (j < ny - 1) ? face(c + nz) : T(0);
@@ -287,12 +292,16 @@ __global__ void k_dadj(DiffPtrs<T> g, const T* __restrict__ lp, const T* __restr
 
 // dL/dtheta(c) = (dt/dx) rho0 / (2 rho(c)^2) * sum of dL/dcv over its faces;
 // a wall face's cv is zero whatever theta is, so it contributes nothing, and a
-// solid cell's gradient is zero.
+// solid cell's gradient is zero.  With an occupancy field phi each face's
+// term carries its open-fraction factor (1 - phi_c)(1 - phi_n), and, when
+// out_occ is given, dL/dphi(c) = sum over the faces of dL/dcv * (-base)
+// * (1 - phi_n), base = -(dt/dx)(1/rho_c + 1/rho_n)/2.
 template <typename T, typename E = typename Ext<T>::E>
 __global__ void k_dgrad(const E* __restrict__ theta, const uint8_t* __restrict__ air,
-                        const double* __restrict__ gx, const double* __restrict__ gy,
-                        const double* __restrict__ gz, E* __restrict__ out, int nx, int ny,
-                        int nz, double dt_dx, double rho0) {
+                        const E* __restrict__ occ, const double* __restrict__ gx,
+                        const double* __restrict__ gy, const double* __restrict__ gz,
+                        E* __restrict__ out, E* __restrict__ out_occ, int nx, int ny, int nz,
+                        double dt_dx, double rho0) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -302,19 +311,40 @@ __global__ void k_dgrad(const E* __restrict__ theta, const uint8_t* __restrict__
     using A = GradAcc<T>;
     if (air && !air[c]) {
         out[c] = E(0);
+        if (out_occ) out_occ[c] = E(0);
         return;
     }
     auto open = [&](long long n) { return !air || air[n]; };
-    // high faces (zero on the last plane), then the low ones
-    double s = 0.0;
-    if (i < nx - 1 && open(c + plane)) s += A::load(gx, c);
-    if (j < ny - 1 && open(c + nz)) s += A::load(gy, c);
-    if (k < nz - 1 && open(c + 1)) s += A::load(gz, c);
-    if (i > 0 && open(c - plane)) s += A::load(gx, c - plane);
-    if (j > 0 && open(c - nz)) s += A::load(gy, c - nz);
-    if (k > 0 && open(c - 1)) s += A::load(gz, c - 1);
     const double rho = rho0 * (1.0 + double(theta[c]));
-    out[c] = E(s * dt_dx * rho0 / (2.0 * rho * rho));
+    if (!occ) {
+        // high faces (zero on the last plane), then the low ones
+        double s = 0.0;
+        if (i < nx - 1 && open(c + plane)) s += A::load(gx, c);
+        if (j < ny - 1 && open(c + nz)) s += A::load(gy, c);
+        if (k < nz - 1 && open(c + 1)) s += A::load(gz, c);
+        if (i > 0 && open(c - plane)) s += A::load(gx, c - plane);
+        if (j > 0 && open(c - nz)) s += A::load(gy, c - nz);
+        if (k > 0 && open(c - 1)) s += A::load(gz, c - 1);
+        out[c] = E(s * dt_dx * rho0 / (2.0 * rho * rho));
+        return;
+    }
+    const double b0 = 1.0 / rho, w0 = 1.0 - double(occ[c]);
+    double st = 0.0, so = 0.0;  // sum of dL/dcv * w_n; sum of dL/dcv * (-base) * w_n
+    auto face = [&](const double* gf, long long q, long long n) {
+        const double g = A::load(gf, q);
+        const double wn = 1.0 - double(occ[n]);
+        const double b1 = 1.0 / (rho0 * (1.0 + double(theta[n])));
+        st += g * wn;
+        so += g * (dt_dx * 0.5 * (b0 + b1)) * wn;
+    };
+    if (i < nx - 1 && open(c + plane)) face(gx, c, c + plane);
+    if (j < ny - 1 && open(c + nz)) face(gy, c, c + nz);
+    if (k < nz - 1 && open(c + 1)) face(gz, c, c + 1);
+    if (i > 0 && open(c - plane)) face(gx, c - plane, c - plane);
+    if (j > 0 && open(c - nz)) face(gy, c - nz, c - nz);
+    if (k > 0 && open(c - 1)) face(gz, c - 1, c - 1);
+    out[c] = E(st * w0 * dt_dx * rho0 / (2.0 * rho * rho));
+    if (out_occ) out_occ[c] = E(so);
 }
 
 template <typename T>
@@ -413,18 +443,19 @@ int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, vo
     if (int rc = check_desc(d)) return rc;
     if (!theta || !cvx || !cvy || !cvz) return sf_fail("sf_diff_coefficients: NULL buffer");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const dim3 grd = grid_of(d), blk(32, 8);
     if (d->dtype == 1)
-        k_dcoef<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, d->geometry, (double*)cvx, (double*)cvy, (double*)cvz, d->nx,
-            d->ny, d->nz, d->dt_over_dx, d->rho0);
+        k_dcoef<double><<<grd, blk, 0, st>>>(
+            (const double*)theta, d->geometry, (const double*)d->occupancy, (double*)cvx,
+            (double*)cvy, (double*)cvz, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     else if (d->dtype == 2)
-        k_dcoef<dwf><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, d->geometry, (dwf*)cvx, (dwf*)cvy, (dwf*)cvz, d->nx, d->ny,
-            d->nz, d->dt_over_dx, d->rho0);
+        k_dcoef<dwf><<<grd, blk, 0, st>>>(
+            (const double*)theta, d->geometry, (const double*)d->occupancy, (dwf*)cvx, (dwf*)cvy,
+            (dwf*)cvz, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
     else
-        k_dcoef<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const float*)theta, d->geometry, (float*)cvx, (float*)cvy, (float*)cvz, d->nx,
-            d->ny, d->nz, (float)d->dt_over_dx, (float)d->rho0);
+        k_dcoef<float><<<grd, blk, 0, st>>>(
+            (const float*)theta, d->geometry, (const float*)d->occupancy, (float*)cvx, (float*)cvy,
+            (float*)cvz, d->nx, d->ny, d->nz, (float)d->dt_over_dx, (float)d->rho0);
     return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_coefficients: launch failed");
 }
 
@@ -458,24 +489,37 @@ int sf_diff_adjoint(const sf_diff_desc* d, void* const* cv, void* const* lam0, v
                                           weight, grad_cv, st);
 }
 
-int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* grad_cv, void* out,
-                       void* stream) {
+int sf_diff_grad_fields(const sf_diff_desc* d, const void* theta, void* const* grad_cv,
+                        void* out_theta, void* out_occupancy, void* stream) {
     if (int rc = check_desc(d)) return rc;
-    if (!theta || !grad_cv || !out) return sf_fail("sf_diff_grad_theta: NULL buffer");
+    if (!theta || !grad_cv || !out_theta) return sf_fail("sf_diff_grad_fields: NULL buffer");
+    if (out_occupancy && !d->occupancy)
+        return sf_fail("sf_diff_grad_fields: an occupancy gradient needs the occupancy field");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const double* g0 = (const double*)grad_cv[0];
+    const double* g1 = (const double*)grad_cv[1];
+    const double* g2 = (const double*)grad_cv[2];
     if (d->dtype == 1)
         k_dgrad<double><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, d->geometry, (const double*)grad_cv[0], (const double*)grad_cv[1],
-            (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
+            (const double*)theta, d->geometry, (const double*)d->occupancy, g0, g1, g2,
+            (double*)out_theta, (double*)out_occupancy, d->nx, d->ny, d->nz, d->dt_over_dx,
+            d->rho0);
     else if (d->dtype == 2)
         k_dgrad<dwf><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const double*)theta, d->geometry, (const double*)grad_cv[0], (const double*)grad_cv[1],
-            (const double*)grad_cv[2], (double*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
+            (const double*)theta, d->geometry, (const double*)d->occupancy, g0, g1, g2,
+            (double*)out_theta, (double*)out_occupancy, d->nx, d->ny, d->nz, d->dt_over_dx,
+            d->rho0);
     else
         k_dgrad<float><<<grid_of(d), dim3(32, 8), 0, st>>>(
-            (const float*)theta, d->geometry, (const double*)grad_cv[0], (const double*)grad_cv[1],
-            (const double*)grad_cv[2], (float*)out, d->nx, d->ny, d->nz, d->dt_over_dx, d->rho0);
-    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_grad_theta: launch failed");
+            (const float*)theta, d->geometry, (const float*)d->occupancy, g0, g1, g2,
+            (float*)out_theta, (float*)out_occupancy, d->nx, d->ny, d->nz, d->dt_over_dx,
+            d->rho0);
+    return cudaGetLastError() == cudaSuccess ? 0 : sf_fail("sf_diff_grad_fields: launch failed");
+}
+
+int sf_diff_grad_theta(const sf_diff_desc* d, const void* theta, void* const* grad_cv, void* out,
+                       void* stream) {
+    return sf_diff_grad_fields(d, theta, grad_cv, out, nullptr, stream);
 }
 
 }  // extern "C"

@@ -267,3 +267,89 @@ def test_source_in_a_solid_cell_injects_nothing():
     s = _walled(torch.float64, g, source=(10, 2, 2))
     tr = s.forward(torch.zeros(g.shape, dtype=torch.float64, device="cuda"), 40)[0]
     assert float(tr.abs().max()) == 0.0
+
+
+def _occupancy(shape, seed):
+    """A smooth partial-solid field (0-0.6) on the central region plus the
+    walled slab of _walled_geometry as fully solid cells."""
+    phi = 0.6 * design_field(shape, region=10, seed=seed, sigma=1.5)
+    phi[~_walled_geometry(shape)] = 1.0
+    return phi
+
+
+def test_full_occupancy_is_a_rigid_wall():
+    """phi = 1 on the solid cells of the air mask, 0 elsewhere, gives the
+    walled solve's traces bit for bit (every face it closes has a zero
+    coefficient, the others keep theirs)."""
+    g = _walled_geometry()
+    phi = torch.tensor((~g).astype(np.float64), device="cuda")
+    theta = torch.tensor(design_field(g.shape, region=10, seed=9, sigma=1.5), device="cuda")
+    for dtype in (torch.float64, "dw", torch.float32):
+        walled = _walled(dtype, g).forward(theta, 60, keep_checkpoints=False)[0]
+        free = DifferentiableSolver(g.shape, pml_depth=3, frequency=20000.0, source=(5, 9, 11),
+                                    probes=[(15, 9, 11), (14, 4, 16)], dtype=dtype,
+                                    checkpoint_every=25)
+        occ = free.forward(theta, 60, keep_checkpoints=False, occupancy=phi)[0]
+        assert float(walled.abs().max()) > 0
+        assert torch.equal(walled, occ), dtype
+
+
+@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-9), ("dw", 1e-8)])
+def test_occupancy_and_density_gradients_match_autograd(dtype, rtol):
+    """Gradients with respect to both the density field theta and the
+    occupancy field phi against autograd through the plain PyTorch stepping
+    of the same scheme."""
+    shape = (20, 18, 22)
+    s = DifferentiableSolver(shape, pml_depth=3, frequency=20000.0, source=(5, 9, 11),
+                             probes=[(15, 9, 11), (14, 4, 16)], dtype=dtype, checkpoint_every=25)
+    theta = torch.tensor(design_field(shape, region=10, seed=12, sigma=1.5), device="cuda")
+    phi = torch.tensor(_occupancy(shape, 13), device="cuda")
+    target = s.forward(theta, 80, occupancy=torch.tensor(_occupancy(shape, 14), device="cuda"))[0]
+    th = theta.clone().requires_grad_(True)
+    ph = phi.clone().requires_grad_(True)
+    loss = s.loss(th, target, 80, occupancy=ph)
+    loss.backward()
+    ref_s = DifferentiableSolver(shape, pml_depth=3, frequency=20000.0, source=(5, 9, 11),
+                                 probes=[(15, 9, 11), (14, 4, 16)], dtype=torch.float64,
+                                 checkpoint_every=25)
+    rth = theta.clone().requires_grad_(True)
+    rph = phi.clone().requires_grad_(True)
+    ref = reference_loss_torch(ref_s, rth, target, 80, occupancy=rph)
+    ref.backward()
+    assert float(loss) == pytest.approx(float(ref), rel=rtol * 1e-3)
+    for got, want in ((th.grad, rth.grad), (ph.grad, rph.grad)):
+        w = want.cpu().numpy()
+        assert np.abs(w).max() > 0
+        np.testing.assert_allclose(got.cpu().numpy(), w, rtol=rtol, atol=rtol * 1e-3 * np.abs(w).max())
+
+
+def test_occupancy_gradient_matches_central_differences():
+    """dL/dphi of the FP64 and double-word adjoints against FP64 central
+    differences (h = 1e-3) in partly open cells, rel 1e-5."""
+    shape = (20, 18, 22)
+
+    def make(dtype):
+        return DifferentiableSolver(shape, pml_depth=3, frequency=20000.0, source=(5, 9, 11),
+                                    probes=[(15, 9, 11), (14, 4, 16)], dtype=dtype,
+                                    checkpoint_every=16)
+
+    theta = torch.tensor(design_field(shape, region=10, seed=15, sigma=1.5), device="cuda")
+    phi = torch.tensor(_occupancy(shape, 16), device="cuda")
+    base = make(torch.float64)
+    target = base.forward(theta, 70, occupancy=torch.zeros_like(phi))[0] * 0.5
+    cells = [(9, 8, 10), (12, 9, 11), (8, 12, 8), (13, 10, 12), (7, 6, 14)]
+    h = 1e-3
+    fd = {}
+    for c in cells:
+        assert 0.0 < float(phi[c]) < 1.0
+        pp, pm = phi.clone(), phi.clone()
+        pp[c] += h
+        pm[c] -= h
+        fd[c] = (float(base.loss(theta, target, 70, occupancy=pp))
+                 - float(base.loss(theta, target, 70, occupancy=pm))) / (2 * h)
+    for dtype in (torch.float64, "dw"):
+        s = make(dtype)
+        ph = phi.clone().requires_grad_(True)
+        s.loss(theta, target, 70, occupancy=ph).backward()
+        for c in cells:
+            assert float(ph.grad[c]) == pytest.approx(fd[c], rel=1e-5, abs=1e-14), (dtype, c)
