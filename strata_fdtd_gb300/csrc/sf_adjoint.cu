@@ -12,9 +12,10 @@
 // (boundaries.cpp:66-89, fdtd_step.cpp:84-212) keep them, and the forward and
 // adjoint kernels need no mask of their own.  PML decays and the point source
 // as the reference (pml.cpp:47-149, core/solver.py:2413-2421); probe samples
-// after each step.  The per-cell
-// density is a builder-defined design field: the reference has only a scalar
-// rho.
+// after each step.  The per-cell density, and the optional occupancy field
+// phi that scales each face coefficient by (1 - phi_lo)(1 - phi_hi) (the
+// geometry as a design field), are builder-defined: the reference has only
+// a scalar rho and binary solids.
 //
 // One step is linear in the state u = (p, v):
 //     v' = v + C G p          (C = diag(cv), G = face differences)
