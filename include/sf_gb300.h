@@ -82,7 +82,20 @@ typedef struct {
  *   op 23 SCALE_DIST s0    top distance *= s0
  *   op 24 NEGATE           top distance = -top
  *   op 25 PUSH_ROTATE a, b push the point times rows a, b (and the next
- *                          node's a, op 26 ROTATE_ROW2) of a 3x3 matrix  */
+ *                          node's a, op 26 ROTATE_ROW2) of a 3x3 matrix
+ *   op 4 CONE     a = p1, b = unit axis, s0 = length, s1 = r1; the next
+ *                 node (op 27 DATA) a[0] = r2 - r1
+ *   op 5 HORN     a = throat, b = unit axis, s0 = length, s1 = throat
+ *                 radius, n = flare (0 conical, 1 exponential, 2 hyperbolic,
+ *                 3 tractrix); the next DATA node a[0] = its constant (m,
+ *                 alpha, alpha, R)
+ *   op 6 TUBE n   a tube along the 3-D path of the next n DATA nodes (a =
+ *                 vertex, s0 = radius there, b = segment to the next vertex,
+ *                 s1 = its squared length)
+ *   op 7 SPIRAL n the same in the xy plane, extruded over 0 <= z <= s0
+ *   op 13 SMOOTH_UNION, 14 SMOOTH_INTERSECTION, 15 SMOOTH_DIFFERENCE
+ *                 pop b, a (pushed in that order), push the polynomial blend
+ *                 of a and b (negated b for 15) with radius s0  */
 typedef struct {
     int32_t op, n;
     double a[3], b[3];

@@ -535,6 +535,171 @@ class Cylinder(SDFPrimitive):  # sdf.py:341-433
                         np.sqrt((radial - self.radius) ** 2 + axial**2))
 
 
+class Cone(SDFPrimitive):  # sdf.py:436-541
+    def __init__(self, p1, p2, r1, r2):
+        self.p1 = np.array(p1, dtype=np.float64)
+        self.p2 = np.array(p2, dtype=np.float64)
+        self.r1, self.r2 = float(r1), float(r2)
+        axis = self.p2 - self.p1
+        self.length = np.linalg.norm(axis)
+        self.axis_normalized = axis / self.length
+
+    def sdf(self, points):
+        points = np.asarray(points, dtype=np.float64)
+        t = np.dot(points - self.p1, self.axis_normalized) / self.length
+        tc = np.clip(t, 0, 1)
+        rt = self.r1 + tc * (self.r2 - self.r1)
+        closest = self.p1 + (tc * self.length)[:, np.newaxis] * self.axis_normalized
+        radial = np.linalg.norm(points - closest, axis=1)
+        axial = np.maximum(0, np.abs(t - 0.5) - 0.5) * self.length
+        inside = (t >= 0) & (t <= 1)
+        return np.where(inside, radial - rt, np.sqrt((radial - rt) ** 2 + axial**2))
+
+
+class Horn(SDFPrimitive):  # sdf.py:937-1148
+    def __init__(self, throat_position, mouth_position, throat_radius, mouth_radius,
+                 profile="exponential"):
+        self.throat = np.array(throat_position, dtype=np.float64)
+        mouth = np.array(mouth_position, dtype=np.float64)
+        self.r0, r1 = float(throat_radius), float(mouth_radius)
+        self.profile = profile
+        axis = mouth - self.throat
+        self.L = np.linalg.norm(axis)
+        self.axis = axis / self.L
+        a0, am = np.pi * self.r0**2, np.pi * r1**2
+        if profile == "conical":
+            self.k = np.sqrt(am / a0) - 1
+        elif profile == "exponential":
+            self.k = np.log(am / a0) / (2 * self.L)
+        elif profile == "hyperbolic":
+            self.k = np.arccosh(np.sqrt(am / a0)) / self.L
+        else:
+            self.k = self.L / np.arccos(np.power(a0 / am, 0.25))
+
+    def sdf(self, points):
+        v = np.asarray(points, dtype=np.float64) - self.throat
+        t = np.dot(v, self.axis)
+        tc = np.clip(t / self.L, 0, 1)
+        r = np.linalg.norm(v - np.outer(t, self.axis), axis=1)
+        x = tc * self.L
+        if self.profile == "conical":
+            hr = self.r0 * (1 + self.k * tc)
+        elif self.profile == "exponential":
+            hr = self.r0 * np.exp(self.k * x)
+        elif self.profile == "hyperbolic":
+            hr = self.r0 * np.cosh(self.k * x)
+        else:
+            hr = self.r0 / np.cos(x / self.k) ** 2
+        rd = r - hr
+        inside = (t >= 0) & (t <= self.L)
+        return np.where(inside, rd, np.sqrt(rd**2 + np.maximum(-t, t - self.L) ** 2))
+
+
+def _polyline_distance(points, path):  # geometry/paths.py:226-294
+    best = np.full(points.shape[0], np.inf)
+    for a, b in zip(path[:-1], path[1:]):
+        seg = b - a
+        ll = np.dot(seg, seg)
+        if ll < 1e-14:
+            d = np.linalg.norm(points - a, axis=1)
+        else:
+            t = np.clip(np.dot(points - a, seg) / ll, 0, 1)
+            d = np.linalg.norm(points - (a + t[:, np.newaxis] * seg), axis=1)
+        best = np.minimum(best, d)
+    return best
+
+
+def _nearest_radius(points, path, radii):
+    """Radius at the nearest path vertex (the first of equal distances)."""
+    out = np.empty(points.shape[0])
+    for q in range(points.shape[0]):
+        out[q] = radii[np.argmin(np.linalg.norm(path - points[q], axis=1))]
+    return out
+
+
+class HelicalTube(SDFPrimitive):  # sdf.py:1579-1721, paths.py:137-223
+    def __init__(self, center, helix_radius, tube_radius_start, tube_radius_end, pitch, turns):
+        c = np.array(center, dtype=np.float64)
+        n = max(200, int(100 * float(turns)))
+        theta = np.linspace(0, 2 * np.pi * float(turns), n)
+        self.path = np.stack([c[0] + float(helix_radius) * np.cos(theta),
+                              c[1] + float(helix_radius) * np.sin(theta),
+                              c[2] + (theta / (2 * np.pi)) * float(pitch)], axis=1)
+        t = np.linspace(0, 1, n)
+        r0, r1 = float(tube_radius_start), float(tube_radius_end)
+        self.radii = r0 + (r1 - r0) * t
+
+    def sdf(self, points):
+        points = np.asarray(points, dtype=np.float64)
+        return _polyline_distance(points, self.path) - _nearest_radius(points, self.path,
+                                                                       self.radii)
+
+
+class SpiralHorn(SDFPrimitive):  # sdf.py:1392-1576, paths.py:30-134
+    def __init__(self, center, throat_radius, mouth_radius, inner_spiral_radius,
+                 outer_spiral_radius, turns, height, profile="exponential",
+                 spiral_type="logarithmic"):
+        c = np.array(center, dtype=np.float64)
+        turns = float(turns)
+        n = max(200, int(100 * turns))
+        theta = np.linspace(0, 2 * np.pi * turns, n)
+        ri, ro = float(inner_spiral_radius), float(outer_spiral_radius)
+        if spiral_type == "logarithmic":
+            r = ri * np.exp(np.log(ro / ri) / (2 * np.pi * turns) * theta)
+        else:
+            r = ri + (ro - ri) / (2 * np.pi * turns) * theta
+        self.path = np.stack([c[0] + r * np.cos(theta), c[1] + r * np.sin(theta)], axis=1)
+        t = np.linspace(0, 1, n)
+        r0, r1 = float(throat_radius), float(mouth_radius)
+        if profile == "exponential":
+            self.radii = r0 * (r1 / r0) ** t
+        elif profile == "linear":
+            self.radii = r0 + (r1 - r0) * t
+        else:
+            self.radii = r0 / (1 - t * (1 - r0 / r1))
+        self.height = float(height)
+
+    def sdf(self, points):
+        points = np.asarray(points, dtype=np.float64)
+        xy, z = points[:, :2], points[:, 2]
+        rd = _polyline_distance(xy, self.path) - _nearest_radius(xy, self.path, self.radii)
+        zd = np.maximum(0, np.maximum(-z, z - self.height))
+        inside = (z >= 0) & (z <= self.height)
+        return np.where(inside, rd, np.sqrt(rd**2 + zd**2))
+
+
+class _Smooth(SDFPrimitive):  # sdf.py:736-934
+    sign = -1.0  # -1: smooth minimum (union); +1: smooth maximum
+
+    def __init__(self, a, b, radius):
+        self.a, self.b, self.radius = a, b, radius
+
+    def _d2(self, points):
+        return self.b.sdf(points)
+
+    def sdf(self, points):
+        d1, d2 = self.a.sdf(points), self._d2(points)
+        h = np.clip(0.5 + 0.5 * (d2 - d1) / self.radius, 0, 1)
+        mix = d2 * (1 - h) + d1 * h
+        bump = self.radius * h * (1 - h)
+        return mix + bump if self.sign > 0 else mix - bump
+
+
+class SmoothUnion(_Smooth):
+    sign = -1.0
+
+
+class SmoothIntersection(_Smooth):
+    sign = 1.0
+
+
+class SmoothDifference(_Smooth):
+    sign = 1.0
+
+    def _d2(self, points):
+        return -self.b.sdf(points)
+
+
 class Union(SDFPrimitive):  # sdf.py:549-609
     def __init__(self, *children):
         self.children = children
@@ -1048,5 +1213,8 @@ def make_api():
         GaussianPulse=GaussianPulse,
         Box=Box, Sphere=Sphere, Cylinder=Cylinder, Union=Union, Intersection=Intersection,
         Difference=Difference, HelmholtzResonator=HelmholtzResonator, Pole=Pole,
+        Cone=Cone, Horn=Horn, HelicalTube=HelicalTube, SpiralHorn=SpiralHorn,
+        SmoothUnion=SmoothUnion, SmoothIntersection=SmoothIntersection,
+        SmoothDifference=SmoothDifference,
         PoleType=PoleType, SimpleMaterial=SimpleMaterial,
         MaterializedGeometry=MaterializedGeometry)

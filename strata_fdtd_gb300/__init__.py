@@ -19,8 +19,11 @@ from .microphones import Microphone
 from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
 from .membranes import CircularMembraneSource, MembraneSource, RectangularMembraneSource
 from .resonator import HelmholtzResonator, helmholtz_array
-from .sdf import (Box, CSGNode, Cylinder, Difference, Intersection, Rotate, Scale, SDFPrimitive,
-                  Sphere, Translate, Union, rotation_matrix)
+from .paths import HelixPath, SpiralPath, distance_to_polyline
+from .sdf import (Box, Cone, CSGNode, Cylinder, Difference, HelicalTube, Horn, Intersection,
+                  Rotate, Scale, SDFPrimitive, SmoothDifference, SmoothIntersection, SmoothUnion,
+                  Sphere, SpiralHorn, Translate, Union, conical_horn, exponential_horn,
+                  hyperbolic_horn, rotation_matrix, tractrix_horn)
 from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_native_kernels
 
 __version__ = "0.1.0"
@@ -30,7 +33,9 @@ __all__ = [
     "RigidBoundary", "ABCFirstOrder", "RadiationImpedance", "Pole",
     "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale", "Rotate",
-    "rotation_matrix",
+    "rotation_matrix", "Cone", "Horn", "SpiralHorn", "HelicalTube", "SmoothUnion",
+    "SmoothIntersection", "SmoothDifference", "conical_horn", "exponential_horn",
+    "hyperbolic_horn", "tractrix_horn", "SpiralPath", "HelixPath", "distance_to_polyline",
     "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",
     "NativeError", "BatchedSolver", "DifferentiableSolver", "MembraneSource",
     "CircularMembraneSource", "RectangularMembraneSource", "MaterializedGeometry",

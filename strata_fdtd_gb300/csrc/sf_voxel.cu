@@ -12,10 +12,24 @@
 //   Translate / Scale        sdf.py:1225-1236, 1285-1294
 //   Rotate                   sdf.py:1351-1355: point @ R (rows of R^T
 //                            dotted in the order ((p0 m0 + p1 m1) + p2 m2))
+//   Cone                     sdf.py:490-530  projection over the length,
+//                            linearly interpolated radius, capped ends
+//   Horn                     sdf.py:1085-1133  surface of revolution with
+//                            the conical / exponential / hyperbolic /
+//                            tractrix radius of sdf.py:1039-1060
+//   HelicalTube, SpiralHorn  sdf.py:1666-1695, 1505-1554: distance to a
+//                            polyline sampled on the host (paths.py:226-294)
+//                            minus the radius at the nearest sample, the
+//                            spiral in the xy plane and extruded over z
+//   SmoothUnion / SmoothIntersection / SmoothDifference  sdf.py:760-781,
+//                            827-847, 903-920: polynomial blends of two
 // np.linalg.norm over three components sums ((x0^2 + x1^2) + x2^2).  The
-// cylinder's axis projection uses np.dot (BLAS), whose rounding depends on
-// the BLAS build; here it is ((v0*a0 + v1*a1) + v2*a2), which equals any
-// BLAS result exactly when the axis is a coordinate axis.
+// axis projections of cylinders, cones, horns and path segments use np.dot
+// (BLAS), whose rounding depends on the BLAS build; here they are
+// ((v0*a0 + v1*a1) + v2*a2), which equals any BLAS result exactly when the
+// axis is a coordinate axis.  The horn radii call CUDA's exp, cosh and cos,
+// which may differ from NumPy's in the last place: masks can then differ
+// only at cells whose distance is within that rounding of zero.
 #include <cuda_runtime.h>
 
 #include "sf_common.cuh"
@@ -33,6 +47,52 @@ __device__ __forceinline__ double dmax(double a, double b) {  // np.maximum
 }
 __device__ __forceinline__ double dmin(double a, double b) {  // np.minimum
     return (a <= b || a != a) ? a : b;
+}
+
+__device__ __forceinline__ double clip01(double t) { return dmin(dmax(t, 0.0), 1.0); }
+
+// distance_to_polyline (paths.py:226-294) from (x, y, z) -- or (x, y) when
+// dims == 2 -- to the path in nodes d[0 .. m-1] (a = vertex, b = the vertex's
+// segment to the next one and s1 = its squared length, both computed on the
+// host as the reference does; s0 = the radius there), minus the radius at the
+// nearest vertex (the first of equal distances, as np.argmin).
+__device__ double path_distance(const sf_sdf_node* __restrict__ d, int m, int dims, double x,
+                                double y, double z) {
+    double best = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+    double near = best;
+    double radius = 0.0;
+    for (int q = 0; q < m; ++q) {
+        const sf_sdf_node& P = d[q];
+        const double w0 = d_sub(x, P.a[0]), w1 = d_sub(y, P.a[1]);
+        const double w2 = dims == 3 ? d_sub(z, P.a[2]) : 0.0;
+        // nearest vertex: norm(path - point), squares as those of point - path
+        const double dv = dims == 3 ? norm3(w0, w1, w2)
+                                    : __dsqrt_rn(d_add(d_mul(w0, w0), d_mul(w1, w1)));
+        if (dv < near) {
+            near = dv;
+            radius = P.s0;
+        }
+        if (q + 1 == m) break;
+        double ds;
+        if (P.s1 < 1e-14) {  // a degenerate segment is its first vertex
+            ds = dv;
+        } else {
+            double t = d_add(d_mul(w0, P.b[0]), d_mul(w1, P.b[1]));
+            if (dims == 3) t = d_add(t, d_mul(w2, P.b[2]));
+            const double tc = clip01(__ddiv_rn(t, P.s1));
+            const double c0 = d_add(P.a[0], d_mul(tc, P.b[0]));
+            const double c1 = d_add(P.a[1], d_mul(tc, P.b[1]));
+            if (dims == 3) {
+                const double c2 = d_add(P.a[2], d_mul(tc, P.b[2]));
+                ds = norm3(d_sub(x, c0), d_sub(y, c1), d_sub(z, c2));
+            } else {
+                const double e0 = d_sub(x, c0), e1 = d_sub(y, c1);
+                ds = __dsqrt_rn(d_add(d_mul(e0, e0), d_mul(e1, e1)));
+            }
+        }
+        best = dmin(best, ds);
+    }
+    return d_sub(best, radius);
 }
 
 __device__ double eval_sdf(const sf_sdf_node* __restrict__ prog, int n, double x, double y,
@@ -77,6 +137,84 @@ __device__ double eval_sdf(const sf_sdf_node* __restrict__ prog, int n, double x
                 const double rr = d_sub(radial, N.s1);
                 if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
                 ds[dtop++] = inside ? rr : __dsqrt_rn(d_add(d_mul(rr, rr), d_mul(axial, axial)));
+                break;
+            }
+            case 4: {  // CONE: a = p1, b = unit axis, s0 = length, s1 = r1; next node a[0] = r2 - r1
+                if (q + 1 >= n || prog[q + 1].op != 27) { *err = 4; return 1.0; }
+                const double dr = prog[q + 1].a[0];
+                ++q;
+                const double v0 = d_sub(X, N.a[0]), v1 = d_sub(Y, N.a[1]), v2 = d_sub(Z, N.a[2]);
+                const double L = N.s0;
+                const double t = __ddiv_rn(
+                    d_add(d_add(d_mul(v0, N.b[0]), d_mul(v1, N.b[1])), d_mul(v2, N.b[2])), L);
+                const double tc = clip01(t);
+                const double rt = d_add(N.s1, d_mul(tc, dr));
+                const double tl = d_mul(tc, L);
+                const double c0 = d_add(N.a[0], d_mul(tl, N.b[0]));
+                const double c1 = d_add(N.a[1], d_mul(tl, N.b[1]));
+                const double c2 = d_add(N.a[2], d_mul(tl, N.b[2]));
+                const double radial = norm3(d_sub(X, c0), d_sub(Y, c1), d_sub(Z, c2));
+                const double axial = d_mul(dmax(0.0, d_sub(fabs(d_sub(t, 0.5)), 0.5)), L);
+                const bool inside = (t >= 0.0) && (t <= 1.0);
+                const double rr = d_sub(radial, rt);
+                if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
+                ds[dtop++] = inside ? rr : __dsqrt_rn(d_add(d_mul(rr, rr), d_mul(axial, axial)));
+                break;
+            }
+            case 5: {  // HORN: a = throat, b = unit axis, s0 = length, s1 = throat radius,
+                       // n = profile; next node a[0] = m, alpha, alpha or R
+                if (q + 1 >= n || prog[q + 1].op != 27) { *err = 4; return 1.0; }
+                const double k = prog[q + 1].a[0];
+                ++q;
+                const double v0 = d_sub(X, N.a[0]), v1 = d_sub(Y, N.a[1]), v2 = d_sub(Z, N.a[2]);
+                const double L = N.s0;
+                const double t = d_add(d_add(d_mul(v0, N.b[0]), d_mul(v1, N.b[1])), d_mul(v2, N.b[2]));
+                const double tc = clip01(__ddiv_rn(t, L));
+                const double r = norm3(d_sub(v0, d_mul(t, N.b[0])), d_sub(v1, d_mul(t, N.b[1])),
+                                       d_sub(v2, d_mul(t, N.b[2])));
+                const double xa = d_mul(tc, L);
+                double hr;
+                if (N.n == 0) hr = d_mul(N.s1, d_add(1.0, d_mul(k, tc)));  // conical
+                else if (N.n == 1) hr = d_mul(N.s1, exp(d_mul(k, xa)));   // exponential
+                else if (N.n == 2) hr = d_mul(N.s1, cosh(d_mul(k, xa)));  // hyperbolic
+                else {                                                     // tractrix
+                    const double c = cos(__ddiv_rn(xa, k));
+                    hr = __ddiv_rn(N.s1, d_mul(c, c));
+                }
+                const double rd = d_sub(r, hr);
+                const double cap = dmax(-t, d_sub(t, L));
+                const bool inside = (t >= 0.0) && (t <= L);
+                if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
+                ds[dtop++] = inside ? rd : __dsqrt_rn(d_add(d_mul(rd, rd), d_mul(cap, cap)));
+                break;
+            }
+            case 6:    // TUBE along a 3-D path: n vertices in the next n nodes
+            case 7: {  // SPIRAL: the same in the xy plane, extruded over 0 <= z <= s0
+                if (N.n < 2 || q + N.n >= n) { *err = 4; return 1.0; }
+                const double rd = path_distance(prog + q + 1, N.n, N.op == 6 ? 3 : 2, X, Y, Z);
+                double d = rd;
+                if (N.op == 7) {
+                    const double zd = dmax(0.0, dmax(-Z, d_sub(Z, N.s0)));
+                    const bool inside = (Z >= 0.0) && (Z <= N.s0);
+                    d = inside ? rd : __dsqrt_rn(d_add(d_mul(rd, rd), d_mul(zd, zd)));
+                }
+                q += N.n;
+                if (dtop >= VX_DSTACK) { *err = 1; return 1.0; }
+                ds[dtop++] = d;
+                break;
+            }
+            case 13:    // SMOOTH_UNION: pop b, a; s0 = blend radius
+            case 14:    // SMOOTH_INTERSECTION
+            case 15: {  // SMOOTH_DIFFERENCE (the subtracted shape negated)
+                if (dtop < 2) { *err = 2; return 1.0; }
+                const double d1 = ds[dtop - 2];
+                const double d2 = (N.op == 15) ? -ds[dtop - 1] : ds[dtop - 1];
+                const double k = N.s0;
+                const double h = clip01(d_add(0.5, __ddiv_rn(d_mul(0.5, d_sub(d2, d1)), k)));
+                const double mix = d_add(d_mul(d2, d_sub(1.0, h)), d_mul(d1, h));
+                const double bump = d_mul(d_mul(k, h), d_sub(1.0, h));
+                dtop -= 2;
+                ds[dtop++] = (N.op == 13) ? d_sub(mix, bump) : d_add(mix, bump);
                 break;
             }
             case 10:    // UNION n

@@ -9,10 +9,11 @@ construction (centres, sizes, unit axes, lengths) runs on the host in the
 reference's own NumPy arithmetic, so the constants the kernel sees are the
 reference's constants.
 
-Supported: Box, Sphere, Cylinder, Union, Intersection, Difference, Translate,
+Supported: Box, Sphere, Cylinder, Cone, Horn (conical, exponential,
+hyperbolic, tractrix), SpiralHorn, HelicalTube, Union, Intersection,
+Difference, SmoothUnion, SmoothIntersection, SmoothDifference, Translate,
 Scale, Rotate (axis-angle or matrix, rotate_x/y/z), HelmholtzResonator
-(geometry/resonator.py).  Smooth CSG, cones and horns are outside the
-time-step path and raise on use.
+(geometry/resonator.py).
 """
 from __future__ import annotations
 
@@ -23,10 +24,11 @@ import numpy as np
 
 from . import _native
 
-OP_BOX, OP_SPHERE, OP_CYLINDER = 1, 2, 3
+OP_BOX, OP_SPHERE, OP_CYLINDER, OP_CONE, OP_HORN, OP_TUBE, OP_SPIRAL = 1, 2, 3, 4, 5, 6, 7
 OP_UNION, OP_INTERSECTION, OP_DIFFERENCE = 10, 11, 12
+OP_SMOOTH_UNION, OP_SMOOTH_INTERSECTION, OP_SMOOTH_DIFFERENCE = 13, 14, 15
 OP_PUSH_TRANSLATE, OP_PUSH_SCALE, OP_POP_POINT, OP_SCALE_DIST, OP_NEGATE = 20, 21, 22, 23, 24
-OP_PUSH_ROTATE, OP_ROTATE_ROW2 = 25, 26
+OP_PUSH_ROTATE, OP_ROTATE_ROW2, OP_DATA = 25, 26, 27
 
 
 def _node(op, n=0, a=(0.0, 0.0, 0.0), b=(0.0, 0.0, 0.0), s0=0.0, s1=0.0):
@@ -186,6 +188,229 @@ class Cylinder(SDFPrimitive):
         return np.minimum(self.p1, self.p2) - r, np.maximum(self.p1, self.p2) + r
 
 
+class Cone(SDFPrimitive):
+    """Frustum from radius r1 at p1 to r2 at p2, either radius may be zero
+    (sdf.py:436-541)."""
+
+    def __init__(self, p1, p2, r1, r2):
+        self.p1 = np.array(p1, dtype=np.float64)
+        self.p2 = np.array(p2, dtype=np.float64)
+        self.r1, self.r2 = float(r1), float(r2)
+        if self.r1 < 0 or self.r2 < 0:
+            raise ValueError(f"Cone radii must be non-negative, got r1={r1}, r2={r2}")
+        if self.r1 == 0 and self.r2 == 0:
+            raise ValueError("Cone cannot have both radii zero")
+        self.axis = self.p2 - self.p1
+        self.length = np.linalg.norm(self.axis)
+        if self.length == 0:
+            raise ValueError("Cone endpoints must be distinct")
+        self.axis_normalized = self.axis / self.length
+
+    def _emit(self, prog):
+        prog.append(_node(OP_CONE, a=self.p1, b=self.axis_normalized, s0=self.length,
+                          s1=self.r1))
+        prog.append(_node(OP_DATA, a=(self.r2 - self.r1, 0.0, 0.0)))
+
+    @property
+    def bounding_box(self):
+        r = np.array([max(self.r1, self.r2)] * 3)
+        return np.minimum(self.p1, self.p2) - r, np.maximum(self.p1, self.p2) + r
+
+
+_HORN_PROFILES = ("conical", "exponential", "hyperbolic", "tractrix")
+
+
+class Horn(SDFPrimitive):
+    """Horn from throat to mouth, a surface of revolution whose radius
+    follows a conical, exponential, hyperbolic or tractrix flare
+    (sdf.py:937-1148)."""
+
+    def __init__(self, throat_position, mouth_position, throat_radius, mouth_radius,
+                 profile="exponential"):
+        if profile not in _HORN_PROFILES:
+            raise ValueError(f"profile must be one of {set(_HORN_PROFILES)}, got '{profile}'")
+        self.throat_position = np.array(throat_position, dtype=np.float64)
+        self.mouth_position = np.array(mouth_position, dtype=np.float64)
+        self.throat_radius, self.mouth_radius = float(throat_radius), float(mouth_radius)
+        self.profile = profile
+        if self.throat_radius <= 0 or self.mouth_radius <= 0:
+            raise ValueError(f"Horn radii must be positive, got throat={throat_radius}, "
+                             f"mouth={mouth_radius}")
+        axis = self.mouth_position - self.throat_position
+        self._length = np.linalg.norm(axis)
+        if self._length == 0:
+            raise ValueError("Horn throat and mouth positions must be distinct")
+        self._axis = axis / self._length
+        # flare constant from the area ratio (sdf.py:1013-1037)
+        a0 = np.pi * self.throat_radius ** 2
+        am = np.pi * self.mouth_radius ** 2
+        L = self._length
+        if profile == "conical":  # A = A0 (1 + m t)^2
+            self._m = np.sqrt(am / a0) - 1
+        elif profile == "exponential":  # A = A0 exp(2 alpha x)
+            self._alpha = np.log(am / a0) / (2 * L)
+        elif profile == "hyperbolic":  # A = A0 cosh^2(alpha x)
+            self._alpha = np.arccosh(np.sqrt(am / a0)) / L
+        else:  # A = A0 / cos^4(x / R)
+            self._R = L / np.arccos(np.power(a0 / am, 0.25))
+
+    def _flare(self):
+        return {"conical": getattr(self, "_m", 0.0), "exponential": getattr(self, "_alpha", 0.0),
+                "hyperbolic": getattr(self, "_alpha", 0.0),
+                "tractrix": getattr(self, "_R", 0.0)}[self.profile]
+
+    def radius_at_position(self, t):
+        """Radius at normalised axial position t (0 throat, 1 mouth)."""
+        t = np.asarray(t)
+        x = t * self._length
+        if self.profile == "conical":
+            return self.throat_radius * (1 + self._m * t)
+        if self.profile == "exponential":
+            return self.throat_radius * np.exp(self._alpha * x)
+        if self.profile == "hyperbolic":
+            return self.throat_radius * np.cosh(self._alpha * x)
+        return self.throat_radius / np.cos(x / self._R) ** 2
+
+    @property
+    def cutoff_frequency(self) -> float:
+        """Low-frequency cutoff in Hz at c = 343 m/s (sdf.py:1061-1083)."""
+        c = 343.0
+        if self.profile == "conical":
+            return c / (2 * np.pi * self._length)
+        if self.profile in ("exponential", "hyperbolic"):
+            return c * self._alpha / (2 * np.pi)
+        return c / (4 * self._R)
+
+    def _emit(self, prog):
+        prog.append(_node(OP_HORN, n=_HORN_PROFILES.index(self.profile), a=self.throat_position,
+                          b=self._axis, s0=self._length, s1=self.throat_radius))
+        prog.append(_node(OP_DATA, a=(float(self._flare()), 0.0, 0.0)))
+
+    @property
+    def bounding_box(self):
+        r = np.array([self.mouth_radius] * 3)
+        return (np.minimum(self.throat_position, self.mouth_position) - r,
+                np.maximum(self.throat_position, self.mouth_position) + r)
+
+
+def conical_horn(throat_pos, mouth_pos, throat_r, mouth_r) -> Horn:
+    return Horn(throat_pos, mouth_pos, throat_r, mouth_r, "conical")
+
+
+def exponential_horn(throat_pos, mouth_pos, throat_r, mouth_r) -> Horn:
+    return Horn(throat_pos, mouth_pos, throat_r, mouth_r, "exponential")
+
+
+def hyperbolic_horn(throat_pos, mouth_pos, throat_r, mouth_r) -> Horn:
+    return Horn(throat_pos, mouth_pos, throat_r, mouth_r, "hyperbolic")
+
+
+def tractrix_horn(throat_pos, mouth_pos, throat_r, mouth_r) -> Horn:
+    return Horn(throat_pos, mouth_pos, throat_r, mouth_r, "tractrix")
+
+
+def _emit_path(prog, op, vertices, radii, s0=0.0):
+    """A path shape: the header, then one node per vertex with the vertex, its
+    radius and its segment to the next vertex with the squared length (in the
+    reference's NumPy arithmetic, paths.py:276-281)."""
+    v = np.asarray(vertices, dtype=np.float64)
+    prog.append(_node(op, n=len(v), s0=s0))
+    for q in range(len(v)):
+        a = tuple(v[q]) + (0.0,) * (3 - v.shape[1])
+        if q + 1 < len(v):
+            seg = v[q + 1] - v[q]
+            ll = np.dot(seg, seg)
+            b = tuple(seg) + (0.0,) * (3 - v.shape[1])
+        else:
+            b, ll = (0.0, 0.0, 0.0), 0.0
+        prog.append(_node(OP_DATA, a=a, b=b, s0=float(radii[q]), s1=float(ll)))
+
+
+class SpiralHorn(SDFPrimitive):
+    """Horn along a spiral in the xy plane, extruded over 0 <= z <= height:
+    distance to the sampled spiral minus the radius at the nearest sample
+    (sdf.py:1392-1576)."""
+
+    def __init__(self, center, throat_radius, mouth_radius, inner_spiral_radius,
+                 outer_spiral_radius, turns, height, profile="exponential",
+                 spiral_type="logarithmic"):
+        from .paths import SpiralPath
+
+        self.center_2d = np.array(center, dtype=np.float64)
+        self.throat_radius, self.mouth_radius = float(throat_radius), float(mouth_radius)
+        self.inner_spiral_radius = float(inner_spiral_radius)
+        self.outer_spiral_radius = float(outer_spiral_radius)
+        self.turns, self.height = float(turns), float(height)
+        self.profile, self.spiral_type = profile, spiral_type
+        if self.throat_radius <= 0 or self.mouth_radius <= 0:
+            raise ValueError("Throat and mouth radii must be positive")
+        if self.height <= 0:
+            raise ValueError("Height must be positive")
+        if profile not in ("exponential", "linear", "hyperbolic"):
+            raise ValueError("profile must be 'exponential', 'linear', or 'hyperbolic'")
+        self.spiral = SpiralPath(center=self.center_2d, inner_radius=self.inner_spiral_radius,
+                                 outer_radius=self.outer_spiral_radius, turns=self.turns,
+                                 spiral_type=spiral_type)
+        n = max(200, int(100 * self.turns))  # about 100 samples per turn
+        self.path_2d = self.spiral.sample_points(n)
+        t = np.linspace(0, 1, n)
+        r0, r1 = self.throat_radius, self.mouth_radius
+        if profile == "exponential":
+            self.radii = r0 * (r1 / r0) ** t
+        elif profile == "linear":
+            self.radii = r0 + (r1 - r0) * t
+        else:
+            self.radii = r0 / (1 - t * (1 - r0 / r1))
+
+    def _emit(self, prog):
+        _emit_path(prog, OP_SPIRAL, self.path_2d, self.radii, s0=self.height)
+
+    @property
+    def bounding_box(self):
+        e = self.outer_spiral_radius + max(self.throat_radius, self.mouth_radius)
+        return (np.array([self.center_2d[0] - e, self.center_2d[1] - e, 0.0]),
+                np.array([self.center_2d[0] + e, self.center_2d[1] + e, self.height]))
+
+
+class HelicalTube(SDFPrimitive):
+    """Tube along a helix, its radius tapering linearly from start to end:
+    distance to the sampled helix minus the radius at the nearest sample
+    (sdf.py:1579-1721)."""
+
+    def __init__(self, center, helix_radius, tube_radius_start, tube_radius_end, pitch, turns):
+        from .paths import HelixPath
+
+        self.center = np.array(center, dtype=np.float64)
+        self.helix_radius = float(helix_radius)
+        self.tube_radius_start, self.tube_radius_end = float(tube_radius_start), float(tube_radius_end)
+        self.pitch, self.turns = float(pitch), float(turns)
+        if self.helix_radius <= 0:
+            raise ValueError("helix_radius must be positive")
+        if self.tube_radius_start <= 0 or self.tube_radius_end <= 0:
+            raise ValueError("tube radii must be positive")
+        if self.pitch <= 0:
+            raise ValueError("pitch must be positive")
+        if self.turns <= 0:
+            raise ValueError("turns must be positive")
+        self.helix = HelixPath(center=self.center, radius=self.helix_radius, pitch=self.pitch,
+                               turns=self.turns)
+        n = max(200, int(100 * self.turns))
+        self.path_3d = self.helix.sample_points(n)
+        t = np.linspace(0, 1, n)
+        self.tube_radii = (self.tube_radius_start
+                           + (self.tube_radius_end - self.tube_radius_start) * t)
+
+    def _emit(self, prog):
+        _emit_path(prog, OP_TUBE, self.path_3d, self.tube_radii)
+
+    @property
+    def bounding_box(self):
+        e = self.helix_radius + max(self.tube_radius_start, self.tube_radius_end)
+        return (np.array([self.center[0] - e, self.center[1] - e, self.center[2]]),
+                np.array([self.center[0] + e, self.center[1] + e,
+                          self.center[2] + self.helix.total_height]))
+
+
 def _emit_fold(prog, children, op):
     """Emit an n-ary CSG node as a left fold of two-operand steps
     (c0, c1, op, c2, op, ...): the reference folds its children in the same
@@ -256,6 +481,72 @@ class Difference(CSGNode):
     @cached_property
     def bounding_box(self):
         return self.base.bounding_box
+
+
+class SmoothUnion(CSGNode):
+    """Union of two shapes blended over ``radius`` by the polynomial smooth
+    minimum (sdf.py:736-800)."""
+
+    def __init__(self, a, b, radius):
+        if radius <= 0:
+            raise ValueError(f"radius must be positive, got {radius}")
+        self.a, self.b, self.radius = a, b, radius
+
+    def _emit(self, prog):
+        self.a._emit(prog)
+        self.b._emit(prog)
+        prog.append(_node(OP_SMOOTH_UNION, s0=self.radius))
+
+    @cached_property
+    def bounding_box(self):
+        (la, ha), (lb, hb) = self.a.bounding_box, self.b.bounding_box
+        r = np.array([self.radius] * 3)
+        return np.minimum(la, lb) - r, np.maximum(ha, hb) + r
+
+
+class SmoothIntersection(CSGNode):
+    """Intersection blended by the polynomial smooth maximum
+    (sdf.py:803-877)."""
+
+    def __init__(self, a, b, radius):
+        if radius <= 0:
+            raise ValueError(f"radius must be positive, got {radius}")
+        self.a, self.b, self.radius = a, b, radius
+
+    def _emit(self, prog):
+        self.a._emit(prog)
+        self.b._emit(prog)
+        prog.append(_node(OP_SMOOTH_INTERSECTION, s0=self.radius))
+
+    @cached_property
+    def bounding_box(self):
+        (la, ha), (lb, hb) = self.a.bounding_box, self.b.bounding_box
+        r = np.array([self.radius] * 3)
+        lo, hi = np.maximum(la, lb) + r, np.minimum(ha, hb) - r
+        if np.any(lo > hi):
+            return np.array([np.inf] * 3), np.array([-np.inf] * 3)
+        return lo, hi
+
+
+class SmoothDifference(CSGNode):
+    """``base`` minus ``subtracted``, blended as the smooth intersection with
+    the subtracted shape's complement (sdf.py:880-934)."""
+
+    def __init__(self, base, subtracted, radius):
+        if radius <= 0:
+            raise ValueError(f"radius must be positive, got {radius}")
+        self.base, self.subtracted, self.radius = base, subtracted, radius
+
+    def _emit(self, prog):
+        self.base._emit(prog)
+        self.subtracted._emit(prog)
+        prog.append(_node(OP_SMOOTH_DIFFERENCE, s0=self.radius))
+
+    @cached_property
+    def bounding_box(self):
+        lo, hi = self.base.bounding_box
+        r = np.array([self.radius] * 3)
+        return lo - r, hi + r
 
 
 class Transform(SDFPrimitive):

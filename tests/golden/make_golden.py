@@ -67,6 +67,9 @@ def load_reference():
         GaussianPulse=sf.GaussianPulse, Box=sdf.Box, Sphere=sdf.Sphere,
         Cylinder=sdf.Cylinder, Union=sdf.Union, Intersection=sdf.Intersection,
         Difference=sdf.Difference, HelmholtzResonator=resonator.HelmholtzResonator,
+        Cone=sdf.Cone, Horn=sdf.Horn, SpiralHorn=sdf.SpiralHorn, HelicalTube=sdf.HelicalTube,
+        SmoothUnion=sdf.SmoothUnion, SmoothIntersection=sdf.SmoothIntersection,
+        SmoothDifference=sdf.SmoothDifference,
         Pole=base.Pole, PoleType=base.PoleType, SimpleMaterial=base.SimpleMaterial,
         MaterializedGeometry=material_assignment.MaterializedGeometry,
         kernels=mod, solver_module=sys.modules["strata_fdtd.core.solver"])

@@ -233,3 +233,40 @@ def test_differentiable_source_table_matches_per_step_calls():
             per.append(stub.pulse.waveform(np.array([t]), stub.dt)[0])
             t += stub.dt
         np.testing.assert_array_equal(got.view(np.int64), np.array(per).view(np.int64))
+
+
+def test_curved_shape_constants_match_oracle_construction():
+    """The host-side constants the voxeliser receives for the curved shapes
+    (horn flare constants, sampled spiral and helix vertices and their radii)
+    are the oracle's, computed with the same NumPy calls."""
+    from oracle import oracle as O
+
+    for prof in ("conical", "exponential", "hyperbolic", "tractrix"):
+        a = S.Horn((0.0, 0.0, 0.04), (0.0, 0.0, 0.0), 0.004, 0.012, prof)
+        b = O.Horn((0.0, 0.0, 0.04), (0.0, 0.0, 0.0), 0.004, 0.012, prof)
+        assert a._flare() == b.k
+        assert a.cutoff_frequency > 0
+        np.testing.assert_allclose(a.radius_at_position([0.0, 1.0]), [0.004, 0.012], rtol=1e-12)
+    for spiral in ("logarithmic", "archimedean"):
+        for prof in ("exponential", "linear", "hyperbolic"):
+            a = S.SpiralHorn((0.03, 0.03), 0.003, 0.006, 0.008, 0.022, 2.3, 0.02, prof, spiral)
+            b = O.SpiralHorn((0.03, 0.03), 0.003, 0.006, 0.008, 0.022, 2.3, 0.02, prof, spiral)
+            np.testing.assert_array_equal(a.path_2d, b.path)
+            np.testing.assert_array_equal(a.radii, b.radii)
+            assert len(a.path_2d) == max(200, int(100 * 2.3))  # 229: int() truncates
+            assert a.program()[1] == 1 + len(a.path_2d)
+    a = S.HelicalTube((0.025, 0.025, 0.004), 0.013, 0.003, 0.005, 0.012, 2.0)
+    b = O.HelicalTube((0.025, 0.025, 0.004), 0.013, 0.003, 0.005, 0.012, 2.0)
+    np.testing.assert_array_equal(a.path_3d, b.path)
+    np.testing.assert_array_equal(a.tube_radii, b.radii)
+    assert a.helix.total_height == pytest.approx(0.024)
+    pts = np.random.default_rng(1).uniform(0, 0.05, (200, 3))
+    np.testing.assert_array_equal(S.distance_to_polyline(pts, a.path_3d),
+                                  O._polyline_distance(pts, b.path))
+    for bad in (dict(r1=0.0, r2=0.0), dict(r1=-1.0, r2=0.1)):
+        with pytest.raises(ValueError):
+            S.Cone((0, 0, 0), (0, 0, 1), **bad)
+    with pytest.raises(ValueError):
+        S.Horn((0, 0, 0), (0, 0, 1), 0.1, 0.2, "parabolic")
+    with pytest.raises(ValueError):
+        S.SmoothUnion(S.Sphere((0, 0, 0), 1.0), S.Sphere((1, 0, 0), 1.0), 0.0)

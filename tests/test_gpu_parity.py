@@ -24,6 +24,9 @@ API = types.SimpleNamespace(
     FDTDSolver=S.FDTDSolver, UniformGrid=S.UniformGrid, PML=S.PML, GaussianPulse=S.GaussianPulse,
     Box=S.Box, Sphere=S.Sphere, Cylinder=S.Cylinder, Union=S.Union, Intersection=S.Intersection,
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
+    Cone=S.Cone, Horn=S.Horn, SpiralHorn=S.SpiralHorn, HelicalTube=S.HelicalTube,
+    SmoothUnion=S.SmoothUnion, SmoothIntersection=S.SmoothIntersection,
+    SmoothDifference=S.SmoothDifference,
     PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
     MaterializedGeometry=S.MaterializedGeometry,
     ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance,
@@ -246,7 +249,7 @@ def test_voxelize_matches_reference(name):
     grid = S.UniformGrid(shape, res)
     mask = C.sdf_tree(API, which).voxelize(grid)
     ref = np.unpackbits(golden("voxel")["mask__" + name])[: mask.size].reshape(shape).astype(bool)
-    if which in ("cyl_oblique", "rotated"):
+    if which in C.VOXEL_ROUNDING_CASES:
         # np.dot / matmul round through BLAS; only cells within rounding of a surface may differ
         diff = mask != ref
         if diff.any():
@@ -604,3 +607,16 @@ def test_graph_replays_follow_table_changes_against_oracle():
     for name in ref.get_probe_data():
         np.testing.assert_array_equal(s.get_probe_data()[name], ref.get_probe_data()[name],
                                       err_msg=name)
+
+
+@pytest.mark.parametrize("which", ["cone_smooth", "horns", "horn_oblique", "spiral_horn",
+                                   "helical_tube"])
+def test_curved_shapes_point_evaluation_matches_oracle(which):
+    """Cones, horns, the smooth blends and the path-swept shapes evaluated at
+    random points on the GPU against the oracle's NumPy restatement, within
+    the rounding of BLAS dot products and transcendental functions."""
+    pts = np.random.default_rng(7).uniform(-0.005, 0.065, (3000, 3))
+    got = C.sdf_tree(API, which).sdf(pts)
+    want = C.sdf_tree(ORACLE, which).sdf(pts)
+    assert np.all(np.isfinite(want))
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-15)
