@@ -16,7 +16,7 @@ from .boundaries import PML, ABCFirstOrder, RadiationImpedance, RigidBoundary
 from .grid import NonuniformGrid, UniformGrid
 from .material_assignment import MaterializedGeometry, MaterialVolume
 from .microphones import Microphone
-from .materials import AIR_20C, Pole, PoleType, SimpleMaterial
+from .materials import AIR_20C, AcousticMaterial, Material, Pole, PoleType, SimpleMaterial
 from .membranes import CircularMembraneSource, MembraneSource, RectangularMembraneSource
 from .resonator import HelmholtzResonator, helmholtz_array
 from .paths import HelixPath, SpiralPath, distance_to_polyline
@@ -31,7 +31,7 @@ __version__ = "0.1.0"
 __all__ = [
     "FDTDSolver", "GaussianPulse", "Probe", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
     "RigidBoundary", "ABCFirstOrder", "RadiationImpedance", "Pole",
-    "PoleType", "SimpleMaterial", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
+    "PoleType", "SimpleMaterial", "AcousticMaterial", "Material", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale", "Rotate",
     "rotation_matrix", "Cone", "Horn", "SpiralHorn", "HelicalTube", "SmoothUnion",
     "SmoothIntersection", "SmoothDifference", "conical_horn", "exponential_horn",

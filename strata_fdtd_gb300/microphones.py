@@ -186,9 +186,97 @@ class Microphone:
         return self._data
 
     def get_waveform(self, weighting=None) -> np.ndarray:
-        if weighting not in (None, "Z"):
-            raise NotImplementedError("frequency weighting is outside the GB300 path")
-        return np.array(self.data, dtype=np.float32)
+        """The recorded pressure (float32), A- or C-weighted when asked
+        (core/solver.py:1175-1206)."""
+        waveform = np.array(self.data, dtype=np.float32)
+        if weighting in ("Z", None) or len(waveform) == 0:
+            return waveform
+        from .weighting import apply_weighting
+
+        return apply_weighting(waveform, self.get_sample_rate(), weighting).astype(np.float32)
+
+    def _recorded(self):
+        if len(self.data) == 0:
+            raise RuntimeError("No data recorded. Run simulation first.")
+
+    def get_spl(self, weighting=None, p_ref: float = 2e-5) -> float:
+        """Sound pressure level of the recording in dB (core/solver.py:1226-1258)."""
+        from .weighting import calculate_spl
+
+        self._recorded()
+        return calculate_spl(self.get_waveform(weighting=weighting), p_ref)
+
+    def get_leq(self, weighting=None, duration: float | None = None,
+                p_ref: float = 2e-5) -> float:
+        """Equivalent continuous level, over the latest ``duration`` seconds
+        when given (core/solver.py:1260-1296)."""
+        from .weighting import calculate_leq
+
+        self._recorded()
+        return calculate_leq(self.get_waveform(weighting=weighting), self.get_sample_rate(),
+                             duration, p_ref)
+
+    def get_time_weighted_level(self, weighting=None, time_constant: str = "fast",
+                                p_ref: float = 2e-5) -> np.ndarray:
+        """Fast / slow / impulse time-weighted level per sample
+        (core/solver.py:1298-1335)."""
+        from .weighting import calculate_time_weighted_level
+
+        self._recorded()
+        return calculate_time_weighted_level(self.get_waveform(weighting=weighting),
+                                             self.get_sample_rate(), time_constant, p_ref)
+
+    def to_wav(self, filepath: str, sample_rate: int = 44100, normalize: bool = True,
+               bit_depth: int = 16) -> None:
+        """Mono WAV of the recording, linearly resampled to ``sample_rate``
+        when the step rate differs by more than 1 Hz, peak-normalised to 0.95
+        (core/solver.py:1337-1418)."""
+        import wave
+
+        self._recorded()
+        if bit_depth not in (16, 32):
+            raise ValueError("bit_depth must be 16 or 32")
+        waveform = self.get_waveform()
+        if self._solver_dt is not None:
+            rate = 1.0 / self._solver_dt
+            if abs(rate - sample_rate) > 1.0:
+                n = int(len(waveform) * sample_rate / rate)
+                if n != len(waveform):
+                    waveform = np.interp(np.linspace(0, len(waveform) - 1, n),
+                                         np.arange(len(waveform)), waveform).astype(np.float32)
+        if normalize:
+            peak = np.max(np.abs(waveform))
+            if peak > 0:
+                waveform = waveform / peak * 0.95
+        dtype, full = (np.int16, 32767) if bit_depth == 16 else (np.int32, 2147483647)
+        with wave.open(filepath, "wb") as out:
+            out.setnchannels(1)
+            out.setsampwidth(bit_depth // 8)
+            out.setframerate(sample_rate)
+            out.writeframes((waveform * full).astype(dtype).tobytes())
+
+    def record(self, pressure_field, time: float, vx=None, vy=None, vz=None) -> None:
+        """Record one sample from host fields, as the reference's Python path
+        does (core/solver.py:1004-1058): the pressure (and, for a directional
+        pattern, the three velocities) interpolated with the microphone's
+        weights, combined with its polar pattern."""
+        if getattr(self, "_grid_position", None) is None:
+            raise RuntimeError("Microphone not initialized. Add to solver first.")
+        p = np.asarray(pressure_field)
+        fields = [p]
+        if self.is_directional():
+            if vx is None or vy is None or vz is None:
+                raise ValueError("Velocity fields (vx, vy, vz) are required for directional "
+                                 "microphones")
+            fields += [np.asarray(vx), np.asarray(vy), np.asarray(vz)]
+        row = []
+        for f, cells, w in self._rows(p.shape, python_path=True):
+            acc = np.float32(0.0)
+            flat = fields[f].reshape(-1)
+            for c, wc in zip(cells, w):
+                acc = np.float32(acc + np.float32(wc * flat[c]))
+            row.append(acc)
+        self._append(np.array([row], dtype=np.float32), [float(time)])
 
     def get_time_axis(self) -> np.ndarray:
         self.data  # noqa: B018 - flushes pending samples

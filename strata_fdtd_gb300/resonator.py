@@ -98,6 +98,13 @@ class HelmholtzResonator(SDFPrimitive):
         S, V, L = self.neck_area, self.cavity_volume, self.effective_neck_length
         return float((SPEED_OF_SOUND / (2 * np.pi)) * np.sqrt(S / (V * L)))
 
+    @property
+    def quality_factor(self) -> float:
+        """The reference's placeholder Q estimate: a constant 10
+        (resonator.py:281-297; a real Q needs the neck's viscothermal
+        losses)."""
+        return 10.0
+
 
 def helmholtz_array(region, frequency_range, n_resonators, spacing="log", cavity_shape="box",
                     neck_length=0.01, neck_radius=0.003):

@@ -276,6 +276,54 @@ def host_values(api, manifest):
     np.savez_compressed(os.path.join(HERE, "host_values.npz"), **out)
 
 
+def analysis_values(api, manifest):
+    """Host-side quantities around the solve, from the reference's own code:
+    A/C weighting filters and sound levels (analysis/weighting.py), the
+    frequency-domain material properties (materials/base.py:215-507) and the
+    horn flare functions (geometry/sdf.py:1039-1083)."""
+    import strata_fdtd.analysis.weighting as W
+
+    out = {}
+    dt = 0.5 * (1e-3 / (343.0 * np.sqrt(3)))
+    for fs in (48000.0, 1.0 / dt):
+        for w in ("A", "C"):
+            out[f"sos_{w}__{int(fs)}"] = W.get_weighting_sos(w, fs)
+    rng = np.random.default_rng(5)
+    fs = 48000.0
+    tt = np.arange(4800) / fs
+    wave = (0.3 * np.sin(2 * np.pi * 90 * tt) + 0.2 * np.sin(2 * np.pi * 1000 * tt)
+            + 0.05 * np.sin(2 * np.pi * 9000 * tt) + 0.01 * rng.standard_normal(tt.size))
+    wave = wave.astype(np.float32)
+    out["level_wave"] = wave
+    for w in ("A", "C", None):
+        key = w or "Z"
+        weighted = W.apply_weighting(wave, fs, w)
+        out[f"weighted__{key}"] = weighted[::8]  # every 8th sample kept
+        out[f"spl__{key}"] = np.array([W.calculate_spl(weighted)])
+        out[f"leq_005__{key}"] = np.array([W.calculate_leq(weighted, fs, 0.05)])
+        for tc in ("fast", "slow", "impulse"):
+            out[f"twl_{tc}__{key}"] = W.calculate_time_weighted_level(weighted, fs, tc)[::16]
+    mat = api.SimpleMaterial(name="m", _rho=1.3, _c=330.0, _poles=[
+        api.Pole(pole_type=api.PoleType.DEBYE, delta_chi=0.4, target="density", tau=2e-4),
+        api.Pole(pole_type=api.PoleType.LORENTZ, delta_chi=0.25, target="modulus",
+                 omega_0=2 * np.pi * 2000.0, gamma=900.0)])
+    om = 2 * np.pi * np.array([50.0, 300.0, 1000.0, 2000.0, 4500.0, 12000.0])
+    out["mat_omega"] = om
+    for name in ("effective_density", "effective_modulus", "wavenumber", "phase_velocity",
+                 "group_velocity", "impedance", "attenuation", "attenuation_db_per_meter"):
+        out[f"mat_{name}"] = np.asarray(getattr(mat, name)(om))
+    out["mat_reflection"] = mat.reflection_coefficient(om, 415.0)
+    out["mat_absorption"] = mat.absorption_coefficient(om, 415.0)
+    out["mat_scalars"] = np.array([mat.c_inf, mat.Z_inf,
+                                   api.SimpleMaterial.from_impedance("w", 998.0, 1.48e6).c_inf])
+    ts = np.linspace(0, 1, 11)
+    for prof in ("conical", "exponential", "hyperbolic", "tractrix"):
+        h = api.Horn((0.0, 0.0, 0.05), (0.0, 0.0, 0.0), 0.006, 0.02, prof)
+        out[f"horn_{prof}"] = np.concatenate([[h.cutoff_frequency], h.radius_at_position(ts)])
+    np.savez_compressed(os.path.join(HERE, "analysis_values.npz"), **out)
+    manifest["analysis_values"] = dict(keys=sorted(out))
+
+
 def main():
     only = set(sys.argv[1:])
     api = load_reference()
@@ -294,6 +342,8 @@ def main():
         voxel_cases(api, manifest)
     if not only or "host" in only:
         host_values(api, manifest)
+    if not only or "analysis" in only:
+        analysis_values(api, manifest)
     with open(mpath, "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
 

@@ -1,0 +1,129 @@
+"""Host-side quantities around the solve against values the reference's own
+code produced (tests/golden/analysis_values.npz, tests/golden/make_golden.py
+``analysis``): A/C frequency weighting and sound levels (analysis/
+weighting.py), the frequency-domain material properties (materials/
+base.py:215-507), the horn flare functions (geometry/sdf.py:1039-1083), and
+the microphone's level, WAV and host-record methods on a recorded waveform.
+Tolerance: rel 1e-12 (the same SciPy and NumPy calls; only the filter gain
+is formed in a different expression)."""
+import wave
+
+import numpy as np
+import pytest
+
+import strata_fdtd_gb300 as S
+from conftest import golden
+from strata_fdtd_gb300 import weighting as W
+
+pytest.importorskip("scipy")
+G = golden("analysis_values")
+RTOL = 1e-12
+
+
+def test_weighting_filters_and_levels_match_reference():
+    dt = 0.5 * (1e-3 / (343.0 * np.sqrt(3)))
+    for fs in (48000.0, 1.0 / dt):
+        for w in ("A", "C"):
+            np.testing.assert_allclose(W.get_weighting_sos(w, fs), G[f"sos_{w}__{int(fs)}"],
+                                       rtol=RTOL, atol=1e-300)
+    wave_ = G["level_wave"]
+    fs = 48000.0
+    for w in ("A", "C", None):
+        key = w or "Z"
+        weighted = W.apply_weighting(wave_, fs, w)
+        np.testing.assert_allclose(weighted[::8], G[f"weighted__{key}"], rtol=1e-9, atol=1e-15)
+        assert W.calculate_spl(weighted) == pytest.approx(float(G[f"spl__{key}"][0]), rel=RTOL)
+        assert W.calculate_leq(weighted, fs, 0.05) == pytest.approx(
+            float(G[f"leq_005__{key}"][0]), rel=RTOL)
+        for tc in ("fast", "slow", "impulse"):
+            np.testing.assert_allclose(W.calculate_time_weighted_level(weighted, fs, tc)[::16],
+                                       G[f"twl_{tc}__{key}"], rtol=1e-10)
+    assert W.calculate_spl(np.zeros(8)) == -np.inf
+    with pytest.raises(ValueError):
+        W.get_weighting_sos("B", fs)
+
+
+def test_material_properties_match_reference():
+    mat = S.SimpleMaterial(name="m", _rho=1.3, _c=330.0, _poles=[
+        S.Pole(S.PoleType.DEBYE, delta_chi=0.4, target="density", tau=2e-4),
+        S.Pole(S.PoleType.LORENTZ, delta_chi=0.25, target="modulus", omega_0=2 * np.pi * 2000.0,
+               gamma=900.0)])
+    om = G["mat_omega"]
+    for name in ("effective_density", "effective_modulus", "wavenumber", "phase_velocity",
+                 "group_velocity", "impedance", "attenuation", "attenuation_db_per_meter"):
+        np.testing.assert_allclose(getattr(mat, name)(om), G[f"mat_{name}"], rtol=1e-9,
+                                   err_msg=name)
+    np.testing.assert_allclose(mat.reflection_coefficient(om, 415.0), G["mat_reflection"],
+                               rtol=1e-12)
+    np.testing.assert_allclose(mat.absorption_coefficient(om, 415.0), G["mat_absorption"],
+                               rtol=1e-12)
+    want = G["mat_scalars"]
+    assert mat.c_inf == want[0] and mat.Z_inf == want[1]
+    assert S.SimpleMaterial.from_impedance("w", 998.0, 1.48e6).c_inf == want[2]
+    assert isinstance(mat, S.AcousticMaterial)
+    assert mat.n_density_poles() == 1 and mat.n_modulus_poles() == 1
+    assert "Poles: 2 (1 density, 1 modulus)" in mat.summary()
+
+
+def test_horn_flares_match_reference():
+    ts = np.linspace(0, 1, 11)
+    for prof in ("conical", "exponential", "hyperbolic", "tractrix"):
+        h = S.Horn((0.0, 0.0, 0.05), (0.0, 0.0, 0.0), 0.006, 0.02, prof)
+        want = G[f"horn_{prof}"]
+        assert h.cutoff_frequency == want[0]
+        np.testing.assert_array_equal(h.radius_at_position(ts), want[1:])
+
+
+class _Stub:
+    """The attributes a Microphone reads from its solver."""
+
+    def __init__(self, shape, dx, dt):
+        self.shape, self.dx, self.dt, self.rho, self.c = shape, dx, dt, 1.2, 343.0
+
+    def _flush_traces(self):
+        pass
+
+
+def test_microphone_levels_wav_and_host_record(tmp_path):
+    fs = 48000.0
+    mic = S.Microphone(position=(0.0105, 0.0113, 0.0097), name="m")
+    mic._initialize(_Stub((24, 24, 24), 1e-3, 1.0 / fs))
+    wave_ = G["level_wave"]
+    mic._data.extend(wave_.tolist())
+    mic._times.extend((np.arange(wave_.size) / fs).tolist())
+    for w in ("A", "C", None):
+        key = w or "Z"
+        assert mic.get_spl(weighting=w) == pytest.approx(
+            W.calculate_spl(W.apply_weighting(wave_, fs, w).astype(np.float32)), rel=RTOL)
+        assert mic.get_leq(weighting=w, duration=0.05) == pytest.approx(
+            float(G[f"leq_005__{key}"][0]), rel=1e-6)
+    assert mic.get_time_weighted_level(time_constant="slow").shape == wave_.shape
+    path = tmp_path / "m.wav"
+    mic.to_wav(str(path), sample_rate=48000, bit_depth=16)
+    with wave.open(str(path), "rb") as r:
+        assert (r.getnchannels(), r.getsampwidth(), r.getframerate()) == (1, 2, 48000)
+        frames = np.frombuffer(r.readframes(r.getnframes()), dtype=np.int16)
+    assert frames.size == wave_.size and np.abs(frames).max() == int(0.95 * 32767)
+    mic.to_wav(str(path), sample_rate=24000, bit_depth=32)
+    with wave.open(str(path), "rb") as r:
+        assert r.getnframes() == wave_.size // 2 and r.getsampwidth() == 4
+    with pytest.raises(ValueError):
+        mic.to_wav(str(path), bit_depth=24)
+    # one sample from host fields: the trilinear weights of the reference's
+    # Python path in float32, the same sum the GPU's microphone rows form
+    rng = np.random.default_rng(3)
+    p = rng.standard_normal((24, 24, 24)).astype(np.float32)
+    mic.clear()
+    mic.record(p, 0.0)
+    (_, cells, w), = mic._rows(p.shape, python_path=True)
+    acc = np.float32(0.0)
+    for c, wc in zip(cells, w):
+        acc = np.float32(acc + np.float32(wc * p.reshape(-1)[c]))
+    assert mic.get_waveform()[0] == acc
+    card = S.Microphone(position=(0.0105, 0.0113, 0.0097), pattern="cardioid",
+                        direction=(1.0, 0.0, 0.0))
+    card._initialize(_Stub((24, 24, 24), 1e-3, 1.0 / fs))
+    with pytest.raises(ValueError):
+        card.record(p, 0.0)
+    card.record(p, 0.0, vx=p, vy=p, vz=p)
+    assert len(card.get_waveform()) == 1
