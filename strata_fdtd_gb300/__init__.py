@@ -25,11 +25,12 @@ from .sdf import (Box, Cone, CSGNode, Cylinder, Difference, HelicalTube, Horn, I
                   Sphere, SpiralHorn, Translate, Union, conical_horn, exponential_horn,
                   hyperbolic_horn, rotation_matrix, tractrix_horn)
 from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_native_kernels
+from .waveforms import AudioFileWaveform
 
 __version__ = "0.1.0"
 
 __all__ = [
-    "FDTDSolver", "GaussianPulse", "Probe", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
+    "FDTDSolver", "GaussianPulse", "AudioFileWaveform", "Probe", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
     "RigidBoundary", "ABCFirstOrder", "RadiationImpedance", "Pole",
     "PoleType", "SimpleMaterial", "AcousticMaterial", "Material", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale", "Rotate",

@@ -127,3 +127,37 @@ def test_microphone_levels_wav_and_host_record(tmp_path):
         card.record(p, 0.0)
     card.record(p, 0.0, vx=p, vy=p, vz=p)
     assert len(card.get_waveform()) == 1
+
+
+def test_audio_file_waveform(tmp_path):
+    """AudioFileWaveform (core/waveforms.py): integer PCM scaled to [-1, 1),
+    channel mix or pick, trimming, Fourier resampling to the step rate,
+    zero past the end or wrapped when looping."""
+    from scipy import signal
+    from scipy.io import wavfile
+
+    sr = 8000
+    left = (np.arange(400) % 50 * 600 - 15000).astype(np.int16)
+    right = (-left // 2).astype(np.int16)
+    path = tmp_path / "st.wav"
+    wavfile.write(path, sr, np.stack([left, right], axis=1))
+    mix = S.AudioFileWaveform(str(path), amplitude=2.0)
+    want = np.mean(np.stack([left, right], 1).astype(np.float32) / 32768.0, axis=1)
+    assert mix.num_samples == 400 and mix.native_sample_rate == sr
+    assert mix.duration_seconds == pytest.approx(0.05)
+    dt = 1.0 / sr  # the native rate: no resampling
+    times = np.arange(402) * dt
+    got = mix.waveform(times, dt)
+    np.testing.assert_array_equal(got[:400], 2.0 * want.astype(np.float32))
+    assert got[400] == 0 and got[401] == 0
+    one = S.AudioFileWaveform(str(path), channel=1, start_time=0.01, duration=0.02, loop=True)
+    assert one.num_samples == 160
+    np.testing.assert_array_equal(one.waveform(np.array([0.0, 160 * dt]), dt),
+                                  np.float32(right[80]) / np.float32(32768.0) * np.ones(2))
+    dt2 = 1.0 / 24000
+    np.testing.assert_array_equal(mix._at_rate(dt2),
+                                  signal.resample(want.astype(np.float32), 1200).astype(np.float32))
+    with pytest.raises(ValueError):
+        S.AudioFileWaveform(str(path), channel=2)
+    with pytest.raises(FileNotFoundError):
+        S.AudioFileWaveform(str(tmp_path / "none.wav"))
