@@ -219,3 +219,16 @@ class SimpleMaterial(AcousticMaterial):
 
 
 AIR_20C = SimpleMaterial(name="air_20C", _rho=1.204, _c=343.0)
+
+# the material models and the predefined library, under this module's name
+# as under the reference's materials package
+from .material_models import (  # noqa: E402
+    DampingMaterial, HelmholtzResonator, ImpedanceTube, MembraneAbsorber, PerforatedPanel,
+    PorousMaterial, QuarterWaveResonator, ViscoelasticSolid)
+from .material_library import (  # noqa: E402
+    ACOUSTIC_FOAM_DENSE, ACOUSTIC_FOAM_OPEN, AIR_15C, AIR_25C, BUTYL_RUBBER, COTTON_BATTING,
+    EPDM_RUBBER, FIBERGLASS_24, FIBERGLASS_32, FIBERGLASS_48, FIBERGLASS_96, HARDWOOD_OAK,
+    MATERIALS, MDF_HIGH, MDF_LIGHT, MDF_MEDIUM, MINERAL_WOOL_40, MINERAL_WOOL_60,
+    MINERAL_WOOL_100, NEOPRENE, OSB, PARTICLE_BOARD, PLYWOOD_BIRCH, PLYWOOD_MARINE,
+    PLYWOOD_SOFTWOOD, POLYESTER_BATTING, POLYURETHANE_FOAM, SILICONE_RUBBER, SORBOTHANE,
+    WATER_20C, WOOL_FELT, get_material, list_categories, list_materials, material_summary)

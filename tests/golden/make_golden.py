@@ -320,6 +320,47 @@ def analysis_values(api, manifest):
     for prof in ("conical", "exponential", "hyperbolic", "tractrix"):
         h = api.Horn((0.0, 0.0, 0.05), (0.0, 0.0, 0.0), 0.006, 0.02, prof)
         out[f"horn_{prof}"] = np.concatenate([[h.cutoff_frequency], h.radius_at_position(ts)])
+    # the material library's poles and the models' analytic responses
+    # (materials/library.py, porous.py, solids.py, resonators.py)
+    import strata_fdtd.materials as MM
+
+    def pole_rows(mat):
+        return np.array([[0 if p.is_debye else 1, p.delta_chi, p.tau or 0.0, p.omega_0 or 0.0,
+                          p.gamma or 0.0, 0 if p.target == "density" else 1]
+                         for p in mat.poles]).reshape(-1, 6)
+
+    for name in MM.list_materials():
+        out[f"lib__{name}"] = pole_rows(MM.get_material(name))
+    extra = {
+        "helmholtz": MM.HelmholtzResonator(name="h", neck_radius=0.02, neck_length=0.04,
+                                           cavity_volume=0.015, loss_factor=0.12),
+        "membrane": MM.MembraneAbsorber(name="m", surface_density=4.2, cavity_depth=0.15),
+        "perforated": MM.PerforatedPanel(name="p", hole_diameter=0.003, plate_thickness=0.012,
+                                         perforation_ratio=0.15, cavity_depth=0.2),
+        "quarter": MM.QuarterWaveResonator(name="q", length=0.858, diameter=0.1,
+                                           loss_factor=0.08, n_modes=4),
+        "porous_thick": MM.PorousMaterial(name="pt", flow_resistivity=18000, porosity=0.97,
+                                          tortuosity=1.05, viscous_length=90e-6,
+                                          thermal_length=180e-6, thickness=0.05, num_poles=8),
+    }
+    for key, mat in extra.items():
+        out[f"model__{key}"] = pole_rows(mat)
+    om = 2 * np.pi * np.array([63.0, 125.0, 250.0, 500.0, 1000.0, 2000.0, 4000.0])
+    pt = extra["porous_thick"]
+    tube = MM.ImpedanceTube(length=0.5, diameter=0.1, mic_spacing=0.05, sample_distance=0.1)
+    out["model_resp"] = np.concatenate([
+        pt.jca_impedance(om), pt.surface_impedance(om), pt.surface_impedance(om, backing=900.0),
+        pt.absorption_coefficient_layer(om), tube.absorption_coefficient(pt, om),
+        tube.absorption_coefficient(MM.MDF_MEDIUM, om), MM.MDF_MEDIUM.loss_factor_spectrum(om),
+        MM.SORBOTHANE.quality_factor(om), extra["helmholtz"].absorption_analytical(om),
+        extra["perforated"].impedance_analytical(om)]).astype(complex)
+    fit = pt.validate_pole_fit(om)
+    out["model_scalars"] = np.array([
+        extra["helmholtz"].resonance_frequency, extra["helmholtz"].quality_factor_theoretical,
+        extra["membrane"].resonance_frequency, extra["perforated"].resonance_frequency,
+        extra["quarter"].fundamental_frequency, MM.MDF_MEDIUM.c_longitudinal,
+        tube.max_frequency, tube.min_frequency, fit["density_max_error"],
+        fit["modulus_mean_error"]])
     np.savez_compressed(os.path.join(HERE, "analysis_values.npz"), **out)
     manifest["analysis_values"] = dict(keys=sorted(out))
 

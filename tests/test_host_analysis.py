@@ -161,3 +161,63 @@ def test_audio_file_waveform(tmp_path):
         S.AudioFileWaveform(str(path), channel=2)
     with pytest.raises(FileNotFoundError):
         S.AudioFileWaveform(str(tmp_path / "none.wav"))
+
+
+def _pole_rows(mat):
+    return np.array([[0 if p.is_debye else 1, p.delta_chi, p.tau or 0.0, p.omega_0 or 0.0,
+                      p.gamma or 0.0, 0 if p.target == "density" else 1]
+                     for p in mat.poles]).reshape(-1, 6)
+
+
+def test_material_library_poles_match_reference():
+    """Every predefined material's poles, and those of the resonant absorber
+    models, equal the reference's (the porous fits run the same NumPy and
+    LAPACK calls on the same inputs)."""
+    from strata_fdtd_gb300 import materials as M
+
+    names = M.list_materials()
+    assert len(names) == 31 and M.list_categories()[0] == "fluids"
+    for name in names:
+        np.testing.assert_array_equal(_pole_rows(M.get_material(name)), G[f"lib__{name}"],
+                                      err_msg=name)
+    assert M.get_material("FIBERGLASS_48KG") is M.FIBERGLASS_48
+    with pytest.raises(KeyError):
+        M.get_material("unobtainium")
+    with pytest.raises(KeyError):
+        M.list_materials("metals")
+    extra = {
+        "helmholtz": M.HelmholtzResonator(name="h", neck_radius=0.02, neck_length=0.04,
+                                          cavity_volume=0.015, loss_factor=0.12),
+        "membrane": M.MembraneAbsorber(name="m", surface_density=4.2, cavity_depth=0.15),
+        "perforated": M.PerforatedPanel(name="p", hole_diameter=0.003, plate_thickness=0.012,
+                                        perforation_ratio=0.15, cavity_depth=0.2),
+        "quarter": M.QuarterWaveResonator(name="q", length=0.858, diameter=0.1,
+                                          loss_factor=0.08, n_modes=4),
+        "porous_thick": M.PorousMaterial(name="pt", flow_resistivity=18000, porosity=0.97,
+                                         tortuosity=1.05, viscous_length=90e-6,
+                                         thermal_length=180e-6, thickness=0.05, num_poles=8),
+    }
+    for key, mat in extra.items():
+        np.testing.assert_array_equal(_pole_rows(mat), G[f"model__{key}"], err_msg=key)
+    om = 2 * np.pi * np.array([63.0, 125.0, 250.0, 500.0, 1000.0, 2000.0, 4000.0])
+    pt = extra["porous_thick"]
+    tube = M.ImpedanceTube(length=0.5, diameter=0.1, mic_spacing=0.05, sample_distance=0.1)
+    resp = np.concatenate([
+        pt.jca_impedance(om), pt.surface_impedance(om), pt.surface_impedance(om, backing=900.0),
+        pt.absorption_coefficient_layer(om), tube.absorption_coefficient(pt, om),
+        tube.absorption_coefficient(M.MDF_MEDIUM, om), M.MDF_MEDIUM.loss_factor_spectrum(om),
+        M.SORBOTHANE.quality_factor(om), extra["helmholtz"].absorption_analytical(om),
+        extra["perforated"].impedance_analytical(om)]).astype(complex)
+    np.testing.assert_allclose(resp, G["model_resp"], rtol=1e-12)
+    fit = pt.validate_pole_fit(om)
+    np.testing.assert_allclose([
+        extra["helmholtz"].resonance_frequency, extra["helmholtz"].quality_factor_theoretical,
+        extra["membrane"].resonance_frequency, extra["perforated"].resonance_frequency,
+        extra["quarter"].fundamental_frequency, M.MDF_MEDIUM.c_longitudinal,
+        tube.max_frequency, tube.min_frequency, fit["density_max_error"],
+        fit["modulus_mean_error"]], G["model_scalars"], rtol=1e-12)
+    for bad in (dict(porosity=1.5), dict(tortuosity=0.9), dict(num_poles=1)):
+        with pytest.raises(ValueError):
+            M.PorousMaterial(**bad)
+    with pytest.raises(ValueError):
+        M.ViscoelasticSolid(poissons_ratio=0.5)
