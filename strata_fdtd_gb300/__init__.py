@@ -14,8 +14,9 @@ from .adjoint import DifferentiableSolver
 from .batch import BatchedSolver
 from .boundaries import PML, ABCFirstOrder, RadiationImpedance, RigidBoundary
 from .grid import NonuniformGrid, UniformGrid
+from .loudspeaker import LoudspeakerEnclosure, bookshelf_speaker, tower_speaker
 from .material_assignment import MaterializedGeometry, MaterialVolume
-from .microphones import Microphone
+from .microphones import POLAR_PATTERNS, Microphone
 from .materials import AIR_20C, AcousticMaterial, Material, Pole, PoleType, SimpleMaterial
 from .membranes import CircularMembraneSource, MembraneSource, RectangularMembraneSource
 from .resonator import HelmholtzResonator, helmholtz_array
@@ -26,14 +27,17 @@ from .sdf import (Box, Cone, CSGNode, Cylinder, Difference, HelicalTube, Horn, I
                   hyperbolic_horn, rotation_matrix, tractrix_horn)
 from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_native_kernels
 from .waveforms import AudioFileWaveform
+from .weighting import apply_weighting, calculate_leq, calculate_spl
 
 __version__ = "0.1.0"
 
 __all__ = [
-    "FDTDSolver", "GaussianPulse", "AudioFileWaveform", "Probe", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
+    "FDTDSolver", "GaussianPulse", "AudioFileWaveform", "Probe", "POLAR_PATTERNS",
+    "apply_weighting", "calculate_spl", "calculate_leq", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
     "RigidBoundary", "ABCFirstOrder", "RadiationImpedance", "Pole",
     "PoleType", "SimpleMaterial", "AcousticMaterial", "Material", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale", "Rotate",
+    "LoudspeakerEnclosure", "bookshelf_speaker", "tower_speaker",
     "rotation_matrix", "Cone", "Horn", "SpiralHorn", "HelicalTube", "SmoothUnion",
     "SmoothIntersection", "SmoothDifference", "conical_horn", "exponential_horn",
     "hyperbolic_horn", "tractrix_horn", "SpiralPath", "HelixPath", "distance_to_polyline",

@@ -348,13 +348,33 @@ VOXEL_CASES = {
     "horn_oblique": ((40, 40, 40), 1e-3, "horn_oblique"),
     "spiral_horn": ((60, 60, 26), 1e-3, "spiral_horn"),
     "helical_tube": ((50, 50, 34), 1e-3, "helical_tube"),
+    "bookshelf": ((52, 64, 90), 4e-3, "bookshelf"),
+    "cabinet": ((62, 72, 126), 4e-3, "cabinet"),
 }
 # masks whose reference evaluation rounds through BLAS (np.dot, matmul) or
 # NumPy's transcendental functions, or whose host-side constants come from
 # those functions on the machine that runs them: cells within that rounding
 # of a surface may differ
 VOXEL_ROUNDING_CASES = ("cyl_oblique", "rotated", "cone_smooth", "horns", "horn_oblique",
-                        "spiral_horn", "helical_tube")
+                        "spiral_horn", "helical_tube", "cabinet")
+
+
+def loudspeaker_cabinet(api, waveform=None):
+    """A cabinet with drivers on three faces (one recessed), a divider with
+    holes, a diagonal brace, a flared port, an absorber region and a
+    Helmholtz array (geometry/loudspeaker.py:52-654)."""
+    enc = api.LoudspeakerEnclosure(external_size=(0.24, 0.28, 0.5), wall_thickness=0.018)
+    enc.add_driver((0.12, 0.36), 0.13, mounting_depth=0.01, name="woofer", waveform=waveform)
+    enc.add_driver((0.12, 0.14), 0.05, baffle_face="top", waveform=waveform, mode=(1, 1))
+    enc.add_driver((0.14, 0.42), 0.04, baffle_face="left")
+    enc.add_port((0.14, 0.1), 0.04, 0.12, baffle_face="right", flare_ratio=1.5,
+                 flare_length=0.03)
+    enc.add_chamber_divider(z_position=0.26, thickness=0.016,
+                            hole_positions=[(0.06, 0.08, 0.03), (0.18, 0.2, 0.02)])
+    enc.add_brace((0.05, 0.14, 0.05), (0.19, 0.14, 0.2), 0.02, 0.03)
+    enc.add_absorber_region(((0.03, 0.2, 0.3), (0.21, 0.26, 0.46)), material_id=2)
+    enc.add_helmholtz_array(((0.03, 0.03, 0.03), (0.2, 0.24, 0.22)), (300.0, 1200.0), 4)
+    return enc
 
 
 def sdf_tree(api, which):
@@ -440,6 +460,10 @@ def sdf_tree(api, which):
         return api.SpiralHorn(center=(0.03, 0.03), throat_radius=0.003, mouth_radius=0.006,
                               inner_spiral_radius=0.008, outer_spiral_radius=0.022, turns=1.5,
                               height=0.02, profile="exponential")
+    if which == "bookshelf":  # geometry/loudspeaker.py:703-742
+        return api.bookshelf_speaker(0.2, 0.25, 0.35, 0.13, 0.025).build()
+    if which == "cabinet":  # LoudspeakerEnclosure with every kind of part
+        return loudspeaker_cabinet(api).build()
     if which == "helical_tube":  # HelicalTube (sdf.py:1579-1721)
         return api.HelicalTube(center=(0.025, 0.025, 0.004), helix_radius=0.013,
                                tube_radius_start=0.003, tube_radius_end=0.005, pitch=0.012,

@@ -70,6 +70,9 @@ def load_reference():
         Cone=sdf.Cone, Horn=sdf.Horn, SpiralHorn=sdf.SpiralHorn, HelicalTube=sdf.HelicalTube,
         SmoothUnion=sdf.SmoothUnion, SmoothIntersection=sdf.SmoothIntersection,
         SmoothDifference=sdf.SmoothDifference,
+        LoudspeakerEnclosure=sys.modules["strata_fdtd.geometry.loudspeaker"].LoudspeakerEnclosure,
+        bookshelf_speaker=sys.modules["strata_fdtd.geometry.loudspeaker"].bookshelf_speaker,
+        tower_speaker=sys.modules["strata_fdtd.geometry.loudspeaker"].tower_speaker,
         Pole=base.Pole, PoleType=base.PoleType, SimpleMaterial=base.SimpleMaterial,
         MaterializedGeometry=material_assignment.MaterializedGeometry,
         kernels=mod, solver_module=sys.modules["strata_fdtd.core.solver"])
@@ -361,6 +364,16 @@ def analysis_values(api, manifest):
         extra["quarter"].fundamental_frequency, MM.MDF_MEDIUM.c_longitudinal,
         tube.max_frequency, tube.min_frequency, fit["density_max_error"],
         fit["modulus_mean_error"]])
+    # a cabinet's membrane sources and absorber regions (geometry/loudspeaker.py)
+    enc = C.loudspeaker_cabinet(api, waveform=api.GaussianPulse(position=(0, 0, 0),
+                                                               frequency=400.0))
+    out["cab_sources"] = np.array([list(s.center) + [s.radius, "xyz".index(s.normal_axis),
+                                                     *s.mode] for s in enc.get_membrane_sources()])
+    out["cab_regions"] = np.array([list(b.center) + list(b.size) + [mid]
+                                   for b, mid in enc.get_material_regions()])
+    t = api.tower_speaker(0.22, 0.3, 0.9, 0.17, 0.13, 0.025)
+    out["tower_inside_4mm"] = np.array([int(t.build().voxelize(
+        api.UniformGrid(shape=(55, 75, 225), resolution=4e-3)).sum())])
     np.savez_compressed(os.path.join(HERE, "analysis_values.npz"), **out)
     manifest["analysis_values"] = dict(keys=sorted(out))
 

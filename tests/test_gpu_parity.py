@@ -26,7 +26,8 @@ API = types.SimpleNamespace(
     Difference=S.Difference, HelmholtzResonator=S.HelmholtzResonator, Pole=S.Pole,
     Cone=S.Cone, Horn=S.Horn, SpiralHorn=S.SpiralHorn, HelicalTube=S.HelicalTube,
     SmoothUnion=S.SmoothUnion, SmoothIntersection=S.SmoothIntersection,
-    SmoothDifference=S.SmoothDifference,
+    SmoothDifference=S.SmoothDifference, LoudspeakerEnclosure=S.LoudspeakerEnclosure,
+    bookshelf_speaker=S.bookshelf_speaker, tower_speaker=S.tower_speaker,
     PoleType=S.PoleType, SimpleMaterial=S.SimpleMaterial, NonuniformGrid=S.NonuniformGrid,
     MaterializedGeometry=S.MaterializedGeometry,
     ABCFirstOrder=S.ABCFirstOrder, RadiationImpedance=S.RadiationImpedance,
@@ -253,7 +254,10 @@ def test_voxelize_matches_reference(name):
         # np.dot / matmul round through BLAS; only cells within rounding of a surface may differ
         diff = mask != ref
         if diff.any():
-            d = C.sdf_tree(ORACLE, which).sdf(np.stack(np.meshgrid(
+            # the oracle's distances (the builder's own for the loudspeaker
+            # cabinet, which the oracle does not restate)
+            checker = API if which in ("bookshelf", "cabinet") else ORACLE
+            d = C.sdf_tree(checker, which).sdf(np.stack(np.meshgrid(
                 grid.x_coords, grid.y_coords, grid.z_coords, indexing="ij"), -1).reshape(-1, 3))
             assert np.all(np.abs(d.reshape(shape)[diff]) < 1e-15)
     else:
@@ -684,3 +688,46 @@ def test_library_materials_step_like_the_oracle():
     for n in ("a", "b"):
         np.testing.assert_array_equal(gpu.get_probe_data()[n], ref.get_probe_data()[n])
     assert np.all(np.isfinite(gpu.p)) and np.abs(gpu.get_probe_data()["a"]).max() > 0
+
+
+def test_tower_speaker_and_cabinet_solve():
+    """The three-way tower voxelised at 4 mm has the reference's solid cell
+    count; a bookshelf cabinet's mask, its woofer as a membrane source and
+    an absorber region of a library material step on the GPU exactly as the
+    oracle steps the same inputs."""
+    from strata_fdtd_gb300 import materials as M
+
+    g = golden("analysis_values")
+    tower = S.tower_speaker(0.22, 0.3, 0.9, 0.17, 0.13, 0.025).build()
+    assert int(tower.voxelize(S.UniformGrid((55, 75, 225), 4e-3)).sum()) == int(
+        g["tower_inside_4mm"][0])
+
+    enc = S.bookshelf_speaker(0.06, 0.07, 0.09, 0.03, 0.012, port_diameter=0.012,
+                              port_length=0.03)
+    enc._drivers[1]["waveform"] = S.GaussianPulse(position=(0, 0, 0), frequency=6000.0)
+    enc.add_absorber_region(((0.01, 0.03, 0.05), (0.05, 0.06, 0.08)), material_id=1)
+    grid = S.UniformGrid((40, 46, 56), 2e-3)
+    air = ~enc.build().voxelize(grid)
+    (box, mid), = enc.get_material_regions()
+    src, = enc.get_membrane_sources()
+
+    def build(mod):
+        s = mod.FDTDSolver(shape=grid.shape, resolution=2e-3, c=343.0, rho=1.204, courant=0.5)
+        s.add_boundary(mod.PML(depth=4))
+        s.set_geometry(air)
+        s.register_material(M.POLYESTER_BATTING, material_id=mid)
+        lo = [int(round(v / 2e-3)) for v in box.center - box.size / 2]
+        hi = [int(round(v / 2e-3)) for v in box.center + box.size / 2]
+        s.set_material_box(mid, *zip(lo, hi))
+        s.add_source(mod.CircularMembraneSource(center=src.center, radius=src.radius,
+                                                normal_axis=src.normal_axis, mode=src.mode,
+                                                waveform=src.waveform))
+        s.add_probe("front", (20, 4, 20))
+        return s
+
+    gpu, ref = build(S), build(ORACLE)
+    gpu.run_steps(80)
+    ref.run_steps(80)
+    for f in ("p", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(getattr(gpu, f), getattr(ref, f), err_msg=f)
+    np.testing.assert_array_equal(gpu.get_probe_data()["front"], ref.get_probe_data()["front"])

@@ -221,3 +221,21 @@ def test_material_library_poles_match_reference():
             M.PorousMaterial(**bad)
     with pytest.raises(ValueError):
         M.ViscoelasticSolid(poissons_ratio=0.5)
+
+
+def test_loudspeaker_sources_and_regions_match_reference():
+    """The cabinet builder's membrane sources (one per driver with a
+    waveform: centre on its baffle face, radius, normal axis, mode) and
+    absorber boxes equal the reference's (geometry/loudspeaker.py)."""
+    import cases as C
+
+    enc = C.loudspeaker_cabinet(S, waveform=S.GaussianPulse(position=(0, 0, 0), frequency=400.0))
+    got = np.array([list(s.center) + [s.radius, "xyz".index(s.normal_axis), *s.mode]
+                    for s in enc.get_membrane_sources()])
+    np.testing.assert_array_equal(got, G["cab_sources"])
+    regions = np.array([list(b.center) + list(b.size) + [mid]
+                        for b, mid in enc.get_material_regions()])
+    np.testing.assert_array_equal(regions, G["cab_regions"])
+    with pytest.raises(ValueError):
+        S.LoudspeakerEnclosure((0.2, 0.2, 0.2)).add_driver((0.1, 0.1), 0.05,
+                                                           baffle_face="side").build()
