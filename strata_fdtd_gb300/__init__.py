@@ -13,6 +13,8 @@ from ._native import NativeError, build
 from .adjoint import DifferentiableSolver
 from .batch import BatchedSolver
 from .boundaries import PML, ABCFirstOrder, RadiationImpedance, RigidBoundary
+from .dsp import (Crossover, DelayedWaveform, FilteredWaveform, ParametricEQ,
+                  ThreeWayCrossover)
 from .grid import NonuniformGrid, UniformGrid
 from .loudspeaker import LoudspeakerEnclosure, bookshelf_speaker, tower_speaker
 from .material_assignment import MaterializedGeometry, MaterialVolume
@@ -33,7 +35,8 @@ __version__ = "0.1.0"
 
 __all__ = [
     "FDTDSolver", "GaussianPulse", "AudioFileWaveform", "Probe", "POLAR_PATTERNS",
-    "apply_weighting", "calculate_spl", "calculate_leq", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
+    "apply_weighting", "calculate_spl", "calculate_leq", "Crossover", "ThreeWayCrossover",
+    "FilteredWaveform", "DelayedWaveform", "ParametricEQ", "Microphone", "UniformGrid", "NonuniformGrid", "PML",
     "RigidBoundary", "ABCFirstOrder", "RadiationImpedance", "Pole",
     "PoleType", "SimpleMaterial", "AcousticMaterial", "Material", "AIR_20C", "SDFPrimitive", "CSGNode", "Box", "Sphere",
     "Cylinder", "Union", "Intersection", "Difference", "Translate", "Scale", "Rotate",

@@ -87,6 +87,8 @@ class AudioFileWaveform:
             self._resampled[rate] = out
         return self._resampled[rate]
 
+    _resample_for_dt = _at_rate  # the name the filters look for (dsp.py)
+
     def waveform(self, t, dt: float) -> np.ndarray:
         """Values at times t: the sample at index int(t / dt), scaled by the
         amplitude (zero outside the recording unless it loops)."""

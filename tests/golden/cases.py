@@ -608,3 +608,22 @@ def build_case(api, case, ade=False):
         pos, val = case["impulse"]
         solver.p[pos] = val
     return solver
+
+
+def dsp_waveforms(api, D):
+    """The processed waveforms the dsp check compares (built the same way
+    from either API's classes)."""
+    src = api.GaussianPulse(position=(0, 0, 0), frequency=2500.0, amplitude=1.0)
+    xo = D.Crossover(frequency=1200.0)
+    x3 = D.ThreeWayCrossover(low_freq=400.0, high_freq=4000.0, order=4, type="butterworth")
+    eq = D.ParametricEQ()
+    for f, g, q, kind in ((150.0, 4.0, 0.7, "lowshelf"), (900.0, -3.0, 2.0, "peaking"),
+                          (6000.0, 2.5, 0.05, "highshelf"), (60.0, 0.0, 0.7, "highpass"),
+                          (12000.0, 0.0, 1.0, "lowpass")):
+        eq.add_band(f, g, q, kind)
+    return {"lr_low": xo.lowpass(src), "lr_high": xo.highpass(src),
+            "bw_woofer": x3.woofer(src), "bw_mid": x3.midrange(src), "bw_tweeter": x3.tweeter(src),
+            "bessel_hp": D.FilteredWaveform(src, "highpass", 800.0, order=3, design="bessel"),
+            "delayed": D.DelayedWaveform(xo.highpass(src), delay_seconds=2.5e-4),
+            "eq": eq.apply(src),
+            "baffle": D.create_baffle_step_compensation(0.25).apply(src)}

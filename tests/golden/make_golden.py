@@ -374,6 +374,12 @@ def analysis_values(api, manifest):
     t = api.tower_speaker(0.22, 0.3, 0.9, 0.17, 0.13, 0.025)
     out["tower_inside_4mm"] = np.array([int(t.build().voxelize(
         api.UniformGrid(shape=(55, 75, 225), resolution=4e-3)).sum())])
+    # source-signal processing (dsp/): filters, crossovers, delay, EQ over a
+    # pulse sampled at 48 kHz
+    import strata_fdtd.dsp as D
+
+    for key, wf in C.dsp_waveforms(api, D).items():
+        out[f"dsp__{key}"] = np.asarray(wf.waveform(np.arange(1500) / 48000.0, 1 / 48000.0))
     np.savez_compressed(os.path.join(HERE, "analysis_values.npz"), **out)
     manifest["analysis_values"] = dict(keys=sorted(out))
 

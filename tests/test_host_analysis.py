@@ -239,3 +239,23 @@ def test_loudspeaker_sources_and_regions_match_reference():
     with pytest.raises(ValueError):
         S.LoudspeakerEnclosure((0.2, 0.2, 0.2)).add_driver((0.1, 0.1), 0.05,
                                                            baffle_face="side").build()
+
+
+def test_dsp_waveforms_match_reference():
+    """Crossovers (Linkwitz-Riley, Butterworth, Bessel), a delay and
+    parametric EQ bands over a pulse at 48 kHz equal the reference's
+    (dsp/crossover.py, delay.py, eq.py: the same SciPy filters, biquads by
+    the Audio EQ Cookbook)."""
+    import cases as C
+
+    from strata_fdtd_gb300 import dsp
+
+    t = np.arange(1500) / 48000.0
+    for key, wf in C.dsp_waveforms(S, dsp).items():
+        np.testing.assert_allclose(wf.waveform(t, 1 / 48000.0), G[f"dsp__{key}"], rtol=1e-6,
+                                   atol=1e-7, err_msg=key)
+    with pytest.raises(ValueError):
+        S.ThreeWayCrossover(low_freq=4000.0, high_freq=400.0)
+    with pytest.raises(ValueError):
+        S.FilteredWaveform(S.GaussianPulse(position=(0, 0, 0), frequency=1.0), "lowpass",
+                           30000.0).waveform(t, 1 / 48000.0)
