@@ -31,6 +31,8 @@ from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_nativ
 from .waveforms import AudioFileWaveform
 from .weighting import apply_weighting, calculate_leq, calculate_spl
 
+from . import analysis, dsp, geometry, materials  # noqa: E402  (submodules by name)
+
 __version__ = "0.1.0"
 
 __all__ = [
