@@ -340,3 +340,28 @@ def test_point_and_plane_sources_inject_where_they_are_placed():
     s.step()
     assert np.all(s.p[5] != 0.0)
     assert np.allclose(s.p[10], 0.0, atol=1e-10)
+
+
+def test_geometry_optimizer_voxelises_on_the_gpu():
+    """GeometryOptimizer (geometry/parametric.py): Nelder-Mead over a
+    parametric horn, each evaluation voxelised on the GPU, lowers the
+    objective (the distance of the horn's cell count from a target) and
+    respects its constraints."""
+    from strata_fdtd_gb300 import geometry as G
+
+    grid = S.UniformGrid((40, 40, 60), 5e-3)
+    horn = G.ParametricHorn(throat_radius=0.02, mouth_radius=0.05, length=0.15,
+                            axis_start=(0.1, 0.1, 0.03))
+    cs = G.ConstraintSet()
+    cs.add_ratio_constraint("throat_radius", "mouth_radius", 1.5)
+    opt = G.GeometryOptimizer(horn, grid, constraints=cs)
+    target = 3000
+
+    def objective(mask):
+        return abs(int(mask.sum()) - target)
+
+    start = objective(horn.voxelize(grid))
+    res = opt.optimize(objective, options=dict(maxfev=60))
+    assert res["nfev"] > 0 and res["objective"] <= start
+    assert cs.is_feasible(res["parameters"])
+    assert res["geometry"].voxelize(grid).sum() > 0

@@ -259,3 +259,33 @@ def test_dsp_waveforms_match_reference():
     with pytest.raises(ValueError):
         S.FilteredWaveform(S.GaussianPulse(position=(0, 0, 0), frequency=1.0), "lowpass",
                            30000.0).waveform(t, 1 / 48000.0)
+
+
+def test_parametric_geometry_and_constraints():
+    """Parametric shapes, constraint sets and the optimiser's penalties
+    (geometry/parametric.py), on the host."""
+    from strata_fdtd_gb300 import geometry as G_
+
+    h = G_.ParametricHorn(throat_radius=0.01, mouth_radius=0.04, length=0.1,
+                          axis_start=(0.05, 0.05, 0.0), axis_direction=(0.0, 0.0, 2.0))
+    assert [p.name for p in h.get_parameters()] == ["throat_radius", "mouth_radius", "length"]
+    assert h.to_dict() == {"throat_radius": 0.01, "mouth_radius": 0.04, "length": 0.1}
+    h2 = h.with_parameters(length=0.2)
+    assert h2.length == 0.2 and h.length == 0.1
+    horn = h2.to_sdf()
+    np.testing.assert_allclose(horn.mouth_position, (0.05, 0.05, 0.2))
+    p = G_.Parameter("x", 1.0, (0.0, 2.0))
+    assert p.validate(1.5) and not p.validate(2.5) and p.clip(3.0) == 2.0
+    cs = G_.ConstraintSet()
+    cs.add_min_value("length", 0.08)
+    cs.add_max_value("mouth_radius", 0.05)
+    cs.add_ratio_constraint("throat_radius", "mouth_radius", 2.0)
+    ok = {"length": 0.1, "mouth_radius": 0.04, "throat_radius": 0.01}
+    assert cs.is_feasible(ok) and cs.total_violation(ok) == 0
+    bad = {"length": 0.05, "mouth_radius": 0.06, "throat_radius": 0.04}
+    v = cs.evaluate_all(bad)
+    assert v["min_length"] == pytest.approx(0.03) and v["max_mouth_radius"] == pytest.approx(0.01)
+    assert v["mouth_radius_over_throat_radius"] == pytest.approx(0.02)
+    opt = G_.GeometryOptimizer(h, grid=S.UniformGrid((8, 8, 8), 1e-2), constraints=cs)
+    assert opt.objective(np.array([0.04, 0.06, 0.05]), lambda m: 0.0) == pytest.approx(
+        1e6 * (1 + 0.06))
