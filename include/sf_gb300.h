@@ -414,7 +414,9 @@ typedef struct {
 int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, void* cvy, void* cvz,
                          void* stream);
 /* n_steps forward steps between two state sets (4 pointers each: p, vx,
- * vy, vz), starting from set `cur`; src_vals [n] (device, may be NULL);
+ * vy, vz), starting from set `cur`; src_vals [n] (device, may be NULL; in
+ * the working type: for dtype 2 each value as its nearest (hi, lo) float
+ * pair, as the state arrays);
  * trace [n][n_probe] (may be NULL); p_store [n][N] receives each step's input
  * pressure (may be NULL). */
 int sf_diff_forward(const sf_diff_desc* d, void* const* cv, void* const* set0, void* const* set1,

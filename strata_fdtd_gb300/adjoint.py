@@ -172,6 +172,13 @@ class DifferentiableSolver:
         vals = self.pulse.waveform(times, self.dt)
         return self.torch.tensor(vals, dtype=self.ext_dtype, device=self.dev)
 
+    def _source_table(self, n_steps):
+        """The source values in the working type, as the forward kernel adds
+        them (a double-word solve gets each value's nearest (hi, lo) pair)."""
+        if self.precision != "dw":
+            return self.source_values(n_steps)
+        return self._working(self.source_values(n_steps).cpu().numpy())
+
     def _stream(self):
         return self.torch.cuda.current_stream().cuda_stream
 
@@ -195,7 +202,7 @@ class DifferentiableSolver:
         cv = self.coefficients(theta, occupancy)
         sets = [self._zeros4(), self._zeros4()]
         cur = 0
-        src = self.source_values(n_steps)
+        src = self._source_table(n_steps)
         trace = torch.zeros((n_steps, max(1, len(self.probe_pos))), dtype=self.ext_dtype,
                             device=self.dev)
         ckpts = []

@@ -185,7 +185,7 @@ template <typename T, typename I, typename E = typename Ext<T>::E>
 __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restrict__ vx,
                        const T* __restrict__ vy, const T* __restrict__ vz, T* __restrict__ po,
                        T* __restrict__ vxo, T* __restrict__ vyo, T* __restrict__ vzo,
-                       long long src_cell, const E* __restrict__ src_val, T* __restrict__ p_store,
+                       long long src_cell, const T* __restrict__ src_val, T* __restrict__ p_store,
                        const int64_t* __restrict__ probe_cells, int n_fused, E* __restrict__ trace_row) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -210,7 +210,7 @@ __global__ void k_dfwd(DiffPtrs<T> g, const T* __restrict__ p, const T* __restri
     vyo[c] = uy * dj;
     vzo[c] = uz * dk;
     pn = ((pn * di) * dj) * dk;
-    if ((long long)c == src_cell && src_val != nullptr) pn = pn + Ext<T>::in(*src_val);
+    if ((long long)c == src_cell && src_val != nullptr) pn = pn + *src_val;
     po[c] = pn;
     for (int q = 0; q < n_fused; ++q)
         if ((long long)c == probe_cells[q]) trace_row[q] = Ext<T>::out(pn);
@@ -373,7 +373,7 @@ int forward(const sf_diff_desc* d, const void* const* cv, void* const* set0, voi
     using E = typename Ext<T>::E;
     const DiffPtrs<T> g = ptrs<T>(d, cv);
     const long long N = (long long)d->nx * d->ny * d->nz;
-    const E* sv = static_cast<const E*>(src_vals);
+    const T* sv = static_cast<const T*>(src_vals);  // already in the working type
     E* tr = static_cast<E*>(trace);
     T* ps = static_cast<T*>(p_store);
     const bool fuse = tr && d->n_probe > 0 && d->n_probe <= kFusedProbes;
