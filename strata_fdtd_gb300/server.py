@@ -21,6 +21,8 @@ a solve whose pressure turns non-finite is stopped and marked failed.
 """
 from __future__ import annotations
 
+import queue
+import threading
 import time
 from dataclasses import dataclass, field
 from typing import Any, Callable
@@ -52,9 +54,19 @@ class Request:
     last_group: int = -1      # index of the group that enqueued its last steps
     collect: Any = None       # pipelined executors: waits for and returns the result
 
+    done_event: Any = None    # set when the request leaves the server (posted requests)
+
     @property
     def latency(self) -> float | None:
         return None if self.t_done is None else self.t_done - self.arrival
+
+    def wait(self, timeout: float | None = None) -> bool:
+        """For a request given to a running server (``SolveServer.post``):
+        block until it is done, failed, rejected or cancelled; False on
+        timeout."""
+        if self.done_event is None:
+            raise RuntimeError("wait() is for requests posted to a running server")
+        return self.done_event.wait(timeout)
 
 
 def solve_bytes(shape, geometry=True, debye_poles=0, lorentz_poles=0, probes=2, sources=1) -> int:
@@ -102,12 +114,17 @@ class SolveServer:
         self.peak_active = 0
         self.groups = 0
 
+    def _finish(self, r: Request) -> None:
+        self.finished.append(r)
+        if r.done_event is not None:
+            r.done_event.set()
+
     # -- submission ----------------------------------------------------------
     def submit(self, req: Request) -> Request:
         if req.nbytes > self.budget:
             req.status, req.error = "rejected", (
                 f"needs {req.nbytes} bytes, above the {self.budget}-byte budget")
-            self.finished.append(req)
+            self._finish(req)
             return req
         req.remaining = int(req.steps)
         self.queue.append(req)
@@ -120,13 +137,85 @@ class SolveServer:
                 return True
         return False
 
+    # -- serving in the background ---------------------------------------------
+    def start(self) -> "SolveServer":
+        """Serve in a background thread: requests given to ``post`` from any
+        thread join at the next group boundary, as arrivals at the time they
+        are posted.  ``stop`` ends the thread."""
+        if getattr(self, "_thread", None) is not None:
+            raise RuntimeError("the server is already running")
+        self._inbox: queue.SimpleQueue = queue.SimpleQueue()
+        self._stop_req = threading.Event()
+        self._drain_on_stop = True
+        self.t0 = self.clock()
+        self._thread = threading.Thread(target=self._serve, name="solve-server", daemon=True)
+        self._thread.start()
+        return self
+
+    def post(self, req: Request) -> Request:
+        """Hand a request to the running server (thread-safe); its
+        ``wait()`` returns once it has left the server."""
+        if getattr(self, "_thread", None) is None:
+            raise RuntimeError("post() needs a started server (start())")
+        req.done_event = threading.Event()
+        req.arrival = self.clock() - self.t0
+        self._inbox.put(req)
+        return req
+
+    def stop(self, drain: bool = True, timeout: float | None = None) -> dict:
+        """Stop the background thread: with ``drain`` after every posted
+        request has finished, else cancelling the queued and running ones.
+        Returns the statistics."""
+        self._drain_on_stop = drain
+        self._stop_req.set()
+        self._thread.join(timeout)
+        self._thread = None
+        return self.stats()
+
+    def _drain_inbox(self) -> None:
+        inbox = getattr(self, "_inbox", None)
+        while inbox is not None:
+            try:
+                req = inbox.get_nowait()
+            except queue.Empty:
+                return
+            self.submit(req)
+
+    def _serve(self) -> None:
+        def now():
+            return self.clock() - self.t0
+
+        while True:
+            self._drain_inbox()
+            if self._stop_req.is_set():
+                if not self._drain_on_stop:
+                    for r in self.queue + self.active:
+                        r.cancel_requested = True
+                if not (self.queue or self.active):
+                    return
+            if self.queue or self.active:
+                if getattr(self.ex, "pipelined", False):
+                    self._run_pipelined(now, True)
+                else:
+                    self._run_simple(now, True)
+                continue
+            try:  # idle: wait for the next request
+                self.submit(self._inbox.get(timeout=0.02))
+            except queue.Empty:
+                pass
+
     # -- scheduling ----------------------------------------------------------
     def _admit(self, now: float) -> None:
+        self._drain_inbox()
+        stop = getattr(self, "_stop_req", None)
+        if stop is not None and stop.is_set() and not self._drain_on_stop:
+            for r in self.queue + self.active:  # stop(drain=False): cancel the rest
+                r.cancel_requested = True
         keep = []
         for r in self.queue:
             if r.cancel_requested:
                 r.status, r.t_done = "cancelled", now
-                self.finished.append(r)
+                self._finish(r)
                 continue
             fits_cells = (self.max_cells is None or not self.active
                           or self.active_cells + r.cells <= self.max_cells)
@@ -137,7 +226,7 @@ class SolveServer:
                     r.handle = self.ex.start(r)
                 except Exception as e:  # malformed request or failed allocation
                     r.status, r.error, r.t_done = "failed", f"{type(e).__name__}: {e}", now
-                    self.finished.append(r)
+                    self._finish(r)
                     continue
                 r.status, r.t_admit = "running", now
                 self.in_use += r.nbytes
@@ -167,7 +256,7 @@ class SolveServer:
                 r.t_done = now
                 self.in_use -= r.nbytes
                 self.active_cells -= r.cells
-                self.finished.append(r)
+                self._finish(r)
             else:
                 still.append(r)
         self.active = still
@@ -186,6 +275,10 @@ class SolveServer:
 
         if getattr(self.ex, "pipelined", False):
             return self._run_pipelined(now, realtime)
+        return self._run_simple(now, realtime)
+
+    def _run_simple(self, now, realtime: bool) -> dict:
+        """One group at a time: admit, advance, wait, retire."""
         while self.queue or self.active:
             self._admit(now() if realtime else float("inf"))
             if not self.active:
@@ -292,7 +385,7 @@ class SolveServer:
             r.handle = None
             r.t_done = now
             self.in_use -= r.nbytes
-            self.finished.append(r)
+            self._finish(r)
 
     def stats(self) -> dict:
         done = [r for r in self.finished if r.status == "done"]

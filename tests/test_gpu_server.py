@@ -136,3 +136,38 @@ def test_served_requests_with_the_wider_feature_set_match_goldens():
         for name in g["probe_names"]:
             np.testing.assert_array_equal(results[q][str(name)], g[f"trace__{name}"],
                                           err_msg=f"{key} probe {name}")
+
+
+def test_background_server_serves_posts_from_threads():
+    """The server in its background thread (start / post / wait / stop):
+    requests posted from two client threads share step groups on the GPU
+    and each result equals the request solved alone."""
+    import threading
+    import time
+
+    reqs = served_stream(seed=13, n_requests=8, rate=1e4, edges=(36, 60), steps=(60, 160),
+                         pml=(4, 6), ade_fraction=0.5)
+    alone = served_stream(seed=13, n_requests=8, rate=1e4, edges=(36, 60), steps=(60, 160),
+                          pml=(4, 6), ade_fraction=0.5)
+    srv = SolveServer(GPUExecutor(), hbm_budget=160e9, step_group=32).start()
+
+    def client(part):
+        for r in part:
+            srv.post(r)
+            time.sleep(0.01)
+
+    threads = [threading.Thread(target=client, args=(reqs[k::2],)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for r in reqs:
+        assert r.wait(120), r.rid
+    stats = srv.stop()
+    assert stats["done"] == 8, stats["errors"]
+    assert stats["peak_active"] > 1
+    for r, a in zip(reqs, alone):
+        s = a.build()
+        s.run_steps(a.steps)
+        for name, tr in s.get_probe_data().items():
+            np.testing.assert_array_equal(r.result[name], tr, err_msg=f"request {r.rid}")

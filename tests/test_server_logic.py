@@ -185,3 +185,46 @@ def test_pipelined_loop_keeps_one_group_in_flight_and_retires_after_completion()
     first_with_3 = next(i for i, g in enumerate(ex.groups) if 3 in g)
     assert all(3 not in g for g in ex.groups[:first_with_3])
     assert all(len(g) <= 3 for g in ex.groups)
+
+
+def test_background_server_takes_posts_from_threads():
+    """start() / post() / wait() / stop(): requests posted from several
+    threads while the server runs are admitted at group boundaries and each
+    wait() returns once its request is done; an oversized one is rejected at
+    once; stop(drain=False) cancels what is still queued or running."""
+    import threading
+    import time as _time
+
+    class SlowExecutor(FakeExecutor):
+        def advance(self, handles, counts):
+            super().advance(handles, counts)
+            _time.sleep(0.001)
+
+    ex = SlowExecutor(FakeClock())
+    srv = SolveServer(ex, hbm_budget=100, step_group=10, clock=_time.perf_counter).start()
+    posted = []
+    lock = threading.Lock()
+
+    def client(base):
+        for q in range(5):
+            r = srv.post(_req(base + q, steps=25 + 5 * q, nbytes=10))
+            with lock:
+                posted.append(r)
+            _time.sleep(0.002)
+
+    threads = [threading.Thread(target=client, args=(100 * k,)) for k in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    big = srv.post(_req(999, steps=10, nbytes=1000))
+    assert big.wait(5) and big.status == "rejected"
+    for r in posted:
+        assert r.wait(10), r.rid
+        assert r.status == "done" and r.result == {"steps": r.steps}
+        assert r.latency is not None and r.latency >= 0
+    late = [srv.post(_req(500 + q, steps=10**6, nbytes=10)) for q in range(3)]
+    st = srv.stop(drain=False, timeout=10)
+    assert all(r.status == "cancelled" for r in late)
+    assert st["done"] == 15 and st["rejected"] == 1 and st["cancelled"] == 3
+    assert max(len(g) for g in ex.groups) > 1  # posts shared groups
