@@ -627,3 +627,51 @@ def dsp_waveforms(api, D):
             "delayed": D.DelayedWaveform(xo.highpass(src), delay_seconds=2.5e-4),
             "eq": eq.apply(src),
             "baffle": D.create_baffle_step_compensation(0.25).apply(src)}
+
+
+def random_sdf_tree(api, rng, depth=3):
+    """A seeded random SDF tree over every shape and operator the GPU
+    voxeliser takes (for point-evaluation checks against the oracle)."""
+    def point():
+        return tuple(float(v) for v in rng.uniform(0.008, 0.042, 3))
+
+    def leaf():
+        kind = int(rng.integers(0, 5))
+        if kind == 0:
+            return api.Box(center=point(), size=tuple(float(v) for v in rng.uniform(0.004, 0.02, 3)))
+        if kind == 1:
+            return api.Sphere(center=point(), radius=float(rng.uniform(0.003, 0.012)))
+        if kind == 2:
+            return api.Cylinder(p1=point(), p2=point(), radius=float(rng.uniform(0.002, 0.008)))
+        if kind == 3:
+            return api.Cone(p1=point(), p2=point(), r1=float(rng.uniform(0.0, 0.009)),
+                            r2=float(rng.uniform(0.002, 0.009)))
+        prof = ("conical", "exponential", "hyperbolic", "tractrix")[int(rng.integers(0, 4))]
+        return api.Horn(point(), point(), float(rng.uniform(0.002, 0.004)),
+                        float(rng.uniform(0.005, 0.01)), prof)
+
+    def node(d):
+        if d == 0 or rng.random() < 0.25:
+            return leaf()
+        op = int(rng.integers(0, 9))
+        a, b = node(d - 1), node(d - 1)
+        r = float(rng.uniform(0.001, 0.004))
+        if op == 0:
+            return api.Union(a, b, node(d - 1))
+        if op == 1:
+            return api.Intersection(a, b)
+        if op == 2:
+            return api.Difference(a, b)
+        if op == 3:
+            return api.SmoothUnion(a, b, r)
+        if op == 4:
+            return api.SmoothIntersection(a, b, r)
+        if op == 5:
+            return api.SmoothDifference(a, b, r)
+        if op == 6:
+            return a.translate(tuple(float(v) for v in rng.uniform(-0.004, 0.004, 3)))
+        if op == 7:
+            return a.scale(float(rng.uniform(0.8, 1.25)))
+        return a.rotate(tuple(float(v) for v in rng.uniform(-1, 1, 3)), float(rng.uniform(-1, 1)))
+
+    return node(depth)

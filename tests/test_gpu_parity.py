@@ -731,3 +731,18 @@ def test_tower_speaker_and_cabinet_solve():
     for f in ("p", "vx", "vy", "vz"):
         np.testing.assert_array_equal(getattr(gpu, f), getattr(ref, f), err_msg=f)
     np.testing.assert_array_equal(gpu.get_probe_data()["front"], ref.get_probe_data()["front"])
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_sdf_trees_match_oracle(seed):
+    """Seeded random trees of every shape (box, sphere, cylinder, cone, the
+    four horn flares) under every operator (sharp and smooth CSG, translate,
+    scale, rotate): GPU point evaluation against the oracle's NumPy
+    restatement within the rounding of BLAS products and transcendental
+    functions."""
+    tree_g = C.random_sdf_tree(API, np.random.default_rng(seed))
+    tree_o = C.random_sdf_tree(ORACLE, np.random.default_rng(seed))
+    pts = np.random.default_rng(100 + seed).uniform(0.0, 0.05, (4000, 3))
+    want = tree_o.sdf(pts)
+    assert np.all(np.isfinite(want))
+    np.testing.assert_allclose(tree_g.sdf(pts), want, rtol=0, atol=2e-15)
