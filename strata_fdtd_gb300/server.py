@@ -157,6 +157,8 @@ class SolveServer:
         ``wait()`` returns once it has left the server."""
         if getattr(self, "_thread", None) is None:
             raise RuntimeError("post() needs a started server (start())")
+        if not self._thread.is_alive():
+            raise RuntimeError("the serving thread has stopped") from getattr(self, "error", None)
         req.done_event = threading.Event()
         req.arrival = self.clock() - self.t0
         self._inbox.put(req)
@@ -166,10 +168,14 @@ class SolveServer:
         """Stop the background thread: with ``drain`` after every posted
         request has finished, else cancelling the queued and running ones.
         Returns the statistics."""
+        if getattr(self, "_thread", None) is None:
+            raise RuntimeError("stop() needs a started server (start())")
         self._drain_on_stop = drain
         self._stop_req.set()
         self._thread.join(timeout)
         self._thread = None
+        if getattr(self, "error", None) is not None:
+            raise RuntimeError("the serving thread stopped on an error") from self.error
         return self.stats()
 
     def _drain_inbox(self) -> None:
@@ -182,6 +188,21 @@ class SolveServer:
             self.submit(req)
 
     def _serve(self) -> None:
+        """The background loop; an error in it fails every request still
+        held (so no ``wait`` blocks for ever) and is re-raised by ``stop``."""
+        self.error = None
+        try:
+            self._serve_loop()
+        except BaseException as e:  # noqa: BLE001 - reported through stop()
+            self.error = e
+            t = self.clock() - self.t0
+            self._drain_inbox()
+            for r in self.queue + self.active:
+                r.status, r.error, r.t_done = "failed", f"server error: {e!r}", t
+                self._finish(r)
+            self.queue, self.active = [], []
+
+    def _serve_loop(self) -> None:
         def now():
             return self.clock() - self.t0
 

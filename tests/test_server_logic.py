@@ -228,3 +228,26 @@ def test_background_server_takes_posts_from_threads():
     assert all(r.status == "cancelled" for r in late)
     assert st["done"] == 15 and st["rejected"] == 1 and st["cancelled"] == 3
     assert max(len(g) for g in ex.groups) > 1  # posts shared groups
+
+
+def test_background_server_error_fails_held_requests():
+    """An executor error inside the serving thread fails every request the
+    server still holds (their wait() returns) and stop() raises it."""
+    import time as _time
+
+    import pytest
+
+    class Broken(FakeExecutor):
+        def advance(self, handles, counts):
+            raise RuntimeError("device lost")
+
+    srv = SolveServer(Broken(FakeClock()), hbm_budget=100, step_group=10,
+                      clock=_time.perf_counter).start()
+    reqs = [srv.post(_req(q, steps=50)) for q in range(3)]
+    for r in reqs:
+        assert r.wait(5)
+        assert r.status == "failed" and "device lost" in r.error
+    with pytest.raises(RuntimeError):
+        srv.stop(timeout=5)
+    with pytest.raises(RuntimeError):
+        SolveServer(FakeExecutor(FakeClock())).stop()
