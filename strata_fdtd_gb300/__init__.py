@@ -27,7 +27,8 @@ from .sdf import (Box, Cone, CSGNode, Cylinder, Difference, HelicalTube, Horn, I
                   Rotate, Scale, SDFPrimitive, SmoothDifference, SmoothIntersection, SmoothUnion,
                   Sphere, SpiralHorn, Translate, Union, conical_horn, exponential_horn,
                   hyperbolic_horn, rotation_matrix, tractrix_horn)
-from .solver import FDTDSolver, GaussianPulse, Probe, get_native_info, has_native_kernels
+from .solver import (FDTDSolver, GaussianPulse, Probe, get_native_info, has_gpu_backend,
+                     has_native_kernels)
 from .waveforms import AudioFileWaveform
 from .weighting import apply_weighting, calculate_leq, calculate_spl
 
@@ -46,7 +47,7 @@ __all__ = [
     "rotation_matrix", "Cone", "Horn", "SpiralHorn", "HelicalTube", "SmoothUnion",
     "SmoothIntersection", "SmoothDifference", "conical_horn", "exponential_horn",
     "hyperbolic_horn", "tractrix_horn", "SpiralPath", "HelixPath", "distance_to_polyline",
-    "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "get_native_info", "build",
+    "HelmholtzResonator", "helmholtz_array", "has_native_kernels", "has_gpu_backend", "get_native_info", "build",
     "NativeError", "BatchedSolver", "DifferentiableSolver", "MembraneSource",
     "CircularMembraneSource", "RectangularMembraneSource", "MaterializedGeometry",
     "MaterialVolume",

@@ -6,7 +6,7 @@ from .loudspeaker import LoudspeakerEnclosure, bookshelf_speaker, tower_speaker 
 from .material_assignment import MaterializedGeometry, MaterialVolume  # noqa: F401
 from .parametric import (ConstraintSet, GeometricConstraint, GeometryOptimizer,  # noqa: F401
                          Parameter, ParametricHorn, ParametricPrimitive)
-from .paths import HelixPath, SpiralPath, distance_to_polyline  # noqa: F401
+from .paths import HelixPath, SpiralPath, distance_to_helix, distance_to_polyline  # noqa: F401
 from .resonator import HelmholtzResonator, helmholtz_array  # noqa: F401
 from .sdf import (Box, Cone, CSGNode, Cylinder, Difference, HelicalTube, Horn,  # noqa: F401
                   Intersection, Rotate, Scale, SDFPrimitive, SmoothDifference,

@@ -119,3 +119,17 @@ def distance_to_polyline(points, polyline) -> np.ndarray:
             d = np.linalg.norm(points - (a + t[:, None] * seg), axis=1)
         best = np.minimum(best, d)
     return best
+
+
+def distance_to_helix(points, center, radius: float, pitch: float, turns: float) -> np.ndarray:
+    """Distance from (N, 3) points to the helix of ``HelixPath``, taken as
+    the polyline through max(100, int(50 turns)) of its samples
+    (geometry/paths.py:296-344)."""
+    points = np.asarray(points, dtype=np.float64)
+    center = np.asarray(center, dtype=np.float64)
+    if points.ndim != 2 or points.shape[1] != 3:
+        raise ValueError(f"points must be Nx3 array, got shape {points.shape}")
+    if center.shape != (3,):
+        raise ValueError(f"center must be 3D point, got shape {center.shape}")
+    helix = HelixPath(center=center, radius=radius, pitch=pitch, turns=turns)
+    return distance_to_polyline(points, helix.sample_points(max(100, int(50 * turns))))

@@ -140,6 +140,13 @@ def has_native_kernels() -> bool:
         return False
 
 
+def has_gpu_backend() -> bool:
+    """Whether the reference's PyTorch-MPS backend is available
+    (core/solver.py:143-149): never here, where the CUDA kernels are the
+    "native" backend and ``backend="gpu"`` is not offered."""
+    return False
+
+
 def get_native_info() -> dict:
     import torch
 
@@ -1221,4 +1228,5 @@ class FDTDSolver:
         return np.fft.rfftfreq(n_fft, self.dt), np.abs(spectrum)
 
 
-__all__ = ["FDTDSolver", "GaussianPulse", "Probe", "has_native_kernels", "get_native_info"]
+__all__ = ["FDTDSolver", "GaussianPulse", "Probe", "has_native_kernels", "get_native_info",
+           "has_gpu_backend"]

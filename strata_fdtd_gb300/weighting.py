@@ -90,3 +90,16 @@ def calculate_time_weighted_level(waveform, fs: float, time_constant: str = "fas
     alpha = 1 - np.exp(-1 / (fs * _TAU[time_constant]))
     avg = signal.lfilter([alpha], [1, -(1 - alpha)], np.asarray(waveform) ** 2)
     return 10 * np.log10(np.maximum(avg, 1e-20) / p_ref**2)
+
+
+def weighting_response(weighting, fs: float, n_points: int = 1024):
+    """(frequencies, magnitude in dB) of the weighting filter at n_points
+    frequencies from 0 to fs / 2 (analysis/weighting.py:304-333); flat 0 dB
+    for "Z" or None."""
+    sos = get_weighting_sos(weighting, fs)
+    if sos is None:
+        return np.linspace(0, fs / 2, n_points), np.zeros(n_points)
+    from scipy import signal
+
+    f, h = signal.sosfreqz(sos, worN=n_points, fs=fs)
+    return f, 20 * np.log10(np.maximum(np.abs(h), 1e-20))

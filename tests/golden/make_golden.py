@@ -380,6 +380,18 @@ def analysis_values(api, manifest):
 
     for key, wf in C.dsp_waveforms(api, D).items():
         out[f"dsp__{key}"] = np.asarray(wf.waveform(np.arange(1500) / 48000.0, 1 / 48000.0))
+    # weighting responses (analysis/weighting.py:304-333) and distances to a
+    # helix (geometry/paths.py:296-344)
+    for w in ("A", "C", None):
+        f, mag = W.weighting_response(w, 48000.0, 512)
+        out[f"wresp__{w or 'Z'}"] = np.stack([f, mag])
+    from strata_fdtd.geometry.paths import distance_to_helix
+
+    pts = np.random.default_rng(11).uniform(-0.05, 0.15, size=(64, 3))
+    out["helix_dist"] = np.concatenate([
+        distance_to_helix(pts, (0.05, 0.05, 0.0), 0.04, 0.03, 2.5),
+        distance_to_helix(pts, (0.0, 0.02, 0.01), 0.02, 0.05, 0.7)])
+    out["helix_pts"] = pts
     np.savez_compressed(os.path.join(HERE, "analysis_values.npz"), **out)
     manifest["analysis_values"] = dict(keys=sorted(out))
 

@@ -65,6 +65,26 @@ def test_material_properties_match_reference():
     assert "Poles: 2 (1 density, 1 modulus)" in mat.summary()
 
 
+def test_weighting_response_and_helix_distance_match_reference():
+    from strata_fdtd_gb300.analysis import weighting_response
+    from strata_fdtd_gb300.geometry import distance_to_helix
+
+    for w in ("A", "C", None):
+        f, mag = weighting_response(w, 48000.0, 512)
+        np.testing.assert_allclose(f, G[f"wresp__{w or 'Z'}"][0], rtol=RTOL)
+        np.testing.assert_allclose(mag, G[f"wresp__{w or 'Z'}"][1], rtol=1e-9, atol=1e-9)
+    f, mag = weighting_response("A", 48000.0, 4800)
+    assert f[200] == 1000.0 and abs(mag[200]) < 0.05  # 0 dB at 1 kHz
+    pts = G["helix_pts"]
+    got = np.concatenate([distance_to_helix(pts, (0.05, 0.05, 0.0), 0.04, 0.03, 2.5),
+                          distance_to_helix(pts, (0.0, 0.02, 0.01), 0.02, 0.05, 0.7)])
+    np.testing.assert_allclose(got, G["helix_dist"], rtol=RTOL, atol=1e-15)
+    with pytest.raises(ValueError):
+        distance_to_helix(pts[:, :2], (0, 0, 0), 0.1, 0.1, 1.0)
+    with pytest.raises(ValueError):
+        distance_to_helix(pts, (0, 0), 0.1, 0.1, 1.0)
+
+
 def test_horn_flares_match_reference():
     ts = np.linspace(0, 1, 11)
     for prof in ("conical", "exponential", "hyperbolic", "tractrix"):
