@@ -73,54 +73,98 @@ class UniformGrid:
         return tuple(n * self.resolution for n in self.shape)
 
 
+def _axis_coords(values, axis: str) -> np.ndarray:
+    """One axis's cell centres as a flat float64 array: two or more of them,
+    strictly increasing."""
+    c = np.asarray(values, dtype=np.float64).ravel()
+    if c.size < 2:
+        raise ValueError(f"{axis}_coords: a nonuniform axis needs two or more cell centres")
+    if np.any(c[1:] <= c[:-1]):
+        raise ValueError(f"{axis}_coords: cell centres must increase strictly")
+    return c
+
+
+def _cell_widths(c: np.ndarray) -> np.ndarray:
+    """Width of each cell: half the distance between its neighbours' centres
+    inside, the distance to the one neighbour at either end."""
+    w = np.empty_like(c)
+    w[1:-1] = (c[2:] - c[:-2]) / 2
+    w[0], w[-1] = c[1] - c[0], c[-1] - c[-2]
+    return w
+
+
+def _geometric_centres(n: int, h0: float, ratio: float, from_centre: bool) -> np.ndarray:
+    """Centres of n cells whose widths grow by ``ratio`` per cell: outward
+    from the middle (mirrored halves, an extra centre cell for odd n) or
+    from the low end; h0 is the smallest width and the first centre sits at
+    h0 / 2.  A ratio of 1 gives the uniform centres."""
+    if ratio == 1.0:
+        return np.arange(n, dtype=np.float64) * h0 + h0 / 2
+    if not from_centre:
+        widths = h0 * ratio ** np.arange(n, dtype=np.float64)
+        return np.cumsum(widths) - widths / 2
+    widths = h0 * ratio ** np.arange(n // 2, dtype=np.float64)
+    outer = (np.cumsum(widths) - widths[0] / 2) + widths / 2  # one half, mirrored below
+    mirrored = -outer[::-1]
+    c = (np.concatenate([mirrored, outer]) if n % 2 == 0
+         else np.concatenate([mirrored, [0.0], outer[1:]]))
+    return (c - c[0]) + h0 / 2
+
+
+def _piecewise_centres(regions) -> np.ndarray:
+    """Centres of consecutive (start, end, resolution) regions: each region
+    holds round(length / resolution) (at least one) equal cells; a region's
+    first centre is dropped when it lies within half a cell of the previous
+    region's last one."""
+    regions = list(regions or [])
+    if not regions:
+        raise ValueError("from_regions: give at least one (start, end, resolution) region")
+    for n, (lo, hi, res) in enumerate(regions):
+        if not hi > lo:
+            raise ValueError(f"from_regions: region {n} has end {hi} not above start {lo}")
+        if not res > 0:
+            raise ValueError(f"from_regions: region {n} has a non-positive resolution {res}")
+        if n and abs(lo - regions[n - 1][1]) > 1e-10:
+            raise ValueError(f"from_regions: region {n} starts at {lo}, not where region "
+                             f"{n - 1} ends ({regions[n - 1][1]})")
+    out: list = []
+    for lo, hi, res in regions:
+        cells = max(1, int(round((hi - lo) / res)))
+        h = (hi - lo) / cells
+        centres = lo + (np.arange(cells) + 0.5) * h
+        if out and abs(centres[0] - out[-1]) < h / 2:
+            centres = centres[1:]
+        out.extend(centres.tolist())
+    return np.array(out, dtype=np.float64)
+
+
 class NonuniformGrid:
-    """Variable spacing from cell-centre coordinates per axis (core/grid.py:
-    148-532 of rjwalters/strata-fdtd): spacing[i] = (x[i+1] - x[i-1]) / 2
-    inside, the neighbour distance at both ends; the stencil's face
-    spacings are the centre distances.  Same constructors and properties as
-    the reference, with its FP64 arithmetic (the spacing arrays handed to the
-    kernels are rounded to float32 as the reference rounds them)."""
+    """A grid with its own cell centres per axis (core/grid.py:148-532 of
+    rjwalters/strata-fdtd): cell widths from the centres (``_cell_widths``),
+    face spacings as the centre distances, geometric and piecewise
+    generators, and the float32 inverse spacings the kernels take.  Every
+    value is the reference's FP64 number, which the nonuniform parity cases
+    rely on."""
 
     def __init__(self, x_coords, y_coords, z_coords):
-        self._x_coords = np.asarray(x_coords, dtype=np.float64).ravel()
-        self._y_coords = np.asarray(y_coords, dtype=np.float64).ravel()
-        self._z_coords = np.asarray(z_coords, dtype=np.float64).ravel()
-        for name, c in (("x", self._x_coords), ("y", self._y_coords), ("z", self._z_coords)):
-            if len(c) < 2:
-                raise ValueError(f"{name}_coords must have at least 2 points")
-            if not np.all(np.diff(c) > 0):
-                raise ValueError(f"{name}_coords must be monotonically increasing")
-        self._dx = self._compute_spacing(self._x_coords)
-        self._dy = self._compute_spacing(self._y_coords)
-        self._dz = self._compute_spacing(self._z_coords)
-        self._shape = (len(self._x_coords), len(self._y_coords), len(self._z_coords))
+        self._c = tuple(_axis_coords(v, a) for v, a in zip((x_coords, y_coords, z_coords), "xyz"))
+        self._w = tuple(_cell_widths(c) for c in self._c)
 
-    @staticmethod
-    def _compute_spacing(coords):
-        """core/grid.py:217-235."""
-        n = len(coords)
-        spacing = np.zeros(n, dtype=np.float64)
-        for i in range(1, n - 1):
-            spacing[i] = (coords[i + 1] - coords[i - 1]) / 2
-        spacing[0] = coords[1] - coords[0]
-        spacing[-1] = coords[-1] - coords[-2]
-        return spacing
-
-    shape = property(lambda s: s._shape)
-    dx = property(lambda s: s._dx)
-    dy = property(lambda s: s._dy)
-    dz = property(lambda s: s._dz)
-    x_coords = property(lambda s: s._x_coords)
-    y_coords = property(lambda s: s._y_coords)
-    z_coords = property(lambda s: s._z_coords)
+    shape = property(lambda s: tuple(c.size for c in s._c))
+    x_coords = property(lambda s: s._c[0])
+    y_coords = property(lambda s: s._c[1])
+    z_coords = property(lambda s: s._c[2])
+    dx = property(lambda s: s._w[0])
+    dy = property(lambda s: s._w[1])
+    dz = property(lambda s: s._w[2])
 
     @property
     def min_spacing(self) -> float:
-        return float(min(np.min(self._dx), np.min(self._dy), np.min(self._dz)))
+        return float(min(w.min() for w in self._w))
 
     @property
     def max_spacing(self) -> float:
-        return float(max(np.max(self._dx), np.max(self._dy), np.max(self._dz)))
+        return float(max(w.max() for w in self._w))
 
     @property
     def is_uniform(self) -> bool:
@@ -128,99 +172,38 @@ class NonuniformGrid:
 
     @property
     def num_cells(self) -> int:
-        return int(np.prod(self._shape))
+        return int(np.prod(self.shape))
 
     @property
     def stretch_ratio(self):
-        return (float(np.max(self._dx) / np.min(self._dx)),
-                float(np.max(self._dy) / np.min(self._dy)),
-                float(np.max(self._dz) / np.min(self._dz)))
+        return tuple(float(w.max() / w.min()) for w in self._w)
 
     def physical_extent(self):
-        return (
-            float(self._x_coords[-1] - self._x_coords[0] + self._dx[-1] / 2 + self._dx[0] / 2),
-            float(self._y_coords[-1] - self._y_coords[0] + self._dy[-1] / 2 + self._dy[0] / 2),
-            float(self._z_coords[-1] - self._z_coords[0] + self._dz[-1] / 2 + self._dz[0] / 2),
-        )
+        """Span of each axis from the low face of its first cell to the high
+        face of its last."""
+        return tuple(float(c[-1] - c[0] + w[-1] / 2 + w[0] / 2) for c, w in zip(self._c, self._w))
 
     @classmethod
     def from_stretch(cls, shape, base_resolution: float, stretch_x: float = 1.0,
                      stretch_y: float = 1.0, stretch_z: float = 1.0, center_fine: bool = True):
-        """Geometric growth per axis from the centre or from 0 (core/grid.py:325-407)."""
-        nx, ny, nz = shape
-        return cls(x_coords=cls._generate_stretched_coords(nx, base_resolution, stretch_x,
-                                                           center_fine),
-                   y_coords=cls._generate_stretched_coords(ny, base_resolution, stretch_y,
-                                                           center_fine),
-                   z_coords=cls._generate_stretched_coords(nz, base_resolution, stretch_z,
-                                                           center_fine))
-
-    @staticmethod
-    def _generate_stretched_coords(n, base_dx, stretch, center_fine):
-        if stretch == 1.0:
-            return np.arange(n, dtype=np.float64) * base_dx + base_dx / 2
-        if center_fine:
-            n_half = n // 2
-            sizes = base_dx * (stretch ** np.arange(n_half, dtype=np.float64))
-            positions = np.cumsum(sizes) - sizes[0] / 2
-            if n % 2 == 0:
-                left = -positions[::-1] - sizes[::-1] / 2
-                right = positions + sizes / 2
-                coords = np.concatenate([left, right])
-            else:
-                left = -positions[::-1] - sizes[::-1] / 2
-                center = np.array([0.0])
-                right = positions[1:] + sizes[1:] / 2 if n_half > 0 else np.array([])
-                coords = np.concatenate([left, center, right])
-            coords = coords - coords[0] + base_dx / 2
-        else:
-            sizes = base_dx * (stretch ** np.arange(n, dtype=np.float64))
-            coords = np.cumsum(sizes) - sizes / 2
-        return coords
+        """Widths growing geometrically per axis, finest at the centre or at
+        the low end (core/grid.py:325-407)."""
+        ratios = (stretch_x, stretch_y, stretch_z)
+        return cls(*(_geometric_centres(int(n), base_resolution, r, center_fine)
+                     for n, r in zip(shape, ratios)))
 
     @classmethod
     def from_regions(cls, x_regions, y_regions=None, z_regions=None):
-        """Piecewise-constant resolution (core/grid.py:409-491)."""
-        if y_regions is None:
-            y_regions = x_regions
-        if z_regions is None:
-            z_regions = x_regions
-        return cls(x_coords=cls._generate_region_coords(x_regions),
-                   y_coords=cls._generate_region_coords(y_regions),
-                   z_coords=cls._generate_region_coords(z_regions))
-
-    @staticmethod
-    def _generate_region_coords(regions):
-        if not regions:
-            raise ValueError("At least one region must be specified")
-        coords_list: list = []
-        for i, (start, end, resolution) in enumerate(regions):
-            if end <= start:
-                raise ValueError(f"Region {i}: end ({end}) must be > start ({start})")
-            if resolution <= 0:
-                raise ValueError(f"Region {i}: resolution must be positive")
-            if i > 0:
-                prev_end = regions[i - 1][1]
-                if abs(start - prev_end) > 1e-10:
-                    raise ValueError(f"Regions must be contiguous: region {i-1} ends at "
-                                     f"{prev_end}, region {i} starts at {start}")
-            n_cells = max(1, int(round((end - start) / resolution)))
-            actual_resolution = (end - start) / n_cells
-            region_coords = start + (np.arange(n_cells) + 0.5) * actual_resolution
-            if coords_list and len(region_coords) > 0:
-                if abs(region_coords[0] - coords_list[-1]) < actual_resolution / 2:
-                    region_coords = region_coords[1:]
-            coords_list.extend(region_coords.tolist())
-        return np.array(coords_list, dtype=np.float64)
+        """Piecewise-constant resolution per axis; y and z default to the x
+        regions (core/grid.py:409-491)."""
+        return cls(*(_piecewise_centres(r if r is not None else x_regions)
+                     for r in (x_regions, y_regions, z_regions)))
 
     def get_spacing_arrays_for_stencil(self) -> dict:
         """float32 inverse spacings: faces (centre distances, n-1) for the
         velocity update, cells (n) for the divergence (core/grid.py:493-532)."""
-        return {
-            "inv_dx_face": (1.0 / np.diff(self._x_coords)).astype(np.float32),
-            "inv_dx_cell": (1.0 / self._dx).astype(np.float32),
-            "inv_dy_face": (1.0 / np.diff(self._y_coords)).astype(np.float32),
-            "inv_dy_cell": (1.0 / self._dy).astype(np.float32),
-            "inv_dz_face": (1.0 / np.diff(self._z_coords)).astype(np.float32),
-            "inv_dz_cell": (1.0 / self._dz).astype(np.float32),
-        }
+        out = {}
+        for a, c, w in zip("xyz", self._c, self._w):
+            out[f"inv_d{a}_face"] = (1.0 / np.diff(c)).astype(np.float32)
+            out[f"inv_d{a}_cell"] = (1.0 / w).astype(np.float32)
+        return out
