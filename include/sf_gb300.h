@@ -409,6 +409,13 @@ typedef struct {
      * = 1 closes every face of a cell (a rigid wall), phi in (0, 1) a
      * partly open one, so the solve is differentiable in the geometry. */
     const void* occupancy;
+    /* Per axis a, the indices [unit_lo[a], unit_hi[a]) whose decay[a] is
+     * exactly 1 together with both neighbours' (an index past either end
+     * counts as 1); empty when unit_hi <= unit_lo, as a zero-filled
+     * descriptor leaves it.  Blocks of cells inside all three ranges skip
+     * their products with the decays, which changes no value (x * 1 == x
+     * in every working type). */
+    int32_t unit_lo[3], unit_hi[3];
 } sf_diff_desc;
 /* cv arrays (3 x N) from theta (N). */
 int sf_diff_coefficients(const sf_diff_desc* d, const void* theta, void* cvx, void* cvy, void* cvz,

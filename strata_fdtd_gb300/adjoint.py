@@ -32,7 +32,24 @@ class _Desc(ctypes.Structure):
                 ("rho0", ctypes.c_double), ("decay", ctypes.c_void_p * 3),
                 ("src_cell", ctypes.c_int64), ("n_probe", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("probe_cells", ctypes.c_void_p),
-                ("geometry", ctypes.c_void_p), ("occupancy", ctypes.c_void_p)]
+                ("geometry", ctypes.c_void_p), ("occupancy", ctypes.c_void_p),
+                ("unit_lo", ctypes.c_int32 * 3), ("unit_hi", ctypes.c_int32 * 3)]
+
+
+def _unit_range(decay: np.ndarray) -> tuple:
+    """[lo, hi): the longest run of indices whose decay is exactly 1 along
+    with both neighbours' (an index past either end counts as 1)."""
+    one = np.concatenate([[True], decay == 1.0, [True]])
+    ok = one[:-2] & one[1:-1] & one[2:]
+    best, start = (0, 0), None
+    for i, v in enumerate(np.append(ok, False)):
+        if v and start is None:
+            start = i
+        elif not v and start is not None:
+            if i - start > best[1] - best[0]:
+                best = (start, i)
+            start = None
+    return best
 
 
 def _ptrs(ts):
@@ -102,10 +119,11 @@ class DifferentiableSolver:
         stub = _S()
         stub.shape, stub.c, stub.grid = self.shape, c, self.grid
         pml.initialize(stub)
-        self.decay = []
+        self.decay, self._unit = [], []
         for n in self.shape:
             d = np.exp(-pml._create_profile(n, np.float64) * self.dt)
             self.decay.append(self._working(d))
+            self._unit.append(_unit_range(d))
         self.source = tuple(source) if source is not None else tuple(n // 2 for n in self.shape)
         self.pulse = GaussianPulse(position=self.source, frequency=frequency)
         self.probe_pos = [tuple(p) for p in probes]
@@ -149,6 +167,8 @@ class DifferentiableSolver:
         d.probe_cells = self.probe_cells.data_ptr()
         d.geometry = self._air.data_ptr() if self._air is not None else None
         d.occupancy = occupancy.data_ptr() if occupancy is not None else None
+        for a in range(3):
+            d.unit_lo[a], d.unit_hi[a] = self._unit[a]
         return d
 
     def _occupancy(self, occupancy):

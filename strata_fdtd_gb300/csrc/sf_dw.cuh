@@ -12,6 +12,16 @@
 // multiply-add.  Every operation is written with explicit round-to-nearest
 // intrinsics, so the compiler's contraction setting cannot change it.
 //
+// The stencil arithmetic (operator+ and operator-) uses a cheaper sum, their
+// SloppyDWPlusDW with the final Fast2Sum replaced by a 2Sum: 2Sum of the high
+// parts, the low parts added to its error term in two float additions, 2Sum
+// of the two (14 operations against 20).  The first and last 2Sums are
+// exact, so the result differs from x + y only by the two roundings of the
+// low-order additions: |error| <= 3u^2 (|x| + |y|) (1 + u).  That is an
+// absolute bound at the operands' scale, not a relative one when x and y
+// cancel; the accurate sum (sf_dw::add) stays where a long running sum is
+// formed (gradient accumulators, the loss injection).
+//
 // GB300 runs FP64 at a small fraction of its FP32 rate; a double-word solve
 // keeps FP64-class accuracy on the FP32 pipe (the differentiable solve's
 // "dw" working precision).
@@ -54,7 +64,21 @@ __device__ __forceinline__ dwf add(dwf x, dwf y) {
     return dwf(zh, zl);
 }
 
+// x + y with |error| <= 3u^2 (|x| + |y|) (1 + u) (see the header)
+__device__ __forceinline__ dwf add_fast(dwf x, dwf y) {
+    float sh, sl, zh, zl;
+    two_sum(x.hi, y.hi, sh, sl);
+    two_sum(sh, __fadd_rn(sl, __fadd_rn(x.lo, y.lo)), zh, zl);
+    return dwf(zh, zl);
+}
+
 __device__ __forceinline__ dwf neg(dwf x) { return dwf(-x.hi, -x.lo); }
+
+// x == 1 exactly.  Every double-word this header produces satisfies
+// fl(hi + lo) == hi, and for such an x, mul(x, one) and mul(one, x) return x
+// (the same hi and lo, up to the sign of a zero lo), so a product with a
+// factor known to be one may be skipped without changing any value.
+__device__ __forceinline__ bool is_one(dwf x) { return x.hi == 1.0f && x.lo == 0.0f; }
 
 __device__ __forceinline__ dwf mul(dwf x, dwf y) {
     const float ch = __fmul_rn(x.hi, y.hi);
@@ -79,8 +103,8 @@ __device__ __forceinline__ dwf mul(dwf x, float y) {
 
 }  // namespace sf_dw
 
-__device__ __forceinline__ dwf operator+(dwf a, dwf b) { return sf_dw::add(a, b); }
-__device__ __forceinline__ dwf operator-(dwf a, dwf b) { return sf_dw::add(a, sf_dw::neg(b)); }
+__device__ __forceinline__ dwf operator+(dwf a, dwf b) { return sf_dw::add_fast(a, b); }
+__device__ __forceinline__ dwf operator-(dwf a, dwf b) { return sf_dw::add_fast(a, sf_dw::neg(b)); }
 __device__ __forceinline__ dwf operator*(dwf a, dwf b) { return sf_dw::mul(a, b); }
 __device__ __forceinline__ dwf& operator+=(dwf& a, dwf b) { return a = a + b; }
 __device__ __forceinline__ dwf& operator-=(dwf& a, dwf b) { return a = a - b; }

@@ -270,3 +270,53 @@ def test_curved_shape_constants_match_oracle_construction():
         S.Horn((0, 0, 0), (0, 0, 1), 0.1, 0.2, "parabolic")
     with pytest.raises(ValueError):
         S.SmoothUnion(S.Sphere((0, 0, 0), 1.0), S.Sphere((1, 0, 0), 1.0), 0.0)
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every ctypes mirror of a struct in include/sf_gb300.h has the C
+    compiler's size and field offsets (a program built from the header by
+    the host compiler prints them)."""
+    import shutil
+    import subprocess
+
+    from strata_fdtd_gb300 import adjoint as A
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    mirrors = {"sf_grid_desc": _native.SfGridDesc, "sf_source": _native.SfSource,
+               "sf_pole": _native.SfPole, "sf_plane_bc": _native.SfPlaneBC,
+               "sf_sdf_node": _native.SfSdfNode, "sf_device_info_t": _native.SfDeviceInfo,
+               "sf_diff_desc": A._Desc}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sf_gb300.h"',
+             'int main(void) {']
+    for cname, cls in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in
+               subprocess.run([str(exe)], check=True, capture_output=True,
+                              text=True).stdout.splitlines())
+    for cname, cls in mirrors.items():
+        assert int(got[f"{cname} size"]) == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(got[f"{cname} {fname}"]) == getattr(cls, fname).offset, (cname, fname)
+
+
+def test_unit_decay_ranges():
+    """The differentiable solve's unit-decay ranges: the longest run of
+    indices whose decay and both neighbours' are exactly 1 (past either end
+    counts as 1)."""
+    from strata_fdtd_gb300.adjoint import _unit_range
+
+    assert _unit_range(np.array([0.5, 0.9, 1, 1, 1, 1, 0.9, 0.5])) == (3, 5)
+    assert _unit_range(np.ones(5)) == (0, 5)
+    assert _unit_range(np.array([0.5, 1.0, 0.5])) == (0, 0)
+    assert _unit_range(np.array([1, 1, 0.5, 1, 1, 1, 1])) == (4, 7)
+    assert _unit_range(np.array([1, 1, 1, 0.5, 1, 1])) == (0, 2)

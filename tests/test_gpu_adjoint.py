@@ -162,6 +162,33 @@ def test_probe_gather_paths_and_many_probe_gradients():
     assert err_dw < 1e-9, err_dw
 
 
+def test_unit_decay_blocks_change_no_value():
+    """Blocks whose cells and neighbours all have decay 1 skip the decay
+    products in the forward and adjoint kernels: traces and gradients must
+    equal, bit for bit, those of the same solve with that path switched off
+    (empty unit-decay ranges), in every precision."""
+    shape = (24, 28, 72)  # interior blocks of 32 k x 8 j exist at PML 3
+    theta = torch.tensor(design_field(shape, region=12, seed=7, sigma=2.0), device="cuda")
+    for dtype in (torch.float32, torch.float64, "dw"):
+        out = []
+        for unit in (True, False):
+            s = DifferentiableSolver(shape, pml_depth=3, frequency=20000.0, source=(8, 14, 30),
+                                     probes=[(16, 14, 50), (10, 20, 20)], dtype=dtype,
+                                     checkpoint_every=20)
+            if unit:
+                assert s._unit[2][1] - s._unit[2][0] >= 40 and s._unit[1][1] - s._unit[1][0] >= 16
+            else:
+                s._unit = [(0, 0)] * 3
+            th = theta.clone().to(s.ext_dtype).requires_grad_(True)
+            target = torch.zeros((60, 2), dtype=s.ext_dtype, device="cuda")
+            loss = s.loss(th, target, 60)
+            loss.backward()
+            out.append((s.forward(theta.to(s.ext_dtype), 60)[0], th.grad.clone(), loss.detach()))
+        (t1, g1, l1), (t0, g0, l0) = out
+        assert float(t1.abs().max()) > 0 and float(g1.abs().max()) > 0
+        assert torch.equal(t1, t0) and torch.equal(g1, g0) and torch.equal(l1, l0), dtype
+
+
 def _walled_geometry(shape=(20, 18, 22)):
     """A rigid slab across x = 10-11 with a 4x4 aperture, and a solid block
     beside the source: faces on every axis touch a solid cell."""
