@@ -32,7 +32,7 @@ from .solver import (FDTDSolver, GaussianPulse, Probe, get_native_info, has_gpu_
 from .waveforms import AudioFileWaveform
 from .weighting import apply_weighting, calculate_leq, calculate_spl
 
-from . import analysis, dsp, geometry, materials  # noqa: E402  (submodules by name)
+from . import analysis, dsp, geometry, io, materials  # noqa: E402  (submodules by name)
 
 __version__ = "0.1.0"
 

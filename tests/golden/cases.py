@@ -16,6 +16,9 @@ geometry/resonator.py:59, Pole/SimpleMaterial materials/base.py:55,509.
 """
 from __future__ import annotations
 
+import json
+import os
+
 import numpy as np
 
 AIR = dict(c=343.0, rho=1.204)
@@ -675,3 +678,75 @@ def random_sdf_tree(api, rng, depth=3):
         return a.rotate(tuple(float(v) for v in rng.uniform(-1, 1, 3)), float(rng.uniform(-1, 1)))
 
     return node(depth)
+
+
+# The legacy (binary + JSON) result files: fixed arrays through every
+# exporter option, and a small solve with pressure and velocity snapshots
+# exported whole (io/legacy.py).  The same calls run against the reference's
+# module (tests/golden/make_golden.py ``legacy``) and this package's.
+LEGACY_CASE = dict(
+    shape=(22, 18, 26), res=1e-3, courant=0.5, pml=dict(depth=3),
+    geometry=dict(kind="blocks", seed=5),
+    sources=[("point", (7, 9, 12), 25000.0, 1.0),
+             ("plane", {"axis": 2, "index": 20}, 15000.0, 0.5)],
+    probes=[("a", (15, 9, 12)), ("b", (4, 3, 20))],
+    steps=45, snapshot_interval=10,
+)
+
+
+def _collect(d):
+    """{relative path: bytes} of every file under d, with the directory's
+    own path written as <dir> inside the JSON files (they record paths)."""
+    out = {}
+    for root, _, names in os.walk(d):
+        for n in sorted(names):
+            path = os.path.join(root, n)
+            data = open(path, "rb").read()
+            if n.endswith(".json"):
+                data = data.replace(str(d).encode(), b"<dir>")
+            out[os.path.relpath(path, d)] = data
+    return out
+
+
+def _meta(m, d):
+    return json.dumps(m).replace(str(d), "<dir>")
+
+
+def legacy_array_exports(L, d):
+    """Every array exporter option on fixed arrays (float16 overflow and
+    subnormals, a constant field for uint8, both geometry encodings).
+    Returns ({call: metadata JSON}, {file: bytes})."""
+    rng = np.random.default_rng(21)
+    p = (rng.standard_normal((9, 10, 11)) * 50).astype(np.float32)
+    p[0, 0, 0], p[1, 1, 1], p[2, 2, 2] = 7.0e4, 1.0e-6, -3.3e-8
+    vel = [rng.standard_normal((9, 10, 11)).astype(np.float32) * 1e-3 for _ in range(3)]
+    geom = rng.random((9, 10, 11)) > 0.3
+    meta = {}
+    for fmt in ("float16", "float32", "uint8"):
+        for ds in (1, 2):
+            meta[f"snap_{fmt}_{ds}"] = L.export_snapshot(p, os.path.join(d, f"s_{fmt}_{ds}.bin"),
+                                                         format=fmt, downsample=ds)
+    meta["snap_flat_uint8"] = L.export_snapshot(np.full((4, 5, 6), 2.5, np.float32),
+                                                os.path.join(d, "flat.bin"), format="uint8")
+    for fmt in ("float16", "float32"):
+        for inter in (True, False):
+            meta[f"vel_{fmt}_{inter}"] = L.export_velocity_snapshot(
+                *vel, os.path.join(d, f"v_{fmt}_{int(inter)}"), format=fmt, downsample=3,
+                interleaved=inter)
+    meta["geom_bin"] = L.export_geometry(geom, os.path.join(d, "g.bin"))
+    meta["geom_json"] = L.export_geometry(geom, os.path.join(d, "g.json"), format="json")
+    return {k: _meta(v, d) for k, v in meta.items()}, _collect(d)
+
+
+def legacy_solve_exports(L, solver, d):
+    """A finished solve through export_simulation (defaults; float32 at half
+    resolution without velocity), export_probe_data of one probe and
+    export_metadata with extra keys.  Returns ({call: metadata JSON},
+    {file: bytes})."""
+    meta = {"sim": L.export_simulation(solver, d, prefix="run"),
+            "sim_alt": L.export_simulation(solver, os.path.join(d, "alt"), prefix="alt",
+                                           include_velocity=False, snapshot_format="float32",
+                                           snapshot_downsample=2),
+            "probe_b": L.export_probe_data(solver, os.path.join(d, "b.json"), probe_names=["b"])}
+    L.export_metadata(solver, os.path.join(d, "meta_extra.json"), extra={"run": 3, "tag": "x"})
+    return {k: _meta(v, d) for k, v in meta.items()}, _collect(d)

@@ -396,6 +396,40 @@ def analysis_values(api, manifest):
     manifest["analysis_values"] = dict(keys=sorted(out))
 
 
+def legacy_io(api, manifest):
+    """The reference's legacy result files (io/legacy.py, loaded from its
+    file: the io package imports h5py): the array exporters on fixed
+    arrays, and a small solve with pressure and velocity snapshots exported
+    whole.  Stored: each call's returned metadata and every file's bytes
+    (paths inside the JSON files written as <dir>)."""
+    import tempfile
+
+    spec = importlib.util.spec_from_file_location(
+        "ref_legacy", os.path.join(REF_ROOT, "src", "strata_fdtd", "io", "legacy.py"))
+    L = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(L)
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        meta, files = C.legacy_array_exports(L, d)
+    for k, v in meta.items():
+        out[f"meta__arrays__{k}"] = np.array(v)
+    for k, v in files.items():
+        out[f"file__arrays__{k}"] = np.frombuffer(v, dtype=np.uint8)
+    case = C.LEGACY_CASE
+    solver = C.build_case(api, case)
+    solver.enable_snapshots(case["snapshot_interval"], capture_velocity=True)
+    for _ in range(case["steps"]):
+        solver.step()
+    with tempfile.TemporaryDirectory() as d:
+        meta, files = C.legacy_solve_exports(L, solver, d)
+    for k, v in meta.items():
+        out[f"meta__solve__{k}"] = np.array(v)
+    for k, v in files.items():
+        out[f"file__solve__{k}"] = np.frombuffer(v, dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "legacy_io.npz"), **out)
+    manifest["legacy_io"] = dict(keys=sorted(out))
+
+
 def main():
     only = set(sys.argv[1:])
     api = load_reference()
@@ -416,6 +450,8 @@ def main():
         host_values(api, manifest)
     if not only or "analysis" in only:
         analysis_values(api, manifest)
+    if not only or "legacy" in only:
+        legacy_io(api, manifest)
     with open(mpath, "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
 
