@@ -17,9 +17,7 @@
 // gather, and a one-thread kernel that advances the device step counter and
 // resets the queue.  The kernels read the step number from device memory, so
 // a run of steps can be captured once as a CUDA graph and replayed.  Grids
-// drop out of the work when they reach their own step count: members are
-// listed longest run first, so a finished grid's items end their segment of
-// the queue and the warps skip them without claiming them one by one.
+// drop out of the work when they reach their own step count.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -251,14 +249,7 @@ __global__ void __launch_bounds__(32 * W, MINB) k_batch_warp(
         if (it >= n_items) return;  // warp-uniform
         const int4 T = items[it];   // grid, i-chunk, row block, k block
         const SfGridDev& g = grids[T.x];
-        if (s >= g.n_steps) {
-            // Members are listed by step count, longest first, so every later
-            // item of this segment belongs to a finished member too: skip to
-            // the plain items, or stop after them.
-            if (it >= n_ade) return;
-            if (lane == 0) atomicMax(queue, n_ade);
-            continue;
-        }
+        if (s >= g.n_steps) continue;
         const bool geom = g.flags != nullptr;
         const int j0 = T.z * g.jspan;
         if (it < n_ade || KIND == 0) {
@@ -328,7 +319,7 @@ __global__ void __launch_bounds__(32 * W, MINB) k_batch_warp_nu(
         if (it >= n_items) return;  // warp-uniform
         const int4 T = items[it];
         const SfGridDev& g = grids[T.x];
-        if (s >= g.n_steps) return;  // the rest belong to finished members too
+        if (s >= g.n_steps) continue;
         const bool geom = g.flags != nullptr;
         const int j0 = T.z * g.jspan;
         const int in = (int)((g.cur0 + s) & 1);
@@ -530,15 +521,11 @@ int build(sf_batch* B) {
     std::vector<SfGridDev> grids;
     std::vector<int4> tiles, tiles_ade, tiles_nu;
     std::vector<int> ade_ids;
-    // members by step count, longest first (then by work): at every step the
-    // items of the members still running are a prefix of each segment (ADE,
-    // plain, nonuniform), so the kernels stop at the first finished one
+    // largest grids first, so the queue hands out the long work early
     std::vector<int> order(B->members.size());
     for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        const auto &ma = B->members[a], &mb = B->members[b];
-        if (ma.steps != mb.steps) return ma.steps > mb.steps;
-        return ma.plan->n * ma.steps > mb.plan->n * mb.steps;
+        return B->members[a].plan->n * B->members[a].steps > B->members[b].plan->n * B->members[b].steps;
     });
     B->max_steps = 0;
     long long ade_cells = 0;
