@@ -17,7 +17,9 @@
 // gather, and a one-thread kernel that advances the device step counter and
 // resets the queue.  The kernels read the step number from device memory, so
 // a run of steps can be captured once as a CUDA graph and replayed.  Grids
-// drop out of the work when they reach their own step count.
+// drop out of the work when they reach their own step count: members are
+// listed longest run first, so a finished grid's items end their segment of
+// the queue, and the first warp to claim one skips the rest of the segment.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -244,9 +246,23 @@ __global__ void __launch_bounds__(32 * W, MINB) k_batch_warp(
     const long long s = *step_ptr;
     for (;;) {
         int it = 0;
-        if (lane == 0) it = atomicAdd(queue, 1);
+        if (lane == 0) {
+            it = atomicAdd(queue, 1);
+            // members are listed longest run first, so a finished member's
+            // item is followed by finished members' items only: skip to the
+            // plain items, or stop after them
+            if (it < n_items && s >= grids[items[it].x].n_steps) {
+                if (it < n_ade) {
+                    atomicMax(queue, n_ade);
+                    it = -1;
+                } else {
+                    it = n_items;
+                }
+            }
+        }
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= n_items) return;  // warp-uniform
+        if (it < 0) continue;
         const int4 T = items[it];   // grid, i-chunk, row block, k block
         const SfGridDev& g = grids[T.x];
         if (s >= g.n_steps) continue;
@@ -314,7 +330,11 @@ __global__ void __launch_bounds__(32 * W, MINB) k_batch_warp_nu(
     const long long s = *step_ptr;
     for (;;) {
         int it = 0;
-        if (lane == 0) it = atomicAdd(queue, 1);
+        if (lane == 0) {
+            it = atomicAdd(queue, 1);
+            // a finished member's item: only finished members' items follow
+            if (it < n_items && s >= grids[items[it].x].n_steps) it = n_items;
+        }
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= n_items) return;  // warp-uniform
         const int4 T = items[it];
@@ -521,11 +541,16 @@ int build(sf_batch* B) {
     std::vector<SfGridDev> grids;
     std::vector<int4> tiles, tiles_ade, tiles_nu;
     std::vector<int> ade_ids;
-    // largest grids first, so the queue hands out the long work early
+    // members by step count, longest first (then the largest work first):
+    // at every step the items of the members still running are a prefix of
+    // each segment (ADE, plain, nonuniform), so the kernels stop at the
+    // first item of a finished member
     std::vector<int> order(B->members.size());
     for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return B->members[a].plan->n * B->members[a].steps > B->members[b].plan->n * B->members[b].steps;
+        const auto &ma = B->members[a], &mb = B->members[b];
+        if (ma.steps != mb.steps) return ma.steps > mb.steps;
+        return ma.plan->n * ma.steps > mb.plan->n * mb.steps;
     });
     B->max_steps = 0;
     long long ade_cells = 0;
