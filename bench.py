@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--requests", type=int, default=1000)
     ap.add_argument("--step-group", type=int, default=250)
-    ap.add_argument("--max-active-cells", type=int, default=1 << 27,
+    ap.add_argument("--max-active-cells", type=int, default=1 << 28,
                     help="served stream: cap on the cells of the running solves (0 = none)")
     ap.add_argument("--solo-cells", type=int, default=1 << 24,
                     help="served stream: solves this large step alone (0 = batch all)")
