@@ -508,16 +508,21 @@ ENCLOSURE_FP64_ERRORS = {
 }
 
 
-def extras(args):
-    """The second half of the metric on the same GPU, each on its configured
-    workload: the batched heterogeneous launch, the served request stream
-    (p50/p99 beside throughput, against one request at a time) and the
-    differentiable solve, plus the parity record."""
-    import torch
+def _guarded(fn):
+    """fn() or, if it raises, {"error": ...} with the traceback on stderr:
+    a failing part leaves the rest of the line, the headline included."""
+    import traceback
 
-    out = {}
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001
+        traceback.print_exc()
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def _batched_part(args):
     b = run_batch(args)
-    out["batched"] = {
+    return {
         "value": b["value"], "unit": b["unit"], "workload": b["config"]["workload"],
         "cell_updates": b["config"]["cell_updates"],
         "sequential_value": (b["sequential"] or {}).get("value"),
@@ -525,9 +530,11 @@ def extras(args):
         "traces_identical": b["traces_identical"], "plain_kernel": b["config"]["plain_kernel"],
         "rejected_materials": b["config"]["rejected_materials"],
         "cpu_baseline": b.get("cpu_baseline")}
-    torch.cuda.empty_cache()
+
+
+def _served_part(args):
     sv = run_serve(args)
-    out["served"] = {
+    return {
         "value": sv["value"], "unit": sv["unit"], "workload": sv["config"]["workload"],
         "p50_latency_s": sv["served"]["p50_latency_s"],
         "p99_latency_s": sv["served"]["p99_latency_s"],
@@ -537,16 +544,32 @@ def extras(args):
         "sequential_p99_latency_s": sv["sequential"]["p99_latency_s"],
         "throughput_ratio": sv["throughput_ratio"], "results_identical": sv["results_identical"],
         "done": sv["served"]["done"], "peak_active": sv["served"]["peak_active"],
-        "cpu_baseline": sv.get("cpu_baseline")}
-    torch.cuda.empty_cache()
+        "max_active_cells": args.max_active_cells, "cpu_baseline": sv.get("cpu_baseline")}
+
+
+def _adjoint_part(args):
     a = run_adjoint(args)
-    out["adjoint"] = {"value": a["value"], "unit": a["unit"], "workload": a["config"]["workload"],
-                      "accuracy": a["config"]["accuracy"],
-                      **{k: {q: a[k][q] for q in ("gradient_seconds", "forward_seconds",
-                                                   "gradient_gcell_updates_per_s")}
-                         for k in ("dw", "f32", "f64")}}
-    torch.cuda.empty_cache()
-    out["parity"] = {"quick_start_100": parity_quick_start(),
+    return {"value": a["value"], "unit": a["unit"], "workload": a["config"]["workload"],
+            "accuracy": a["config"]["accuracy"],
+            **{k: {q: a[k][q] for q in ("gradient_seconds", "forward_seconds",
+                                         "gradient_gcell_updates_per_s")}
+               for k in ("dw", "f32", "f64")}}
+
+
+def extras(args):
+    """The second half of the metric on the same GPU, each on its configured
+    workload: the batched heterogeneous launch, the served request stream
+    (p50/p99 beside throughput, against one request at a time) and the
+    differentiable solve, plus the parity record.  Each part is guarded, so
+    one that fails is reported as an error beside the others."""
+    import torch
+
+    out = {}
+    for key, part in (("batched", _batched_part), ("served", _served_part),
+                      ("adjoint", _adjoint_part)):
+        out[key] = _guarded(lambda: part(args))
+        torch.cuda.empty_cache()
+    out["parity"] = {"quick_start_100": _guarded(parity_quick_start),
                      "enclosure_400": ENCLOSURE_FP64_ERRORS}
     return out
 

@@ -2,6 +2,7 @@
 workload with no collective on the data path; the bench line reports the
 whole-job rate over the slowest rank's time.  This checks that host logic
 with two gloo ranks on the CPU (no GPU involved)."""
+import types
 import os
 import socket
 import sys
@@ -54,3 +55,28 @@ def test_single_process_needs_no_process_group():
 
     assert bench.max_over_ranks(3.0, None, "cpu") == 3.0
     assert bench.replica_rate(1, 10**9, 1.0) == 1.0
+
+
+def test_bench_extras_report_a_failing_part_and_keep_the_rest(monkeypatch):
+    """A sub-benchmark that raises becomes {"error": ...} in its key; the
+    other parts, and so the printed line, are still produced."""
+    import bench
+
+    def boom(args):
+        raise RuntimeError("no device")
+
+    monkeypatch.setattr(bench, "run_batch", boom)
+    monkeypatch.setattr(bench, "run_serve", lambda args: {
+        "value": 1.0, "unit": "u", "config": {"workload": "w"}, "throughput_ratio": 1.0,
+        "results_identical": True,
+        "served": {"p50_latency_s": 1.0, "p99_latency_s": 2.0, "makespan_s": 3.0, "done": 4,
+                   "peak_active": 5},
+        "sequential": {"gcell_updates_per_s": 0.5, "p50_latency_s": 1.5, "p99_latency_s": 2.5}})
+    monkeypatch.setattr(bench, "run_adjoint", boom)
+    monkeypatch.setattr(bench, "parity_quick_start", lambda: {"ok": True})
+    args = types.SimpleNamespace(max_active_cells=1 << 28)
+    out = bench.extras(args)
+    assert out["batched"] == {"error": "RuntimeError: no device"}
+    assert out["adjoint"] == {"error": "RuntimeError: no device"}
+    assert out["served"]["value"] == 1.0 and out["served"]["max_active_cells"] == 1 << 28
+    assert out["parity"]["quick_start_100"] == {"ok": True}
