@@ -2,10 +2,10 @@
 workload with no collective on the data path; the bench line reports the
 whole-job rate over the slowest rank's time.  This checks that host logic
 with two gloo ranks on the CPU (no GPU involved)."""
-import types
 import os
 import socket
 import sys
+import types
 
 import pytest
 
