@@ -420,8 +420,7 @@ def run_gpu(args):
                               "run_steps(inner), solver.p and get_probe_data() read back, "
                               "in line"}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline and n_edge == 400:
+    def cpu_point():
         from oracle import oracle as O
 
         o = oracle_enclosure(s.geometry)
@@ -431,11 +430,15 @@ def run_gpu(args):
         v1, n1, _ = time_oracle(o, min(5.0, args.cpu_seconds))
         O.set_threads(th)
         del o
-        cpu = {"value": v, "unit": METRIC, "cores": th, "kind": "port",
-               "sample": f"{n} FDTD steps of the same 400^3 enclosure workload on the CPU "
-                         "oracle (bit-exact C restatement of the reference native kernels, "
-                         "OpenMP, all host threads)",
-               "value_1_thread": v1, "sample_1_thread": f"{n1} FDTD steps, 1 thread"}
+        return {"value": v, "unit": METRIC, "cores": th, "kind": "port",
+                "sample": f"{n} FDTD steps of the same 400^3 enclosure workload on the CPU "
+                          "oracle (bit-exact C restatement of the reference native kernels, "
+                          "OpenMP, all host threads)",
+                "value_1_thread": v1, "sample_1_thread": f"{n1} FDTD steps, 1 thread"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and n_edge == 400:
+        cpu = _guarded(cpu_point)
 
     if rank == 0:
         line = {
