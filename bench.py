@@ -542,9 +542,9 @@ def _served_part(args):
         "p50_latency_s": sv["served"]["p50_latency_s"],
         "p99_latency_s": sv["served"]["p99_latency_s"],
         "makespan_s": sv["served"]["makespan_s"],
-        "sequential_value": sv["sequential"]["gcell_updates_per_s"],
-        "sequential_p50_latency_s": sv["sequential"]["p50_latency_s"],
-        "sequential_p99_latency_s": sv["sequential"]["p99_latency_s"],
+        "sequential_value": (sv["sequential"] or {}).get("gcell_updates_per_s"),
+        "sequential_p50_latency_s": (sv["sequential"] or {}).get("p50_latency_s"),
+        "sequential_p99_latency_s": (sv["sequential"] or {}).get("p99_latency_s"),
         "throughput_ratio": sv["throughput_ratio"], "results_identical": sv["results_identical"],
         "done": sv["served"]["done"], "peak_active": sv["served"]["peak_active"],
         "max_active_cells": args.max_active_cells, "cpu_baseline": sv.get("cpu_baseline")}
