@@ -797,7 +797,8 @@ def run_adjoint(args):
         theta = torch.tensor(design_field(shape, 64, seed=0), device="cuda", dtype=s.ext_dtype)
         target = s.forward(torch.tensor(design_field(shape, 64, seed=1), device="cuda"), n)[0]
         th = theta.clone().requires_grad_(True)
-        s.loss(th, target[:200], 200).backward()  # warm-up
+        w = min(200, n)
+        s.loss(th, target[:w], w).backward()  # warm-up
         torch.cuda.synchronize()
         torch.cuda.reset_peak_memory_stats()
         e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
