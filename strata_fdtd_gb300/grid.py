@@ -78,9 +78,10 @@ def _axis_coords(values, axis: str) -> np.ndarray:
     strictly increasing."""
     c = np.asarray(values, dtype=np.float64).ravel()
     if c.size < 2:
-        raise ValueError(f"{axis}_coords: a nonuniform axis needs two or more cell centres")
+        raise ValueError(f"{axis}_coords: a nonuniform axis needs at least 2 cell centres")
     if np.any(c[1:] <= c[:-1]):
-        raise ValueError(f"{axis}_coords: cell centres must increase strictly")
+        raise ValueError(f"{axis}_coords: cell centres must be monotonically increasing "
+                         "(strictly)")
     return c
 
 
@@ -123,10 +124,10 @@ def _piecewise_centres(regions) -> np.ndarray:
         if not hi > lo:
             raise ValueError(f"from_regions: region {n} has end {hi} not above start {lo}")
         if not res > 0:
-            raise ValueError(f"from_regions: region {n} has a non-positive resolution {res}")
+            raise ValueError(f"from_regions: region {n}: resolution must be positive, got {res}")
         if n and abs(lo - regions[n - 1][1]) > 1e-10:
-            raise ValueError(f"from_regions: region {n} starts at {lo}, not where region "
-                             f"{n - 1} ends ({regions[n - 1][1]})")
+            raise ValueError(f"from_regions: regions must be contiguous; region {n} starts "
+                             f"at {lo}, region {n - 1} ends at {regions[n - 1][1]}")
     out: list = []
     for lo, hi, res in regions:
         cells = max(1, int(round((hi - lo) / res)))

@@ -36,18 +36,21 @@ class HelmholtzResonator(SDFPrimitive):
 
     def _build_geometry(self):
         """resonator.py:142-185."""
+        def sizes(n, names):
+            got = tuple(self.cavity_size)
+            if len(got) != n:
+                raise ValueError(f"a {self.cavity_shape} cavity requires {n} size "
+                                 f"parameter{'s' if n > 1 else ''} ({names}), got {len(got)}")
+            if any(v <= 0 for v in got):
+                raise ValueError(f"cavity sizes must be positive, got {got}")
+            return got
+
         if self.cavity_shape == "box":
-            if len(self.cavity_size) != 3 or any(s <= 0 for s in self.cavity_size):
-                raise ValueError(f"Box cavity requires 3 positive sizes, got {self.cavity_size}")
-            self._cavity = Box(center=tuple(self.position), size=self.cavity_size)
+            self._cavity = Box(center=tuple(self.position), size=sizes(3, "x, y, z"))
         elif self.cavity_shape == "sphere":
-            if len(self.cavity_size) != 1 or self.cavity_size[0] <= 0:
-                raise ValueError("Sphere cavity requires 1 positive size parameter (radius)")
-            self._cavity = Sphere(center=tuple(self.position), radius=self.cavity_size[0])
+            self._cavity = Sphere(center=tuple(self.position), radius=sizes(1, "radius")[0])
         elif self.cavity_shape == "cylinder":
-            if len(self.cavity_size) != 2 or any(s <= 0 for s in self.cavity_size):
-                raise ValueError("Cylinder cavity requires 2 positive size parameters")
-            r, length = self.cavity_size
+            r, length = sizes(2, "radius, length")
             axis = self.neck_direction * length
             self._cavity = Cylinder(p1=tuple(self.position - axis / 2),
                                     p2=tuple(self.position + axis / 2), radius=r)
